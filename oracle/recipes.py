@@ -1,0 +1,164 @@
+"""Composed IB-LBM time steps built from the oracle operators (test infrastructure only).
+
+Each recipe chains the oracle functions in the order of the reference's example
+``update_step`` it cites.  The reference itself has no driver: users write this
+sequence inside ``jax.jit`` + ``lax.scan``.
+"""
+
+import math
+
+import numpy as np
+
+from . import dyn, ib
+from . import lbm2d as L2
+from . import lbm3d as L3
+
+_BC2 = {
+    "nee": L2.boundary_nee, "nebb": L2.boundary_nebb, "eq": L2.boundary_equilibrium,
+    "vnee": L2.boundary_velocity_nee, "vnebb": L2.boundary_velocity_nebb,
+    "veq": L2.boundary_velocity_equilibrium, "pnee": L2.boundary_pressure_nee,
+    "pnebb": L2.boundary_pressure_nebb, "peq": L2.boundary_pressure_equilibrium,
+    "fcnee": L2.boundary_force_corrected_nee, "fcnebb": L2.boundary_force_corrected_nebb,
+    "fceq": L2.boundary_force_corrected_equilibrium,
+}
+_BC3 = {
+    "nee": L3.boundary_nee, "nebb": L3.boundary_nebb, "eq": L3.boundary_equilibrium,
+    "vnee": L3.boundary_velocity_nee, "vnebb": L3.boundary_velocity_nebb,
+    "veq": L3.boundary_velocity_equilibrium, "pnee": L3.boundary_pressure_nee,
+    "pnebb": L3.boundary_pressure_nebb, "peq": L3.boundary_pressure_equilibrium,
+    "fcnee": L3.boundary_force_corrected_nee, "fcnebb": L3.boundary_force_corrected_nebb,
+    "fceq": L3.boundary_force_corrected_equilibrium,
+}
+
+
+def _collide(L, f, feq, kind, omega, mrt_op):
+    if kind == "bgk":
+        return L.collision_bgk(f, feq, omega)
+    if kind == "kbc":
+        return L.collision_kbc(f, feq, omega)
+    if kind == "reg":
+        return L.collision_reg(f, feq, omega)
+    if kind == "mrt":
+        return L.collision_mrt(f, feq, mrt_op)
+    raise ValueError(kind)
+
+
+def _apply_bcs(L, table, f_post, f, bcs):
+    for name, loc, kw in bcs:
+        if name == "bb":
+            f = L.boundary_bounce_back(f_post, f, loc, **kw)
+        elif name == "spec":
+            f = L.boundary_specular_reflection(f_post, f, loc, **kw)
+        else:
+            f = table[name](f, loc, **kw)
+    return f
+
+
+def cavity_step(f, omega, u_lid):
+    """examples/2d/lid_driven_cavity.py:55-63: BGK, stream, NEE top(lid)/left/right/bottom."""
+    rho, u = L2.get_macroscopic(f)
+    f = L2.collision_bgk(f, L2.get_equilibrium(rho, u), omega)
+    f = L2.streaming(f)
+    f = L2.boundary_nee(f, "top", ux_wall=u_lid)
+    f = L2.boundary_nee(f, "left")
+    f = L2.boundary_nee(f, "right")
+    return L2.boundary_nee(f, "bottom")
+
+
+def lbm_step_2d(f, collision, omega=None, mrt_op=None, bcs=(), g=None, forcing="edm"):
+    """Plain D2Q9 step with an optional body-force field (examples/2d/poiseuille_channel.py:82-143)."""
+    rho, u = L2.get_macroscopic(f)
+    if g is not None and forcing in ("guo_bgk", "guo_mrt"):
+        u = u + L2.get_velocity_correction(g, rho)
+    feq = L2.get_equilibrium(rho, u)
+    f = _collide(L2, f, feq, collision, omega, mrt_op)
+    if g is not None:
+        if forcing == "edm":
+            f = L2.forcing_edm(f, g, u)
+        elif forcing == "guo_bgk":
+            f = L2.forcing_guo_bgk(f, g, u, omega)
+        else:
+            f = L2.forcing_guo_mrt(f, g, u, L2.get_mrt_forcing_operator(omega, f.dtype))
+    f_post = f
+    f = L2.streaming(f)
+    return _apply_bcs(L2, _BC2, f_post, f, bcs)
+
+
+class Body2D:
+    """Rigid 2-DOF body carried between steps: markers relative to a displacement d."""
+
+    def __init__(self, X0, Y0, ds, mass, stiffness, damping, area, free=(False, True),
+                 kernel="peskin4", radius=2, n_iter=3, d=None, v=None, a=None):
+        self.X0, self.Y0 = np.asarray(X0), np.asarray(Y0)
+        self.ds, self.mass, self.k, self.c, self.area = ds, mass, stiffness, damping, area
+        self.free = tuple(bool(x) for x in free)
+        self.kernel, self.radius, self.n_iter = kernel, radius, n_iter
+        dt = self.X0.dtype
+        self.d = np.zeros(2, dt) if d is None else np.asarray(d, dt)
+        self.v = np.zeros(2, dt) if v is None else np.asarray(v, dt)
+        self.a = np.zeros(2, dt) if a is None else np.asarray(a, dt)
+
+
+def ib_lbm_step_2d(f, body, collision, omega=None, mrt_op=None, bcs=()):
+    """One VIV step, examples/2d/vortex_induced_vibration.py:96-148.
+
+    Full-grid stencil (the IB window of the example covers the whole grid); the free
+    degrees of freedom of ``body`` advance with Newmark, fixed ones stay zero.
+    Returns ``(f_next, h)`` and updates ``body`` in place.
+    """
+    ny = f.shape[2]
+    rho, u = L2.get_macroscopic(f)
+    feq = L2.get_equilibrium(rho, u)
+    f = _collide(L2, f, feq, collision, omega, mrt_op)
+    mx, my = dyn.get_markers_coords_2dof(body.X0, body.Y0, body.d)
+    W, I = ib.get_ib_stencil(mx, my, ny, ib.KERNELS[body.kernel], body.radius)
+    M = body.X0.shape[0]
+    mv = np.repeat(body.v[None, :], M, axis=0)
+    g, mh = ib.multi_direct_forcing(u, W, I, mv, body.ds, body.n_iter)
+    h = dyn.get_force_to_obj(mh)
+    h = h + body.a * body.area
+    a, v, d = body.a.copy(), body.v.copy(), body.d.copy()
+    for k in range(2):
+        if body.free[k]:
+            a[k], v[k], d[k] = dyn.newmark(body.a[k], body.v[k], body.d[k], h[k], body.mass, body.k, body.c)
+    body.a, body.v, body.d = a, v, d
+    f = L2.forcing_edm(f, g, u)
+    f_post = f
+    f = L2.streaming(f)
+    return _apply_bcs(L2, _BC2, f_post, f, bcs), h
+
+
+def lbm_step_3d(f, collision, omega=None, mrt_op=None, bcs=()):
+    """Plain D3Q19 step (examples/3d/abc_flow.py update loop)."""
+    rho, u = L3.get_macroscopic(f)
+    f = _collide(L3, f, L3.get_equilibrium(rho, u), collision, omega, mrt_op)
+    f_post = f
+    f = L3.streaming(f)
+    return _apply_bcs(L3, _BC3, f_post, f, bcs)
+
+
+def ib_lbm_step_3d(f, W, I, marker_u, ds, collision, omega=None, mrt_op=None, bcs=(), n_iter=3):
+    """Fixed-body 3D step with a static stencil, examples/3d/flow_past_sphere.py:139-180.
+
+    Returns ``(f_next, h)`` with ``h`` the total force on the body.
+    """
+    rho, u = L3.get_macroscopic(f)
+    f = _collide(L3, f, L3.get_equilibrium(rho, u), collision, omega, mrt_op)
+    g, mh = ib.multi_direct_forcing(u, W, I, marker_u, ds, n_iter)
+    f = L3.forcing_edm(f, g, u)
+    f_post = f
+    f = L3.streaming(f)
+    h = mh[0].copy()
+    for i in range(1, mh.shape[0]):
+        h = h + mh[i]
+    return _apply_bcs(L3, _BC3, f_post, f, bcs), h
+
+
+def fibonacci_sphere(n, radius, center):
+    """Marker cloud on a sphere: golden-angle spiral, equal area per marker."""
+    k = np.arange(n) + 0.5
+    phi = np.arccos(1 - 2 * k / n)
+    theta = math.pi * (1 + 5 ** 0.5) * k
+    return np.stack([center[0] + radius * np.cos(theta) * np.sin(phi),
+                     center[1] + radius * np.sin(theta) * np.sin(phi),
+                     center[2] + radius * np.cos(phi)], axis=1)

@@ -1,0 +1,279 @@
+"""Pin the oracle: every oracle function against golden vectors from the reference's own code.
+
+The golden vectors come from running the reference vivsim source (through a NumPy
+backend for its JAX calls) in float32 (``jax_enable_x64`` off) and float64 (on).
+Tolerances are norm-relative (max|a-b| / max|b|): float64 1e-12, float32 2e-6 for
+single operators and 2e-5 for multi-step recipes (summation order of ``einsum``
+contractions is the only difference).
+"""
+
+import math
+
+import numpy as np
+import pytest
+
+from conftest import golden, rel_err
+from oracle import dyn, ib
+from oracle import lbm2d as L2
+from oracle import lbm3d as L3
+from oracle import recipes
+from oracle.lattice import Q9_FACES, Q19_FACES
+
+TOL = {"f32": 2e-6, "f64": 1e-12}
+TOL_RECIPE = {"f32": 2e-5, "f64": 1e-11}
+
+
+def check(mode, got, key, tol=None):
+    G = golden(mode)
+    err = rel_err(got, G[key])
+    assert err <= (tol or TOL[mode]), f"{key}: rel err {err:.3e}"
+
+
+def test_d2_basic(mode):
+    G = golden(mode)
+    f = G["d2.f"]
+    check(mode, L2.streaming(f), "d2.streaming")
+    r, u = L2.get_macroscopic(f)
+    check(mode, r, "d2.macro.rho")
+    check(mode, u, "d2.macro.u")
+    feq = L2.get_equilibrium(G["d2.rho_in"], G["d2.u_in"])
+    check(mode, feq, "d2.equilibrium")
+    om = 1.7
+    check(mode, L2.collision_bgk(f, feq, om), "d2.bgk")
+    check(mode, L2.collision_kbc(f, feq, om), "d2.kbc")
+    check(mode, L2.collision_reg(f, feq, om), "d2.reg")
+    dt = f.dtype
+    check(mode, L2.get_mrt_collision_operator(om, dt), "d2.mrt_op")
+    check(mode, L2.collision_mrt(f, feq, G["d2.mrt_op"]), "d2.mrt")
+    g, u0 = G["d2.g"], G["d2.u_in"]
+    check(mode, L2.get_guo_forcing_term(g, u0), "d2.guo_term")
+    check(mode, L2.forcing_edm(f, g, u0), "d2.edm")
+    check(mode, L2.forcing_guo_bgk(f, g, u0, om), "d2.guo_bgk")
+    check(mode, L2.get_mrt_forcing_operator(om, dt), "d2.mrt_fop")
+    check(mode, L2.forcing_guo_mrt(f, g, u0, G["d2.mrt_fop"]), "d2.guo_mrt")
+    check(mode, L2.get_velocity_correction(g, G["d2.rho_in"]), "d2.vel_corr")
+    check(mode, L2.obstacle_bounce_back(f, G["d2.mask"]), "d2.obb")
+
+
+@pytest.mark.parametrize("loc", ["left", "right", "top", "bottom"])
+def test_d2_boundaries(mode, loc):
+    G = golden(mode)
+    f, fp = G["d2.f"], G["d2.f_pre"]
+    wall = (slice(None),) + Q9_FACES[loc].wall
+
+    def cw(out, key):
+        rest = np.ones(f.shape[1:], bool)
+        rest[Q9_FACES[loc].wall] = False
+        assert np.array_equal(out[:, rest], f[:, rest])
+        check(mode, out[wall], key)
+
+    kw = dict(rho_wall=1.02, ux_wall=0.03, uy_wall=-0.01)
+    cw(L2.boundary_nee(f, loc, **kw), f"d2.nee.{loc}")
+    cw(L2.boundary_nebb(f, loc, **kw), f"d2.nebb.{loc}")
+    cw(L2.boundary_equilibrium(f, loc, **kw), f"d2.eq.{loc}")
+    vk = dict(ux_wall=0.04, uy_wall=0.01)
+    cw(L2.boundary_velocity_nee(f, loc, **vk), f"d2.vnee.{loc}")
+    cw(L2.boundary_velocity_nebb(f, loc, **vk), f"d2.vnebb.{loc}")
+    cw(L2.boundary_velocity_equilibrium(f, loc, **vk), f"d2.veq.{loc}")
+    cw(L2.boundary_pressure_nee(f, loc, rho_wall=1.01), f"d2.pnee.{loc}")
+    cw(L2.boundary_pressure_nebb(f, loc, rho_wall=1.01), f"d2.pnebb.{loc}")
+    cw(L2.boundary_pressure_equilibrium(f, loc, rho_wall=1.01), f"d2.peq.{loc}")
+    fk = dict(rho_wall=1.0, ux_wall=0.05, uy_wall=0.002, gx_wall=1e-4, gy_wall=-2e-4)
+    cw(L2.boundary_force_corrected_nee(f, loc, **fk), f"d2.fcnee.{loc}")
+    cw(L2.boundary_force_corrected_nebb(f, loc, **fk), f"d2.fcnebb.{loc}")
+    cw(L2.boundary_force_corrected_equilibrium(f, loc, **fk), f"d2.fceq.{loc}")
+    cw(L2.boundary_bounce_back(fp, f, loc, ux_wall=0.02, uy_wall=0.01), f"d2.bb.{loc}")
+    cw(L2.boundary_specular_reflection(fp, f, loc, ux_wall=0.02, uy_wall=0.01), f"d2.spec.{loc}")
+    rc, uc = L2.boundary_characteristic(G["d2.rho_in"], G["d2.u_in"], loc)
+    check(mode, rc, f"d2.cbc.{loc}.rho")
+    check(mode, uc, f"d2.cbc.{loc}.u")
+
+
+def test_d3_basic(mode):
+    G = golden(mode)
+    f = G["d3.f"]
+    check(mode, L3.streaming(f), "d3.streaming")
+    r, u = L3.get_macroscopic(f)
+    check(mode, r, "d3.macro.rho")
+    check(mode, u, "d3.macro.u")
+    feq = L3.get_equilibrium(G["d3.rho_in"], G["d3.u_in"])
+    check(mode, feq, "d3.equilibrium")
+    assert np.array_equal(L3.SECOND_ORDER_PROJECTION, G["d3.projection"].astype(np.float32))
+    om = 1.9
+    check(mode, L3.collision_bgk(f, feq, om), "d3.bgk")
+    check(mode, L3.collision_kbc(f, feq, om), "d3.kbc")
+    check(mode, L3.collision_reg(f, feq, om), "d3.reg")
+    dt = f.dtype
+    check(mode, L3.get_mrt_collision_operator(om, dt), "d3.mrt_op")
+    check(mode, L3.collision_mrt(f, feq, G["d3.mrt_op"]), "d3.mrt")
+    g, u0 = G["d3.g"], G["d3.u_in"]
+    check(mode, L3.get_guo_forcing_term(g, u0), "d3.guo_term")
+    check(mode, L3.forcing_edm(f, g, u0), "d3.edm")
+    check(mode, L3.forcing_guo_bgk(f, g, u0, om), "d3.guo_bgk")
+    check(mode, L3.get_mrt_forcing_operator(om, dt), "d3.mrt_fop")
+    check(mode, L3.forcing_guo_mrt(f, g, u0, G["d3.mrt_fop"]), "d3.guo_mrt")
+    check(mode, L3.obstacle_bounce_back(f, G["d3.mask"]), "d3.obb")
+
+
+@pytest.mark.parametrize("loc", ["left", "right", "bottom", "top", "back", "front"])
+def test_d3_boundaries(mode, loc):
+    G = golden(mode)
+    f, fp = G["d3.f"], G["d3.f_pre"]
+    wall = (slice(None),) + Q19_FACES[loc].wall
+
+    def cw(out, key):
+        check(mode, out[wall], key)
+
+    kw = dict(rho_wall=1.02, ux_wall=0.03, uy_wall=-0.01, uz_wall=0.02)
+    cw(L3.boundary_nee(f, loc, **kw), f"d3.nee.{loc}")
+    cw(L3.boundary_nebb(f, loc, **kw), f"d3.nebb.{loc}")
+    cw(L3.boundary_equilibrium(f, loc, **kw), f"d3.eq.{loc}")
+    vk = dict(ux_wall=0.04, uy_wall=0.01, uz_wall=-0.02)
+    cw(L3.boundary_velocity_nee(f, loc, **vk), f"d3.vnee.{loc}")
+    cw(L3.boundary_velocity_nebb(f, loc, **vk), f"d3.vnebb.{loc}")
+    cw(L3.boundary_velocity_equilibrium(f, loc, **vk), f"d3.veq.{loc}")
+    cw(L3.boundary_pressure_nee(f, loc, rho_wall=1.01), f"d3.pnee.{loc}")
+    cw(L3.boundary_pressure_nebb(f, loc, rho_wall=1.01), f"d3.pnebb.{loc}")
+    cw(L3.boundary_pressure_equilibrium(f, loc, rho_wall=1.01), f"d3.peq.{loc}")
+    fk = dict(rho_wall=1.0, ux_wall=0.05, uy_wall=0.002, uz_wall=-0.001,
+              gx_wall=1e-4, gy_wall=-2e-4, gz_wall=3e-4)
+    cw(L3.boundary_force_corrected_nee(f, loc, **fk), f"d3.fcnee.{loc}")
+    cw(L3.boundary_force_corrected_nebb(f, loc, **fk), f"d3.fcnebb.{loc}")
+    cw(L3.boundary_force_corrected_equilibrium(f, loc, **fk), f"d3.fceq.{loc}")
+    bk = dict(ux_wall=0.02, uy_wall=0.01, uz_wall=-0.01)
+    cw(L3.boundary_bounce_back(fp, f, loc, **bk), f"d3.bb.{loc}")
+    cw(L3.boundary_specular_reflection(fp, f, loc, **bk), f"d3.spec.{loc}")
+    rc, uc = L3.boundary_characteristic(G["d3.rho_in"], G["d3.u_in"], loc)
+    check(mode, rc, f"d3.cbc.{loc}.rho")
+    check(mode, uc, f"d3.cbc.{loc}.u")
+
+
+def test_ib_ops(mode):
+    G = golden(mode)
+    r = G["ib.r"]
+    check(mode, ib.kernel_peskin_3pt(r), "ib.k_peskin3")
+    check(mode, ib.kernel_peskin_4pt(r), "ib.k_peskin4")
+    check(mode, ib.kernel_cosine_4pt(r), "ib.k_cosine4")
+    mx, my = G["ib2.mx"], G["ib2.my"]
+    for name in ("peskin4", "peskin3", "cosine4"):
+        W, I = ib.get_ib_stencil(mx, my, 24, ib.KERNELS[name], 2)
+        assert np.array_equal(I, G[f"ib2.I.{name}"])
+        check(mode, W, f"ib2.W.{name}")
+    W, I = ib.get_ib_stencil(mx, my, 24, ib.kernel_peskin_3pt, 1)
+    assert np.array_equal(I, G["ib2.I.r1"])
+    check(mode, W, "ib2.W.r1")
+    W, I = G["ib2.W.peskin4"], G["ib2.I.peskin4"]
+    check(mode, ib.interpolate(G["ib2.ugrid"], W, I), "ib2.interp")
+    check(mode, ib.spread(G["ib2.Fm"], G["ib2.grid0"], W, I), "ib2.spread")
+    g, h = ib.multi_direct_forcing(G["ib2.ugrid"], W, I, G["ib2.ut"], G["ib2.ds"], 3)
+    check(mode, g, "ib2.mdf.g")
+    check(mode, h, "ib2.mdf.h")
+    g, h = ib.multi_direct_forcing(G["ib2.ugrid"], W, I, G["ib2.ut"], 1.3, 5)
+    check(mode, g, "ib2.mdf5.g")
+    check(mode, h, "ib2.mdf5.h")
+    X = np.stack([mx, my], axis=1)
+    check(mode, ib.get_ds(X), "ib2.ds_curve")
+    check(mode, ib.get_ds(X, closed=False), "ib2.ds_open")
+    W3, I3 = ib.get_ib_stencil_3d(G["ib3.X"], (16, 14, 12))
+    assert np.array_equal(I3, G["ib3.I"])
+    check(mode, W3, "ib3.W")
+    W3c, I3c = ib.get_ib_stencil_3d(G["ib3.X"], (16, 14, 12), ib.kernel_cosine_4pt)
+    assert np.array_equal(I3c, G["ib3.I.cosine4"])
+    check(mode, W3c, "ib3.W.cosine4")
+    check(mode, ib.interpolate(G["ib3.ugrid"], W3, I3), "ib3.interp")
+    z = np.zeros((3, 16, 14, 12), dtype=W3.dtype)
+    check(mode, ib.spread(G["ib3.Fm"], z, W3, I3), "ib3.spread")
+    g, h = ib.multi_direct_forcing(G["ib3.ugrid"], W3, I3, G["ib3.ut"], 0.9, 3)
+    check(mode, g, "ib3.mdf.g")
+    check(mode, h, "ib3.mdf.h")
+
+
+def test_dyn(mode):
+    G = golden(mode)
+    dt = G["d2.f"].dtype
+    check(mode, np.array(dyn.newmark(0.01, -0.02, 0.3, 1.5, 12.0, 3.0, 0.4), dtype=dt), "dyn.scalar")
+    a, v, d, h = G["dyn.vec.in"]
+    check(mode, np.stack(dyn.newmark(a, v, d, h, 12.0, 3.0, 0.4)), "dyn.vec")
+    a, v, d, h = G["dyn.mat.in"]
+    check(mode, np.stack(dyn.newmark(a, v, d, h, G["dyn.mat.m"], G["dyn.mat.k"], G["dyn.mat.c"])), "dyn.mat")
+    mx, my = G["ib2.mx"], G["ib2.my"]
+    dv = G["dyn.vec.in"][2]
+    check(mode, np.stack(dyn.get_markers_coords_2dof(mx, my, dv)), "dyn.coords2")
+    d3 = G["dyn.mat.in"][2]
+    v3 = G["dyn.mat.in"][1]
+    x3, y3 = dyn.get_markers_coords_3dof(mx, my, 14.3, 11.7, d3)
+    check(mode, np.stack([x3, y3]), "dyn.coords3")
+    check(mode, dyn.get_markers_velocity_3dof(x3, y3, 14.3, 11.7, d3, v3), "dyn.vel3")
+    check(mode, dyn.get_force_to_obj(G["ib2.Fm"]), "dyn.force")
+    check(mode, dyn.get_torque_to_obj(x3, y3, 14.3, 11.7, d3, G["ib2.Fm"]), "dyn.torque")
+
+
+def test_recipe_cavity(mode):
+    G = golden(mode)
+    f = G["cav.f0"].copy()
+    om = L2.get_omega(0.0256)
+    for step in range(1, 31):
+        f = recipes.cavity_step(f, om, 0.1)
+        if step in (1, 10, 30):
+            check(mode, f, f"cav.f{step}", TOL_RECIPE[mode])
+
+
+def _viv_body(G, dt):
+    D, U0 = 8.0, 0.05
+    M = 24
+    area = math.pi * (D / 2) ** 2
+    mass = area * 10.0
+    fn = U0 / (5.0 * D)
+    K = (2 * math.pi * fn) ** 2 * mass * (1 + 1 / 10.0)
+    return recipes.Body2D(G["viv.X0"], G["viv.Y0"], math.pi * D / M, mass, K, 0.0, area,
+                          free=(False, True), n_iter=3)
+
+
+@pytest.mark.parametrize("coll", ["kbc", "mrt", "reg", "bgk"])
+def test_recipe_viv(mode, coll):
+    G = golden(mode)
+    dt = G["viv.X0"].dtype
+    nx, ny, U0 = 40, 24, 0.05
+    om = L2.get_omega(U0 * 8.0 / 20.0)
+    u = np.zeros((2, nx, ny), dt)
+    u[0] = U0
+    u[1] = G["viv.pert"]
+    f = L2.get_equilibrium(np.ones((nx, ny), dt), u)
+    body = _viv_body(G, dt)
+    op = L2.get_mrt_collision_operator(om, dt)
+    bcs = [("eq", "left", dict(ux_wall=U0)), ("pnee", "right", dict(rho_wall=1.0))]
+    for step in range(1, 7):
+        f, h = recipes.ib_lbm_step_2d(f, body, coll, om, op, bcs)
+        if step == 1:
+            r, uu = L2.get_macroscopic(f)
+            check(mode, r, f"viv.{coll}.rho1", TOL_RECIPE[mode])
+            check(mode, uu, f"viv.{coll}.u1", TOL_RECIPE[mode])
+        if step in (1, 6):
+            check(mode, h, f"viv.{coll}.h{step}", 1e-4 if mode == "f32" else 1e-10)
+            check(mode, np.stack([body.a, body.v, body.d]), f"viv.{coll}.body{step}",
+                  1e-4 if mode == "f32" else 1e-10)
+    check(mode, f, f"viv.{coll}.f6", TOL_RECIPE[mode])
+
+
+@pytest.mark.parametrize("coll", ["reg", "bgk", "kbc"])
+def test_recipe_sphere(mode, coll):
+    G = golden(mode)
+    X = G["sph.X"]
+    dt = X.dtype
+    nx, ny, nz, D, U0, M = 16, 12, 12, 5.0, 0.05, 79
+    om = L3.get_omega(U0 * D / 30.0)
+    W, I = ib.get_ib_stencil_3d(X, (nx, ny, nz))
+    ds = 4 * math.pi * (D / 2) ** 2 / M
+    u = G["sph.pert"].copy()
+    u[0] = u[0] + U0
+    f = L3.get_equilibrium(np.ones((nx, ny, nz), dt), u)
+    bcs = [("eq", "left", dict(ux_wall=U0)), ("pnee", "right", dict(rho_wall=1.0))]
+    for step in range(1, 5):
+        f, h = recipes.ib_lbm_step_3d(f, W, I, np.zeros((M, 3), dt), ds, coll, om, None, bcs)
+        if step == 1:
+            r, uu = L3.get_macroscopic(f)
+            check(mode, r, f"sph.{coll}.rho1", TOL_RECIPE[mode])
+            check(mode, uu, f"sph.{coll}.u1", TOL_RECIPE[mode])
+        if step in (1, 4):
+            check(mode, h, f"sph.{coll}.h{step}", 1e-4 if mode == "f32" else 1e-10)
+    check(mode, f, f"sph.{coll}.f4", TOL_RECIPE[mode])
