@@ -1,0 +1,409 @@
+#!/usr/bin/env python
+"""Benchmark of the fused IB-LBM time step (MLUPS) on one GB300, plus HBM-roofline cases.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Headline workload (default): the 2-D cylinder VIV case, D2Q9 KBC on 1024 x 512 with a
+126-marker spring-mounted cylinder, MDF 3 iterations (vivsim_gb300.configs.viv2d).  One
+bench step = `--chunk` time steps replayed from a CUDA graph; L2 is flushed (a 512 MiB
+write) before every bench step, so each bench step starts from HBM.  MLUPS = nodes x
+time steps / seconds / 1e6.
+
+Extra measurements on the same line: the grid kernel's HBM roofline on this case and on
+two HBM-bound cases (D3Q19 regularised sphere 256 x 128 x 128, D2Q9 KBC 8192 x 8192),
+the end-to-end rate through the public API with host buffers, and a CPU baseline (the
+NumPy oracle on the host).  ``--impl reference`` times the CPU implementation alone.
+
+Multi-GPU (torchrun): every rank advances its own replica (no exchange): weak scaling.
+"""
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+BYTES_PER_UPDATE = {9: 72, 19: 152}  # f32: each population read once and written once
+
+
+def parse():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--workload", choices=["viv2d", "cavity", "sphere3d", "periodic2d"], default="viv2d")
+    ap.add_argument("--chunk", type=int, default=50, help="time steps per bench step")
+    ap.add_argument("--no-extras", action="store_true", help="skip the HBM-bound roofline cases")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU-baseline sample budget")
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------------ utilities
+
+def dist_info():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def peaks():
+    path = os.path.join(HERE, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def traffic_from_profiles(workload):
+    """Per-launch DRAM bytes of the grid kernel from the committed ncu summary, if any."""
+    path = os.path.join(HERE, "profiles", "dram_traffic.txt")
+    try:
+        for line in open(path):
+            parts = line.split()
+            if len(parts) >= 2 and parts[0] == workload:
+                return float(parts[1])
+    except OSError:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.proc = None
+        self.gpu = gpu_index
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(self.gpu)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [ln for ln in out.splitlines() if ln.strip()]
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in getattr(self, "lines", []):
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax = float(p[2])
+            except ValueError:
+                continue
+            for name, val in zip(names, p[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------------- GPU timing
+
+def build_case(name, chunk_hint=None):
+    from vivsim_gb300 import configs
+    return configs.CASES[name]()
+
+
+def time_chunks(torch, run, K, W, flush):
+    """W untimed + K timed bench steps; L2 flushed before each; device time per step."""
+    for _ in range(W):
+        flush()
+        run()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    for k in range(K):
+        flush()
+        ev[k][0].record()
+        run()
+        ev[k][1].record()
+    torch.cuda.synchronize()
+    return sum(a.elapsed_time(b) for a, b in ev) / 1e3
+
+
+def grid_kernel_time(torch, step, body, sim, launches, flush):
+    """Average duration of the grid kernel alone (vs_step_grid_only), L2 flushed once."""
+    from vivsim_gb300 import _lib as V
+    a = sim.f
+    b = torch.empty_like(a)
+    bh = body.handle if body is not None else None
+    flush()
+    V.call("vs_step_grid_only", step.handle, bh, V.ptr(a), V.ptr(b), V.stream())
+    torch.cuda.synchronize()
+    flush()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    src, dst = a, b
+    for _ in range(launches):
+        V.call("vs_step_grid_only", step.handle, bh, V.ptr(src), V.ptr(dst), V.stream())
+        src, dst = dst, src
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / 1e3 / launches
+
+
+def roofline(torch, case, step, body, sim, flush, peak, peak_kind, launches):
+    t = grid_kernel_time(torch, step, body, sim, launches, flush)
+    n = int(math.prod(case["shape"]))
+    bytes_per_launch = BYTES_PER_UPDATE[case["q"]] * n
+    achieved = bytes_per_launch / t / 1e9
+    return {"kernel": "k_step (grid: collide + force + push-stream)", "workload": case["name"], "bound": "hbm",
+            "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
+            "peak_source": f"{peak_kind} hbm_gbs", "bytes_per_launch": bytes_per_launch,
+            "traffic": traffic_from_profiles(case["name"]), "kernel_us": round(t * 1e6, 3),
+            "kernel_mlups": round(n / t / 1e6, 1)}
+
+
+def gb300_arm(args, world, rank, local):
+    import numpy as np
+    import torch
+    import __graft_entry__ as g
+    g.build()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    peak, peak_kind = peaks()
+    stream = torch.cuda.Stream()
+    flush_buf = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def flush():
+        flush_buf.fill_(1.0)
+
+    from vivsim_gb300 import configs
+    case = build_case(args.workload)
+    n = int(math.prod(case["shape"]))
+    with torch.cuda.stream(stream):
+        step, body, sim = configs.build_solver(case)
+        run = lambda: sim.run(args.chunk, graph=True)  # noqa: E731
+        run()  # capture the graph once (untimed)
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+        try:
+            gpu_id = "GPU-" + str(torch.cuda.get_device_properties(local).uuid)
+        except Exception:
+            gpu_id = str(local)
+        with ClockSampler(gpu_id) as clk:
+            secs = time_chunks(torch, run, args.steps, args.warmup, flush)
+        torch.cuda.synchronize()
+        if dist is not None:
+            t = torch.tensor([secs], device="cuda", dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            secs = float(t.item())
+            dist.barrier()
+        mlups = n * args.chunk * args.steps * world / secs / 1e6
+        launches_per_step = (1 if body is not None else 0) + 1 + step_groups(case)
+        rl = roofline(torch, case, step, body, sim, flush, peak, peak_kind, 2 * args.chunk)
+
+        # end to end through the public API with host buffers: H2D f, chunk, D2H f
+        f_host = torch.from_numpy(case["f0"]).pin_memory()
+        out_host = torch.empty_like(f_host).pin_memory()
+        e2e_sim = configs.build_solver(case)[2]
+
+        def e2e_run():
+            e2e_sim.f.copy_(f_host, non_blocking=True)
+            e2e_sim.run(args.chunk, graph=True)
+            out_host.copy_(e2e_sim.f, non_blocking=True)
+
+        e2e_run()
+        torch.cuda.synchronize()
+        e2e_secs = time_chunks(torch, e2e_run, max(3, args.steps // 2), 2, flush)
+        e2e_mlups = n * args.chunk * max(3, args.steps // 2) / e2e_secs / 1e6
+        fbytes = int(f_host.numel() * f_host.element_size())
+
+        extras = {}
+        if not args.no_extras and rank == 0:
+            del e2e_sim
+            for name in ("sphere3d", "periodic2d"):
+                if name == args.workload:
+                    continue
+                c2 = build_case(name)
+                st2, bd2, sm2 = configs.build_solver(c2)
+                r2 = lambda: sm2.run(10, graph=True)  # noqa: E731
+                r2()
+                torch.cuda.synchronize()
+                s2 = time_chunks(torch, r2, 5, 2, flush)
+                extras[name] = {
+                    "workload": c2["name"], "mlups": round(int(math.prod(c2["shape"])) * 10 * 5 / s2 / 1e6, 1),
+                    "roofline": roofline(torch, c2, st2, bd2, sm2, flush, peak, peak_kind, 10)}
+                del st2, bd2, sm2, c2
+                torch.cuda.empty_cache()
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+    cpu = cpu_baseline(case, args.cpu_seconds)
+    clocks = clk.summary()
+    line = {
+        "metric": "MLUPS (fused IB-LBM step; HBM roofline per fused step)",
+        "value": round(mlups, 1),
+        "unit": "MLUPS",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(secs / args.steps * 1e3, 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded numpy draws of the named configuration)",
+        "config": {"workload": case["name"], "time_steps_per_bench_step": args.chunk, "nodes": n,
+                   "l2": "flushed (512 MiB write) before every bench step; the two population buffers "
+                         f"({2 * n * BYTES_PER_UPDATE[case['q']] // 2 / 1e6:.1f} MB) stay L2-resident within one",
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+        "roofline": rl,
+        "roofline_hbm_bound": extras,
+        "e2e": {"value": round(e2e_mlups, 1), "unit": "MLUPS", "h2d_bytes_per_step": fbytes,
+                "d2h_bytes_per_step": fbytes,
+                "path": "vivsim_gb300.solver.Simulation.run from pinned host populations"},
+        "gpu_launches": launches_per_step * args.chunk * args.steps,
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def step_groups(case):
+    """Face-kernel launches per step (opposite faces of one axis share a launch)."""
+    groups, size, prev = 0, 0, None
+    axis = {"left": 0, "right": 0, "bottom": 1, "top": 1, "back": 2, "front": 2}
+    for (_, loc, _, _) in case["boundaries"]:
+        if prev is not None and size == 1 and axis[prev] == axis[loc] and prev != loc:
+            size = 2
+        else:
+            groups += 1
+            size = 1
+        prev = loc
+    return groups
+
+
+# -------------------------------------------------------------------- CPU side
+
+def oracle_stepper(case):
+    """A closure running one time step of `case` with the NumPy oracle."""
+    import numpy as np
+
+    from oracle import ib as OIB
+    from oracle import lbm2d as L2
+    from oracle import recipes
+    names = {("nee", "given"): "nee", ("nebb", "given"): "nebb", ("equilibrium", "given"): "eq",
+             ("nee", "pressure"): "pnee", ("nee", "velocity"): "vnee", ("nebb", "force_corrected"): "fcnebb"}
+    bcs = [(names[(k, m)], loc, kw) for (k, loc, m, kw) in case["boundaries"]]
+    state = {"f": case["f0"].copy()}
+    q, coll, om = case["q"], case["collision"], case["omega"]
+    b = case["body"]
+    if q == 9 and b is not None:
+        X = b["markers"].astype(np.float32)
+        body = recipes.Body2D(X[:, 0], X[:, 1], b["ds"], b["mass"], b["stiffness"], b["damping"],
+                              b["added_mass_area"], free=b["free_dof"][:2], kernel=b["kernel"], n_iter=b["n_iter"])
+        op = L2.get_mrt_collision_operator(om, np.float32) if coll == "mrt" else None
+
+        def one():
+            state["f"], _ = recipes.ib_lbm_step_2d(state["f"], body, coll, om, op, bcs)
+    elif q == 19 and b is not None:
+        X = b["markers"].astype(np.float32)
+        W, I = OIB.get_ib_stencil_3d(X, case["shape"])
+        zero = np.zeros((X.shape[0], 3), np.float32)
+
+        def one():
+            state["f"], _ = recipes.ib_lbm_step_3d(state["f"], W, I, zero, b["ds"], coll, om, None, bcs, b["n_iter"])
+    elif q == 9 and coll == "bgk" and len(bcs) == 4:
+        def one():
+            state["f"] = recipes.cavity_step(state["f"], om, case["boundaries"][0][3].get("ux_wall", 0.0))
+    else:
+        def one():
+            state["f"] = recipes.lbm_step_2d(state["f"], coll, om, None, bcs) if q == 9 else \
+                recipes.lbm_step_3d(state["f"], coll, om, None, bcs)
+    return one
+
+
+def cpu_baseline(case, budget_s):
+    """Oracle (NumPy, one core) on a bounded sample of the same workload: full grid, few steps."""
+    one = oracle_stepper(case)
+    n = int(math.prod(case["shape"]))
+    t0 = time.perf_counter()
+    one()  # first step (allocation warm-up) is timed too, it is a full step
+    steps = 1
+    while time.perf_counter() - t0 < budget_s and steps < 200:
+        one()
+        steps += 1
+    secs = time.perf_counter() - t0
+    return {"value": round(n * steps / secs / 1e6, 3), "unit": "MLUPS", "cores": 1, "kind": "port",
+            "sample": f"{steps} time steps of {case['name']} on the full grid (NumPy oracle, single thread)"}
+
+
+def reference_arm(args, world, rank):
+    if rank != 0:
+        return
+    from vivsim_gb300 import configs
+    case = configs.CASES[args.workload]()
+    one = oracle_stepper(case)
+    n = int(math.prod(case["shape"]))
+    for _ in range(args.warmup):
+        one()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        one()
+    secs = time.perf_counter() - t0
+    v = n * args.steps / secs / 1e6
+    line = {
+        "impl": "reference", "metric": "MLUPS (fused IB-LBM step; HBM roofline per fused step)", "value": round(v, 3),
+        "unit": "MLUPS", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(secs / args.steps * 1e3, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded numpy draws of the named configuration)",
+        "config": {"workload": case["name"], "time_steps_per_bench_step": 1, "nodes": n},
+        "cpu_baseline": {"value": round(v, 3), "unit": "MLUPS", "cores": 1, "kind": "port",
+                         "sample": f"{args.steps} timed time steps of {case['name']} on the full grid "
+                                   "(NumPy restatement of the reference; JAX is not installed)"},
+        "e2e": {"value": round(v, 3), "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_info()
+    if args.impl == "reference":
+        reference_arm(args, world, rank)
+    else:
+        gb300_arm(args, world, rank, local)
+
+
+if __name__ == "__main__":
+    main()

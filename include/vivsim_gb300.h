@@ -1,0 +1,252 @@
+/*
+ * vivsim_gb300 — C ABI of the GB300 (sm_103a) IB-LBM kernels.
+ *
+ * Each entry point replaces one pure function of the reference library haimingz/vivsim
+ * (cited as path:line inside that project) or a composed step of it.  Conventions:
+ *
+ *   - every function returns an int status (VS_OK = 0); the message of the last failure
+ *     on the calling thread is available from vs_last_error();
+ *   - all array arguments are DEVICE pointers unless named *_host; the caller owns them;
+ *   - arrays are C-order, structure of arrays: populations f[q][x][y] (D2Q9) and
+ *     f[q][x][y][z] (D3Q19), velocities u[d][...], marker arrays [marker][component];
+ *   - dtype selects float (VS_F32) or double (VS_F64) for every floating array of a call;
+ *   - `stream` is a cudaStream_t (0 = legacy default stream); work is enqueued, not
+ *     synchronised, exactly like a JAX/XLA custom call or a PyTorch op;
+ *   - unless stated otherwise `out` may not alias an input.
+ */
+#ifndef VIVSIM_GB300_H
+#define VIVSIM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ constants */
+enum {
+  VS_OK = 0,
+  VS_ERR_INVALID_ARG = 1, /* bad shape, enum, pointer or size                      */
+  VS_ERR_CUDA = 2,        /* a CUDA runtime call failed                            */
+  VS_ERR_UNSUPPORTED = 3, /* valid request this build does not implement           */
+  VS_ERR_RANGE = 4,       /* a stencil index / window fell outside its grid        */
+  VS_ERR_TIMEOUT = 5,     /* a bounded device-side wait gave up                    */
+  VS_ERR_NONFINITE = 6    /* the NaN/Inf watchdog saw a non-finite population      */
+};
+enum { VS_F32 = 0, VS_F64 = 1 };
+enum { VS_COLLIDE_BGK = 0, VS_COLLIDE_KBC = 1, VS_COLLIDE_MRT = 2, VS_COLLIDE_REG = 3 };
+enum { VS_FORCE_NONE = 0, VS_FORCE_EDM = 1, VS_FORCE_GUO_BGK = 2, VS_FORCE_GUO_MRT = 3 };
+/* face locations; D2Q9 uses the first four (left/right: x = 0 / NX-1, bottom/top: y = 0 / NY-1) */
+enum { VS_LEFT = 0, VS_RIGHT = 1, VS_BOTTOM = 2, VS_TOP = 3, VS_BACK = 4, VS_FRONT = 5 };
+/* boundary schemes */
+enum { VS_BC_NEE = 0, VS_BC_NEBB = 1, VS_BC_EQ = 2, VS_BC_BB = 3, VS_BC_SPECULAR = 4 };
+/* how the wall state is completed (lbm/boundary/_helpers.py:175-239 wrappers) */
+enum {
+  VS_WALL_GIVEN = 0,          /* rho_wall and u_wall given                          */
+  VS_WALL_VELOCITY = 1,       /* u_wall given, rho_wall recovered (wrap_velocity)    */
+  VS_WALL_PRESSURE = 2,       /* rho_wall given, u_wall recovered (wrap_pressure)    */
+  VS_WALL_FORCE_CORRECTED = 3 /* u_wall shifted by -g/(2 rho) (wrap_force_corrected) */
+};
+/* 1-D discrete delta kernels, vivsim/ib/kernels.py */
+enum { VS_KERNEL_PESKIN3 = 0, VS_KERNEL_PESKIN4 = 1, VS_KERNEL_COSINE4 = 2 };
+
+const char* vs_last_error(void);
+const char* vs_status_string(int status);
+int vs_version(void);
+
+/* ===================================================================== LBM ops ===
+ * q = 9 (D2Q9, vivsim/lbm) or 19 (D3Q19, vivsim/lbm3d); n = number of nodes.      */
+
+/* periodic streaming — lbm/basic.py:60-85, lbm3d/basic.py:52-87 (nz = 1 for D2Q9) */
+int vs_streaming(int q, int dtype, const void* f, void* out, int nx, int ny, int nz, void* stream);
+/* rho, u = get_macroscopic(f) — lbm/basic.py:88-111, lbm3d/basic.py:90-106 */
+int vs_get_macroscopic(int q, int dtype, const void* f, void* rho, void* u, int64_t n, void* stream);
+/* feq = get_equilibrium(rho, u) — lbm/basic.py:114-135, lbm3d/basic.py:109-130 */
+int vs_get_equilibrium(int q, int dtype, const void* rho, const void* u, void* feq, int64_t n, void* stream);
+/* collision_bgk / collision_kbc / collision_reg (f, feq, omega)
+ *   lbm/basic.py:138-156, lbm/collision/kbc.py:10-60, lbm/collision/reg.py:4-49,
+ *   lbm3d/basic.py:133-146, lbm3d/collision/kbc.py:8-42, lbm3d/collision/reg.py:44-62 */
+int vs_collision(int q, int dtype, int kind, const void* f, const void* feq, double omega, void* out,
+                 int64_t n, void* stream);
+/* collision_mrt(f, feq, op) with a q*q row-major host operator — lbm/collision/mrt.py:66-88,
+ * lbm3d/collision/mrt.py:88-98 */
+int vs_collision_mrt(int q, int dtype, const void* f, const void* feq, const double* op_host, void* out,
+                     int64_t n, void* stream);
+/* get_guo_forcing_term(g, u) — lbm/forcing/guo.py:6-35, lbm3d/forcing/guo.py:13-38 */
+int vs_guo_forcing_term(int q, int dtype, const void* g, const void* u, void* out, int64_t n, void* stream);
+/* forcing_edm / forcing_guo_bgk: out = f + scale * guo(g, u) with scale 1 (edm.py:4-31)
+ * or 1 - omega/2 (guo.py:38-59); pass kind = VS_FORCE_EDM or VS_FORCE_GUO_BGK */
+int vs_forcing(int q, int dtype, int kind, const void* f, const void* g, const void* u, double omega, void* out,
+               int64_t n, void* stream);
+/* forcing_guo_mrt(f, g, u, op) — lbm/forcing/guo.py:83-107, lbm3d/forcing/guo.py:71-87 */
+int vs_forcing_guo_mrt(int q, int dtype, const void* f, const void* g, const void* u, const double* op_host,
+                       void* out, int64_t n, void* stream);
+/* get_velocity_correction(g, rho) = g * 0.5 / rho, g of shape (d, n) — lbm/basic.py:175-194 */
+int vs_velocity_correction(int q, int dtype, const void* g, const void* rho, void* out, int64_t n, void* stream);
+
+/* Wall data for one boundary call.  Scalars are used where the matching device array
+ * pointer is NULL; arrays have the face's shape (N for D2Q9, the 2-D face for D3Q19). */
+typedef struct vs_wall {
+  double rho, ux, uy, uz, gx, gy, gz;
+  const void* rho_arr;
+  const void* ux_arr;
+  const void* uy_arr;
+  const void* uz_arr;
+} vs_wall;
+
+/* boundary_{nee,nebb,equilibrium,bounce_back,specular_reflection} and their velocity /
+ * pressure / force-corrected wrappers: f_out = f_in with the face at `loc` rewritten.
+ *   lbm/boundary/{nee.py:19-65, nebb.py:20-62, eq.py:25-61, bb.py:15-95, _helpers.py:50-239}
+ *   lbm3d/boundary/{nee.py:13-37, nebb.py:13-37, eq.py:13-31, bb.py:8-53, _helpers.py:9-133}
+ * f_before_stream is required for VS_BC_BB / VS_BC_SPECULAR, ignored otherwise.
+ * f_out may equal f_in (in-place update of the face only). */
+int vs_boundary(int q, int dtype, int kind, int mode, int loc, const void* f_in, void* f_out,
+                const void* f_before_stream, int nx, int ny, int nz, const vs_wall* wall, void* stream);
+/* obstacle_bounce_back(f, mask), mask one byte per node — lbm/boundary/bb.py:98-110, lbm3d/boundary/bb.py:56-59 */
+int vs_obstacle_bounce_back(int q, int dtype, const void* f_in, void* f_out, const uint8_t* mask, int64_t n,
+                            void* stream);
+/* boundary_characteristic(rho, u, loc) -> rho_next (face), u_next (d, face)
+ *   lbm/boundary/cbc.py:14-53, lbm3d/boundary/cbc.py:16-51 */
+int vs_boundary_characteristic(int q, int dtype, int loc, const void* rho, const void* u, int nx, int ny, int nz,
+                               void* rho_next, void* u_next, void* stream);
+
+/* ====================================================================== IB ops === */
+
+/* kernel_peskin_3pt / kernel_peskin_4pt / kernel_cosine_4pt — ib/kernels.py:4-61 */
+int vs_ib_kernel(int kernel, int dtype, const void* r, void* out, int64_t n, void* stream);
+/* get_ib_stencil(marker_x, marker_y, ny, kernel, radius) -> W (m, (2r)^2), I int32 — ib/stencil.py:7-51 */
+int vs_ib_stencil_2d(int kernel, int radius, int dtype, const void* marker_x, const void* marker_y, int m,
+                     int ny, void* W, int32_t* I, void* stream);
+/* ib3d.get_ib_stencil(coords (m,3), (nx,ny,nz), kernel, radius) -> W (m, (2r)^3), I — ib3d/stencil.py:7-59 */
+int vs_ib_stencil_3d(int kernel, int radius, int dtype, const void* coords, int m, int nx, int ny, int nz,
+                     void* W, int32_t* I, void* stream);
+/* interpolate(grid (c, n_grid), W (m,s), I (m,s)) -> (m, c) — ib/stencil.py:54-78 */
+int vs_ib_interpolate(int dtype, const void* grid, int c, int64_t n_grid, const void* W, const int32_t* I, int m,
+                      int s, void* out, void* stream);
+/* Scratch bytes for vs_ib_spread / vs_ib_mdf with m markers of s stencil points. */
+size_t vs_ib_workspace_bytes(int m, int s);
+/* spread(marker_values (m,c), grid_in (c,n_grid), W, I) -> grid_out — ib/stencil.py:81-110.
+ * Deterministic: contributions to a node are summed in (marker, stencil point) order,
+ * the order of the reference's scatter-add; no floating-point atomics.  grid_out may
+ * equal grid_in. */
+int vs_ib_spread(int dtype, const void* marker_values, const void* grid_in, void* grid_out, int c, int64_t n_grid,
+                 const void* W, const int32_t* I, int m, int s, void* workspace, size_t workspace_bytes,
+                 void* stream);
+/* multi_direct_forcing(grid_u, W, I, u_target, ds, n_iter) -> (grid_force (c,n_grid),
+ * marker_force (m,c)) — ib/mdf.py:10-64.  ds is per marker (m,) when ds != NULL, else
+ * the scalar ds_scalar. */
+int vs_ib_mdf(int dtype, const void* grid_u, int c, int64_t n_grid, const void* W, const int32_t* I, int m, int s,
+              const void* u_target, const void* ds, double ds_scalar, int n_iter, void* grid_force,
+              void* marker_force, void* workspace, size_t workspace_bytes, void* stream);
+
+/* Read (and optionally clear) the IB status word: bit 0 is set when a stencil index fell
+ * outside [0, n_grid) in an IB call (that contribution is dropped / read as zero).
+ * Synchronous with respect to the device. */
+int vs_ib_status(unsigned* status_out, int reset);
+
+/* ===================================================================== dynamics ===
+ * newmark(a, v, d, h, m, k, c, dt, gamma, beta) — dyn.py:5-51.  a, v, d, h are device
+ * arrays of ndof.  Scalar branch (dyn.py:42-45): m, k, c are the host scalars and every
+ * DOF advances independently; matrix branch (dyn.py:36-41) when m_mat != NULL: ndof x
+ * ndof row-major device matrices, solved by Gaussian elimination with partial pivoting.
+ * Outputs may alias inputs. */
+int vs_newmark(int dtype, int ndof, const void* a, const void* v, const void* d, const void* h, double m, double k,
+               double c, const void* m_mat, const void* k_mat, const void* c_mat, double dt, double gamma,
+               double beta, void* a_next, void* v_next, void* d_next, void* stream);
+/* get_markers_coords_2dof / _3dof, get_markers_velocity_3dof, get_force_to_obj,
+ * get_torque_to_obj — dyn.py:68-154.  x0,y0,x,y are (m,); d, v device (2|3,); h (m,2). */
+int vs_markers_coords_2dof(int dtype, const void* x0, const void* y0, int m, const void* d, void* x, void* y,
+                           void* stream);
+int vs_markers_coords_3dof(int dtype, const void* x0, const void* y0, int m, double xc, double yc, const void* d,
+                           void* x, void* y, void* stream);
+int vs_markers_velocity_3dof(int dtype, const void* x, const void* y, int m, double xc, double yc, const void* d,
+                             const void* v, void* vel, void* stream);
+int vs_force_to_obj(int dtype, const void* h, int m, int c, void* out, void* stream);
+int vs_torque_to_obj(int dtype, const void* x, const void* y, int m, double xc, double yc, const void* d,
+                     const void* h, void* out, void* stream);
+
+/* ================================================================ fused step ===
+ * One IB-LBM time step of the reference's composed update loop
+ * (examples/2d/vortex_induced_vibration.py:96-148, examples/2d/lid_driven_cavity.py:55-63,
+ * examples/3d/flow_past_sphere.py:139-180): moments, equilibrium, collision, forcing,
+ * periodic streaming and the ordered face boundaries in ONE grid pass (push streaming,
+ * one read and one write per population) plus a small ordered face epilogue.       */
+
+typedef struct vs_bc {
+  int kind; /* VS_BC_* */
+  int mode; /* VS_WALL_* */
+  int loc;  /* VS_LEFT ... */
+  double rho, ux, uy, uz, gx, gy, gz;
+} vs_bc;
+
+#define VS_MAX_BC 8
+typedef struct vs_lattice_cfg {
+  int q;         /* 9 or 19 */
+  int dtype;     /* VS_F32 / VS_F64 */
+  int nx, ny, nz;/* nz = 1 for D2Q9 */
+  int collision; /* VS_COLLIDE_* */
+  double omega;
+  double mrt_op[19 * 19];  /* q*q collision operator when collision == VS_COLLIDE_MRT */
+  int forcing;             /* VS_FORCE_* applied to g_uniform + IB force window       */
+  double g_uniform[3];     /* body-force density added at every node                */
+  double mrt_fop[19 * 19]; /* q*q forcing operator when forcing == VS_FORCE_GUO_MRT   */
+  int n_bc;                /* boundaries applied in this order after streaming      */
+  vs_bc bc[VS_MAX_BC];
+} vs_lattice_cfg;
+
+typedef struct vs_lattice_plan vs_lattice_plan;
+int vs_lattice_plan_create(const vs_lattice_cfg* cfg, vs_lattice_plan** out);
+int vs_lattice_plan_destroy(vs_lattice_plan* plan);
+
+/* Immersed body advanced by the IB step (dyn.py + ib/mdf.py).  Markers follow a rigid
+ * 2-DOF translation d (get_markers_coords_2dof); DOFs with free[k] = 0 stay at zero. */
+typedef struct vs_body_cfg {
+  int dim;        /* 2 or 3, must match the lattice                                    */
+  int dtype;
+  int n_markers;
+  const double* x0_host; /* (n_markers,) initial marker coordinates                    */
+  const double* y0_host;
+  const double* z0_host; /* NULL in 2-D                                                */
+  const double* ds_host; /* (n_markers,) or NULL to use ds_scalar                      */
+  double ds_scalar;
+  int kernel;            /* VS_KERNEL_*                                                */
+  int radius;            /* stencil half-width (2 for the 4-point kernels)             */
+  int n_iter;            /* MDF iterations                                             */
+  int moving;            /* 0: stencil built once (fixed body), 1: rebuilt every step  */
+  int free_dof[3];       /* Newmark-integrated translational DOFs                      */
+  double mass, stiffness, damping, added_mass_area; /* h += a * area, vortex_induced_vibration.py:136 */
+  double d0[3], v0[3], a0[3];                       /* initial body state                 */
+  int window_margin;     /* extra nodes around the marker stencils reserved for motion */
+} vs_body_cfg;
+
+typedef struct vs_body_plan vs_body_plan;
+int vs_body_plan_create(const vs_body_cfg* cfg, const vs_lattice_plan* lattice, vs_body_plan** out);
+int vs_body_plan_destroy(vs_body_plan* plan);
+/* Copy the body state out: (a, v, d, h) as 4 x 3 doubles (device state, synchronises the stream). */
+int vs_body_get_state(const vs_body_plan* plan, double* state_host, void* stream);
+int vs_body_set_state(vs_body_plan* plan, const double* state_host, void* stream);
+
+/* One step: f_out = step(f_in).  body may be NULL.  force_hist, when not NULL, receives
+ * the body force h (3 values of the plan dtype) of this step.  f_out must not alias f_in. */
+int vs_step(const vs_lattice_plan* lattice, vs_body_plan* body, const void* f_in, void* f_out, void* force_hist,
+            void* stream);
+/* n_steps steps ping-ponging between f_a (input) and f_b; the result ends in f_a when
+ * n_steps is even, else in f_b.  force_hist (n_steps x 3) may be NULL. */
+int vs_run(const vs_lattice_plan* lattice, vs_body_plan* body, void* f_a, void* f_b, int n_steps,
+           void* force_hist, void* stream);
+/* As vs_run, but the n_steps launches are captured once into a CUDA graph owned by the
+ * lattice plan (re-captured when the arguments change) and replayed. */
+int vs_run_graph(vs_lattice_plan* lattice, vs_body_plan* body, void* f_a, void* f_b, int n_steps,
+                 void* force_hist, void* stream);
+
+/* Profiling entry point: launches only the grid kernel of vs_step (collide, force from the
+ * body's current window, push-stream), without the body and face kernels, so that the
+ * dominant kernel can be timed on its own. */
+int vs_step_grid_only(const vs_lattice_plan* lattice, const vs_body_plan* body, const void* f_in, void* f_out,
+                      void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VIVSIM_GB300_H */

@@ -1,0 +1,265 @@
+"""Fused time step (vs_step / vs_run / vs_run_graph) against the reference and the oracle.
+
+Golden trajectories come from the reference's own functions chained as its examples do
+(tests/golden/make_golden.py); larger cases compare with the oracle recipes.  Tolerance,
+norm-relative per field: float32 1e-6 after one step, 1e-5 after a few steps (the fused
+kernel contracts multiply-adds, the reference rounds each one); float64 1e-12.
+"""
+
+import math
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import golden, rel_err
+from oracle import ib as OIB
+from oracle import lbm2d as L2
+from oracle import lbm3d as L3
+from oracle import recipes
+
+pytestmark = pytest.mark.gpu
+
+
+def T(x):
+    return torch.from_numpy(np.ascontiguousarray(x)).cuda()
+
+
+def N(t):
+    return t.detach().cpu().numpy()
+
+
+def tol(mode, steps=1):
+    if mode == "f64":
+        return 1e-12
+    return 1e-6 if steps <= 1 else 1e-5
+
+
+@pytest.fixture(scope="module")
+def S():
+    import vivsim_gb300
+    vivsim_gb300.build()
+    from vivsim_gb300 import solver
+    return solver
+
+
+def test_cavity_golden(S, mode):
+    G = golden(mode)
+    dt = torch.float64 if mode == "f64" else torch.float32
+    om = L2.get_omega(0.0256)
+    bcs = [S.boundary("nee", "top", ux_wall=0.1), S.boundary("nee", "left"), S.boundary("nee", "right"),
+           S.boundary("nee", "bottom")]
+    step = S.LatticeStep(9, (16, 12), "bgk", om, dtype=dt, boundaries=bcs)
+    sim = S.Simulation(step, T(G["cav.f0"]))
+    done = 0
+    for target in (1, 10, 30):
+        sim.run(target - done)
+        done = target
+        err = rel_err(N(sim.f), G[f"cav.f{target}"])
+        assert err <= tol(mode, target), (target, err)
+
+
+def _viv_body(S, step, G, dt, mode):
+    D, U0, M = 8.0, 0.05, 24
+    area = math.pi * (D / 2) ** 2
+    mass = area * 10.0
+    fn = U0 / (5.0 * D)
+    K = (2 * math.pi * fn) ** 2 * mass * (1 + 1 / 10.0)
+    X = np.stack([G["viv.X0"], G["viv.Y0"]], axis=1)
+    return S.RigidBody(step, X, math.pi * D / M, kernel="peskin4", radius=2, n_iter=3, moving=True,
+                       free_dof=(False, True), mass=mass, stiffness=K, damping=0.0, added_mass_area=area)
+
+
+@pytest.mark.parametrize("coll", ["kbc", "mrt", "reg", "bgk"])
+def test_viv_golden(S, mode, coll):
+    G = golden(mode)
+    dt = torch.float64 if mode == "f64" else torch.float32
+    nx, ny, U0 = 40, 24, 0.05
+    om = L2.get_omega(U0 * 8.0 / 20.0)
+    u = np.zeros((2, nx, ny), G["viv.X0"].dtype)
+    u[0] = U0
+    u[1] = G["viv.pert"]
+    f0 = L2.get_equilibrium(np.ones((nx, ny), u.dtype), u)
+    step = S.LatticeStep(9, (nx, ny), coll, om, dtype=dt, forcing="edm",
+                         boundaries=[S.boundary("equilibrium", "left", ux_wall=U0),
+                                     S.boundary("nee", "right", mode="pressure", rho_wall=1.0)])
+    body = _viv_body(S, step, G, dt, mode)
+    sim = S.Simulation(step, T(f0), body)
+    h1 = sim.run(1, force_history=True)
+    st = body.state()
+    assert rel_err(N(h1)[0, :2], G[f"viv.{coll}.h1"]) <= (1e-4 if mode == "f32" else 1e-10)
+    assert rel_err(np.stack([st["a"][:2], st["v"][:2], st["d"][:2]]), G[f"viv.{coll}.body1"]) <= \
+        (1e-4 if mode == "f32" else 1e-10)
+    sim.run(5)
+    err = rel_err(N(sim.f), G[f"viv.{coll}.f6"])
+    assert err <= tol(mode, 6), err
+    st = body.state()
+    assert rel_err(st["h"][:2], G[f"viv.{coll}.h6"]) <= (1e-4 if mode == "f32" else 1e-9)
+
+
+@pytest.mark.parametrize("coll", ["reg", "bgk", "kbc"])
+def test_sphere_golden(S, mode, coll):
+    G = golden(mode)
+    dt = torch.float64 if mode == "f64" else torch.float32
+    X = G["sph.X"]
+    nx, ny, nz, D, U0, M = 16, 12, 12, 5.0, 0.05, 79
+    om = L3.get_omega(U0 * D / 30.0)
+    u = G["sph.pert"].copy()
+    u[0] = u[0] + U0
+    f0 = L3.get_equilibrium(np.ones((nx, ny, nz), X.dtype), u)
+    step = S.LatticeStep(19, (nx, ny, nz), coll, om, dtype=dt, forcing="edm",
+                         boundaries=[S.boundary("equilibrium", "left", ux_wall=U0),
+                                     S.boundary("nee", "right", mode="pressure", rho_wall=1.0)])
+    body = S.RigidBody(step, X, 4 * math.pi * (D / 2) ** 2 / M, kernel="peskin4", n_iter=3, moving=False)
+    sim = S.Simulation(step, T(f0), body)
+    h = sim.run(4, force_history=True)
+    assert rel_err(N(h)[0], G[f"sph.{coll}.h1"]) <= (1e-4 if mode == "f32" else 1e-9)
+    assert rel_err(N(h)[3], G[f"sph.{coll}.h4"]) <= (1e-4 if mode == "f32" else 1e-9)
+    err = rel_err(N(sim.f), G[f"sph.{coll}.f4"])
+    assert err <= tol(mode, 4), err
+
+
+def _forcing_case(S, forcing, dt):
+    nx, ny = 20, 14
+    gx = 1e-5
+    om = L2.get_omega(0.1)
+    g = np.zeros((2, nx, ny), np.float64 if dt == torch.float64 else np.float32)
+    g[0] = gx
+    rho = np.ones((nx, ny), g.dtype)
+    u = np.zeros((2, nx, ny), g.dtype)
+    f0 = L2.get_equilibrium(rho, u - g / 2)
+    bcs = [S.boundary("nebb", "top", mode="force_corrected", gx_wall=gx),
+           S.boundary("nebb", "bottom", mode="force_corrected", gx_wall=gx)]
+    coll = "mrt" if forcing == "guo_mrt" else "bgk"
+    step = S.LatticeStep(9, (nx, ny), coll, om, dtype=dt, forcing=forcing, g=(gx, 0.0), boundaries=bcs)
+    obcs = [("fcnebb", "top", dict(gx_wall=gx)), ("fcnebb", "bottom", dict(gx_wall=gx))]
+    return step, f0, g, om, obcs, coll
+
+
+@pytest.mark.parametrize("forcing", ["edm", "guo_bgk", "guo_mrt"])
+def test_body_force_recipes(S, forcing):
+    """examples/2d/poiseuille_channel.py:82-143 recipes (uniform force, force-corrected NEBB)."""
+    for dt in (torch.float32, torch.float64):
+        step, f0, g, om, obcs, coll = _forcing_case(S, forcing, dt)
+        sim = S.Simulation(step, T(f0))
+        f = f0.copy()
+        op = L2.get_mrt_collision_operator(om, f.dtype)
+        for k in range(8):
+            f = recipes.lbm_step_2d(f, coll, om, op, obcs, g=g, forcing=forcing)
+        sim.run(8)
+        assert rel_err(N(sim.f), f) <= (1e-5 if dt == torch.float32 else 1e-12)
+
+
+def test_bounce_back_and_velocity_walls(S):
+    """Fused bounce-back / specular faces and velocity-mode walls against the oracle."""
+    nx, ny = 18, 16
+    rng = np.random.default_rng(5)
+    rho = 1 + 0.01 * rng.standard_normal((nx, ny))
+    u = 0.02 * rng.standard_normal((2, nx, ny))
+    f0 = L2.get_equilibrium(rho, u)
+    om = 1.6
+    bcs = [S.boundary("bounce_back", "top", ux_wall=0.05), S.boundary("specular_reflection", "bottom"),
+           S.boundary("nebb", "left", mode="velocity", ux_wall=0.03),
+           S.boundary("nee", "right", mode="pressure", rho_wall=1.0)]
+    obcs = [("bb", "top", dict(ux_wall=0.05)), ("spec", "bottom", {}), ("vnebb", "left", dict(ux_wall=0.03)),
+            ("pnee", "right", dict(rho_wall=1.0))]
+    step = S.LatticeStep(9, (nx, ny), "kbc", om, dtype=torch.float64, boundaries=bcs)
+    sim = S.Simulation(step, T(f0))
+    f = f0.copy()
+    for _ in range(5):
+        f = recipes.lbm_step_2d(f, "kbc", om, None, obcs)
+    sim.run(5)
+    assert rel_err(N(sim.f), f) <= 1e-12
+
+
+def test_viv_oracle_larger(S):
+    """64 x 48 VIV case, KBC, 20 steps, float32, against the oracle recipe."""
+    nx, ny, D, U0, M = 64, 48, 12.0, 0.05, 38
+    om = L2.get_omega(U0 * D / 60.0)
+    th = np.linspace(0, 2 * np.pi, M, endpoint=False)
+    X0 = (20.0 + 0.5 * D * np.cos(th)).astype(np.float32)
+    Y0 = (24.0 + 0.5 * D * np.sin(th)).astype(np.float32)
+    rng = np.random.default_rng(0)
+    u = np.zeros((2, nx, ny), np.float32)
+    u[0] = U0
+    u[1] = 1e-4 * rng.standard_normal((nx, ny))
+    f0 = L2.get_equilibrium(np.ones((nx, ny), np.float32), u)
+    area = math.pi * (D / 2) ** 2
+    mass = 10 * area
+    K = (2 * math.pi * U0 / (5 * D)) ** 2 * mass * 1.1
+    ds = math.pi * D / M
+    bcs = [("eq", "left", dict(ux_wall=U0)), ("pnee", "right", dict(rho_wall=1.0))]
+    body_o = recipes.Body2D(X0, Y0, ds, mass, K, 0.0, area, free=(False, True), n_iter=3,
+                            v=np.array([0, 1e-3], np.float32))
+    step = S.LatticeStep(9, (nx, ny), "kbc", om, forcing="edm",
+                         boundaries=[S.boundary("equilibrium", "left", ux_wall=U0),
+                                     S.boundary("nee", "right", mode="pressure", rho_wall=1.0)])
+    body = S.RigidBody(step, np.stack([X0, Y0], 1), ds, moving=True, free_dof=(False, True), mass=mass,
+                       stiffness=K, added_mass_area=area, v0=(0, 1e-3, 0))
+    sim = S.Simulation(step, T(f0), body)
+    f = f0
+    for _ in range(20):
+        f, h = recipes.ib_lbm_step_2d(f, body_o, "kbc", om, None, bcs)
+    sim.run(20)
+    assert rel_err(N(sim.f), f) <= 1e-5
+    st = body.state()
+    assert rel_err(st["d"][:2], body_o.d) <= 1e-4
+    assert rel_err(st["h"][:2], h) <= 1e-4
+
+
+def test_graph_replay_matches_eager_and_is_deterministic(S):
+    nx, ny = 96, 64
+    rng = np.random.default_rng(3)
+    u = np.zeros((2, nx, ny), np.float32)
+    u[0] = 0.05
+    u[1] = 1e-3 * rng.standard_normal((nx, ny))
+    f0 = T(L2.get_equilibrium(np.ones((nx, ny), np.float32), u))
+    th = np.linspace(0, 2 * np.pi, 40, endpoint=False)
+    X = np.stack([30 + 6 * np.cos(th), 32 + 6 * np.sin(th)], 1)
+
+    def make():
+        step = S.LatticeStep(9, (nx, ny), "kbc", 1.8, forcing="edm",
+                             boundaries=[S.boundary("equilibrium", "left", ux_wall=0.05),
+                                         S.boundary("nee", "right", mode="pressure")])
+        body = S.RigidBody(step, X, 0.94, moving=True, free_dof=(False, True), mass=500.0, stiffness=0.05,
+                           added_mass_area=113.0)
+        return S.Simulation(step, f0, body), body
+
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        a, ba = make()
+        a.run(25)
+        b, bb = make()
+        b.run(25, graph=True)
+        c, bc = make()
+        c.run(25, graph=True)
+    torch.cuda.synchronize()
+    assert torch.equal(a.f, b.f)
+    assert torch.equal(b.f, c.f)
+    assert np.array_equal(ba.state()["d"], bb.state()["d"])
+
+
+def test_sphere_oracle_larger(S):
+    """32 x 24 x 24 D3Q19 regularised sphere, 3 steps, float32, against the oracle recipe."""
+    nx, ny, nz, D, U0 = 32, 24, 24, 8.0, 0.05
+    M = 201
+    X = recipes.fibonacci_sphere(M, D / 2, (12.3, 11.8, 12.1)).astype(np.float32)
+    om = L3.get_omega(U0 * D / 50.0)
+    rng = np.random.default_rng(1)
+    u = (1e-4 * rng.standard_normal((3, nx, ny, nz))).astype(np.float32)
+    u[0] += U0
+    f0 = L3.get_equilibrium(np.ones((nx, ny, nz), np.float32), u)
+    ds = 4 * math.pi * (D / 2) ** 2 / M
+    W, I = OIB.get_ib_stencil_3d(X, (nx, ny, nz))
+    bcs = [("eq", "left", dict(ux_wall=U0)), ("pnee", "right", dict(rho_wall=1.0))]
+    f = f0
+    for _ in range(3):
+        f, h = recipes.ib_lbm_step_3d(f, W, I, np.zeros((M, 3), np.float32), ds, "reg", om, None, bcs)
+    step = S.LatticeStep(19, (nx, ny, nz), "reg", om, forcing="edm",
+                         boundaries=[S.boundary("equilibrium", "left", ux_wall=U0),
+                                     S.boundary("nee", "right", mode="pressure", rho_wall=1.0)])
+    body = S.RigidBody(step, X, ds, moving=False)
+    sim = S.Simulation(step, T(f0), body)
+    hist = sim.run(3, force_history=True)
+    assert rel_err(N(sim.f), f) <= 1e-5
+    assert rel_err(N(hist)[2], h) <= 1e-4

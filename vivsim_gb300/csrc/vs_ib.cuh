@@ -1,0 +1,50 @@
+// Immersed-boundary device helpers shared by the per-op IB entry points and the fused
+// IB step: the 1-D discrete delta kernels of vivsim/ib/kernels.py and the stencil
+// geometry of vivsim/ib/stencil.py and vivsim/ib3d/stencil.py.
+#pragma once
+
+#include "vs_common.cuh"
+
+namespace vs {
+
+// Peskin 3-point, vivsim/ib/kernels.py:4-22
+template <typename T>
+__device__ __forceinline__ T delta_peskin3(T r) {
+  const T a = fabs(r);
+  if (a > T(1.5)) return T(0);
+  if (a < T(0.5)) return (T(1) + sqrt(T(1) - T(3) * (a * a))) / T(3);
+  return ((T(5) - T(3) * a) - sqrt((T(-2) + T(6) * a) - T(3) * (a * a))) / T(6);
+}
+// Peskin 4-point, vivsim/ib/kernels.py:25-43
+template <typename T>
+__device__ __forceinline__ T delta_peskin4(T r) {
+  const T a = fabs(r);
+  if (a > T(2)) return T(0);
+  if (a < T(1)) return ((T(3) - T(2) * a) + sqrt((T(1) + T(4) * a) - T(4) * (a * a))) * T(0.125);
+  return ((T(5) - T(2) * a) - sqrt((T(-7) + T(12) * a) - T(4) * (a * a))) * T(0.125);
+}
+// Cosine 4-point, vivsim/ib/kernels.py:46-61
+template <typename T>
+__device__ __forceinline__ T delta_cosine4(T r) {
+  const T a = fabs(r);
+  if (a > T(2)) return T(0);
+  return (T(1) + cos(((T)3.14159265358979323846 * a) * T(0.5))) * T(0.25);
+}
+template <typename T>
+__device__ __forceinline__ T delta(int kernel, T r) {
+  return kernel == VS_KERNEL_PESKIN3 ? delta_peskin3(r) : (kernel == VS_KERNEL_PESKIN4 ? delta_peskin4(r) : delta_cosine4(r));
+}
+
+// floor() to int32 as in jnp.floor(x).astype(jnp.int32)
+template <typename T>
+__device__ __forceinline__ int ifloor(T x) { return (int)floor(x); }
+
+}  // namespace vs
+
+namespace vs {
+// Multi-direct forcing over the pair CSR in `workspace`; with csr_ready the CSR built by
+// an earlier call for the same stencil indices is reused (defined in vs_ops_ib.cu).
+int ib_mdf_run(int dtype, bool csr_ready, const void* grid_u, int c, int64_t n_grid, const void* W, const int32_t* I,
+               int m, int s, const void* u_target, const void* ds, double ds_scalar, int n_iter, void* grid_force,
+               void* marker_force, void* workspace, size_t workspace_bytes, void* stream);
+}  // namespace vs

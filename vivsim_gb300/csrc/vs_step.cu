@@ -1,0 +1,1047 @@
+// Fused IB-LBM time step (D2Q9 / D3Q19).
+//
+// One step of the reference's composed update loop
+//   rho,u = get_macroscopic(f); feq = get_equilibrium(rho,u); f = collision(f,feq)
+//   IB: markers -> stencil -> multi_direct_forcing -> Newmark;  f += forcing(g, u)
+//   f = streaming(f); f = boundary_k(f) for each face boundary in order
+// (examples/2d/vortex_induced_vibration.py:96-148, examples/2d/lid_driven_cavity.py:55-63,
+//  examples/3d/flow_past_sphere.py:139-180) runs as
+//   [body kernel]  markers, stencil, CSR, MDF, Newmark -> force window g (device)
+//   [grid kernel]  per node: load f (1 read/population), moments, equilibrium, collision,
+//                  forcing from g, push-stream to the neighbours (1 write/population)
+//   [face kernels] the ordered boundary conditions on the streamed populations
+// The grid kernel carries all of the HBM traffic; the other two touch O(surface) nodes.
+#include <climits>
+#include <cmath>
+#include <new>
+#include <vector>
+
+#include "vs_boundary.cuh"
+#include "vs_dispatch.cuh"
+#include "vs_ib.cuh"
+
+namespace vs {
+
+// device window descriptor (int[8]): origin, extent, sticky status
+enum { META_OX = 0, META_OY, META_OZ, META_WX, META_WY, META_WZ, META_STATUS, META_N = 8 };
+
+// ------------------------------------------------------------------ grid kernel
+template <class L, typename T>
+struct StepParams {
+  const T* fin;
+  T* fout;
+  int nx, ny, nz, n;
+  CollideParams<T> cp;
+  int forcing;
+  int has_g0;
+  T g0[3];
+  T guo_scale;                   // 1 - omega / 2 (Guo-BGK)
+  const T* gw;                   // IB force window (D, wx, wy, wz) or null
+  const int* meta;               // window descriptor (device)
+  int n_pre;                     // faces whose pre-stream populations are kept (bounce-back)
+  int pre_loc[VS_MAX_BC];
+  T* pre_buf[VS_MAX_BC];
+  T op[L::Q * L::Q];             // MRT collision operator
+  T fop[L::Q * L::Q];            // MRT forcing operator
+};
+
+template <class L, typename T, int COLL>
+__global__ void __launch_bounds__(256) k_step(const __grid_constant__ StepParams<L, T> P) {
+  constexpr int Q = L::Q;
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= P.n) return;
+  const int nyz = P.ny * P.nz;
+  const int x = p / nyz;
+  const int r = p - x * nyz;
+  const int y = r / P.nz;
+  const int z = r - y * P.nz;
+
+  T f[Q];
+#pragma unroll
+  for (int i = 0; i < Q; ++i) f[i] = __ldg(P.fin + (size_t)i * P.n + p);
+
+  T rho, u[3] = {T(0), T(0), T(0)};
+  macro(L{}, f, rho, u);
+
+  T g[3] = {T(0), T(0), T(0)};
+  bool has_g = P.has_g0;
+  if (has_g) {
+#pragma unroll
+    for (int d = 0; d < L::D; ++d) g[d] = P.g0[d];
+  }
+  if (P.gw) {
+    const int wx = x - P.meta[META_OX], wy = y - P.meta[META_OY], wz = z - P.meta[META_OZ];
+    const int ex = P.meta[META_WX], ey = P.meta[META_WY], ez = P.meta[META_WZ];
+    if (wx >= 0 && wx < ex && wy >= 0 && wy < ey && wz >= 0 && wz < ez) {
+      const int cells = ex * ey * ez;
+      const int c = (wx * ey + wy) * ez + wz;
+#pragma unroll
+      for (int d = 0; d < L::D; ++d) g[d] = has_g ? g[d] + P.gw[d * cells + c] : P.gw[d * cells + c];
+      has_g = true;
+    }
+  }
+
+  // Guo forcing uses the half-force corrected velocity in the equilibrium
+  // (examples/2d/poiseuille_channel.py:103-105); EDM uses the plain one.
+  T ue[3] = {u[0], u[1], u[2]};
+  const bool guo = has_g && (P.forcing == VS_FORCE_GUO_BGK || P.forcing == VS_FORCE_GUO_MRT);
+  if (guo) {
+#pragma unroll
+    for (int d = 0; d < L::D; ++d) ue[d] = u[d] + (g[d] * T(0.5)) / rho;
+  }
+  T feq[Q];
+  equilibrium<L>(rho, ue, feq);
+  if constexpr (COLL == VS_COLLIDE_BGK) collide_bgk<L>(f, feq, P.cp);
+  else if constexpr (COLL == VS_COLLIDE_KBC) collide_kbc(L{}, f, feq, P.cp);
+  else if constexpr (COLL == VS_COLLIDE_REG) collide_reg(L{}, f, feq, P.cp);
+  else collide_mrt<L>(f, feq, P.op);
+
+  if (has_g && P.forcing != VS_FORCE_NONE) {
+    if (P.forcing == VS_FORCE_EDM) {
+#pragma unroll
+      for (int i = 0; i < Q; ++i) f[i] = f[i] + guo_i(L{}, i, g, u);
+    } else if (P.forcing == VS_FORCE_GUO_BGK) {
+#pragma unroll
+      for (int i = 0; i < Q; ++i) f[i] = f[i] + guo_i(L{}, i, g, ue) * P.guo_scale;
+    } else {
+      T gl[Q];
+#pragma unroll
+      for (int i = 0; i < Q; ++i) gl[i] = guo_i(L{}, i, g, ue);
+#pragma unroll
+      for (int i = 0; i < Q; ++i) {
+        T acc = P.fop[i * Q] * gl[0];
+#pragma unroll
+        for (int j = 1; j < Q; ++j) acc = acc + P.fop[i * Q + j] * gl[j];
+        f[i] = f[i] + acc;
+      }
+    }
+  }
+
+  // keep the pre-stream populations of bounce-back faces (lbm/boundary/bb.py needs them)
+  for (int k = 0; k < P.n_pre; ++k) {
+    const int loc = P.pre_loc[k];
+    const int a = loc_axis(loc);
+    const int coord = a == 0 ? x : (a == 1 ? y : z);
+    const int nn[3] = {P.nx, P.ny, P.nz};
+    if (coord != (loc_sign(loc) > 0 ? 0 : nn[a] - 1)) continue;
+    const int b0 = a == 0 ? 1 : 0, b1 = a == 2 ? 1 : 2;
+    const int cc[3] = {x, y, z};
+    const int64_t nf = face_size(loc, nn);
+    const int64_t j = (int64_t)cc[b0] * nn[b1] + cc[b1];
+#pragma unroll
+    for (int i = 0; i < Q; ++i) P.pre_buf[k][i * nf + j] = f[i];
+  }
+
+  // push streaming with periodic wrap on every axis (lbm/basic.py:60-85)
+  const int xp = x + 1 == P.nx ? 0 : x + 1, xm = x == 0 ? P.nx - 1 : x - 1;
+  const int yp = y + 1 == P.ny ? 0 : y + 1, ym = y == 0 ? P.ny - 1 : y - 1;
+  const int zp = z + 1 == P.nz ? 0 : z + 1, zm = z == 0 ? P.nz - 1 : z - 1;
+#pragma unroll
+  for (int i = 0; i < Q; ++i) {
+    const int cx = L::c(i, 0), cy = L::c(i, 1), cz = L::c(i, 2);
+    const int xd = cx > 0 ? xp : (cx < 0 ? xm : x);
+    const int yd = cy > 0 ? yp : (cy < 0 ? ym : y);
+    const int zd = cz > 0 ? zp : (cz < 0 ? zm : z);
+    P.fout[(size_t)i * P.n + (xd * P.ny + yd) * P.nz + zd] = f[i];
+  }
+}
+
+// ------------------------------------------------------------------ face kernels
+template <typename T>
+struct BcGroup {
+  int count;
+  int64_t nf[2];
+  WallArgs<T> A[2];
+};
+
+template <class L, typename T>
+__global__ void k_bc(const __grid_constant__ BcGroup<T> G, T* f) {
+  const int g = blockIdx.y;
+  if (g >= G.count) return;
+  const WallArgs<T>& A = G.A[g];
+  const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (j >= G.nf[g]) return;
+  const int64_t n = (int64_t)A.n[0] * A.n[1] * A.n[2];
+  const int64_t pw = face_node(A.loc, A.n, j, 0);
+  T w[L::Q], nb[L::Q], pre[L::Q], out[L::Q];
+#pragma unroll
+  for (int i = 0; i < L::Q; ++i) w[i] = f[i * n + pw];
+  if (bc_needs_neighbor<L>(A.kind, A.mode)) {
+    const int64_t pn = face_node(A.loc, A.n, j, 1);
+#pragma unroll
+    for (int i = 0; i < L::Q; ++i) nb[i] = f[i * n + pn];
+  }
+  if (A.kind == VS_BC_BB || A.kind == VS_BC_SPECULAR) {
+#pragma unroll
+    for (int i = 0; i < L::Q; ++i) pre[i] = A.f_pre[i * A.pre_stride + j];
+  }
+  bc_node<L, T>(A, j, w, nb, pre, out);
+#pragma unroll
+  for (int i = 0; i < L::Q; ++i) f[i * n + pw] = out[i];
+}
+
+// ------------------------------------------------------------------ body kernel (2-D)
+template <typename T>
+struct BodyParams {
+  const T* fin;
+  int nx, ny;
+  const T* X0;
+  const T* Y0;
+  const T* ds_arr;
+  T ds2_scalar;  // 2 * ds as the reference forms it: (T)ds * 2
+  int M, radius, kernel, n_iter;
+  int cap_x, cap_y;
+  T* state;  // a[3], v[3], d[3], h[3]
+  T* gw;
+  int* meta;
+  T* force_hist;
+  int free_dof[3];
+  T k1, k2, c1, c2, dt, damp, stiff, den, area;
+};
+
+// Exclusive block scan of cnt[0..B) into start[0..B], start[B] = total.
+__device__ void block_exclusive_scan(const int* cnt, int* start, int B, int* warp_sums) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int chunk = (B + nt - 1) / nt;
+  const int lo = min(B, tid * chunk), hi = min(B, lo + chunk);
+  int local = 0;
+  for (int k = lo; k < hi; ++k) local += cnt[k];
+  // warp inclusive scan
+  const int lane = tid & 31, wid = tid >> 5;
+  int v = local;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(0xffffffffu, v, o);
+    if (lane >= o) v += t;
+  }
+  if (lane == 31) warp_sums[wid] = v;
+  __syncthreads();
+  if (wid == 0) {
+    const int nw = (nt + 31) >> 5;
+    int s = lane < nw ? warp_sums[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, s, o);
+      if (lane >= o) s += t;
+    }
+    if (lane < nw) warp_sums[lane] = s;
+  }
+  __syncthreads();
+  int run = v - local + (wid > 0 ? warp_sums[wid - 1] : 0);
+  for (int k = lo; k < hi; ++k) {
+    start[k] = run;
+    run += cnt[k];
+  }
+  if (tid == nt - 1) start[B] = run;
+  __syncthreads();
+}
+
+// One CTA advances one 2-D rigid body by one step: marker positions from the body
+// displacement, stencil weights, a counting-sort CSR of (node, pair) in shared memory,
+// interpolation of u from f at the touched nodes, the multi-direct-forcing iterations,
+// the force window for the grid kernel, the total force and the Newmark update.
+// The CSR keeps every node's contributions in increasing (marker, stencil point) order,
+// so all sums follow the reference's order and no floating-point atomics are used.
+template <typename T>
+__global__ void __launch_bounds__(1024) k_body2d(const BodyParams<T> B) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int M = B.M, w = 2 * B.radius, S = w * w, P = M * S;
+  const int Bcap = B.cap_x * B.cap_y;
+  T* X = (T*)smem;
+  T* Y = X + M;
+  T* W = Y + M;
+  T* U = W + P;
+  T* Fs = U + 2 * M;
+  T* Ft = Fs + 2 * M;
+  T* nu = Ft + 2 * M;      // node u / node force: [2][Bcap]
+  T* nv = nu + 2 * Bcap;   // spread accumulators:  [2][Bcap]
+  int* key = (int*)(nv + 2 * Bcap);
+  int* sorted = key + P;
+  int* cnt = sorted + P;
+  int* start = cnt + Bcap;
+  int* misc = start + Bcap + 1;  // [0..3] bbox, [4..35] warp sums
+
+  T a[3], v[3], d[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    a[c] = B.state[c];
+    v[c] = B.state[3 + c];
+    d[c] = B.state[6 + c];
+  }
+  if (tid == 0) {
+    misc[0] = INT_MAX; misc[1] = INT_MIN; misc[2] = INT_MAX; misc[3] = INT_MIN;
+  }
+  // markers follow the body (dyn.py:68-81)
+  for (int m = tid; m < M; m += nt) {
+    X[m] = B.X0[m] + d[0];
+    Y[m] = B.Y0[m] + d[1];
+  }
+  __syncthreads();
+  for (int m = tid; m < M; m += nt) {
+    const int fx = ifloor(X[m]), fy = ifloor(Y[m]);
+    atomicMin(&misc[0], fx); atomicMax(&misc[1], fx);
+    atomicMin(&misc[2], fy); atomicMax(&misc[3], fy);
+  }
+  __syncthreads();
+  const int bx0 = misc[0] - B.radius + 1, by0 = misc[2] - B.radius + 1;
+  const int BW = misc[1] - misc[0] + w, BH = misc[3] - misc[2] + w;
+  const bool bad = BW > B.cap_x || BH > B.cap_y || bx0 < 0 || by0 < 0 || bx0 + BW > B.nx || by0 + BH > B.ny;
+  if (bad) {
+    if (tid == 0) {
+      B.meta[META_STATUS] = VS_ERR_RANGE;
+      B.meta[META_WX] = 0; B.meta[META_WY] = 0; B.meta[META_WZ] = 0;
+    }
+    return;
+  }
+  const int NB = BW * BH;
+  for (int k = tid; k < NB; k += nt) cnt[k] = 0;
+  __syncthreads();
+  // stencil (ib/stencil.py:7-51) with bounding-box-local node keys
+  for (int p = tid; p < P; p += nt) {
+    const int m = p / S, k = p - m * S;
+    const int ox = k / w - B.radius + 1, oy = k % w - B.radius + 1;
+    const int sx = ifloor(X[m]) + ox, sy = ifloor(Y[m]) + oy;
+    W[p] = delta(B.kernel, (T)sx - X[m]) * delta(B.kernel, (T)sy - Y[m]);
+    const int kk = (sx - bx0) * BH + (sy - by0);
+    key[p] = kk;
+    atomicAdd(&cnt[kk], 1);
+  }
+  __syncthreads();
+  block_exclusive_scan(cnt, start, NB, misc + 4);
+  for (int k = tid; k < NB; k += nt) cnt[k] = 0;
+  __syncthreads();
+  for (int p = tid; p < P; p += nt) {
+    const int kk = key[p];
+    sorted[start[kk] + atomicAdd(&cnt[kk], 1)] = p;
+  }
+  __syncthreads();
+  // order each node's pairs by pair id (= the reference's scatter order) and read u there
+  for (int k = tid; k < NB; k += nt) {
+    const int lo = start[k], hi = start[k + 1];
+    for (int i = lo + 1; i < hi; ++i) {
+      const int val = sorted[i];
+      int j = i - 1;
+      while (j >= lo && sorted[j] > val) {
+        sorted[j + 1] = sorted[j];
+        --j;
+      }
+      sorted[j + 1] = val;
+    }
+    if (hi > lo) {
+      const int gx = bx0 + k / BH, gy = by0 + k % BH;
+      const int64_t n = (int64_t)B.nx * B.ny;
+      const int64_t pn = (int64_t)gx * B.ny + gy;
+      T fl[9];
+#pragma unroll
+      for (int i = 0; i < 9; ++i) fl[i] = B.fin[i * n + pn];
+      T r, uu[3];
+      macro(L9{}, fl, r, uu);
+      nu[k] = uu[0];
+      nu[Bcap + k] = uu[1];
+    }
+  }
+  __syncthreads();
+  // U = interpolate(u) and the first force step (ib/mdf.py:38-48); target = body velocity
+  for (int q = tid; q < 2 * M; q += nt) {
+    const int m = q >> 1, c = q & 1;
+    T acc = T(0);
+    for (int s = 0; s < S; ++s) {
+      const T t = W[m * S + s] * nu[c * Bcap + key[m * S + s]];
+      acc = s == 0 ? t : acc + t;
+    }
+    U[q] = acc;
+    const T d2 = B.ds_arr ? B.ds_arr[m] * T(2) : B.ds2_scalar;
+    const T fs = (v[c] - acc) * d2;
+    Fs[q] = fs;
+    Ft[q] = B.n_iter > 0 ? fs : T(0);
+  }
+  __syncthreads();
+  for (int it = 0; it < B.n_iter; ++it) {
+    // 0.5 * spread(F_step) at the touched nodes (ib/mdf.py:50-51)
+    for (int k = tid; k < NB; k += nt) {
+      const int lo = start[k], hi = start[k + 1];
+      if (hi == lo) continue;
+#pragma unroll
+      for (int c = 0; c < 2; ++c) {
+        T acc = T(0);
+        for (int i = lo; i < hi; ++i) {
+          const int p = sorted[i];
+          const T t = Fs[(p / S) * 2 + c] * W[p];
+          acc = i == lo ? t : acc + t;
+        }
+        nv[c * Bcap + k] = acc * T(0.5);
+      }
+    }
+    __syncthreads();
+    const bool last = it == B.n_iter - 1;
+    for (int q = tid; q < 2 * M; q += nt) {
+      const int m = q >> 1, c = q & 1;
+      T acc = T(0);
+      for (int s = 0; s < S; ++s) {
+        const T t = W[m * S + s] * nv[c * Bcap + key[m * S + s]];
+        acc = s == 0 ? t : acc + t;
+      }
+      const T uq = U[q] + acc;
+      U[q] = uq;
+      if (!last) {
+        const T d2 = B.ds_arr ? B.ds_arr[m] * T(2) : B.ds2_scalar;
+        const T fs = (v[c] - uq) * d2;
+        Fs[q] = fs;
+        Ft[q] = Ft[q] + fs;
+      }
+    }
+    __syncthreads();
+  }
+  // g = spread(F_total) over the window (ib/mdf.py:60-62); zero where no marker reaches
+  for (int k = tid; k < NB; k += nt) {
+    const int lo = start[k], hi = start[k + 1];
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      T acc = T(0);
+      for (int i = lo; i < hi; ++i) {
+        const int p = sorted[i];
+        const T t = Ft[(p / S) * 2 + c] * W[p];
+        acc = i == lo ? t : acc + t;
+      }
+      B.gw[c * NB + k] = acc;
+    }
+  }
+  if (tid == 0) {
+    B.meta[META_OX] = bx0; B.meta[META_OY] = by0; B.meta[META_OZ] = 0;
+    B.meta[META_WX] = BW; B.meta[META_WY] = BH; B.meta[META_WZ] = 1;
+  }
+  // total force on the body h = sum(-F_total) (dyn.py:126-136), added mass, Newmark (dyn.py:5-51)
+  if (tid < 2) {
+    const int c = tid;
+    T h = -Ft[c];
+    for (int m = 1; m < M; ++m) h = h + (-Ft[m * 2 + c]);
+    h = h + a[c] * B.area;
+    T an = a[c], vn = v[c], dn = d[c];
+    if (B.free_dof[c]) {
+      const T v1 = v[c] + B.k1 * a[c];
+      const T v2 = (d[c] + B.dt * v[c]) + B.k2 * a[c];
+      an = ((h - B.damp * v1) - B.stiff * v2) / B.den;
+      vn = B.c1 * an + v1;
+      dn = B.c2 * an + v2;
+    }
+    B.state[c] = an;
+    B.state[3 + c] = vn;
+    B.state[6 + c] = dn;
+    B.state[9 + c] = h;
+    if (B.force_hist) B.force_hist[c] = h;
+  }
+  if (tid == 2) {
+    B.state[9 + 2] = T(0);
+    if (B.force_hist) B.force_hist[2] = T(0);
+  }
+}
+
+// u over a fixed window (3-D fixed body): u_win[d][cell] from f
+template <class L, typename T>
+__global__ void k_window_u(const T* __restrict__ fin, int nx, int ny, int nz, const int* __restrict__ meta,
+                           T* __restrict__ uw) {
+  const int ex = meta[META_WX], ey = meta[META_WY], ez = meta[META_WZ];
+  const int cells = ex * ey * ez;
+  const int64_t n = (int64_t)nx * ny * nz;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < cells; c += gridDim.x * blockDim.x) {
+    const int wx = c / (ey * ez), wy = (c / ez) % ey, wz = c % ez;
+    const int64_t pn = ((int64_t)(meta[META_OX] + wx) * ny + (meta[META_OY] + wy)) * nz + (meta[META_OZ] + wz);
+    T fl[L::Q];
+#pragma unroll
+    for (int i = 0; i < L::Q; ++i) fl[i] = fin[i * n + pn];
+    T r, uu[3] = {T(0), T(0), T(0)};
+    macro(L{}, fl, r, uu);
+#pragma unroll
+    for (int d = 0; d < L::D; ++d) uw[d * cells + c] = uu[d];
+  }
+}
+
+// total force of a fixed body: h = sum_m marker_force[m] in marker order
+template <typename T>
+__global__ void k_body_force(const T* __restrict__ mf, int M, int C, T* state, T* force_hist) {
+  const int c = threadIdx.x;
+  if (c >= 3) return;
+  T h = T(0);
+  if (c < C) {
+    h = mf[c];
+    for (int m = 1; m < M; ++m) h = h + mf[m * C + c];
+  }
+  state[9 + c] = h;
+  if (force_hist) force_hist[c] = h;
+}
+
+template <typename T>
+__global__ void k_fill(T* p, T v, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = v;
+}
+
+}  // namespace vs
+
+using namespace vs;
+
+// ====================================================================== plans
+struct vs_lattice_plan {
+  vs_lattice_cfg cfg;
+  int dim;
+  int64_t n;
+  void* pre_buf[VS_MAX_BC];  // bounce-back face buffers
+  int bc_group[VS_MAX_BC];   // group id of each boundary op
+  int n_groups;
+  // graph cache
+  cudaGraphExec_t graph;
+  const void* g_fa;
+  const void* g_fb;
+  const void* g_hist;
+  const void* g_body;
+  int g_steps;
+  cudaStream_t g_stream;
+};
+
+struct vs_body_plan {
+  vs_body_cfg cfg;
+  int dim, M, S, C;
+  int cap[3];
+  void* d_X0;     // (M) x, (M) y [, (M) z]  or (M,3) coords for 3-D
+  void* d_ds;     // (M) or null
+  void* d_state;  // 12 values
+  void* d_gw;     // window force (C, cells)
+  int* d_meta;
+  // 3-D fixed body
+  void* d_W;
+  int32_t* d_I;
+  void* d_uw;
+  void* d_target;
+  void* d_mf;
+  void* d_ws;
+  size_t ws_bytes;
+  int csr_ready;
+  size_t smem;
+  double nm[9];  // k1, k2, c1, c2, dt, damping, stiffness, den, area
+};
+
+static size_t dsize(int dtype) { return dtype == VS_F64 ? 8 : 4; }
+
+static void free_lattice(vs_lattice_plan* p) {
+  if (!p) return;
+  for (int k = 0; k < VS_MAX_BC; ++k)
+    if (p->pre_buf[k]) cudaFree(p->pre_buf[k]);
+  if (p->graph) cudaGraphExecDestroy(p->graph);
+  delete p;
+}
+
+static void free_body(vs_body_plan* b) {
+  if (!b) return;
+  void* ptrs[] = {b->d_X0, b->d_ds, b->d_state, b->d_gw, b->d_meta, b->d_W, b->d_I, b->d_uw, b->d_target, b->d_mf,
+                  b->d_ws};
+  for (void* q : ptrs)
+    if (q) cudaFree(q);
+  delete b;
+}
+
+template <typename T>
+static WallArgs<T> wall_args_from_bc(const vs_bc& bc, const vs_lattice_plan* L, int k) {
+  WallArgs<T> A{};
+  A.kind = bc.kind;
+  A.mode = bc.mode;
+  A.loc = bc.loc;
+  A.n[0] = L->cfg.nx;
+  A.n[1] = L->cfg.ny;
+  A.n[2] = L->cfg.nz;
+  double rho = bc.rho, u3[3] = {bc.ux, bc.uy, bc.uz};
+  if (bc.mode == VS_WALL_FORCE_CORRECTED) {
+    const double g3[3] = {bc.gx, bc.gy, bc.gz};
+    for (int d = 0; d < 3; ++d) u3[d] = u3[d] - (g3[d] * 0.5) / rho;
+  }
+  A.un_scalar = bc.mode != VS_WALL_PRESSURE;
+  A.all_scalar = bc.mode == VS_WALL_GIVEN || bc.mode == VS_WALL_FORCE_CORRECTED;
+  wall_args_scalars(A, rho, u3, L->dim);
+  A.f_pre = (const T*)L->pre_buf[k];
+  A.pre_stride = face_size(bc.loc, A.n);
+  A.pre_face = 1;
+  return A;
+}
+
+static int enqueue_bcs(const vs_lattice_plan* L, void* f, cudaStream_t st) {
+  const vs_lattice_cfg& c = L->cfg;
+  return dispatch(c.q, c.dtype, [&](auto l, auto t) -> int {
+    using LL = decltype(l);
+    using T = typename decltype(t)::type;
+    int k = 0;
+    while (k < c.n_bc) {
+      BcGroup<T> G{};
+      const int gid = L->bc_group[k];
+      int64_t nfmax = 0;
+      while (k < c.n_bc && L->bc_group[k] == gid && G.count < 2) {
+        G.A[G.count] = wall_args_from_bc<T>(c.bc[k], L, k);
+        G.nf[G.count] = face_size(c.bc[k].loc, G.A[G.count].n);
+        nfmax = G.nf[G.count] > nfmax ? G.nf[G.count] : nfmax;
+        ++G.count;
+        ++k;
+      }
+      dim3 grid(grid_for(nfmax, 128), G.count);
+      k_bc<LL, T><<<grid, 128, 0, st>>>(G, (T*)f);
+      VS_CHECK_LAUNCH("vs_step face kernel");
+    }
+    return VS_OK;
+  });
+}
+
+template <class L, typename T>
+static StepParams<L, T> make_step_params(const vs_lattice_plan* LP, const vs_body_plan* B, const void* fin,
+                                         void* fout) {
+  const vs_lattice_cfg& c = LP->cfg;
+  StepParams<L, T> P{};
+  P.fin = (const T*)fin;
+  P.fout = (T*)fout;
+  P.nx = c.nx;
+  P.ny = c.ny;
+  P.nz = c.nz;
+  P.n = (int)LP->n;
+  P.cp.omega = (T)c.omega;
+  P.cp.one_m_omega = (T)(1.0 - c.omega);
+  P.cp.inv_omega = (T)(1.0 / c.omega);
+  P.cp.one_m_inv = (T)(1.0 - 1.0 / c.omega);
+  P.cp.mrt = nullptr;
+  P.forcing = c.forcing;
+  P.has_g0 = (c.g_uniform[0] != 0.0 || c.g_uniform[1] != 0.0 || c.g_uniform[2] != 0.0) && c.forcing != VS_FORCE_NONE;
+  for (int d = 0; d < 3; ++d) P.g0[d] = (T)c.g_uniform[d];
+  P.guo_scale = (T)(1.0 - 0.5 * c.omega);
+  P.gw = B ? (const T*)B->d_gw : nullptr;
+  P.meta = B ? B->d_meta : nullptr;
+  P.n_pre = 0;
+  for (int k = 0; k < c.n_bc; ++k) {
+    if (c.bc[k].kind == VS_BC_BB || c.bc[k].kind == VS_BC_SPECULAR) {
+      P.pre_loc[P.n_pre] = c.bc[k].loc;
+      P.pre_buf[P.n_pre] = (T*)LP->pre_buf[k];
+      ++P.n_pre;
+    }
+  }
+  for (int i = 0; i < L::Q * L::Q; ++i) {
+    P.op[i] = (T)c.mrt_op[i];
+    P.fop[i] = (T)c.mrt_fop[i];
+  }
+  return P;
+}
+
+static int enqueue_body(vs_body_plan* B, const vs_lattice_plan* LP, const void* fin, void* force_hist,
+                        cudaStream_t st) {
+  const int dtype = B->cfg.dtype;
+  if (B->dim == 2) {
+    return dispatch_t(dtype, [&](auto t) -> int {
+      using T = typename decltype(t)::type;
+      BodyParams<T> P{};
+      P.fin = (const T*)fin;
+      P.nx = LP->cfg.nx;
+      P.ny = LP->cfg.ny;
+      P.X0 = (const T*)B->d_X0;
+      P.Y0 = (const T*)B->d_X0 + B->M;
+      P.ds_arr = (const T*)B->d_ds;
+      P.ds2_scalar = (T)B->cfg.ds_scalar * T(2);
+      P.M = B->M;
+      P.radius = B->cfg.radius;
+      P.kernel = B->cfg.kernel;
+      P.n_iter = B->cfg.n_iter;
+      P.cap_x = B->cap[0];
+      P.cap_y = B->cap[1];
+      P.state = (T*)B->d_state;
+      P.gw = (T*)B->d_gw;
+      P.meta = B->d_meta;
+      P.force_hist = (T*)force_hist;
+      for (int c = 0; c < 3; ++c) P.free_dof[c] = B->cfg.free_dof[c];
+      P.k1 = (T)B->nm[0]; P.k2 = (T)B->nm[1]; P.c1 = (T)B->nm[2]; P.c2 = (T)B->nm[3]; P.dt = (T)B->nm[4];
+      P.damp = (T)B->nm[5]; P.stiff = (T)B->nm[6]; P.den = (T)B->nm[7]; P.area = (T)B->nm[8];
+      k_body2d<T><<<1, 1024, B->smem, st>>>(P);
+      VS_CHECK_LAUNCH("vs_step body kernel");
+      return VS_OK;
+    });
+  }
+  // 3-D fixed body: static stencil over a fixed window, CSR built once
+  return dispatch(LP->cfg.q, dtype, [&](auto l, auto t) -> int {
+    using L = decltype(l);
+    using T = typename decltype(t)::type;
+    const int cells = B->cap[0] * B->cap[1] * B->cap[2];
+    k_window_u<L, T><<<grid_for(cells, 256), 256, 0, st>>>((const T*)fin, LP->cfg.nx, LP->cfg.ny, LP->cfg.nz,
+                                                           B->d_meta, (T*)B->d_uw);
+    VS_CHECK_LAUNCH("vs_step window u");
+    int rc = ib_mdf_run(dtype, B->csr_ready != 0, B->d_uw, 3, cells, B->d_W, B->d_I, B->M, B->S, B->d_target,
+                        B->d_ds, B->cfg.ds_scalar, B->cfg.n_iter, B->d_gw, B->d_mf, B->d_ws, B->ws_bytes, st);
+    if (rc) return rc;
+    B->csr_ready = 1;
+    k_body_force<T><<<1, 32, 0, st>>>((const T*)B->d_mf, B->M, 3, (T*)B->d_state, (T*)force_hist);
+    VS_CHECK_LAUNCH("vs_step body force");
+    return VS_OK;
+  });
+}
+
+static int enqueue_grid(const vs_lattice_plan* LP, const vs_body_plan* B, const void* fin, void* fout,
+                        cudaStream_t st) {
+  const vs_lattice_cfg& c = LP->cfg;
+  int rc = dispatch(c.q, c.dtype, [&](auto l, auto t) -> int {
+    using L = decltype(l);
+    using T = typename decltype(t)::type;
+    const StepParams<L, T> P = make_step_params<L, T>(LP, B, fin, fout);
+    const unsigned grid = grid_for(LP->n, 256);
+    switch (c.collision) {
+      case VS_COLLIDE_BGK: k_step<L, T, VS_COLLIDE_BGK><<<grid, 256, 0, st>>>(P); break;
+      case VS_COLLIDE_KBC: k_step<L, T, VS_COLLIDE_KBC><<<grid, 256, 0, st>>>(P); break;
+      case VS_COLLIDE_REG: k_step<L, T, VS_COLLIDE_REG><<<grid, 256, 0, st>>>(P); break;
+      default: k_step<L, T, VS_COLLIDE_MRT><<<grid, 256, 0, st>>>(P); break;
+    }
+    VS_CHECK_LAUNCH("vs_step grid kernel");
+    return VS_OK;
+  });
+  return rc;
+}
+
+static int enqueue_step(const vs_lattice_plan* LP, vs_body_plan* B, const void* fin, void* fout, void* force_hist,
+                        cudaStream_t st) {
+  if (B) {
+    int rc = enqueue_body(B, LP, fin, force_hist, st);
+    if (rc) return rc;
+  }
+  int rc = enqueue_grid(LP, B, fin, fout, st);
+  if (rc) return rc;
+  return enqueue_bcs(LP, fout, st);
+}
+
+extern "C" {
+
+int vs_lattice_plan_create(const vs_lattice_cfg* cfg, vs_lattice_plan** out) {
+  VS_REQUIRE(cfg && out, "vs_lattice_plan_create: null argument");
+  VS_REQUIRE(cfg->q == 9 || cfg->q == 19, "q must be 9 or 19");
+  VS_REQUIRE(cfg->dtype == VS_F32 || cfg->dtype == VS_F64, "bad dtype");
+  const int nz = cfg->q == 9 ? 1 : cfg->nz;
+  VS_REQUIRE(cfg->nx >= 4 && cfg->ny >= 4 && (cfg->q == 9 ? cfg->nz == 1 : cfg->nz >= 4),
+             "grid %d x %d x %d too small (>= 4 per axis; nz = 1 for D2Q9)", cfg->nx, cfg->ny, cfg->nz);
+  const int64_t n = (int64_t)cfg->nx * cfg->ny * nz;
+  VS_REQUIRE(n < (1ll << 31), "grid of %lld nodes too large for 32-bit node indices", (long long)n);
+  VS_REQUIRE(cfg->collision >= VS_COLLIDE_BGK && cfg->collision <= VS_COLLIDE_REG, "bad collision %d",
+             cfg->collision);
+  VS_REQUIRE(cfg->forcing >= VS_FORCE_NONE && cfg->forcing <= VS_FORCE_GUO_MRT, "bad forcing %d", cfg->forcing);
+  VS_REQUIRE(cfg->n_bc >= 0 && cfg->n_bc <= VS_MAX_BC, "n_bc must be 0..%d", VS_MAX_BC);
+  const int dim = cfg->q == 9 ? 2 : 3;
+  for (int k = 0; k < cfg->n_bc; ++k) {
+    const vs_bc& b = cfg->bc[k];
+    VS_REQUIRE(b.loc >= 0 && b.loc < 2 * dim, "boundary %d: loc %d invalid", k, b.loc);
+    VS_REQUIRE(b.kind >= VS_BC_NEE && b.kind <= VS_BC_SPECULAR, "boundary %d: bad kind", k);
+    VS_REQUIRE(b.mode >= VS_WALL_GIVEN && b.mode <= VS_WALL_FORCE_CORRECTED, "boundary %d: bad mode", k);
+    VS_REQUIRE(!((b.kind == VS_BC_BB || b.kind == VS_BC_SPECULAR) && b.mode != VS_WALL_GIVEN),
+               "boundary %d: bounce-back takes no wall mode", k);
+  }
+  vs_lattice_plan* p = new (std::nothrow) vs_lattice_plan();
+  if (!p) {
+    set_error("out of host memory");
+    return VS_ERR_INVALID_ARG;
+  }
+  p->cfg = *cfg;
+  p->cfg.nz = nz;
+  p->dim = dim;
+  p->n = n;
+  const int nn[3] = {cfg->nx, cfg->ny, nz};
+  for (int k = 0; k < cfg->n_bc; ++k) {
+    const vs_bc& b = cfg->bc[k];
+    if (b.kind == VS_BC_BB || b.kind == VS_BC_SPECULAR) {
+      cudaError_t e = cudaMalloc(&p->pre_buf[k], dsize(cfg->dtype) * cfg->q * face_size(b.loc, nn));
+      if (e != cudaSuccess) {
+        free_lattice(p);
+        return cuda_status(e, "vs_lattice_plan_create");
+      }
+    }
+  }
+  // Consecutive boundaries on the two opposite faces of one axis touch disjoint nodes
+  // (wall + neighbour planes at 0,1 and N-1,N-2 with N >= 4): launch them together.
+  int gid = 0, gsize = 0;
+  for (int k = 0; k < cfg->n_bc; ++k) {
+    if (k > 0) {
+      const vs_bc& a = cfg->bc[k - 1];
+      const vs_bc& b = cfg->bc[k];
+      const bool pair = gsize == 1 && loc_axis(a.loc) == loc_axis(b.loc) && a.loc != b.loc &&
+                        nn[loc_axis(a.loc)] >= 4;
+      if (!pair) {
+        ++gid;
+        gsize = 0;
+      }
+    }
+    p->bc_group[k] = gid;
+    ++gsize;
+  }
+  p->n_groups = cfg->n_bc ? gid + 1 : 0;
+  *out = p;
+  return VS_OK;
+}
+
+int vs_lattice_plan_destroy(vs_lattice_plan* plan) {
+  free_lattice(plan);
+  return VS_OK;
+}
+
+int vs_body_plan_create(const vs_body_cfg* cfg, const vs_lattice_plan* lattice, vs_body_plan** out) {
+  VS_REQUIRE(cfg && lattice && out, "vs_body_plan_create: null argument");
+  VS_REQUIRE(cfg->dim == lattice->dim, "body dim %d does not match the lattice", cfg->dim);
+  VS_REQUIRE(cfg->dtype == lattice->cfg.dtype, "body dtype does not match the lattice");
+  VS_REQUIRE(cfg->n_markers > 0 && cfg->x0_host && cfg->y0_host && (cfg->dim == 2 || cfg->z0_host),
+             "vs_body_plan_create: marker coordinates required");
+  VS_REQUIRE(cfg->radius >= 1 && cfg->radius <= 3, "stencil radius must be 1..3");
+  VS_REQUIRE(cfg->kernel >= VS_KERNEL_PESKIN3 && cfg->kernel <= VS_KERNEL_COSINE4, "bad kernel");
+  VS_REQUIRE(cfg->n_iter >= 0 && cfg->n_iter <= 64, "n_iter must be 0..64");
+  VS_REQUIRE(lattice->cfg.forcing == VS_FORCE_EDM || lattice->cfg.forcing == VS_FORCE_GUO_BGK ||
+                 lattice->cfg.forcing == VS_FORCE_GUO_MRT,
+             "an immersed body needs a forcing scheme on the lattice (EDM or Guo)");
+  VS_REQUIRE(cfg->dim == 2 || !cfg->moving, "moving 3-D bodies are not supported by this build");
+  vs_body_plan* b = new (std::nothrow) vs_body_plan();
+  if (!b) {
+    set_error("out of host memory");
+    return VS_ERR_INVALID_ARG;
+  }
+  b->cfg = *cfg;
+  b->cfg.x0_host = b->cfg.y0_host = b->cfg.z0_host = b->cfg.ds_host = nullptr;
+  b->dim = cfg->dim;
+  b->M = cfg->n_markers;
+  const int w = 2 * cfg->radius;
+  b->S = cfg->dim == 2 ? w * w : w * w * w;
+  b->C = cfg->dim;
+  const size_t ts = dsize(cfg->dtype);
+  const int M = b->M;
+  auto fail = [&](cudaError_t e) {
+    free_body(b);
+    return cuda_status(e, "vs_body_plan_create");
+  };
+  // host marker data in the plan precision
+  std::vector<unsigned char> hx(ts * M * 3);
+  auto put = [&](int idx, double v) {
+    if (ts == 8) ((double*)hx.data())[idx] = v;
+    else ((float*)hx.data())[idx] = (float)v;
+  };
+  // extents of the marker cloud (for the window capacity)
+  double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+  const double* src[3] = {cfg->x0_host, cfg->y0_host, cfg->z0_host};
+  for (int m = 0; m < M; ++m)
+    for (int d = 0; d < cfg->dim; ++d) {
+      const double v = src[d][m];
+      lo[d] = v < lo[d] ? v : lo[d];
+      hi[d] = v > hi[d] ? v : hi[d];
+      if (cfg->dim == 2) put(d * M + m, v);
+      else put(m * 3 + d, v);
+    }
+  for (int d = 0; d < cfg->dim; ++d) b->cap[d] = (int)(floor(hi[d]) - floor(lo[d])) + w + 2;
+  if (cfg->dim == 2) b->cap[2] = 1;
+  cudaError_t e;
+  if ((e = cudaMalloc(&b->d_X0, ts * M * 3)) != cudaSuccess) return fail(e);
+  if ((e = cudaMemcpy(b->d_X0, hx.data(), ts * M * 3, cudaMemcpyHostToDevice)) != cudaSuccess) return fail(e);
+  if (cfg->ds_host) {
+    std::vector<unsigned char> hd(ts * M);
+    for (int m = 0; m < M; ++m) {
+      if (ts == 8) ((double*)hd.data())[m] = cfg->ds_host[m];
+      else ((float*)hd.data())[m] = (float)cfg->ds_host[m];
+    }
+    if ((e = cudaMalloc(&b->d_ds, ts * M)) != cudaSuccess) return fail(e);
+    if ((e = cudaMemcpy(b->d_ds, hd.data(), ts * M, cudaMemcpyHostToDevice)) != cudaSuccess) return fail(e);
+  }
+  if ((e = cudaMalloc(&b->d_state, ts * 12)) != cudaSuccess) return fail(e);
+  {
+    double st[12] = {0};
+    for (int c = 0; c < 3; ++c) {
+      st[c] = cfg->a0[c];
+      st[3 + c] = cfg->v0[c];
+      st[6 + c] = cfg->d0[c];
+    }
+    const int rc = vs_body_set_state(b, st, nullptr);
+    if (rc) {
+      free_body(b);
+      return rc;
+    }
+  }
+  const int64_t cells = (int64_t)b->cap[0] * b->cap[1] * b->cap[2];
+  if ((e = cudaMalloc(&b->d_gw, ts * b->C * cells)) != cudaSuccess) return fail(e);
+  if ((e = cudaMalloc(&b->d_meta, sizeof(int) * META_N)) != cudaSuccess) return fail(e);
+  {
+    int meta[META_N] = {0, 0, 0, 0, 0, 0, 0, 0};
+    if ((e = cudaMemcpy(b->d_meta, meta, sizeof(meta), cudaMemcpyHostToDevice)) != cudaSuccess) return fail(e);
+  }
+  // Newmark scalars formed in double as the reference's Python floats (dyn.py:31-49)
+  const double dt = 1.0, gamma = 0.5, beta = 0.25;
+  b->nm[0] = dt * (1 - gamma);
+  b->nm[1] = dt * dt * (0.5 - beta);
+  b->nm[2] = gamma * dt;
+  b->nm[3] = beta * dt * dt;
+  b->nm[4] = dt;
+  b->nm[5] = cfg->damping;
+  b->nm[6] = cfg->stiffness;
+  b->nm[7] = cfg->mass + b->nm[2] * cfg->damping + b->nm[3] * cfg->stiffness;
+  b->nm[8] = cfg->added_mass_area;
+  if (cfg->dim == 2) {
+    const int P = M * b->S;
+    const int Bcap = b->cap[0] * b->cap[1];
+    b->smem = ts * (2 * M + P + 6 * M + 4 * Bcap) + sizeof(int) * (2 * P + 2 * Bcap + 1 + 40);
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if ((int64_t)b->smem > optin) {
+      free_body(b);
+      set_error("body of %d markers needs %zu bytes of shared memory (> %d available)", M, b->smem, optin);
+      return VS_ERR_UNSUPPORTED;
+    }
+    e = ts == 8 ? cudaFuncSetAttribute(k_body2d<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->smem)
+                : cudaFuncSetAttribute(k_body2d<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->smem);
+    if (e != cudaSuccess) return fail(e);
+  } else {
+    // fixed 3-D body: stencil once over a fixed window around the markers
+    const int nn[3] = {lattice->cfg.nx, lattice->cfg.ny, lattice->cfg.nz};
+    int org[3];
+    for (int d = 0; d < 3; ++d) {
+      org[d] = (int)floor(lo[d]) - cfg->radius + 1;
+      b->cap[d] = (int)(floor(hi[d]) - floor(lo[d])) + w;
+      if (org[d] < 0 || org[d] + b->cap[d] > nn[d]) {
+        free_body(b);
+        set_error("body stencil leaves the grid along axis %d", d);
+        return VS_ERR_RANGE;
+      }
+    }
+    int meta[META_N] = {org[0], org[1], org[2], b->cap[0], b->cap[1], b->cap[2], 0, 0};
+    if ((e = cudaMemcpy(b->d_meta, meta, sizeof(meta), cudaMemcpyHostToDevice)) != cudaSuccess) return fail(e);
+    const int64_t wcells = (int64_t)b->cap[0] * b->cap[1] * b->cap[2];
+    const int64_t P = (int64_t)M * b->S;
+    // window-relative marker coordinates
+    std::vector<unsigned char> hr(ts * M * 3);
+    for (int m = 0; m < M; ++m)
+      for (int d = 0; d < 3; ++d) {
+        const double v = src[d][m] - org[d];
+        if (ts == 8) ((double*)hr.data())[m * 3 + d] = v;
+        else ((float*)hr.data())[m * 3 + d] = (float)((float)src[d][m] - (float)org[d]);
+      }
+    void* d_rel = nullptr;
+    if ((e = cudaMalloc(&d_rel, ts * M * 3)) != cudaSuccess) return fail(e);
+    cudaMemcpy(d_rel, hr.data(), ts * M * 3, cudaMemcpyHostToDevice);
+    if ((e = cudaMalloc(&b->d_W, ts * P)) != cudaSuccess) return fail(e);
+    if ((e = cudaMalloc(&b->d_I, sizeof(int32_t) * P)) != cudaSuccess) return fail(e);
+    int rc = vs_ib_stencil_3d(cfg->kernel, cfg->radius, cfg->dtype, d_rel, M, b->cap[0], b->cap[1], b->cap[2],
+                              b->d_W, b->d_I, nullptr);
+    cudaFree(d_rel);
+    if (rc) {
+      free_body(b);
+      return rc;
+    }
+    if ((e = cudaFree(b->d_gw)) != cudaSuccess) return fail(e);
+    if ((e = cudaMalloc(&b->d_gw, ts * 3 * wcells)) != cudaSuccess) return fail(e);
+    if ((e = cudaMalloc(&b->d_uw, ts * 3 * wcells)) != cudaSuccess) return fail(e);
+    if ((e = cudaMalloc(&b->d_target, ts * 3 * M)) != cudaSuccess) return fail(e);
+    if ((e = cudaMemset(b->d_target, 0, ts * 3 * M)) != cudaSuccess) return fail(e);
+    if ((e = cudaMalloc(&b->d_mf, ts * 3 * M)) != cudaSuccess) return fail(e);
+    b->ws_bytes = vs_ib_workspace_bytes(M, b->S);
+    if ((e = cudaMalloc(&b->d_ws, b->ws_bytes)) != cudaSuccess) return fail(e);
+    // build the (static) pair CSR once, on a zero velocity window
+    if ((e = cudaMemset(b->d_uw, 0, ts * 3 * wcells)) != cudaSuccess) return fail(e);
+    rc = ib_mdf_run(cfg->dtype, false, b->d_uw, 3, wcells, b->d_W, b->d_I, M, b->S, b->d_target, b->d_ds,
+                    cfg->ds_scalar, cfg->n_iter, b->d_gw, b->d_mf, b->d_ws, b->ws_bytes, nullptr);
+    if (rc) {
+      free_body(b);
+      return rc;
+    }
+    b->csr_ready = 1;
+    if ((e = cudaDeviceSynchronize()) != cudaSuccess) return fail(e);
+  }
+  *out = b;
+  return VS_OK;
+}
+
+int vs_body_plan_destroy(vs_body_plan* plan) {
+  free_body(plan);
+  return VS_OK;
+}
+
+int vs_body_set_state(vs_body_plan* plan, const double* state_host, void* stream) {
+  VS_REQUIRE(plan && state_host, "vs_body_set_state: null argument");
+  const size_t ts = dsize(plan->cfg.dtype);
+  unsigned char buf[12 * 8];
+  for (int i = 0; i < 12; ++i) {
+    if (ts == 8) ((double*)buf)[i] = state_host[i];
+    else ((float*)buf)[i] = (float)state_host[i];
+  }
+  cudaStream_t st = as_stream(stream);
+  cudaError_t e = cudaMemcpyAsync(plan->d_state, buf, ts * 12, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  return cuda_status(e, "vs_body_set_state");
+}
+
+int vs_body_get_state(const vs_body_plan* plan, double* state_host, void* stream) {
+  VS_REQUIRE(plan && state_host, "vs_body_get_state: null argument");
+  const size_t ts = dsize(plan->cfg.dtype);
+  unsigned char buf[12 * 8];
+  int meta[META_N];
+  cudaStream_t st = as_stream(stream);
+  cudaError_t e = cudaMemcpyAsync(buf, plan->d_state, ts * 12, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(meta, plan->d_meta, sizeof(meta), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_status(e, "vs_body_get_state");
+  for (int i = 0; i < 12; ++i) state_host[i] = ts == 8 ? ((double*)buf)[i] : (double)((float*)buf)[i];
+  if (meta[META_STATUS] != 0) {
+    set_error("immersed body left its window or the grid (stencil out of range)");
+    return meta[META_STATUS];
+  }
+  return VS_OK;
+}
+
+int vs_step(const vs_lattice_plan* lattice, vs_body_plan* body, const void* f_in, void* f_out, void* force_hist,
+            void* stream) {
+  VS_REQUIRE(lattice && f_in && f_out && f_in != f_out, "vs_step: f_in and f_out must be distinct device buffers");
+  return enqueue_step(lattice, body, f_in, f_out, force_hist, as_stream(stream));
+}
+
+int vs_step_grid_only(const vs_lattice_plan* lattice, const vs_body_plan* body, const void* f_in, void* f_out,
+                      void* stream) {
+  VS_REQUIRE(lattice && f_in && f_out && f_in != f_out, "vs_step_grid_only: bad arguments");
+  return enqueue_grid(lattice, body, f_in, f_out, as_stream(stream));
+}
+
+int vs_run(const vs_lattice_plan* lattice, vs_body_plan* body, void* f_a, void* f_b, int n_steps, void* force_hist,
+           void* stream) {
+  VS_REQUIRE(lattice && f_a && f_b && f_a != f_b && n_steps >= 0, "vs_run: bad arguments");
+  const size_t hs = 3 * dsize(lattice->cfg.dtype);
+  for (int s = 0; s < n_steps; ++s) {
+    void* src = (s % 2 == 0) ? f_a : f_b;
+    void* dst = (s % 2 == 0) ? f_b : f_a;
+    void* hist = force_hist ? (void*)((char*)force_hist + hs * s) : nullptr;
+    int rc = enqueue_step(lattice, body, src, dst, hist, as_stream(stream));
+    if (rc) return rc;
+  }
+  return VS_OK;
+}
+
+int vs_run_graph(vs_lattice_plan* lattice, vs_body_plan* body, void* f_a, void* f_b, int n_steps, void* force_hist,
+                 void* stream) {
+  VS_REQUIRE(lattice && f_a && f_b && f_a != f_b && n_steps > 0, "vs_run_graph: bad arguments");
+  cudaStream_t st = as_stream(stream);
+  VS_REQUIRE(st != nullptr, "vs_run_graph: needs a non-default stream (stream capture)");
+  const bool hit = lattice->graph && lattice->g_fa == f_a && lattice->g_fb == f_b && lattice->g_steps == n_steps &&
+                   lattice->g_hist == force_hist && lattice->g_body == body && lattice->g_stream == st;
+  if (!hit) {
+    if (lattice->graph) {
+      cudaGraphExecDestroy(lattice->graph);
+      lattice->graph = nullptr;
+    }
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return cuda_status(e, "vs_run_graph capture");
+    int rc = vs_run(lattice, body, f_a, f_b, n_steps, force_hist, stream);
+    e = cudaStreamEndCapture(st, &g);
+    if (rc) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    if (e != cudaSuccess) return cuda_status(e, "vs_run_graph end capture");
+    e = cudaGraphInstantiate(&lattice->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_status(e, "vs_run_graph instantiate");
+    lattice->g_fa = f_a;
+    lattice->g_fb = f_b;
+    lattice->g_steps = n_steps;
+    lattice->g_hist = force_hist;
+    lattice->g_body = body;
+    lattice->g_stream = st;
+  }
+  return cuda_status(cudaGraphLaunch(lattice->graph, st), "vs_run_graph launch");
+}
+
+}  // extern "C"

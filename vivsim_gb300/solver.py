@@ -1,0 +1,207 @@
+"""Fused IB-LBM time stepping: one plan per lattice, one per immersed body.
+
+The reference has no driver; its examples compose the per-operator functions into an
+``update_step`` run under ``jax.jit`` + ``lax.scan`` (e.g.
+examples/2d/vortex_induced_vibration.py:96-157).  ``Simulation`` is that loop, executed by
+the fused kernels of ``vs_step``/``vs_run``/``vs_run_graph`` with the body state kept on
+the device, so a multi-step run never synchronises with the host.
+"""
+
+import ctypes as C
+
+import numpy as np
+import torch
+
+from . import _lib as V
+from ._ops import mrt_collision_operator, mrt_forcing_operator
+
+COLLISIONS = {"bgk": V.VS_COLLIDE_BGK, "kbc": V.VS_COLLIDE_KBC, "mrt": V.VS_COLLIDE_MRT, "reg": V.VS_COLLIDE_REG}
+FORCINGS = {"none": V.VS_FORCE_NONE, "edm": V.VS_FORCE_EDM, "guo_bgk": V.VS_FORCE_GUO_BGK,
+            "guo_mrt": V.VS_FORCE_GUO_MRT}
+BC_KINDS = {"nee": V.VS_BC_NEE, "nebb": V.VS_BC_NEBB, "equilibrium": V.VS_BC_EQ, "eq": V.VS_BC_EQ,
+            "bounce_back": V.VS_BC_BB, "specular_reflection": V.VS_BC_SPECULAR}
+WALL_MODES = {"given": V.VS_WALL_GIVEN, "velocity": V.VS_WALL_VELOCITY, "pressure": V.VS_WALL_PRESSURE,
+              "force_corrected": V.VS_WALL_FORCE_CORRECTED}
+KERNELS = {"peskin3": V.VS_KERNEL_PESKIN3, "peskin4": V.VS_KERNEL_PESKIN4, "cosine4": V.VS_KERNEL_COSINE4}
+
+
+def boundary(kind, loc, mode="given", rho_wall=1.0, ux_wall=0.0, uy_wall=0.0, uz_wall=0.0, gx_wall=0.0,
+             gy_wall=0.0, gz_wall=0.0):
+    """One face boundary of the step, e.g. ``boundary("nee", "right", mode="pressure")``.
+
+    ``kind`` names the reference scheme (boundary_nee / _nebb / _equilibrium /
+    _bounce_back / _specular_reflection) and ``mode`` its wrapper (velocity / pressure /
+    force_corrected, lbm/boundary/_helpers.py:175-239).
+    """
+    return dict(kind=kind, loc=loc, mode=mode, rho=rho_wall, ux=ux_wall, uy=uy_wall, uz=uz_wall, gx=gx_wall,
+                gy=gy_wall, gz=gz_wall)
+
+
+def _tdtype(dtype):
+    return torch.float64 if dtype in (torch.float64, "float64", np.float64) else torch.float32
+
+
+class LatticeStep:
+    """Plan of the fused collide-force-stream-boundary step on one grid."""
+
+    def __init__(self, q, shape, collision="bgk", omega=1.0, dtype=torch.float32, mrt_op=None, forcing="none",
+                 g=None, boundaries=()):
+        if q not in (9, 19):
+            raise ValueError("q must be 9 (D2Q9) or 19 (D3Q19)")
+        self.q = q
+        self.dim = 2 if q == 9 else 3
+        self.shape = tuple(int(s) for s in shape)
+        if len(self.shape) != self.dim:
+            raise ValueError(f"shape must have {self.dim} entries")
+        self.dtype = _tdtype(dtype)
+        self.collision = collision
+        self.omega = float(omega)
+        cfg = V.vs_lattice_cfg()
+        cfg.q = q
+        cfg.dtype = V.VS_F64 if self.dtype == torch.float64 else V.VS_F32
+        cfg.nx, cfg.ny = self.shape[0], self.shape[1]
+        cfg.nz = self.shape[2] if self.dim == 3 else 1
+        cfg.collision = COLLISIONS[collision]
+        cfg.omega = self.omega
+        if collision == "mrt":
+            op = mrt_collision_operator(q, omega, self.dtype) if mrt_op is None else mrt_op
+            a = np.asarray(op.cpu().double() if isinstance(op, torch.Tensor) else op, dtype=np.float64).reshape(-1)
+            for i, v in enumerate(a):
+                cfg.mrt_op[i] = float(v)
+        cfg.forcing = FORCINGS[forcing]
+        if forcing == "guo_mrt":
+            a = mrt_forcing_operator(q, omega, self.dtype).double().numpy().reshape(-1)
+            for i, v in enumerate(a):
+                cfg.mrt_fop[i] = float(v)
+        if g is not None:
+            for i, v in enumerate(g):
+                cfg.g_uniform[i] = float(v)
+        if len(boundaries) > V.VS_MAX_BC:
+            raise ValueError(f"at most {V.VS_MAX_BC} boundaries")
+        cfg.n_bc = len(boundaries)
+        for k, b in enumerate(boundaries):
+            s = cfg.bc[k]
+            s.kind = BC_KINDS[b["kind"]]
+            s.mode = WALL_MODES[b["mode"]]
+            s.loc = V.LOCS[b["loc"]]
+            for name in ("rho", "ux", "uy", "uz", "gx", "gy", "gz"):
+                setattr(s, name, float(b[name]))
+        self.cfg = cfg
+        handle = C.c_void_p()
+        V.call("vs_lattice_plan_create", C.byref(cfg), C.byref(handle))
+        self.handle = handle
+
+    @property
+    def n_nodes(self):
+        return int(np.prod(self.shape))
+
+    def close(self):
+        if getattr(self, "handle", None) and self.handle.value:
+            V.lib().vs_lattice_plan_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class RigidBody:
+    """Immersed rigid body: markers, IB stencil, MDF and a Newmark spring-mass update."""
+
+    def __init__(self, step, markers, ds, kernel="peskin4", radius=2, n_iter=3, moving=False,
+                 free_dof=(False, False, False), mass=1.0, stiffness=0.0, damping=0.0, added_mass_area=0.0,
+                 d0=(0, 0, 0), v0=(0, 0, 0), a0=(0, 0, 0)):
+        X = np.asarray(markers.cpu() if isinstance(markers, torch.Tensor) else markers, dtype=np.float64)
+        if X.ndim != 2 or X.shape[1] != step.dim:
+            raise ValueError(f"markers must have shape (n_markers, {step.dim})")
+        self.step = step
+        self.M = X.shape[0]
+        self._cols = [np.ascontiguousarray(X[:, d]) for d in range(step.dim)]
+        cfg = V.vs_body_cfg()
+        cfg.dim = step.dim
+        cfg.dtype = step.cfg.dtype
+        cfg.n_markers = self.M
+        P = C.POINTER(C.c_double)
+        cfg.x0_host = self._cols[0].ctypes.data_as(P)
+        cfg.y0_host = self._cols[1].ctypes.data_as(P)
+        cfg.z0_host = self._cols[2].ctypes.data_as(P) if step.dim == 3 else None
+        if np.ndim(ds) == 0:
+            cfg.ds_scalar = float(ds)
+            cfg.ds_host = None
+        else:
+            self._ds = np.ascontiguousarray(np.asarray(ds, dtype=np.float64).reshape(-1))
+            cfg.ds_host = self._ds.ctypes.data_as(P)
+        cfg.kernel = KERNELS[kernel]
+        cfg.radius = int(radius)
+        cfg.n_iter = int(n_iter)
+        cfg.moving = 1 if moving else 0
+        for i in range(3):
+            cfg.free_dof[i] = 1 if (i < len(free_dof) and free_dof[i]) else 0
+        cfg.mass, cfg.stiffness, cfg.damping = float(mass), float(stiffness), float(damping)
+        cfg.added_mass_area = float(added_mass_area)
+        for name, val in (("d0", d0), ("v0", v0), ("a0", a0)):
+            arr = getattr(cfg, name)
+            for i in range(3):
+                arr[i] = float(val[i]) if i < len(val) else 0.0
+        self.cfg = cfg
+        handle = C.c_void_p()
+        V.call("vs_body_plan_create", C.byref(cfg), step.handle, C.byref(handle))
+        self.handle = handle
+
+    def state(self):
+        """Body state as float64 numpy arrays a, v, d, h (3 each); synchronises."""
+        buf = (C.c_double * 12)()
+        V.call("vs_body_get_state", self.handle, buf, V.stream())
+        a = np.frombuffer(buf, dtype=np.float64).copy()
+        return dict(a=a[0:3], v=a[3:6], d=a[6:9], h=a[9:12])
+
+    def set_state(self, a=(0, 0, 0), v=(0, 0, 0), d=(0, 0, 0)):
+        buf = (C.c_double * 12)(*([float(x) for x in a] + [float(x) for x in v] + [float(x) for x in d] + [0.0] * 3))
+        V.call("vs_body_set_state", self.handle, buf, V.stream())
+
+    def close(self):
+        if getattr(self, "handle", None) and self.handle.value:
+            V.lib().vs_body_plan_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Simulation:
+    """Populations in two ping-pong device buffers advanced by the fused step."""
+
+    def __init__(self, step, f0, body=None):
+        V.require_cuda(f0)
+        if tuple(f0.shape) != (step.q,) + step.shape:
+            raise ValueError(f"f0 must have shape {(step.q,) + step.shape}")
+        self.step = step
+        self.body = body
+        self._a = f0.to(step.dtype).contiguous().clone()
+        self._b = torch.empty_like(self._a)
+        self._cur_is_a = True
+
+    @property
+    def f(self):
+        """Current populations (reference convention: after streaming and boundaries)."""
+        return self._a if self._cur_is_a else self._b
+
+    def run(self, n_steps, graph=False, force_history=False):
+        """Advance n_steps; returns the (n_steps, 3) body-force history when asked."""
+        if n_steps <= 0:
+            return None
+        src, dst = (self._a, self._b) if self._cur_is_a else (self._b, self._a)
+        hist = None
+        if force_history:
+            hist = torch.empty((n_steps, 3), dtype=self.step.dtype, device=self._a.device)
+        body = self.body.handle if self.body is not None else None
+        fn = "vs_run_graph" if graph else "vs_run"
+        V.call(fn, self.step.handle, body, V.ptr(src), V.ptr(dst), int(n_steps), V.ptr(hist), V.stream())
+        if n_steps % 2 == 1:
+            self._cur_is_a = not self._cur_is_a
+        return hist
