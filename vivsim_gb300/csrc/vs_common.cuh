@@ -269,13 +269,41 @@ __device__ __forceinline__ void projection19(const T* n, T* s) {
   s[16] = eight * (byz - T(2) * dyz); s[17] = s[16];
 }
 
+// Entry (q, r) of the reference's 19x19 projection table, rounded to float32 as the
+// reference declares it (vivsim/lbm3d/collision/reg.py:10-32): w_q/(2 cs^4) H_q : c_r c_r.
+__host__ __device__ constexpr double p19_entry(int q, int r) {
+  double s = 0.0;
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < 3; ++b)
+      s += ((double)(q19_c(q, a) * q19_c(q, b)) - (a == b ? 1.0 / 3.0 : 0.0)) * (double)(q19_c(r, a) * q19_c(r, b));
+  const double wq = q == 0 ? 1.0 / 3.0 : (q <= 6 ? 1.0 / 18.0 : 1.0 / 36.0);
+  return (double)(float)(wq / (2.0 * (1.0 / 3.0) * (1.0 / 3.0)) * s);
+}
+
+// In float64 the reference multiplies by the float32-rounded table, so the double kernels
+// apply that table literally (sum over r in order); float kernels use the moment form.
+template <typename T>
+__device__ __forceinline__ void projection19_any(const T* n, T* s) {
+  if constexpr (sizeof(T) == 8) {
+#pragma unroll
+    for (int q = 0; q < 19; ++q) {
+      T acc = T(0);
+#pragma unroll
+      for (int r = 1; r < 19; ++r) acc = r == 1 ? (T)p19_entry(q, r) * n[r] : acc + (T)p19_entry(q, r) * n[r];
+      s[q] = acc;
+    }
+  } else {
+    projection19(n, s);
+  }
+}
+
 // D3Q19 regularised: feq + (1 - omega) P fneq, vivsim/lbm3d/collision/reg.py:44-62.
 template <typename T>
 __device__ __forceinline__ void collide_reg(L19, T* f, const T* feq, const CollideParams<T>& p) {
   T n[19], s[19];
 #pragma unroll
   for (int i = 0; i < 19; ++i) n[i] = f[i] - feq[i];
-  projection19(n, s);
+  projection19_any(n, s);
 #pragma unroll
   for (int i = 0; i < 19; ++i) f[i] = feq[i] + p.one_m_omega * s[i];
 }
@@ -286,7 +314,7 @@ __device__ __forceinline__ void collide_kbc(L19, T* f, const T* feq, const Colli
   T n[19], s[19];
 #pragma unroll
   for (int i = 0; i < 19; ++i) n[i] = f[i] - feq[i];
-  projection19(n, s);
+  projection19_any(n, s);
   T ish = T(0), ihh = T(0);
 #pragma unroll
   for (int i = 0; i < 19; ++i) {

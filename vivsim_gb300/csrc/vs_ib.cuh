@@ -42,6 +42,18 @@ __device__ __forceinline__ int ifloor(T x) { return (int)floor(x); }
 }  // namespace vs
 
 namespace vs {
+// Views into the sorted (node, pair) CSR of a stencil: sorted keys and pair ids, segment
+// heads, 0-based unique-node ids per sorted position, and the unique-node id of each pair.
+struct IbCsrView {
+  int32_t* skeys;
+  int32_t* sids;
+  int32_t* head;
+  int32_t* uid;
+  int32_t* pair_uid;
+};
+int ib_build_csr(const int32_t* I, int64_t P, int64_t n_grid, void* workspace, int m, int s, IbCsrView* out,
+                 cudaStream_t st);
+
 // Multi-direct forcing over the pair CSR in `workspace`; with csr_ready the CSR built by
 // an earlier call for the same stencil indices is reused (defined in vs_ops_ib.cu).
 int ib_mdf_run(int dtype, bool csr_ready, const void* grid_u, int c, int64_t n_grid, const void* W, const int32_t* I,

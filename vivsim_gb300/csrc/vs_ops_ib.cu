@@ -132,9 +132,10 @@ __global__ void k_pair_uid(const int32_t* __restrict__ sids, const int32_t* __re
 
 // MDF marker update (vivsim/ib/mdf.py:41-56), one thread per (marker, component):
 //   first: U = interp(grid_u)   else: U += interp(nodes)   (nodes already hold 0.5 * spread)
-//   F_step = (U_target - U) * (2 ds);  F_total += F_step
+//   F_step = (U_target - U) * (2 ds);  F_total = F_step (first, if any iteration) or += F_step
+//   write_force: marker_force = -F_total
 template <typename T>
-__global__ void k_mdf_marker(int first, int last, const T* __restrict__ grid_u, int64_t n_grid,
+__global__ void k_mdf_marker(int first, int use_step, int write_force, const T* __restrict__ grid_u, int64_t n_grid,
                              const T* __restrict__ nodes, int64_t n_nodes, const int32_t* __restrict__ I,
                              const int32_t* __restrict__ pair_uid, const T* __restrict__ W, int m, int s, int c,
                              const T* __restrict__ ut, const T* __restrict__ ds, T ds_scalar, T* __restrict__ U,
@@ -158,14 +159,12 @@ __global__ void k_mdf_marker(int first, int last, const T* __restrict__ grid_u, 
     }
     const T u = first ? acc : U[p] + acc;
     U[p] = u;
-    if (last) {
-      marker_force[p] = -Ftot[p];
-      continue;
-    }
     const T d2 = (ds ? ds[mk] : ds_scalar) * T(2);
     const T fs = (ut[p] - u) * d2;
     Fstep[p] = fs;
-    Ftot[p] = first ? fs : Ftot[p] + fs;
+    const T ft = first ? (use_step ? fs : T(0)) : Ftot[p] + fs;
+    Ftot[p] = ft;
+    if (write_force) marker_force[p] = -ft;
   }
 }
 
@@ -249,6 +248,25 @@ static int build_csr(const int32_t* I, int64_t P, int64_t n_grid, IbWorkspace& w
   e = cub::DeviceScan::InclusiveSum(w.cub_tmp, sb, w.head, w.uid, (int)P, st);
   if (e != cudaSuccess) return cuda_status(e, "ib csr scan");
   VS_CHECK_LAUNCH("ib csr");
+  return VS_OK;
+}
+
+__global__ void k_uid_minus_one(int32_t* uid, int64_t P);
+
+// Sorted pair CSR of a static stencil, built in `workspace` (vivsim_gb300 fixed bodies).
+int ib_build_csr(const int32_t* I, int64_t P, int64_t n_grid, void* workspace, int m, int s, IbCsrView* out,
+                 cudaStream_t st) {
+  IbWorkspace w = carve(workspace, m, s);
+  int rc = build_csr(I, P, n_grid, w, st);
+  if (rc) return rc;
+  k_uid_minus_one<<<grid_for(P, 256), 256, 0, st>>>(w.uid, P);
+  k_pair_uid<<<grid_for(P, 256), 256, 0, st>>>(w.sids, w.skeys, w.uid, P, w.pair_uid);
+  VS_CHECK_LAUNCH("ib_build_csr");
+  out->skeys = w.skeys;
+  out->sids = w.sids;
+  out->head = w.head;
+  out->uid = w.uid;
+  out->pair_uid = w.pair_uid;
   return VS_OK;
 }
 
@@ -390,20 +408,18 @@ int ib_mdf_run(int dtype, bool csr_ready, const void* grid_u, int c, int64_t n_g
       k_pair_uid<<<grid_for(P, 256), 256, 0, st>>>(w.sids, w.skeys, w.uid, P, w.pair_uid);
     }
     const unsigned gm = grid_for((int64_t)m * c, 128);
-    if (n_iter == 0) {  // no iteration: F_total stays zero
-      cudaError_t e0 = cudaMemsetAsync(Ftot, 0, sizeof(T) * m * c, st);
-      if (e0 != cudaSuccess) return cuda_status(e0, "vs_ib_mdf memset");
-    }
-    // U = interp(grid_u); F_step = (U_t - U) 2ds; F_tot = F_step
-    k_mdf_marker<T><<<gm, 128, 0, st>>>(1, n_iter == 0, (const T*)grid_u, n_grid, nodes, n_nodes, I, w.pair_uid,
-                                        (const T*)W, m, s, c, (const T*)u_target, (const T*)ds, (T)ds_scalar, U,
-                                        Fstep, Ftot, (T*)marker_force);
-    for (int it = 0; it < n_iter; ++it) {
+    // U = interp(grid_u); F_step = (U_t - U) 2ds; F_tot = F_step (mdf.py:38-48)
+    k_mdf_marker<T><<<gm, 128, 0, st>>>(1, n_iter > 0, n_iter <= 1, (const T*)grid_u, n_grid, nodes, n_nodes, I,
+                                        w.pair_uid, (const T*)W, m, s, c, (const T*)u_target, (const T*)ds,
+                                        (T)ds_scalar, U, Fstep, Ftot, (T*)marker_force);
+    // iterations 1..n_iter-1; the spread and interpolation after the last force step only
+    // update a marker velocity the reference discards (mdf.py:57-64), so they are skipped
+    for (int it = 0; it + 1 < n_iter; ++it) {
       // nodes = 0.5 * spread(F_step)   (mdf.py:50-51)
       k_segment_sum<T><<<grid_for(P, 256), 256, 0, st>>>(1, w.skeys, w.sids, w.head, w.uid, P, Fstep, (const T*)W, c,
                                                          s, nullptr, nullptr, n_grid, nodes, n_nodes, T(0.5));
-      // U += interp(nodes); next F_step unless this was the last iteration
-      k_mdf_marker<T><<<gm, 128, 0, st>>>(0, it == n_iter - 1, (const T*)grid_u, n_grid, nodes, n_nodes, I,
+      // U += interp(nodes); next F_step; F_tot += F_step
+      k_mdf_marker<T><<<gm, 128, 0, st>>>(0, 1, it + 2 == n_iter, (const T*)grid_u, n_grid, nodes, n_nodes, I,
                                           w.pair_uid, (const T*)W, m, s, c, (const T*)u_target, (const T*)ds,
                                           (T)ds_scalar, U, Fstep, Ftot, (T*)marker_force);
     }

@@ -18,6 +18,7 @@
 
 #include "vs_boundary.cuh"
 #include "vs_dispatch.cuh"
+#include "vs_fast.cuh"
 #include "vs_ib.cuh"
 
 namespace vs {
@@ -31,6 +32,7 @@ struct StepParams {
   const T* fin;
   T* fout;
   int nx, ny, nz, n;
+  int chunks;                    // blocks along the contiguous axis (3-D)
   CollideParams<T> cp;
   int forcing;
   int has_g0;
@@ -45,23 +47,33 @@ struct StepParams {
   T fop[L::Q * L::Q];            // MRT forcing operator
 };
 
+// One thread per node.  blockIdx.y = x; blockIdx.x = (y, chunk of the contiguous axis)
+// in 3-D or the chunk of y in 2-D; threads run along the contiguous axis, so every load
+// and store of a warp covers 32 consecutive addresses.  Wrap-around offsets of the push
+// are per-block uniform except along the contiguous axis.
 template <class L, typename T, int COLL>
 __global__ void __launch_bounds__(256) k_step(const __grid_constant__ StepParams<L, T> P) {
   constexpr int Q = L::Q;
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= P.n) return;
-  const int nyz = P.ny * P.nz;
-  const int x = p / nyz;
-  const int r = p - x * nyz;
-  const int y = r / P.nz;
-  const int z = r - y * P.nz;
+  const int x = blockIdx.y;
+  int y, z;
+  if constexpr (L::D == 2) {
+    y = blockIdx.x * blockDim.x + threadIdx.x;
+    z = 0;
+    if (y >= P.ny) return;
+  } else {
+    y = blockIdx.x / P.chunks;
+    z = (blockIdx.x - y * P.chunks) * blockDim.x + threadIdx.x;
+    if (z >= P.nz) return;
+  }
+  const int syz = P.ny * P.nz;
+  const int p = x * syz + y * P.nz + z;
 
   T f[Q];
 #pragma unroll
   for (int i = 0; i < Q; ++i) f[i] = __ldg(P.fin + (size_t)i * P.n + p);
 
   T rho, u[3] = {T(0), T(0), T(0)};
-  macro(L{}, f, rho, u);
+  fast::macro<L>(f, rho, u);
 
   T g[3] = {T(0), T(0), T(0)};
   bool has_g = P.has_g0;
@@ -90,11 +102,8 @@ __global__ void __launch_bounds__(256) k_step(const __grid_constant__ StepParams
     for (int d = 0; d < L::D; ++d) ue[d] = u[d] + (g[d] * T(0.5)) / rho;
   }
   T feq[Q];
-  equilibrium<L>(rho, ue, feq);
-  if constexpr (COLL == VS_COLLIDE_BGK) collide_bgk<L>(f, feq, P.cp);
-  else if constexpr (COLL == VS_COLLIDE_KBC) collide_kbc(L{}, f, feq, P.cp);
-  else if constexpr (COLL == VS_COLLIDE_REG) collide_reg(L{}, f, feq, P.cp);
-  else collide_mrt<L>(f, feq, P.op);
+  fast::equilibrium<L>(rho, ue, feq);
+  fast::collide<L, COLL>(f, feq, P.cp, P.op);
 
   if (has_g && P.forcing != VS_FORCE_NONE) {
     if (P.forcing == VS_FORCE_EDM) {
@@ -132,17 +141,20 @@ __global__ void __launch_bounds__(256) k_step(const __grid_constant__ StepParams
     for (int i = 0; i < Q; ++i) P.pre_buf[k][i * nf + j] = f[i];
   }
 
-  // push streaming with periodic wrap on every axis (lbm/basic.py:60-85)
-  const int xp = x + 1 == P.nx ? 0 : x + 1, xm = x == 0 ? P.nx - 1 : x - 1;
-  const int yp = y + 1 == P.ny ? 0 : y + 1, ym = y == 0 ? P.ny - 1 : y - 1;
-  const int zp = z + 1 == P.nz ? 0 : z + 1, zm = z == 0 ? P.nz - 1 : z - 1;
+  // push streaming with periodic wrap on every axis (lbm/basic.py:60-85):
+  // destination = p + per-axis offsets, each offset wrapping at the domain edge
+  const int dxp = x == P.nx - 1 ? -(P.nx - 1) * syz : syz;
+  const int dxm = x == 0 ? (P.nx - 1) * syz : -syz;
+  const int dyp = y == P.ny - 1 ? -(P.ny - 1) * P.nz : P.nz;
+  const int dym = y == 0 ? (P.ny - 1) * P.nz : -P.nz;
+  const int dzp = z == P.nz - 1 ? -(P.nz - 1) : 1;
+  const int dzm = z == 0 ? P.nz - 1 : -1;
 #pragma unroll
   for (int i = 0; i < Q; ++i) {
     const int cx = L::c(i, 0), cy = L::c(i, 1), cz = L::c(i, 2);
-    const int xd = cx > 0 ? xp : (cx < 0 ? xm : x);
-    const int yd = cy > 0 ? yp : (cy < 0 ? ym : y);
-    const int zd = cz > 0 ? zp : (cz < 0 ? zm : z);
-    P.fout[(size_t)i * P.n + (xd * P.ny + yd) * P.nz + zd] = f[i];
+    const int d = (cx > 0 ? dxp : (cx < 0 ? dxm : 0)) + (cy > 0 ? dyp : (cy < 0 ? dym : 0)) +
+                  (cz > 0 ? dzp : (cz < 0 ? dzm : 0));
+    P.fout[(size_t)i * P.n + (p + d)] = f[i];
   }
 }
 
@@ -189,7 +201,7 @@ struct BodyParams {
   const T* Y0;
   const T* ds_arr;
   T ds2_scalar;  // 2 * ds as the reference forms it: (T)ds * 2
-  int M, radius, kernel, n_iter;
+  int M, kernel, n_iter;
   int cap_x, cap_y;
   T* state;  // a[3], v[3], d[3], h[3]
   T* gw;
@@ -199,14 +211,15 @@ struct BodyParams {
   T k1, k2, c1, c2, dt, damp, stiff, den, area;
 };
 
-// Exclusive block scan of cnt[0..B) into start[0..B], start[B] = total.
-__device__ void block_exclusive_scan(const int* cnt, int* start, int B, int* warp_sums) {
+constexpr int kBodyThreads = 512;
+
+// Exclusive block scan of cnt[0..B) into start[0..B] (start[B] = total); cur = start.
+__device__ void block_exclusive_scan(const int* cnt, int* start, int* cur, int B, int* warp_sums) {
   const int tid = threadIdx.x, nt = blockDim.x;
   const int chunk = (B + nt - 1) / nt;
   const int lo = min(B, tid * chunk), hi = min(B, lo + chunk);
   int local = 0;
   for (int k = lo; k < hi; ++k) local += cnt[k];
-  // warp inclusive scan
   const int lane = tid & 31, wid = tid >> 5;
   int v = local;
 #pragma unroll
@@ -218,22 +231,45 @@ __device__ void block_exclusive_scan(const int* cnt, int* start, int B, int* war
   __syncthreads();
   if (wid == 0) {
     const int nw = (nt + 31) >> 5;
-    int s = lane < nw ? warp_sums[lane] : 0;
+    int sum = lane < nw ? warp_sums[lane] : 0;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      const int t = __shfl_up_sync(0xffffffffu, s, o);
-      if (lane >= o) s += t;
+      const int t = __shfl_up_sync(0xffffffffu, sum, o);
+      if (lane >= o) sum += t;
     }
-    if (lane < nw) warp_sums[lane] = s;
+    if (lane < nw) warp_sums[lane] = sum;
   }
   __syncthreads();
   int run = v - local + (wid > 0 ? warp_sums[wid - 1] : 0);
   for (int k = lo; k < hi; ++k) {
     start[k] = run;
+    cur[k] = run;
     run += cnt[k];
   }
   if (tid == nt - 1) start[B] = run;
-  __syncthreads();
+}
+
+// interpolation of node values to the markers, LN lanes per (marker, component):
+// lane l sums its contiguous quarter of the stencil in order, the quarters are then
+// combined in a fixed pattern, so the result is deterministic.
+template <typename T, int S, int LN>
+__device__ __forceinline__ T interp_group(const T* W, const int* key, const T* nodes, int m) {
+  const int sub = threadIdx.x & (LN - 1);
+  constexpr int PER = S / LN;
+  T acc = T(0);
+#pragma unroll
+  for (int j = 0; j < PER; ++j) {
+    const int s = sub * PER + j;
+    const T t = W[m * S + s] * nodes[key[m * S + s]];
+    acc = j == 0 ? t : acc + t;
+  }
+  if constexpr (LN > 1) {
+    const unsigned lane = threadIdx.x & 31;
+    const unsigned mask = ((1u << LN) - 1u) << (lane & ~(unsigned)(LN - 1));
+#pragma unroll
+    for (int o = LN / 2; o >= 1; o >>= 1) acc = acc + __shfl_down_sync(mask, acc, o, LN);
+  }
+  return acc;
 }
 
 // One CTA advances one 2-D rigid body by one step: marker positions from the body
@@ -241,12 +277,16 @@ __device__ void block_exclusive_scan(const int* cnt, int* start, int B, int* war
 // interpolation of u from f at the touched nodes, the multi-direct-forcing iterations,
 // the force window for the grid kernel, the total force and the Newmark update.
 // The CSR keeps every node's contributions in increasing (marker, stencil point) order,
-// so all sums follow the reference's order and no floating-point atomics are used.
-template <typename T>
-__global__ void __launch_bounds__(1024) k_body2d(const BodyParams<T> B) {
+// the order of the reference's scatter-add; no floating-point atomics are used.
+// The last MDF iteration only adds its force step: its spread and interpolation feed a
+// marker velocity that the reference computes and then discards (ib/mdf.py:57-64).
+template <typename T, int R>
+__global__ void __launch_bounds__(kBodyThreads) k_body2d(const BodyParams<T> B) {
+  constexpr int WD = 2 * R, S = WD * WD;
+  constexpr int LN = S >= 16 ? 4 : 1;
   extern __shared__ __align__(16) unsigned char smem[];
   const int tid = threadIdx.x, nt = blockDim.x;
-  const int M = B.M, w = 2 * B.radius, S = w * w, P = M * S;
+  const int M = B.M, P = M * S;
   const int Bcap = B.cap_x * B.cap_y;
   T* X = (T*)smem;
   T* Y = X + M;
@@ -254,17 +294,18 @@ __global__ void __launch_bounds__(1024) k_body2d(const BodyParams<T> B) {
   T* U = W + P;
   T* Fs = U + 2 * M;
   T* Ft = Fs + 2 * M;
-  T* nu = Ft + 2 * M;      // node u / node force: [2][Bcap]
-  T* nv = nu + 2 * Bcap;   // spread accumulators:  [2][Bcap]
+  T* nu = Ft + 2 * M;      // node u: [2][Bcap]
+  T* nv = nu + 2 * Bcap;   // node force: [2][Bcap]
   int* key = (int*)(nv + 2 * Bcap);
   int* sorted = key + P;
   int* cnt = sorted + P;
   int* start = cnt + Bcap;
-  int* misc = start + Bcap + 1;  // [0..3] bbox, [4..35] warp sums
+  int* cur = start + Bcap + 1;
+  int* misc = cur + Bcap;  // [0..3] bbox, [4..35] warp sums
 
-  T a[3], v[3], d[3];
+  T a[2], v[2], d[2];
 #pragma unroll
-  for (int c = 0; c < 3; ++c) {
+  for (int c = 0; c < 2; ++c) {
     a[c] = B.state[c];
     v[c] = B.state[3 + c];
     d[c] = B.state[6 + c];
@@ -272,20 +313,20 @@ __global__ void __launch_bounds__(1024) k_body2d(const BodyParams<T> B) {
   if (tid == 0) {
     misc[0] = INT_MAX; misc[1] = INT_MIN; misc[2] = INT_MAX; misc[3] = INT_MIN;
   }
+  for (int k = tid; k < Bcap; k += nt) cnt[k] = 0;
+  __syncthreads();
   // markers follow the body (dyn.py:68-81)
   for (int m = tid; m < M; m += nt) {
-    X[m] = B.X0[m] + d[0];
-    Y[m] = B.Y0[m] + d[1];
-  }
-  __syncthreads();
-  for (int m = tid; m < M; m += nt) {
-    const int fx = ifloor(X[m]), fy = ifloor(Y[m]);
+    const T xm = B.X0[m] + d[0], ym = B.Y0[m] + d[1];
+    X[m] = xm;
+    Y[m] = ym;
+    const int fx = ifloor(xm), fy = ifloor(ym);
     atomicMin(&misc[0], fx); atomicMax(&misc[1], fx);
     atomicMin(&misc[2], fy); atomicMax(&misc[3], fy);
   }
   __syncthreads();
-  const int bx0 = misc[0] - B.radius + 1, by0 = misc[2] - B.radius + 1;
-  const int BW = misc[1] - misc[0] + w, BH = misc[3] - misc[2] + w;
+  const int bx0 = misc[0] - R + 1, by0 = misc[2] - R + 1;
+  const int BW = misc[1] - misc[0] + WD, BH = misc[3] - misc[2] + WD;
   const bool bad = BW > B.cap_x || BH > B.cap_y || bx0 < 0 || by0 < 0 || bx0 + BW > B.nx || by0 + BH > B.ny;
   if (bad) {
     if (tid == 0) {
@@ -295,30 +336,25 @@ __global__ void __launch_bounds__(1024) k_body2d(const BodyParams<T> B) {
     return;
   }
   const int NB = BW * BH;
-  for (int k = tid; k < NB; k += nt) cnt[k] = 0;
-  __syncthreads();
   // stencil (ib/stencil.py:7-51) with bounding-box-local node keys
   for (int p = tid; p < P; p += nt) {
     const int m = p / S, k = p - m * S;
-    const int ox = k / w - B.radius + 1, oy = k % w - B.radius + 1;
-    const int sx = ifloor(X[m]) + ox, sy = ifloor(Y[m]) + oy;
+    const int sx = ifloor(X[m]) + k / WD - R + 1, sy = ifloor(Y[m]) + k % WD - R + 1;
     W[p] = delta(B.kernel, (T)sx - X[m]) * delta(B.kernel, (T)sy - Y[m]);
     const int kk = (sx - bx0) * BH + (sy - by0);
     key[p] = kk;
     atomicAdd(&cnt[kk], 1);
   }
   __syncthreads();
-  block_exclusive_scan(cnt, start, NB, misc + 4);
-  for (int k = tid; k < NB; k += nt) cnt[k] = 0;
+  block_exclusive_scan(cnt, start, cur, NB, misc + 4);
   __syncthreads();
-  for (int p = tid; p < P; p += nt) {
-    const int kk = key[p];
-    sorted[start[kk] + atomicAdd(&cnt[kk], 1)] = p;
-  }
+  for (int p = tid; p < P; p += nt) sorted[atomicAdd(&cur[key[p]], 1)] = p;
   __syncthreads();
   // order each node's pairs by pair id (= the reference's scatter order) and read u there
+  const int64_t n = (int64_t)B.nx * B.ny;
   for (int k = tid; k < NB; k += nt) {
     const int lo = start[k], hi = start[k + 1];
+    if (hi == lo) continue;
     for (int i = lo + 1; i < hi; ++i) {
       const int val = sorted[i];
       int j = i - 1;
@@ -328,63 +364,54 @@ __global__ void __launch_bounds__(1024) k_body2d(const BodyParams<T> B) {
       }
       sorted[j + 1] = val;
     }
-    if (hi > lo) {
-      const int gx = bx0 + k / BH, gy = by0 + k % BH;
-      const int64_t n = (int64_t)B.nx * B.ny;
-      const int64_t pn = (int64_t)gx * B.ny + gy;
-      T fl[9];
+    const int64_t pn = (int64_t)(bx0 + k / BH) * B.ny + (by0 + k % BH);
+    T fl[9];
 #pragma unroll
-      for (int i = 0; i < 9; ++i) fl[i] = B.fin[i * n + pn];
-      T r, uu[3];
-      macro(L9{}, fl, r, uu);
-      nu[k] = uu[0];
-      nu[Bcap + k] = uu[1];
-    }
+    for (int i = 0; i < 9; ++i) fl[i] = __ldg(B.fin + i * n + pn);
+    T r, uu[3];
+    macro(L9{}, fl, r, uu);
+    nu[k] = uu[0];
+    nu[Bcap + k] = uu[1];
   }
   __syncthreads();
   // U = interpolate(u) and the first force step (ib/mdf.py:38-48); target = body velocity
-  for (int q = tid; q < 2 * M; q += nt) {
-    const int m = q >> 1, c = q & 1;
-    T acc = T(0);
-    for (int s = 0; s < S; ++s) {
-      const T t = W[m * S + s] * nu[c * Bcap + key[m * S + s]];
-      acc = s == 0 ? t : acc + t;
+  for (int t = tid; t < 2 * M * LN; t += nt) {
+    const int q = t / LN, m = q >> 1, c = q & 1;
+    const T acc = interp_group<T, S, LN>(W, key, nu + c * Bcap, m);
+    if ((t & (LN - 1)) == 0) {
+      U[q] = acc;
+      const T d2 = B.ds_arr ? B.ds_arr[m] * T(2) : B.ds2_scalar;
+      const T fs = (v[c] - acc) * d2;
+      Fs[q] = fs;
+      Ft[q] = B.n_iter > 0 ? fs : T(0);
     }
-    U[q] = acc;
-    const T d2 = B.ds_arr ? B.ds_arr[m] * T(2) : B.ds2_scalar;
-    const T fs = (v[c] - acc) * d2;
-    Fs[q] = fs;
-    Ft[q] = B.n_iter > 0 ? fs : T(0);
   }
   __syncthreads();
-  for (int it = 0; it < B.n_iter; ++it) {
+  for (int it = 0; it + 1 < B.n_iter; ++it) {
     // 0.5 * spread(F_step) at the touched nodes (ib/mdf.py:50-51)
     for (int k = tid; k < NB; k += nt) {
       const int lo = start[k], hi = start[k + 1];
       if (hi == lo) continue;
-#pragma unroll
-      for (int c = 0; c < 2; ++c) {
-        T acc = T(0);
-        for (int i = lo; i < hi; ++i) {
-          const int p = sorted[i];
-          const T t = Fs[(p / S) * 2 + c] * W[p];
-          acc = i == lo ? t : acc + t;
-        }
-        nv[c * Bcap + k] = acc * T(0.5);
+      T a0 = T(0), a1 = T(0);
+      for (int i = lo; i < hi; ++i) {
+        const int p = sorted[i];
+        const int m = p / S;
+        const T w = W[p];
+        const T t0 = Fs[2 * m] * w, t1 = Fs[2 * m + 1] * w;
+        a0 = i == lo ? t0 : a0 + t0;
+        a1 = i == lo ? t1 : a1 + t1;
       }
+      nv[k] = a0 * T(0.5);
+      nv[Bcap + k] = a1 * T(0.5);
     }
     __syncthreads();
-    const bool last = it == B.n_iter - 1;
-    for (int q = tid; q < 2 * M; q += nt) {
-      const int m = q >> 1, c = q & 1;
-      T acc = T(0);
-      for (int s = 0; s < S; ++s) {
-        const T t = W[m * S + s] * nv[c * Bcap + key[m * S + s]];
-        acc = s == 0 ? t : acc + t;
-      }
-      const T uq = U[q] + acc;
-      U[q] = uq;
-      if (!last) {
+    // U += interpolate(0.5 spread); next force step (ib/mdf.py:41-52)
+    for (int t = tid; t < 2 * M * LN; t += nt) {
+      const int q = t / LN, m = q >> 1, c = q & 1;
+      const T acc = interp_group<T, S, LN>(W, key, nv + c * Bcap, m);
+      if ((t & (LN - 1)) == 0) {
+        const T uq = U[q] + acc;
+        U[q] = uq;
         const T d2 = B.ds_arr ? B.ds_arr[m] * T(2) : B.ds2_scalar;
         const T fs = (v[c] - uq) * d2;
         Fs[q] = fs;
@@ -396,16 +423,17 @@ __global__ void __launch_bounds__(1024) k_body2d(const BodyParams<T> B) {
   // g = spread(F_total) over the window (ib/mdf.py:60-62); zero where no marker reaches
   for (int k = tid; k < NB; k += nt) {
     const int lo = start[k], hi = start[k + 1];
-#pragma unroll
-    for (int c = 0; c < 2; ++c) {
-      T acc = T(0);
-      for (int i = lo; i < hi; ++i) {
-        const int p = sorted[i];
-        const T t = Ft[(p / S) * 2 + c] * W[p];
-        acc = i == lo ? t : acc + t;
-      }
-      B.gw[c * NB + k] = acc;
+    T a0 = T(0), a1 = T(0);
+    for (int i = lo; i < hi; ++i) {
+      const int p = sorted[i];
+      const int m = p / S;
+      const T w = W[p];
+      const T t0 = Ft[2 * m] * w, t1 = Ft[2 * m + 1] * w;
+      a0 = i == lo ? t0 : a0 + t0;
+      a1 = i == lo ? t1 : a1 + t1;
     }
+    B.gw[k] = a0;
+    B.gw[NB + k] = a1;
   }
   if (tid == 0) {
     B.meta[META_OX] = bx0; B.meta[META_OY] = by0; B.meta[META_OZ] = 0;
@@ -437,38 +465,154 @@ __global__ void __launch_bounds__(1024) k_body2d(const BodyParams<T> B) {
   }
 }
 
-// u over a fixed window (3-D fixed body): u_win[d][cell] from f
-template <class L, typename T>
-__global__ void k_window_u(const T* __restrict__ fin, int nx, int ny, int nz, const int* __restrict__ meta,
-                           T* __restrict__ uw) {
-  const int ex = meta[META_WX], ey = meta[META_WY], ez = meta[META_WZ];
-  const int cells = ex * ey * ez;
-  const int64_t n = (int64_t)nx * ny * nz;
-  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < cells; c += gridDim.x * blockDim.x) {
-    const int wx = c / (ey * ez), wy = (c / ez) % ey, wz = c % ez;
-    const int64_t pn = ((int64_t)(meta[META_OX] + wx) * ny + (meta[META_OY] + wy)) * nz + (meta[META_OZ] + wz);
-    T fl[L::Q];
-#pragma unroll
-    for (int i = 0; i < L::Q; ++i) fl[i] = fin[i * n + pn];
-    T r, uu[3] = {T(0), T(0), T(0)};
-    macro(L{}, fl, r, uu);
-#pragma unroll
-    for (int d = 0; d < L::D; ++d) uw[d * cells + c] = uu[d];
+template <typename T>
+static size_t body2d_smem(int M, int R, int Bcap) {
+  const int S = 4 * R * R, P = M * S;
+  return sizeof(T) * (8 * (size_t)M + P + 4 * (size_t)Bcap) + sizeof(int) * (2 * (size_t)P + 3 * (size_t)Bcap + 1 + 40);
+}
+
+template <typename T>
+static cudaError_t body2d_attr(int R, int smem) {
+  switch (R) {
+    case 1: return cudaFuncSetAttribute(k_body2d<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    case 2: return cudaFuncSetAttribute(k_body2d<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    default: return cudaFuncSetAttribute(k_body2d<T, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   }
 }
 
-// total force of a fixed body: h = sum_m marker_force[m] in marker order
 template <typename T>
-__global__ void k_body_force(const T* __restrict__ mf, int M, int C, T* state, T* force_hist) {
-  const int c = threadIdx.x;
-  if (c >= 3) return;
-  T h = T(0);
-  if (c < C) {
-    h = mf[c];
-    for (int m = 1; m < M; ++m) h = h + mf[m * C + c];
+static void body2d_launch(int R, size_t smem, cudaStream_t st, const BodyParams<T>& P) {
+  switch (R) {
+    case 1: k_body2d<T, 1><<<1, kBodyThreads, smem, st>>>(P); break;
+    case 2: k_body2d<T, 2><<<1, kBodyThreads, smem, st>>>(P); break;
+    default: k_body2d<T, 3><<<1, kBodyThreads, smem, st>>>(P); break;
   }
-  state[9 + c] = h;
-  if (force_hist) force_hist[c] = h;
+}
+
+// ------------------------------------------------------------------ body kernels (3-D fixed)
+// The stencil of a fixed body never moves, so its (node, pair) CSR is built once; each
+// step then runs node-parallel and marker-parallel kernels over the compacted node list.
+
+// u at the touched nodes (vivsim/lbm3d/basic.py:90-106)
+template <class L, typename T>
+__global__ void k_static_node_u(const T* __restrict__ fin, int nx, int ny, int nz, const int* __restrict__ meta,
+                                const int32_t* __restrict__ node_cell, int U, T* __restrict__ nu) {
+  const int ey = meta[META_WY], ez = meta[META_WZ];
+  const int ox = meta[META_OX], oy = meta[META_OY], oz = meta[META_OZ];
+  const int64_t n = (int64_t)nx * ny * nz;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < U; k += gridDim.x * blockDim.x) {
+    const int cell = node_cell[k];
+    const int wx = cell / (ey * ez), wy = (cell / ez) % ey, wz = cell % ez;
+    const int64_t pn = ((int64_t)(ox + wx) * ny + (oy + wy)) * nz + (oz + wz);
+    T fl[L::Q];
+#pragma unroll
+    for (int i = 0; i < L::Q; ++i) fl[i] = __ldg(fin + i * n + pn);
+    T r, uu[3] = {T(0), T(0), T(0)};
+    macro(L{}, fl, r, uu);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) nu[d * U + k] = uu[d];
+  }
+}
+
+// One warp per marker: U (+)= sum_s W nodes[uid] per component, lanes over the stencil,
+// shuffle-reduced in a fixed tree; then F_step = (v_body - U) 2 ds, F_total (ib/mdf.py:38-52).
+template <typename T>
+__global__ void k_static_marker(int first, int use_step, const T* __restrict__ W, const int32_t* __restrict__ pair_uid,
+                                int M, int S, const T* __restrict__ nodes, int U, const T* __restrict__ state,
+                                const T* __restrict__ ds, T ds_scalar, T* __restrict__ Ua, T* __restrict__ Fs,
+                                T* __restrict__ Ft) {
+  const int lane = threadIdx.x & 31;
+  const int m = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (m >= M) return;
+  T acc[3] = {T(0), T(0), T(0)};
+  bool firstterm = true;
+  for (int s = lane; s < S; s += 32) {
+    const int64_t q = (int64_t)m * S + s;
+    const T w = W[q];
+    const int id = pair_uid[q];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const T t = w * nodes[c * U + id];
+      acc[c] = firstterm ? t : acc[c] + t;
+    }
+    firstterm = false;
+  }
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) acc[c] = acc[c] + __shfl_down_sync(0xffffffffu, acc[c], o);
+  if (lane == 0) {
+    const T d2 = (ds ? ds[m] : ds_scalar) * T(2);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const int64_t q = (int64_t)m * 3 + c;
+      const T u = first ? acc[c] : Ua[q] + acc[c];
+      Ua[q] = u;
+      const T fs = (state[3 + c] - u) * d2;
+      Fs[q] = fs;
+      Ft[q] = first ? (use_step ? fs : T(0)) : Ft[q] + fs;
+    }
+  }
+}
+
+// Node-parallel spread in pair order: out[c][k] = scale * sum F[m(p)][c] W[p].  With
+// gw != null the sums land in the force window at node_cell[k] instead (scale 1), and
+// block 0 then also forms the total force h = sum_m(-F_total) (dyn.py:126-136).
+template <typename T>
+__global__ void k_static_spread(const int32_t* __restrict__ seg, const int32_t* __restrict__ sids,
+                                const int32_t* __restrict__ node_cell, const T* __restrict__ W,
+                                const T* __restrict__ F, int U, int S, T scale, T* __restrict__ out, T* gw, int cells,
+                                int M, T* state, T* force_hist) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < U; k += gridDim.x * blockDim.x) {
+    const int lo = seg[k], hi = seg[k + 1];
+    T a[3] = {T(0), T(0), T(0)};
+    for (int i = lo; i < hi; ++i) {
+      const int p = sids[i];
+      const int m = p / S;
+      const T w = W[p];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const T t = F[m * 3 + c] * w;
+        a[c] = i == lo ? t : a[c] + t;
+      }
+    }
+    if (gw) {
+      const int cell = node_cell[k];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) gw[c * cells + cell] = a[c];
+    } else {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) out[c * U + k] = a[c] * scale;
+    }
+  }
+  if (!gw || blockIdx.x != 0) return;
+  __shared__ T red[3][256];
+  const int tid = threadIdx.x;
+  for (int c = 0; c < 3; ++c) {
+    T acc = T(0);
+    for (int m = tid; m < M; m += blockDim.x) acc = m == tid ? -F[m * 3 + c] : acc + (-F[m * 3 + c]);
+    red[c][tid] = acc;
+  }
+  __syncthreads();
+  for (int o = blockDim.x / 2; o >= 1; o >>= 1) {
+    if (tid < o)
+      for (int c = 0; c < 3; ++c) red[c][tid] = red[c][tid] + red[c][tid + o];
+    __syncthreads();
+  }
+  if (tid < 3) {
+    state[9 + tid] = red[tid][0];
+    if (force_hist) force_hist[tid] = red[tid][0];
+  }
+}
+
+__global__ void k_compact_csr(const int32_t* __restrict__ skeys, const int32_t* __restrict__ head,
+                              const int32_t* __restrict__ uid, int64_t P, int32_t* __restrict__ node_cell,
+                              int32_t* __restrict__ seg) {
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < P; p += (int64_t)gridDim.x * blockDim.x)
+    if (head[p]) {
+      node_cell[uid[p]] = skeys[p];
+      seg[uid[p]] = (int32_t)p;
+    }
 }
 
 template <typename T>
@@ -508,15 +652,19 @@ struct vs_body_plan {
   void* d_state;  // 12 values
   void* d_gw;     // window force (C, cells)
   int* d_meta;
-  // 3-D fixed body
+  // 3-D fixed body: stencil and its compacted CSR (built once)
   void* d_W;
   int32_t* d_I;
-  void* d_uw;
-  void* d_target;
-  void* d_mf;
-  void* d_ws;
+  void* d_ws;       // CSR workspace (holds the sorted pair ids and pair -> node ids)
   size_t ws_bytes;
-  int csr_ready;
+  int32_t* sids;    // views into d_ws
+  int32_t* pair_uid;
+  int32_t* d_node_cell;
+  int32_t* d_seg;
+  int U;            // touched nodes
+  void* d_nu;       // 3 x U node velocity
+  void* d_nv;       // 3 x U node force step
+  void* d_mk;       // U, F_step, F_total: 3 x (3 M)
   size_t smem;
   double nm[9];  // k1, k2, c1, c2, dt, damping, stiffness, den, area
 };
@@ -533,8 +681,8 @@ static void free_lattice(vs_lattice_plan* p) {
 
 static void free_body(vs_body_plan* b) {
   if (!b) return;
-  void* ptrs[] = {b->d_X0, b->d_ds, b->d_state, b->d_gw, b->d_meta, b->d_W, b->d_I, b->d_uw, b->d_target, b->d_mf,
-                  b->d_ws};
+  void* ptrs[] = {b->d_X0, b->d_ds, b->d_state, b->d_gw, b->d_meta, b->d_W, b->d_I, b->d_ws, b->d_node_cell,
+                  b->d_seg, b->d_nu, b->d_nv, b->d_mk};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   delete b;
@@ -640,7 +788,6 @@ static int enqueue_body(vs_body_plan* B, const vs_lattice_plan* LP, const void* 
       P.ds_arr = (const T*)B->d_ds;
       P.ds2_scalar = (T)B->cfg.ds_scalar * T(2);
       P.M = B->M;
-      P.radius = B->cfg.radius;
       P.kernel = B->cfg.kernel;
       P.n_iter = B->cfg.n_iter;
       P.cap_x = B->cap[0];
@@ -652,25 +799,36 @@ static int enqueue_body(vs_body_plan* B, const vs_lattice_plan* LP, const void* 
       for (int c = 0; c < 3; ++c) P.free_dof[c] = B->cfg.free_dof[c];
       P.k1 = (T)B->nm[0]; P.k2 = (T)B->nm[1]; P.c1 = (T)B->nm[2]; P.c2 = (T)B->nm[3]; P.dt = (T)B->nm[4];
       P.damp = (T)B->nm[5]; P.stiff = (T)B->nm[6]; P.den = (T)B->nm[7]; P.area = (T)B->nm[8];
-      k_body2d<T><<<1, 1024, B->smem, st>>>(P);
+      body2d_launch<T>(B->cfg.radius, B->smem, st, P);
       VS_CHECK_LAUNCH("vs_step body kernel");
       return VS_OK;
     });
   }
-  // 3-D fixed body: static stencil over a fixed window, CSR built once
+  // 3-D fixed body: static stencil and CSR; node- and marker-parallel kernels
   return dispatch(LP->cfg.q, dtype, [&](auto l, auto t) -> int {
     using L = decltype(l);
     using T = typename decltype(t)::type;
+    const int U = B->U, M = B->M, S = B->S;
     const int cells = B->cap[0] * B->cap[1] * B->cap[2];
-    k_window_u<L, T><<<grid_for(cells, 256), 256, 0, st>>>((const T*)fin, LP->cfg.nx, LP->cfg.ny, LP->cfg.nz,
-                                                           B->d_meta, (T*)B->d_uw);
-    VS_CHECK_LAUNCH("vs_step window u");
-    int rc = ib_mdf_run(dtype, B->csr_ready != 0, B->d_uw, 3, cells, B->d_W, B->d_I, B->M, B->S, B->d_target,
-                        B->d_ds, B->cfg.ds_scalar, B->cfg.n_iter, B->d_gw, B->d_mf, B->d_ws, B->ws_bytes, st);
-    if (rc) return rc;
-    B->csr_ready = 1;
-    k_body_force<T><<<1, 32, 0, st>>>((const T*)B->d_mf, B->M, 3, (T*)B->d_state, (T*)force_hist);
-    VS_CHECK_LAUNCH("vs_step body force");
+    T* Ua = (T*)B->d_mk;
+    T* Fs = Ua + 3 * M;
+    T* Ft = Fs + 3 * M;
+    const T ds2 = (T)B->cfg.ds_scalar;
+    const unsigned gn = grid_for(U, 128), gm = grid_for((int64_t)M * 32, 128);
+    k_static_node_u<L, T><<<gn, 128, 0, st>>>((const T*)fin, LP->cfg.nx, LP->cfg.ny, LP->cfg.nz, B->d_meta,
+                                               B->d_node_cell, U, (T*)B->d_nu);
+    k_static_marker<T><<<gm, 128, 0, st>>>(1, B->cfg.n_iter > 0, (const T*)B->d_W, B->pair_uid, M, S,
+                                           (const T*)B->d_nu, U, (const T*)B->d_state, (const T*)B->d_ds, ds2, Ua, Fs,
+                                           Ft);
+    for (int it = 0; it + 1 < B->cfg.n_iter; ++it) {
+      k_static_spread<T><<<gn, 128, 0, st>>>(B->d_seg, B->sids, B->d_node_cell, (const T*)B->d_W, Fs, U, S, T(0.5),
+                                             (T*)B->d_nv, nullptr, cells, M, nullptr, nullptr);
+      k_static_marker<T><<<gm, 128, 0, st>>>(0, 1, (const T*)B->d_W, B->pair_uid, M, S, (const T*)B->d_nv, U,
+                                             (const T*)B->d_state, (const T*)B->d_ds, ds2, Ua, Fs, Ft);
+    }
+    k_static_spread<T><<<gn, 256, 0, st>>>(B->d_seg, B->sids, B->d_node_cell, (const T*)B->d_W, Ft, U, S, T(1),
+                                           nullptr, (T*)B->d_gw, cells, M, (T*)B->d_state, (T*)force_hist);
+    VS_CHECK_LAUNCH("vs_step fixed-body kernels");
     return VS_OK;
   });
 }
@@ -681,13 +839,17 @@ static int enqueue_grid(const vs_lattice_plan* LP, const vs_body_plan* B, const 
   int rc = dispatch(c.q, c.dtype, [&](auto l, auto t) -> int {
     using L = decltype(l);
     using T = typename decltype(t)::type;
-    const StepParams<L, T> P = make_step_params<L, T>(LP, B, fin, fout);
-    const unsigned grid = grid_for(LP->n, 256);
+    StepParams<L, T> P = make_step_params<L, T>(LP, B, fin, fout);
+    // threads along the contiguous axis (y in 2-D, z in 3-D)
+    const int nlast = L::D == 2 ? c.ny : c.nz;
+    const int tb = nlast >= 256 ? 256 : (nlast >= 128 ? 128 : ((nlast + 31) / 32) * 32);
+    P.chunks = (nlast + tb - 1) / tb;
+    const dim3 grid(L::D == 2 ? P.chunks : P.chunks * c.ny, c.nx);
     switch (c.collision) {
-      case VS_COLLIDE_BGK: k_step<L, T, VS_COLLIDE_BGK><<<grid, 256, 0, st>>>(P); break;
-      case VS_COLLIDE_KBC: k_step<L, T, VS_COLLIDE_KBC><<<grid, 256, 0, st>>>(P); break;
-      case VS_COLLIDE_REG: k_step<L, T, VS_COLLIDE_REG><<<grid, 256, 0, st>>>(P); break;
-      default: k_step<L, T, VS_COLLIDE_MRT><<<grid, 256, 0, st>>>(P); break;
+      case VS_COLLIDE_BGK: k_step<L, T, VS_COLLIDE_BGK><<<grid, tb, 0, st>>>(P); break;
+      case VS_COLLIDE_KBC: k_step<L, T, VS_COLLIDE_KBC><<<grid, tb, 0, st>>>(P); break;
+      case VS_COLLIDE_REG: k_step<L, T, VS_COLLIDE_REG><<<grid, tb, 0, st>>>(P); break;
+      default: k_step<L, T, VS_COLLIDE_MRT><<<grid, tb, 0, st>>>(P); break;
     }
     VS_CHECK_LAUNCH("vs_step grid kernel");
     return VS_OK;
@@ -717,6 +879,8 @@ int vs_lattice_plan_create(const vs_lattice_cfg* cfg, vs_lattice_plan** out) {
              "grid %d x %d x %d too small (>= 4 per axis; nz = 1 for D2Q9)", cfg->nx, cfg->ny, cfg->nz);
   const int64_t n = (int64_t)cfg->nx * cfg->ny * nz;
   VS_REQUIRE(n < (1ll << 31), "grid of %lld nodes too large for 32-bit node indices", (long long)n);
+  VS_REQUIRE(cfg->nx <= 65535 && (cfg->q == 9 || (int64_t)cfg->ny * ((nz + 127) / 128) < (1ll << 31)),
+             "grid extent too large for the launch geometry");
   VS_REQUIRE(cfg->collision >= VS_COLLIDE_BGK && cfg->collision <= VS_COLLIDE_REG, "bad collision %d",
              cfg->collision);
   VS_REQUIRE(cfg->forcing >= VS_FORCE_NONE && cfg->forcing <= VS_FORCE_GUO_MRT, "bad forcing %d", cfg->forcing);
@@ -872,9 +1036,8 @@ int vs_body_plan_create(const vs_body_cfg* cfg, const vs_lattice_plan* lattice, 
   b->nm[7] = cfg->mass + b->nm[2] * cfg->damping + b->nm[3] * cfg->stiffness;
   b->nm[8] = cfg->added_mass_area;
   if (cfg->dim == 2) {
-    const int P = M * b->S;
     const int Bcap = b->cap[0] * b->cap[1];
-    b->smem = ts * (2 * M + P + 6 * M + 4 * Bcap) + sizeof(int) * (2 * P + 2 * Bcap + 1 + 40);
+    b->smem = ts == 8 ? body2d_smem<double>(M, cfg->radius, Bcap) : body2d_smem<float>(M, cfg->radius, Bcap);
     int dev = 0, optin = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
@@ -883,8 +1046,7 @@ int vs_body_plan_create(const vs_body_cfg* cfg, const vs_lattice_plan* lattice, 
       set_error("body of %d markers needs %zu bytes of shared memory (> %d available)", M, b->smem, optin);
       return VS_ERR_UNSUPPORTED;
     }
-    e = ts == 8 ? cudaFuncSetAttribute(k_body2d<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->smem)
-                : cudaFuncSetAttribute(k_body2d<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->smem);
+    e = ts == 8 ? body2d_attr<double>(cfg->radius, (int)b->smem) : body2d_attr<float>(cfg->radius, (int)b->smem);
     if (e != cudaSuccess) return fail(e);
   } else {
     // fixed 3-D body: stencil once over a fixed window around the markers
@@ -923,23 +1085,34 @@ int vs_body_plan_create(const vs_body_cfg* cfg, const vs_lattice_plan* lattice, 
       free_body(b);
       return rc;
     }
-    if ((e = cudaFree(b->d_gw)) != cudaSuccess) return fail(e);
+    e = cudaFree(b->d_gw);
+    b->d_gw = nullptr;
+    if (e != cudaSuccess) return fail(e);
     if ((e = cudaMalloc(&b->d_gw, ts * 3 * wcells)) != cudaSuccess) return fail(e);
-    if ((e = cudaMalloc(&b->d_uw, ts * 3 * wcells)) != cudaSuccess) return fail(e);
-    if ((e = cudaMalloc(&b->d_target, ts * 3 * M)) != cudaSuccess) return fail(e);
-    if ((e = cudaMemset(b->d_target, 0, ts * 3 * M)) != cudaSuccess) return fail(e);
-    if ((e = cudaMalloc(&b->d_mf, ts * 3 * M)) != cudaSuccess) return fail(e);
+    if ((e = cudaMemset(b->d_gw, 0, ts * 3 * wcells)) != cudaSuccess) return fail(e);
     b->ws_bytes = vs_ib_workspace_bytes(M, b->S);
     if ((e = cudaMalloc(&b->d_ws, b->ws_bytes)) != cudaSuccess) return fail(e);
-    // build the (static) pair CSR once, on a zero velocity window
-    if ((e = cudaMemset(b->d_uw, 0, ts * 3 * wcells)) != cudaSuccess) return fail(e);
-    rc = ib_mdf_run(cfg->dtype, false, b->d_uw, 3, wcells, b->d_W, b->d_I, M, b->S, b->d_target, b->d_ds,
-                    cfg->ds_scalar, cfg->n_iter, b->d_gw, b->d_mf, b->d_ws, b->ws_bytes, nullptr);
+    IbCsrView v{};
+    rc = ib_build_csr(b->d_I, P, wcells, b->d_ws, M, b->S, &v, nullptr);
     if (rc) {
       free_body(b);
       return rc;
     }
-    b->csr_ready = 1;
+    int32_t last_uid = 0;
+    if ((e = cudaMemcpy(&last_uid, v.uid + (P - 1), sizeof(int32_t), cudaMemcpyDeviceToHost)) != cudaSuccess)
+      return fail(e);
+    b->U = last_uid + 1;
+    b->sids = v.sids;
+    b->pair_uid = v.pair_uid;
+    if ((e = cudaMalloc(&b->d_node_cell, sizeof(int32_t) * b->U)) != cudaSuccess) return fail(e);
+    if ((e = cudaMalloc(&b->d_seg, sizeof(int32_t) * (b->U + 1))) != cudaSuccess) return fail(e);
+    k_compact_csr<<<grid_for(P, 256), 256>>>(v.skeys, v.head, v.uid, P, b->d_node_cell, b->d_seg);
+    const int32_t endP = (int32_t)P;
+    if ((e = cudaMemcpy(b->d_seg + b->U, &endP, sizeof(int32_t), cudaMemcpyHostToDevice)) != cudaSuccess)
+      return fail(e);
+    if ((e = cudaMalloc(&b->d_nu, ts * 3 * b->U)) != cudaSuccess) return fail(e);
+    if ((e = cudaMalloc(&b->d_nv, ts * 3 * b->U)) != cudaSuccess) return fail(e);
+    if ((e = cudaMalloc(&b->d_mk, ts * 9 * M)) != cudaSuccess) return fail(e);
     if ((e = cudaDeviceSynchronize()) != cudaSuccess) return fail(e);
   }
   *out = b;
