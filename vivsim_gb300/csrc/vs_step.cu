@@ -33,6 +33,9 @@ struct StepParams {
   T* fout;
   int nx, ny, nz, n;
   int chunks;                    // blocks along the contiguous axis (3-D)
+  int off[3], ext[3];            // launch domain: nodes off .. off + ext - 1
+  int skip;                      // 1: nodes inside box[] are left to another launch
+  int box[6];                    // x0, x1, y0, y1, z0, z1 (half-open)
   CollideParams<T> cp;
   int forcing;
   int has_g0;
@@ -54,17 +57,22 @@ struct StepParams {
 template <class L, typename T, int COLL>
 __global__ void __launch_bounds__(256) k_step(const __grid_constant__ StepParams<L, T> P) {
   constexpr int Q = L::Q;
-  const int x = blockIdx.y;
+  const int x = P.off[0] + blockIdx.y;
   int y, z;
   if constexpr (L::D == 2) {
-    y = blockIdx.x * blockDim.x + threadIdx.x;
+    const int ly = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ly >= P.ext[1]) return;
+    y = P.off[1] + ly;
     z = 0;
-    if (y >= P.ny) return;
   } else {
-    y = blockIdx.x / P.chunks;
-    z = (blockIdx.x - y * P.chunks) * blockDim.x + threadIdx.x;
-    if (z >= P.nz) return;
+    const int by = blockIdx.x / P.chunks;
+    const int lz = (blockIdx.x - by * P.chunks) * blockDim.x + threadIdx.x;
+    if (lz >= P.ext[2]) return;
+    y = P.off[1] + by;
+    z = P.off[2] + lz;
   }
+  if (P.skip && x >= P.box[0] && x < P.box[1] && y >= P.box[2] && y < P.box[3] && z >= P.box[4] && z < P.box[5])
+    return;
   const int syz = P.ny * P.nz;
   const int p = x * syz + y * P.nz + z;
 
@@ -203,6 +211,7 @@ struct BodyParams {
   T ds2_scalar;  // 2 * ds as the reference forms it: (T)ds * 2
   int M, kernel, n_iter;
   int cap_x, cap_y;
+  int box[4];  // the window must stay inside x0..x1, y0..y1 (half-open)
   T* state;  // a[3], v[3], d[3], h[3]
   T* gw;
   int* meta;
@@ -213,13 +222,13 @@ struct BodyParams {
 
 constexpr int kBodyThreads = 512;
 
-// Exclusive block scan of cnt[0..B) into start[0..B] (start[B] = total); cur = start.
-__device__ void block_exclusive_scan(const int* cnt, int* start, int* cur, int B, int* warp_sums) {
+// Exclusive block scan of v[0..B) into out[0..B] (out[B] = total).
+__device__ void block_exclusive_scan(const int* v_in, int* out, int B, int* warp_sums) {
   const int tid = threadIdx.x, nt = blockDim.x;
   const int chunk = (B + nt - 1) / nt;
   const int lo = min(B, tid * chunk), hi = min(B, lo + chunk);
   int local = 0;
-  for (int k = lo; k < hi; ++k) local += cnt[k];
+  for (int k = lo; k < hi; ++k) local += v_in[k];
   const int lane = tid & 31, wid = tid >> 5;
   int v = local;
 #pragma unroll
@@ -242,25 +251,24 @@ __device__ void block_exclusive_scan(const int* cnt, int* start, int* cur, int B
   __syncthreads();
   int run = v - local + (wid > 0 ? warp_sums[wid - 1] : 0);
   for (int k = lo; k < hi; ++k) {
-    start[k] = run;
-    cur[k] = run;
-    run += cnt[k];
+    out[k] = run;
+    run += v_in[k];
   }
-  if (tid == nt - 1) start[B] = run;
+  if (tid == nt - 1) out[B] = run;
 }
 
 // interpolation of node values to the markers, LN lanes per (marker, component):
-// lane l sums its contiguous quarter of the stencil in order, the quarters are then
+// lane l sums its contiguous share of the stencil in order, the shares are then
 // combined in a fixed pattern, so the result is deterministic.
 template <typename T, int S, int LN>
-__device__ __forceinline__ T interp_group(const T* W, const int* key, const T* nodes, int m) {
+__device__ __forceinline__ T interp_group(const T* W, const int* slot, const T* nodes, int m) {
   const int sub = threadIdx.x & (LN - 1);
   constexpr int PER = S / LN;
   T acc = T(0);
 #pragma unroll
   for (int j = 0; j < PER; ++j) {
     const int s = sub * PER + j;
-    const T t = W[m * S + s] * nodes[key[m * S + s]];
+    const T t = W[m * S + s] * nodes[slot[m * S + s]];
     acc = j == 0 ? t : acc + t;
   }
   if constexpr (LN > 1) {
@@ -276,7 +284,7 @@ __device__ __forceinline__ T interp_group(const T* W, const int* key, const T* n
 // displacement, stencil weights, a counting-sort CSR of (node, pair) in shared memory,
 // interpolation of u from f at the touched nodes, the multi-direct-forcing iterations,
 // the force window for the grid kernel, the total force and the Newmark update.
-// The CSR keeps every node's contributions in increasing (marker, stencil point) order,
+// Each touched node keeps its contributions in increasing (marker, stencil point) order,
 // the order of the reference's scatter-add; no floating-point atomics are used.
 // The last MDF iteration only adds its force step: its spread and interpolation feed a
 // marker velocity that the reference computes and then discards (ib/mdf.py:57-64).
@@ -294,14 +302,16 @@ __global__ void __launch_bounds__(kBodyThreads) k_body2d(const BodyParams<T> B) 
   T* U = W + P;
   T* Fs = U + 2 * M;
   T* Ft = Fs + 2 * M;
-  T* nu = Ft + 2 * M;      // node u: [2][Bcap]
-  T* nv = nu + 2 * Bcap;   // node force: [2][Bcap]
-  int* key = (int*)(nv + 2 * Bcap);
-  int* sorted = key + P;
-  int* cnt = sorted + P;
-  int* start = cnt + Bcap;
-  int* cur = start + Bcap + 1;
-  int* misc = cur + Bcap;  // [0..3] bbox, [4..35] warp sums
+  T* nu = Ft + 2 * M;      // per touched node: u [2][Bcap]
+  T* nv = nu + 2 * Bcap;   // per touched node: 0.5 spread(F_step) [2][Bcap]
+  int* key = (int*)(nv + 2 * Bcap);  // pair -> window cell
+  int* slot = key + P;               // pair -> touched-node slot
+  int* sorted = slot + P;            // pairs grouped by touched node, in pair order
+  int* cnt = sorted + P;             // per cell: pair count | (1 << 16) if touched
+  int* off = cnt + Bcap;             // exclusive scan of cnt (packed)
+  int* tcell = off + Bcap + 1;       // touched slot -> cell
+  int* tstart = tcell + Bcap;        // touched slot -> first sorted position (+ end)
+  int* misc = tstart + Bcap + 1;     // [0..3] bbox, [4..35] warp sums
 
   T a[2], v[2], d[2];
 #pragma unroll
@@ -327,7 +337,8 @@ __global__ void __launch_bounds__(kBodyThreads) k_body2d(const BodyParams<T> B) 
   __syncthreads();
   const int bx0 = misc[0] - R + 1, by0 = misc[2] - R + 1;
   const int BW = misc[1] - misc[0] + WD, BH = misc[3] - misc[2] + WD;
-  const bool bad = BW > B.cap_x || BH > B.cap_y || bx0 < 0 || by0 < 0 || bx0 + BW > B.nx || by0 + BH > B.ny;
+  const bool bad = BW > B.cap_x || BH > B.cap_y || bx0 < B.box[0] || by0 < B.box[2] || bx0 + BW > B.box[1] ||
+                   by0 + BH > B.box[3];
   if (bad) {
     if (tid == 0) {
       B.meta[META_STATUS] = VS_ERR_RANGE;
@@ -336,48 +347,78 @@ __global__ void __launch_bounds__(kBodyThreads) k_body2d(const BodyParams<T> B) 
     return;
   }
   const int NB = BW * BH;
-  // stencil (ib/stencil.py:7-51) with bounding-box-local node keys
+  // stencil (ib/stencil.py:7-51) with window-local node keys; count pairs per cell and
+  // flag touched cells in the high half-word
   for (int p = tid; p < P; p += nt) {
     const int m = p / S, k = p - m * S;
     const int sx = ifloor(X[m]) + k / WD - R + 1, sy = ifloor(Y[m]) + k % WD - R + 1;
     W[p] = delta(B.kernel, (T)sx - X[m]) * delta(B.kernel, (T)sy - Y[m]);
     const int kk = (sx - bx0) * BH + (sy - by0);
     key[p] = kk;
+    atomicOr(&cnt[kk], 1 << 16);
     atomicAdd(&cnt[kk], 1);
   }
   __syncthreads();
-  block_exclusive_scan(cnt, start, cur, NB, misc + 4);
+  // one scan gives both the CSR offsets (low half) and the touched-node slots (high half)
+  block_exclusive_scan(cnt, off, NB, misc + 4);
   __syncthreads();
-  for (int p = tid; p < P; p += nt) sorted[atomicAdd(&cur[key[p]], 1)] = p;
-  __syncthreads();
-  // order each node's pairs by pair id (= the reference's scatter order) and read u there
-  const int64_t n = (int64_t)B.nx * B.ny;
+  const int NT = off[NB] >> 16;  // touched nodes
   for (int k = tid; k < NB; k += nt) {
-    const int lo = start[k], hi = start[k + 1];
-    if (hi == lo) continue;
-    for (int i = lo + 1; i < hi; ++i) {
-      const int val = sorted[i];
-      int j = i - 1;
-      while (j >= lo && sorted[j] > val) {
-        sorted[j + 1] = sorted[j];
-        --j;
-      }
-      sorted[j + 1] = val;
+    const int c = cnt[k];
+    if (c >> 16) {
+      const int j = off[k] >> 16;
+      tcell[j] = k;
+      tstart[j] = off[k] & 0xffff;
     }
-    const int64_t pn = (int64_t)(bx0 + k / BH) * B.ny + (by0 + k % BH);
-    T fl[9];
+    cnt[k] = off[k] & 0xffff;  // reused as the scatter cursor
+  }
+  if (tid == 0) tstart[NT] = P;
+  __syncthreads();
+  for (int p = tid; p < P; p += nt) {
+    const int kk = key[p];
+    sorted[atomicAdd(&cnt[kk], 1)] = p;
+    slot[p] = off[kk] >> 16;
+  }
+  __syncthreads();
+  // order each node's pairs by pair id, and read u there (four nodes per pass for ILP)
+  const int64_t n = (int64_t)B.nx * B.ny;
+  for (int base = 0; base < NT; base += 4 * nt) {
+    T fl[4][9];
+    int jj[4];
 #pragma unroll
-    for (int i = 0; i < 9; ++i) fl[i] = __ldg(B.fin + i * n + pn);
-    T r, uu[3];
-    macro(L9{}, fl, r, uu);
-    nu[k] = uu[0];
-    nu[Bcap + k] = uu[1];
+    for (int q = 0; q < 4; ++q) {
+      jj[q] = base + q * nt + tid;
+      if (jj[q] < NT) {
+        const int k = tcell[jj[q]];
+        const int64_t pn = (int64_t)(bx0 + k / BH) * B.ny + (by0 + k % BH);
+#pragma unroll
+        for (int i = 0; i < 9; ++i) fl[q][i] = __ldg(B.fin + i * n + pn);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      if (jj[q] >= NT) continue;
+      const int lo = tstart[jj[q]], hi = tstart[jj[q] + 1];
+      for (int i = lo + 1; i < hi; ++i) {
+        const int val = sorted[i];
+        int j = i - 1;
+        while (j >= lo && sorted[j] > val) {
+          sorted[j + 1] = sorted[j];
+          --j;
+        }
+        sorted[j + 1] = val;
+      }
+      T r, uu[3];
+      macro(L9{}, fl[q], r, uu);
+      nu[jj[q]] = uu[0];
+      nu[Bcap + jj[q]] = uu[1];
+    }
   }
   __syncthreads();
   // U = interpolate(u) and the first force step (ib/mdf.py:38-48); target = body velocity
   for (int t = tid; t < 2 * M * LN; t += nt) {
     const int q = t / LN, m = q >> 1, c = q & 1;
-    const T acc = interp_group<T, S, LN>(W, key, nu + c * Bcap, m);
+    const T acc = interp_group<T, S, LN>(W, slot, nu + c * Bcap, m);
     if ((t & (LN - 1)) == 0) {
       U[q] = acc;
       const T d2 = B.ds_arr ? B.ds_arr[m] * T(2) : B.ds2_scalar;
@@ -389,9 +430,8 @@ __global__ void __launch_bounds__(kBodyThreads) k_body2d(const BodyParams<T> B) 
   __syncthreads();
   for (int it = 0; it + 1 < B.n_iter; ++it) {
     // 0.5 * spread(F_step) at the touched nodes (ib/mdf.py:50-51)
-    for (int k = tid; k < NB; k += nt) {
-      const int lo = start[k], hi = start[k + 1];
-      if (hi == lo) continue;
+    for (int j = tid; j < NT; j += nt) {
+      const int lo = tstart[j], hi = tstart[j + 1];
       T a0 = T(0), a1 = T(0);
       for (int i = lo; i < hi; ++i) {
         const int p = sorted[i];
@@ -401,14 +441,14 @@ __global__ void __launch_bounds__(kBodyThreads) k_body2d(const BodyParams<T> B) 
         a0 = i == lo ? t0 : a0 + t0;
         a1 = i == lo ? t1 : a1 + t1;
       }
-      nv[k] = a0 * T(0.5);
-      nv[Bcap + k] = a1 * T(0.5);
+      nv[j] = a0 * T(0.5);
+      nv[Bcap + j] = a1 * T(0.5);
     }
     __syncthreads();
     // U += interpolate(0.5 spread); next force step (ib/mdf.py:41-52)
     for (int t = tid; t < 2 * M * LN; t += nt) {
       const int q = t / LN, m = q >> 1, c = q & 1;
-      const T acc = interp_group<T, S, LN>(W, key, nv + c * Bcap, m);
+      const T acc = interp_group<T, S, LN>(W, slot, nv + c * Bcap, m);
       if ((t & (LN - 1)) == 0) {
         const T uq = U[q] + acc;
         U[q] = uq;
@@ -422,7 +462,12 @@ __global__ void __launch_bounds__(kBodyThreads) k_body2d(const BodyParams<T> B) 
   }
   // g = spread(F_total) over the window (ib/mdf.py:60-62); zero where no marker reaches
   for (int k = tid; k < NB; k += nt) {
-    const int lo = start[k], hi = start[k + 1];
+    B.gw[k] = T(0);
+    B.gw[NB + k] = T(0);
+  }
+  __syncthreads();
+  for (int j = tid; j < NT; j += nt) {
+    const int lo = tstart[j], hi = tstart[j + 1];
     T a0 = T(0), a1 = T(0);
     for (int i = lo; i < hi; ++i) {
       const int p = sorted[i];
@@ -432,6 +477,7 @@ __global__ void __launch_bounds__(kBodyThreads) k_body2d(const BodyParams<T> B) 
       a0 = i == lo ? t0 : a0 + t0;
       a1 = i == lo ? t1 : a1 + t1;
     }
+    const int k = tcell[j];
     B.gw[k] = a0;
     B.gw[NB + k] = a1;
   }
@@ -439,36 +485,48 @@ __global__ void __launch_bounds__(kBodyThreads) k_body2d(const BodyParams<T> B) 
     B.meta[META_OX] = bx0; B.meta[META_OY] = by0; B.meta[META_OZ] = 0;
     B.meta[META_WX] = BW; B.meta[META_WY] = BH; B.meta[META_WZ] = 1;
   }
-  // total force on the body h = sum(-F_total) (dyn.py:126-136), added mass, Newmark (dyn.py:5-51)
-  if (tid < 2) {
-    const int c = tid;
-    T h = -Ft[c];
-    for (int m = 1; m < M; ++m) h = h + (-Ft[m * 2 + c]);
-    h = h + a[c] * B.area;
-    T an = a[c], vn = v[c], dn = d[c];
-    if (B.free_dof[c]) {
-      const T v1 = v[c] + B.k1 * a[c];
-      const T v2 = (d[c] + B.dt * v[c]) + B.k2 * a[c];
-      an = ((h - B.damp * v1) - B.stiff * v2) / B.den;
-      vn = B.c1 * an + v1;
-      dn = B.c2 * an + v2;
+  // total force h = sum_m(-F_total) (dyn.py:126-136) by warp 0 in a fixed tree, added
+  // mass h += a A (vortex_induced_vibration.py:136), Newmark update (dyn.py:5-51)
+  if (tid < 32) {
+    T h[2];
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      T acc = T(0);
+      for (int m = tid; m < M; m += 32) acc = m == tid ? -Ft[2 * m + c] : acc + (-Ft[2 * m + c]);
+#pragma unroll
+      for (int o = 16; o >= 1; o >>= 1) acc = acc + __shfl_down_sync(0xffffffffu, acc, o);
+      h[c] = acc;
     }
-    B.state[c] = an;
-    B.state[3 + c] = vn;
-    B.state[6 + c] = dn;
-    B.state[9 + c] = h;
-    if (B.force_hist) B.force_hist[c] = h;
-  }
-  if (tid == 2) {
-    B.state[9 + 2] = T(0);
-    if (B.force_hist) B.force_hist[2] = T(0);
+    const T h0 = __shfl_sync(0xffffffffu, h[0], 0), h1 = __shfl_sync(0xffffffffu, h[1], 0);
+    if (tid < 2) {
+      const int c = tid;
+      const T hh = (c == 0 ? h0 : h1) + a[c] * B.area;
+      T an = a[c], vn = v[c], dn = d[c];
+      if (B.free_dof[c]) {
+        const T v1 = v[c] + B.k1 * a[c];
+        const T v2 = (d[c] + B.dt * v[c]) + B.k2 * a[c];
+        an = ((hh - B.damp * v1) - B.stiff * v2) / B.den;
+        vn = B.c1 * an + v1;
+        dn = B.c2 * an + v2;
+      }
+      B.state[c] = an;
+      B.state[3 + c] = vn;
+      B.state[6 + c] = dn;
+      B.state[9 + c] = hh;
+      if (B.force_hist) B.force_hist[c] = hh;
+    }
+    if (tid == 2) {
+      B.state[9 + 2] = T(0);
+      if (B.force_hist) B.force_hist[2] = T(0);
+    }
   }
 }
 
 template <typename T>
 static size_t body2d_smem(int M, int R, int Bcap) {
   const int S = 4 * R * R, P = M * S;
-  return sizeof(T) * (8 * (size_t)M + P + 4 * (size_t)Bcap) + sizeof(int) * (2 * (size_t)P + 3 * (size_t)Bcap + 1 + 40);
+  return sizeof(T) * (8 * (size_t)M + P + 4 * (size_t)Bcap) +
+         sizeof(int) * (3 * (size_t)P + 4 * (size_t)Bcap + 2 + 40);
 }
 
 template <typename T>
@@ -667,6 +725,9 @@ struct vs_body_plan {
   void* d_mk;       // U, F_step, F_total: 3 x (3 M)
   size_t smem;
   double nm[9];  // k1, k2, c1, c2, dt, damping, stiffness, den, area
+  int box[6];    // region the body's window never leaves (half-open x0,x1,y0,y1,z0,z1)
+  cudaStream_t side;
+  cudaEvent_t ev_fork, ev_join;
 };
 
 static size_t dsize(int dtype) { return dtype == VS_F64 ? 8 : 4; }
@@ -685,6 +746,9 @@ static void free_body(vs_body_plan* b) {
                   b->d_seg, b->d_nu, b->d_nv, b->d_mk};
   for (void* q : ptrs)
     if (q) cudaFree(q);
+  if (b->ev_fork) cudaEventDestroy(b->ev_fork);
+  if (b->ev_join) cudaEventDestroy(b->ev_join);
+  if (b->side) cudaStreamDestroy(b->side);
   delete b;
 }
 
@@ -792,6 +856,7 @@ static int enqueue_body(vs_body_plan* B, const vs_lattice_plan* LP, const void* 
       P.n_iter = B->cfg.n_iter;
       P.cap_x = B->cap[0];
       P.cap_y = B->cap[1];
+      for (int q = 0; q < 4; ++q) P.box[q] = B->box[q];
       P.state = (T*)B->d_state;
       P.gw = (T*)B->d_gw;
       P.meta = B->d_meta;
@@ -833,18 +898,32 @@ static int enqueue_body(vs_body_plan* B, const vs_lattice_plan* LP, const void* 
   });
 }
 
+// mode 0: every node; 1: every node outside the body's box (no force window read);
+// 2: the nodes of the body's box only
 static int enqueue_grid(const vs_lattice_plan* LP, const vs_body_plan* B, const void* fin, void* fout,
-                        cudaStream_t st) {
+                        cudaStream_t st, int mode = 0) {
   const vs_lattice_cfg& c = LP->cfg;
   int rc = dispatch(c.q, c.dtype, [&](auto l, auto t) -> int {
     using L = decltype(l);
     using T = typename decltype(t)::type;
     StepParams<L, T> P = make_step_params<L, T>(LP, B, fin, fout);
+    const int full[3] = {c.nx, c.ny, c.nz};
+    for (int d = 0; d < 3; ++d) {
+      P.off[d] = mode == 2 ? B->box[2 * d] : 0;
+      P.ext[d] = mode == 2 ? B->box[2 * d + 1] - B->box[2 * d] : full[d];
+      P.box[2 * d] = B ? B->box[2 * d] : 0;
+      P.box[2 * d + 1] = B ? B->box[2 * d + 1] : 0;
+    }
+    P.skip = mode == 1;
+    if (mode == 1) {  // outside the box no node reads the force window
+      P.gw = nullptr;
+      P.meta = nullptr;
+    }
     // threads along the contiguous axis (y in 2-D, z in 3-D)
-    const int nlast = L::D == 2 ? c.ny : c.nz;
+    const int nlast = L::D == 2 ? P.ext[1] : P.ext[2];
     const int tb = nlast >= 256 ? 256 : (nlast >= 128 ? 128 : ((nlast + 31) / 32) * 32);
     P.chunks = (nlast + tb - 1) / tb;
-    const dim3 grid(L::D == 2 ? P.chunks : P.chunks * c.ny, c.nx);
+    const dim3 grid(L::D == 2 ? P.chunks : P.chunks * P.ext[1], P.ext[0]);
     switch (c.collision) {
       case VS_COLLIDE_BGK: k_step<L, T, VS_COLLIDE_BGK><<<grid, tb, 0, st>>>(P); break;
       case VS_COLLIDE_KBC: k_step<L, T, VS_COLLIDE_KBC><<<grid, tb, 0, st>>>(P); break;
@@ -857,13 +936,28 @@ static int enqueue_grid(const vs_lattice_plan* LP, const vs_body_plan* B, const 
   return rc;
 }
 
+// With a body, the body kernel(s) run on the plan's side stream while the grid kernel
+// updates every node outside the body's box; after the join a small grid launch updates
+// the box with the new force window.  Each (node, direction) destination of the push is
+// written by exactly one source node, so the two grid launches never write the same word.
 static int enqueue_step(const vs_lattice_plan* LP, vs_body_plan* B, const void* fin, void* fout, void* force_hist,
                         cudaStream_t st) {
+  int rc;
   if (B) {
-    int rc = enqueue_body(B, LP, fin, force_hist, st);
+    cudaError_t e = cudaEventRecord(B->ev_fork, st);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(B->side, B->ev_fork, 0);
+    if (e != cudaSuccess) return cuda_status(e, "vs_step fork");
+    rc = enqueue_body(B, LP, fin, force_hist, B->side);
     if (rc) return rc;
+    rc = enqueue_grid(LP, B, fin, fout, st, 1);
+    if (rc) return rc;
+    e = cudaEventRecord(B->ev_join, B->side);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(st, B->ev_join, 0);
+    if (e != cudaSuccess) return cuda_status(e, "vs_step join");
+    rc = enqueue_grid(LP, B, fin, fout, st, 2);
+  } else {
+    rc = enqueue_grid(LP, B, fin, fout, st, 0);
   }
-  int rc = enqueue_grid(LP, B, fin, fout, st);
   if (rc) return rc;
   return enqueue_bcs(LP, fout, st);
 }
@@ -991,6 +1085,33 @@ int vs_body_plan_create(const vs_body_cfg* cfg, const vs_lattice_plan* lattice, 
     }
   for (int d = 0; d < cfg->dim; ++d) b->cap[d] = (int)(floor(hi[d]) - floor(lo[d])) + w + 2;
   if (cfg->dim == 2) b->cap[2] = 1;
+  {
+    // region the window can reach: the initial stencil box, widened along free DOFs by the
+    // margin (default: one body extent) and by 2 nodes along every axis, clipped to the grid
+    const int nn[3] = {lattice->cfg.nx, lattice->cfg.ny, lattice->cfg.nz};
+    for (int d = 0; d < 3; ++d) {
+      if (d >= cfg->dim) {
+        b->box[2 * d] = 0;
+        b->box[2 * d + 1] = nn[d];
+        continue;
+      }
+      const int lo_n = (int)floor(lo[d]) - cfg->radius + 1, hi_n = (int)floor(hi[d]) + cfg->radius + 1;
+      int margin = 2;
+      if (cfg->moving && cfg->free_dof[d])
+        margin += cfg->window_margin > 0 ? cfg->window_margin : (hi_n - lo_n);
+      b->box[2 * d] = lo_n - margin < 0 ? 0 : lo_n - margin;
+      b->box[2 * d + 1] = hi_n + margin > nn[d] ? nn[d] : hi_n + margin;
+    }
+  }
+  {
+    cudaError_t es = cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking);
+    if (es == cudaSuccess) es = cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming);
+    if (es == cudaSuccess) es = cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming);
+    if (es != cudaSuccess) {
+      free_body(b);
+      return cuda_status(es, "vs_body_plan_create stream");
+    }
+  }
   cudaError_t e;
   if ((e = cudaMalloc(&b->d_X0, ts * M * 3)) != cudaSuccess) return fail(e);
   if ((e = cudaMemcpy(b->d_X0, hx.data(), ts * M * 3, cudaMemcpyHostToDevice)) != cudaSuccess) return fail(e);
@@ -1037,6 +1158,11 @@ int vs_body_plan_create(const vs_body_cfg* cfg, const vs_lattice_plan* lattice, 
   b->nm[8] = cfg->added_mass_area;
   if (cfg->dim == 2) {
     const int Bcap = b->cap[0] * b->cap[1];
+    if ((int64_t)M * b->S >= 65536 || Bcap >= 65536) {
+      free_body(b);
+      set_error("2-D body with %d markers (%d window cells) exceeds the single-CTA body kernel", M, Bcap);
+      return VS_ERR_UNSUPPORTED;
+    }
     b->smem = ts == 8 ? body2d_smem<double>(M, cfg->radius, Bcap) : body2d_smem<float>(M, cfg->radius, Bcap);
     int dev = 0, optin = 0;
     cudaGetDevice(&dev);
@@ -1062,6 +1188,10 @@ int vs_body_plan_create(const vs_body_cfg* cfg, const vs_lattice_plan* lattice, 
       }
     }
     int meta[META_N] = {org[0], org[1], org[2], b->cap[0], b->cap[1], b->cap[2], 0, 0};
+    for (int d = 0; d < 3; ++d) {
+      b->box[2 * d] = org[d];
+      b->box[2 * d + 1] = org[d] + b->cap[d];
+    }
     if ((e = cudaMemcpy(b->d_meta, meta, sizeof(meta), cudaMemcpyHostToDevice)) != cudaSuccess) return fail(e);
     const int64_t wcells = (int64_t)b->cap[0] * b->cap[1] * b->cap[2];
     const int64_t P = (int64_t)M * b->S;
