@@ -33,9 +33,12 @@ struct StepParams {
   T* fout;
   int nx, ny, nz, n;
   int chunks;                    // blocks along the contiguous axis (3-D)
-  int off[3], ext[3];            // launch domain: nodes off .. off + ext - 1
-  int skip;                      // 1: nodes inside box[] are left to another launch
-  int box[6];                    // x0, x1, y0, y1, z0, z1 (half-open)
+  int nreg;                      // 0: the whole grid; else the union of reg[0..nreg)
+  int reg[3][6];                 // regions x0, x1, y0, y1, z0, z1 (half-open)
+  int rowstart[4];               // first launch row (x plane) of each region
+  int skip_box;                  // nodes inside box[] are left to another launch
+  int box[6];
+  int skip_walls;                // the x = 0 and x = nx-1 planes are left to another launch
   CollideParams<T> cp;
   int forcing;
   int has_g0;
@@ -43,6 +46,8 @@ struct StepParams {
   T guo_scale;                   // 1 - omega / 2 (Guo-BGK)
   const T* gw;                   // IB force window (D, wx, wy, wz) or null
   const int* meta;               // window descriptor (device)
+  int n_lazy;                    // face boundaries of the previous step applied on load
+  WallArgs<T> lazy[2];
   int n_pre;                     // faces whose pre-stream populations are kept (bounce-back)
   int pre_loc[VS_MAX_BC];
   T* pre_buf[VS_MAX_BC];
@@ -54,31 +59,67 @@ struct StepParams {
 // in 3-D or the chunk of y in 2-D; threads run along the contiguous axis, so every load
 // and store of a warp covers 32 consecutive addresses.  Wrap-around offsets of the push
 // are per-block uniform except along the contiguous axis.
-template <class L, typename T, int COLL>
+template <class L, typename T, int COLL, bool WALLS>
 __global__ void __launch_bounds__(256) k_step(const __grid_constant__ StepParams<L, T> P) {
   constexpr int Q = L::Q;
-  const int x = P.off[0] + blockIdx.y;
-  int y, z;
-  if constexpr (L::D == 2) {
-    const int ly = blockIdx.x * blockDim.x + threadIdx.x;
-    if (ly >= P.ext[1]) return;
-    y = P.off[1] + ly;
-    z = 0;
+  int x, y, z;
+  if (P.nreg == 0) {
+    x = blockIdx.y;
+    if constexpr (L::D == 2) {
+      y = blockIdx.x * blockDim.x + threadIdx.x;
+      if (y >= P.ny) return;
+      z = 0;
+    } else {
+      y = blockIdx.x / P.chunks;
+      z = (blockIdx.x - y * P.chunks) * blockDim.x + threadIdx.x;
+      if (z >= P.nz) return;
+    }
   } else {
-    const int by = blockIdx.x / P.chunks;
-    const int lz = (blockIdx.x - by * P.chunks) * blockDim.x + threadIdx.x;
-    if (lz >= P.ext[2]) return;
-    y = P.off[1] + by;
-    z = P.off[2] + lz;
+    const int r = blockIdx.y;
+    const int g = (r >= P.rowstart[1]) + (r >= P.rowstart[2]);
+    const int* R = P.reg[g];
+    x = R[0] + (r - P.rowstart[g]);
+    if constexpr (L::D == 2) {
+      y = R[2] + blockIdx.x * blockDim.x + threadIdx.x;
+      if (y >= R[3]) return;
+      z = 0;
+    } else {
+      const int by = blockIdx.x / P.chunks;
+      y = R[2] + by;
+      z = R[4] + (blockIdx.x - by * P.chunks) * blockDim.x + threadIdx.x;
+      if (y >= R[3] || z >= R[5]) return;
+    }
   }
-  if (P.skip && x >= P.box[0] && x < P.box[1] && y >= P.box[2] && y < P.box[3] && z >= P.box[4] && z < P.box[5])
+  if (P.skip_box && x >= P.box[0] && x < P.box[1] && y >= P.box[2] && y < P.box[3] && z >= P.box[4] &&
+      z < P.box[5])
     return;
+  if (P.skip_walls && (x == 0 || x == P.nx - 1)) return;
   const int syz = P.ny * P.nz;
   const int p = x * syz + y * P.nz + z;
 
   T f[Q];
 #pragma unroll
   for (int i = 0; i < Q; ++i) f[i] = __ldg(P.fin + (size_t)i * P.n + p);
+
+  // the previous step's face boundaries, applied to the wall nodes as they are loaded
+  // (all of them on the x faces, so they touch disjoint nodes and commute)
+  if constexpr (WALLS) for (int k = 0; k < P.n_lazy; ++k) {
+    const WallArgs<T>& A = P.lazy[k];
+    const int a = loc_axis(A.loc), sg = loc_sign(A.loc);
+    const int coord = a == 0 ? x : (a == 1 ? y : z);
+    const int nn[3] = {P.nx, P.ny, P.nz};
+    if (coord != (sg > 0 ? 0 : nn[a] - 1)) continue;
+    T nb[Q], out[Q];
+    if (bc_needs_neighbor<L>(A.kind, A.mode)) {
+      const int stride = a == 0 ? syz : (a == 1 ? P.nz : 1);
+      const int pn = p + sg * stride;
+#pragma unroll
+      for (int i = 0; i < Q; ++i) nb[i] = __ldg(P.fin + (size_t)i * P.n + pn);
+    }
+    bc_node<L, T>(A, 0, f, nb, nullptr, out);
+#pragma unroll
+    for (int i = 0; i < Q; ++i) f[i] = out[i];
+  }
 
   T rho, u[3] = {T(0), T(0), T(0)};
   fast::macro<L>(f, rho, u);
@@ -222,13 +263,16 @@ struct BodyParams {
 
 constexpr int kBodyThreads = 512;
 
-// Exclusive block scan of v[0..B) into out[0..B] (out[B] = total).
-__device__ void block_exclusive_scan(const int* v_in, int* out, int B, int* warp_sums) {
+// Block scan over the window cells: cnt[k] pairs per cell -> CSR.  Writes, per cell,
+// the scatter cursor (first sorted position, into cnt[]) and the touched-node slot (or -1,
+// into cslot[]); per touched slot j its cell tcell[j] and first position tstart[j]
+// (tstart[NT] = total).  Returns the number of touched cells.
+__device__ int block_csr_scan(int* cnt, int* cslot, int* tcell, int* tstart, int B, int* warp_sums) {
   const int tid = threadIdx.x, nt = blockDim.x;
   const int chunk = (B + nt - 1) / nt;
   const int lo = min(B, tid * chunk), hi = min(B, lo + chunk);
-  int local = 0;
-  for (int k = lo; k < hi; ++k) local += v_in[k];
+  int local = 0;  // pairs in the low half-word, touched cells in the high one
+  for (int k = lo; k < hi; ++k) local += cnt[k] + (cnt[k] > 0 ? 65536 : 0);
   const int lane = tid & 31, wid = tid >> 5;
   int v = local;
 #pragma unroll
@@ -251,10 +295,21 @@ __device__ void block_exclusive_scan(const int* v_in, int* out, int B, int* warp
   __syncthreads();
   int run = v - local + (wid > 0 ? warp_sums[wid - 1] : 0);
   for (int k = lo; k < hi; ++k) {
-    out[k] = run;
-    run += v_in[k];
+    const int c = cnt[k];
+    const int pos = run & 0xffff, j = run >> 16;
+    cnt[k] = pos;
+    if (c > 0) {
+      cslot[k] = j;
+      tcell[j] = k;
+      tstart[j] = pos;
+    } else {
+      cslot[k] = -1;
+    }
+    run += c + (c > 0 ? 65536 : 0);
   }
-  if (tid == nt - 1) out[B] = run;
+  const int total = warp_sums[((nt + 31) >> 5) - 1];
+  if (tid == 0) tstart[total >> 16] = total & 0xffff;
+  return total >> 16;
 }
 
 // interpolation of node values to the markers, LN lanes per (marker, component):
@@ -280,12 +335,26 @@ __device__ __forceinline__ T interp_group(const T* W, const int* slot, const T* 
   return acc;
 }
 
+// asynchronous 4- or 8-byte global -> shared copy (completes at cp_async_wait_all)
+template <typename T>
+__device__ __forceinline__ void cp_async(T* dst, const T* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  if constexpr (sizeof(T) == 4)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 // One CTA advances one 2-D rigid body by one step: marker positions from the body
 // displacement, stencil weights, a counting-sort CSR of (node, pair) in shared memory,
 // interpolation of u from f at the touched nodes, the multi-direct-forcing iterations,
 // the force window for the grid kernel, the total force and the Newmark update.
 // Each touched node keeps its contributions in increasing (marker, stencil point) order,
 // the order of the reference's scatter-add; no floating-point atomics are used.
+// The populations of the whole window are copied to shared memory asynchronously as soon
+// as the window is known, so their latency hides behind the CSR construction.
 // The last MDF iteration only adds its force step: its spread and interpolation feed a
 // marker velocity that the reference computes and then discards (ib/mdf.py:57-64).
 template <typename T, int R>
@@ -296,22 +365,24 @@ __global__ void __launch_bounds__(kBodyThreads) k_body2d(const BodyParams<T> B) 
   const int tid = threadIdx.x, nt = blockDim.x;
   const int M = B.M, P = M * S;
   const int Bcap = B.cap_x * B.cap_y;
-  T* X = (T*)smem;
-  T* Y = X + M;
-  T* W = Y + M;
+  T* fwin = (T*)smem;             // window populations [9][Bcap]
+  T* wx = fwin + 9 * Bcap;        // per marker: 2R one-dimensional weights along x
+  T* wy = wx + WD * M;            //                              ... along y
+  T* W = wy + WD * M;
   T* U = W + P;
   T* Fs = U + 2 * M;
   T* Ft = Fs + 2 * M;
-  T* nu = Ft + 2 * M;      // per touched node: u [2][Bcap]
-  T* nv = nu + 2 * Bcap;   // per touched node: 0.5 spread(F_step) [2][Bcap]
+  T* nu = Ft + 2 * M;             // per touched node: u [2][Bcap]
+  T* nv = nu + 2 * Bcap;          // per touched node: 0.5 spread(F_step) [2][Bcap]
   int* key = (int*)(nv + 2 * Bcap);  // pair -> window cell
   int* slot = key + P;               // pair -> touched-node slot
   int* sorted = slot + P;            // pairs grouped by touched node, in pair order
-  int* cnt = sorted + P;             // per cell: pair count | (1 << 16) if touched
-  int* off = cnt + Bcap;             // exclusive scan of cnt (packed)
-  int* tcell = off + Bcap + 1;       // touched slot -> cell
+  int* cnt = sorted + P;             // per cell: pair count, then scatter cursor
+  int* cslot = cnt + Bcap;           // per cell: touched slot or -1
+  int* tcell = cslot + Bcap;         // touched slot -> cell
   int* tstart = tcell + Bcap;        // touched slot -> first sorted position (+ end)
-  int* misc = tstart + Bcap + 1;     // [0..3] bbox, [4..35] warp sums
+  int* fxy = tstart + Bcap + 1;      // per marker: floor(X), floor(Y)
+  int* misc = fxy + 2 * M;           // [0..3] bbox, [4..35] warp sums
 
   T a[2], v[2], d[2];
 #pragma unroll
@@ -325,14 +396,19 @@ __global__ void __launch_bounds__(kBodyThreads) k_body2d(const BodyParams<T> B) 
   }
   for (int k = tid; k < Bcap; k += nt) cnt[k] = 0;
   __syncthreads();
-  // markers follow the body (dyn.py:68-81)
-  for (int m = tid; m < M; m += nt) {
-    const T xm = B.X0[m] + d[0], ym = B.Y0[m] + d[1];
-    X[m] = xm;
-    Y[m] = ym;
-    const int fx = ifloor(xm), fy = ifloor(ym);
-    atomicMin(&misc[0], fx); atomicMax(&misc[1], fx);
-    atomicMin(&misc[2], fy); atomicMax(&misc[3], fy);
+  // markers follow the body (dyn.py:68-81); the tensor-product stencil weight
+  // kernel(sx - X) * kernel(sy - Y) (ib/stencil.py:44-47) is formed from the 2R one-dimensional
+  // values per axis, one thread per (marker, axis, offset)
+  for (int t = tid; t < M * 2 * WD; t += nt) {
+    const int m = t / (2 * WD), r = t - m * (2 * WD), ax = r / WD, o = r - ax * WD;
+    const T xm = (ax == 0 ? B.X0[m] : B.Y0[m]) + d[ax];
+    const int fx = ifloor(xm);
+    (ax == 0 ? wx : wy)[m * WD + o] = delta(B.kernel, (T)(fx + o - R + 1) - xm);
+    if (o == 0) {
+      fxy[2 * m + ax] = fx;
+      atomicMin(&misc[2 * ax], fx);
+      atomicMax(&misc[2 * ax + 1], fx);
+    }
   }
   __syncthreads();
   const int bx0 = misc[0] - R + 1, by0 = misc[2] - R + 1;
@@ -347,72 +423,52 @@ __global__ void __launch_bounds__(kBodyThreads) k_body2d(const BodyParams<T> B) 
     return;
   }
   const int NB = BW * BH;
-  // stencil (ib/stencil.py:7-51) with window-local node keys; count pairs per cell and
-  // flag touched cells in the high half-word
+  const int64_t n = (int64_t)B.nx * B.ny;
+  // start copying the window's populations (consumed after the CSR is built)
+  for (int k = tid; k < NB; k += nt) {
+    const int64_t pn = (int64_t)(bx0 + k / BH) * B.ny + (by0 + k % BH);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) cp_async(fwin + i * Bcap + k, B.fin + i * n + pn);
+  }
+  cp_async_commit();
+  // stencil (ib/stencil.py:7-51) with window-local node keys; pairs per cell
   for (int p = tid; p < P; p += nt) {
-    const int m = p / S, k = p - m * S;
-    const int sx = ifloor(X[m]) + k / WD - R + 1, sy = ifloor(Y[m]) + k % WD - R + 1;
-    W[p] = delta(B.kernel, (T)sx - X[m]) * delta(B.kernel, (T)sy - Y[m]);
-    const int kk = (sx - bx0) * BH + (sy - by0);
+    const int m = p / S, k = p - m * S, ix = k / WD, iy = k % WD;
+    W[p] = wx[m * WD + ix] * wy[m * WD + iy];
+    const int kk = (fxy[2 * m] + ix - R + 1 - bx0) * BH + (fxy[2 * m + 1] + iy - R + 1 - by0);
     key[p] = kk;
-    atomicOr(&cnt[kk], 1 << 16);
     atomicAdd(&cnt[kk], 1);
   }
   __syncthreads();
-  // one scan gives both the CSR offsets (low half) and the touched-node slots (high half)
-  block_exclusive_scan(cnt, off, NB, misc + 4);
-  __syncthreads();
-  const int NT = off[NB] >> 16;  // touched nodes
-  for (int k = tid; k < NB; k += nt) {
-    const int c = cnt[k];
-    if (c >> 16) {
-      const int j = off[k] >> 16;
-      tcell[j] = k;
-      tstart[j] = off[k] & 0xffff;
-    }
-    cnt[k] = off[k] & 0xffff;  // reused as the scatter cursor
-  }
-  if (tid == 0) tstart[NT] = P;
+  const int NT = block_csr_scan(cnt, cslot, tcell, tstart, NB, misc + 4);
   __syncthreads();
   for (int p = tid; p < P; p += nt) {
     const int kk = key[p];
     sorted[atomicAdd(&cnt[kk], 1)] = p;
-    slot[p] = off[kk] >> 16;
+    slot[p] = cslot[kk];
   }
+  cp_async_wait_all();
   __syncthreads();
-  // order each node's pairs by pair id, and read u there (four nodes per pass for ILP)
-  const int64_t n = (int64_t)B.nx * B.ny;
-  for (int base = 0; base < NT; base += 4 * nt) {
-    T fl[4][9];
-    int jj[4];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      jj[q] = base + q * nt + tid;
-      if (jj[q] < NT) {
-        const int k = tcell[jj[q]];
-        const int64_t pn = (int64_t)(bx0 + k / BH) * B.ny + (by0 + k % BH);
-#pragma unroll
-        for (int i = 0; i < 9; ++i) fl[q][i] = __ldg(B.fin + i * n + pn);
+  // order each node's pairs by pair id (= the reference's scatter order); u at the node
+  for (int j = tid; j < NT; j += nt) {
+    const int lo = tstart[j], hi = tstart[j + 1];
+    for (int i = lo + 1; i < hi; ++i) {
+      const int val = sorted[i];
+      int q = i - 1;
+      while (q >= lo && sorted[q] > val) {
+        sorted[q + 1] = sorted[q];
+        --q;
       }
+      sorted[q + 1] = val;
     }
+    const int k = tcell[j];
+    T fl[9];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      if (jj[q] >= NT) continue;
-      const int lo = tstart[jj[q]], hi = tstart[jj[q] + 1];
-      for (int i = lo + 1; i < hi; ++i) {
-        const int val = sorted[i];
-        int j = i - 1;
-        while (j >= lo && sorted[j] > val) {
-          sorted[j + 1] = sorted[j];
-          --j;
-        }
-        sorted[j + 1] = val;
-      }
-      T r, uu[3];
-      macro(L9{}, fl[q], r, uu);
-      nu[jj[q]] = uu[0];
-      nu[Bcap + jj[q]] = uu[1];
-    }
+    for (int i = 0; i < 9; ++i) fl[i] = fwin[i * Bcap + k];
+    T r, uu[3];
+    macro(L9{}, fl, r, uu);
+    nu[j] = uu[0];
+    nu[Bcap + j] = uu[1];
   }
   __syncthreads();
   // U = interpolate(u) and the first force step (ib/mdf.py:38-48); target = body velocity
@@ -462,22 +518,19 @@ __global__ void __launch_bounds__(kBodyThreads) k_body2d(const BodyParams<T> B) 
   }
   // g = spread(F_total) over the window (ib/mdf.py:60-62); zero where no marker reaches
   for (int k = tid; k < NB; k += nt) {
-    B.gw[k] = T(0);
-    B.gw[NB + k] = T(0);
-  }
-  __syncthreads();
-  for (int j = tid; j < NT; j += nt) {
-    const int lo = tstart[j], hi = tstart[j + 1];
+    const int j = cslot[k];
     T a0 = T(0), a1 = T(0);
-    for (int i = lo; i < hi; ++i) {
-      const int p = sorted[i];
-      const int m = p / S;
-      const T w = W[p];
-      const T t0 = Ft[2 * m] * w, t1 = Ft[2 * m + 1] * w;
-      a0 = i == lo ? t0 : a0 + t0;
-      a1 = i == lo ? t1 : a1 + t1;
+    if (j >= 0) {
+      const int lo = tstart[j], hi = tstart[j + 1];
+      for (int i = lo; i < hi; ++i) {
+        const int p = sorted[i];
+        const int m = p / S;
+        const T w = W[p];
+        const T t0 = Ft[2 * m] * w, t1 = Ft[2 * m + 1] * w;
+        a0 = i == lo ? t0 : a0 + t0;
+        a1 = i == lo ? t1 : a1 + t1;
+      }
     }
-    const int k = tcell[j];
     B.gw[k] = a0;
     B.gw[NB + k] = a1;
   }
@@ -525,8 +578,8 @@ __global__ void __launch_bounds__(kBodyThreads) k_body2d(const BodyParams<T> B) 
 template <typename T>
 static size_t body2d_smem(int M, int R, int Bcap) {
   const int S = 4 * R * R, P = M * S;
-  return sizeof(T) * (8 * (size_t)M + P + 4 * (size_t)Bcap) +
-         sizeof(int) * (3 * (size_t)P + 4 * (size_t)Bcap + 2 + 40);
+  return sizeof(T) * ((4 * (size_t)R + 6) * M + P + 13 * (size_t)Bcap) +
+         sizeof(int) * (3 * (size_t)P + 4 * (size_t)Bcap + 2 + 2 * (size_t)M + 40);
 }
 
 template <typename T>
@@ -691,6 +744,7 @@ struct vs_lattice_plan {
   void* pre_buf[VS_MAX_BC];  // bounce-back face buffers
   int bc_group[VS_MAX_BC];   // group id of each boundary op
   int n_groups;
+  int lazy_ok;               // all boundaries in one launch group and none needs pre-stream data
   // graph cache
   cudaGraphExec_t graph;
   const void* g_fa;
@@ -898,38 +952,70 @@ static int enqueue_body(vs_body_plan* B, const vs_lattice_plan* LP, const void* 
   });
 }
 
-// mode 0: every node; 1: every node outside the body's box (no force window read);
-// 2: the nodes of the body's box only
+// mode 0: every node.
+// mode 1: every node except the body's box and, with lazy_walls, the x = 0 / nx-1 planes
+//         (nodes outside the box read no force window).
+// mode 2: the body's box and, with lazy_walls, the x = 0 / nx-1 planes, whose populations
+//         first get the previous step's face boundaries.
 static int enqueue_grid(const vs_lattice_plan* LP, const vs_body_plan* B, const void* fin, void* fout,
-                        cudaStream_t st, int mode = 0) {
+                        cudaStream_t st, int mode = 0, bool lazy_walls = false) {
   const vs_lattice_cfg& c = LP->cfg;
   int rc = dispatch(c.q, c.dtype, [&](auto l, auto t) -> int {
     using L = decltype(l);
     using T = typename decltype(t)::type;
     StepParams<L, T> P = make_step_params<L, T>(LP, B, fin, fout);
-    const int full[3] = {c.nx, c.ny, c.nz};
-    for (int d = 0; d < 3; ++d) {
-      P.off[d] = mode == 2 ? B->box[2 * d] : 0;
-      P.ext[d] = mode == 2 ? B->box[2 * d + 1] - B->box[2 * d] : full[d];
-      P.box[2 * d] = B ? B->box[2 * d] : 0;
-      P.box[2 * d + 1] = B ? B->box[2 * d + 1] : 0;
-    }
-    P.skip = mode == 1;
+    P.nreg = 0;
+    P.skip_box = mode == 1 && B;
+    P.skip_walls = mode == 1 && lazy_walls;
+    for (int q = 0; q < 6; ++q) P.box[q] = B ? B->box[q] : 0;
+    P.n_lazy = 0;
     if (mode == 1) {  // outside the box no node reads the force window
       P.gw = nullptr;
       P.meta = nullptr;
     }
-    // threads along the contiguous axis (y in 2-D, z in 3-D)
-    const int nlast = L::D == 2 ? P.ext[1] : P.ext[2];
-    const int tb = nlast >= 256 ? 256 : (nlast >= 128 ? 128 : ((nlast + 31) / 32) * 32);
-    P.chunks = (nlast + tb - 1) / tb;
-    const dim3 grid(L::D == 2 ? P.chunks : P.chunks * P.ext[1], P.ext[0]);
-    switch (c.collision) {
-      case VS_COLLIDE_BGK: k_step<L, T, VS_COLLIDE_BGK><<<grid, tb, 0, st>>>(P); break;
-      case VS_COLLIDE_KBC: k_step<L, T, VS_COLLIDE_KBC><<<grid, tb, 0, st>>>(P); break;
-      case VS_COLLIDE_REG: k_step<L, T, VS_COLLIDE_REG><<<grid, tb, 0, st>>>(P); break;
-      default: k_step<L, T, VS_COLLIDE_MRT><<<grid, tb, 0, st>>>(P); break;
+    int rows = c.nx, ext_last = L::D == 2 ? c.ny : c.nz, ext_mid = c.ny;
+    if (mode == 2) {
+      int nr = 0;
+      auto add = [&](const int* R) {
+        for (int q = 0; q < 6; ++q) P.reg[nr][q] = R[q];
+        ++nr;
+      };
+      if (B) add(B->box);
+      if (lazy_walls) {
+        int w0[6] = {0, 1, 0, c.ny, 0, c.nz}, w1[6] = {c.nx - 1, c.nx, 0, c.ny, 0, c.nz};
+        if (!B || B->box[0] > 0) add(w0);
+        if (!B || B->box[1] < c.nx) add(w1);
+        for (int k = 0; k < c.n_bc && k < 2; ++k) P.lazy[P.n_lazy++] = wall_args_from_bc<T>(c.bc[k], LP, k);
+      }
+      P.nreg = nr;
+      rows = 0;
+      ext_last = 0;
+      ext_mid = 0;
+      rows = 0;
+      for (int g = 0; g < nr; ++g) {
+        P.rowstart[g] = rows;
+        rows += P.reg[g][1] - P.reg[g][0];
+        const int el = L::D == 2 ? P.reg[g][3] - P.reg[g][2] : P.reg[g][5] - P.reg[g][4];
+        ext_last = el > ext_last ? el : ext_last;
+        ext_mid = P.reg[g][3] - P.reg[g][2] > ext_mid ? P.reg[g][3] - P.reg[g][2] : ext_mid;
+      }
+      for (int g = nr; g < 4; ++g) P.rowstart[g] = 1 << 30;
+      if (nr == 0) return VS_OK;
     }
+    // threads along the contiguous axis (y in 2-D, z in 3-D)
+    const int tb = ext_last >= 256 ? 256 : (ext_last >= 128 ? 128 : ((ext_last + 31) / 32) * 32);
+    P.chunks = (ext_last + tb - 1) / tb;
+    const dim3 grid(L::D == 2 ? P.chunks : P.chunks * ext_mid, rows);
+    const bool walls = mode == 2 && lazy_walls;
+#define VS_LAUNCH_STEP(K)                                                              \
+  (walls ? k_step<L, T, K, true><<<grid, tb, 0, st>>>(P) : k_step<L, T, K, false><<<grid, tb, 0, st>>>(P))
+    switch (c.collision) {
+      case VS_COLLIDE_BGK: VS_LAUNCH_STEP(VS_COLLIDE_BGK); break;
+      case VS_COLLIDE_KBC: VS_LAUNCH_STEP(VS_COLLIDE_KBC); break;
+      case VS_COLLIDE_REG: VS_LAUNCH_STEP(VS_COLLIDE_REG); break;
+      default: VS_LAUNCH_STEP(VS_COLLIDE_MRT); break;
+    }
+#undef VS_LAUNCH_STEP
     VS_CHECK_LAUNCH("vs_step grid kernel");
     return VS_OK;
   });
@@ -940,8 +1026,10 @@ static int enqueue_grid(const vs_lattice_plan* LP, const vs_body_plan* B, const 
 // updates every node outside the body's box; after the join a small grid launch updates
 // the box with the new force window.  Each (node, direction) destination of the push is
 // written by exactly one source node, so the two grid launches never write the same word.
+// lazy_in: fin holds the previous step's populations before its face boundaries (they
+// are applied on load); bc_out: run the face kernels on fout (else the next step will).
 static int enqueue_step(const vs_lattice_plan* LP, vs_body_plan* B, const void* fin, void* fout, void* force_hist,
-                        cudaStream_t st) {
+                        cudaStream_t st, bool lazy_in = false, bool bc_out = true) {
   int rc;
   if (B) {
     cudaError_t e = cudaEventRecord(B->ev_fork, st);
@@ -949,17 +1037,32 @@ static int enqueue_step(const vs_lattice_plan* LP, vs_body_plan* B, const void* 
     if (e != cudaSuccess) return cuda_status(e, "vs_step fork");
     rc = enqueue_body(B, LP, fin, force_hist, B->side);
     if (rc) return rc;
-    rc = enqueue_grid(LP, B, fin, fout, st, 1);
+    rc = enqueue_grid(LP, B, fin, fout, st, 1, lazy_in);
     if (rc) return rc;
     e = cudaEventRecord(B->ev_join, B->side);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(st, B->ev_join, 0);
     if (e != cudaSuccess) return cuda_status(e, "vs_step join");
-    rc = enqueue_grid(LP, B, fin, fout, st, 2);
+    rc = enqueue_grid(LP, B, fin, fout, st, 2, lazy_in);
   } else {
-    rc = enqueue_grid(LP, B, fin, fout, st, 0);
+    rc = enqueue_grid(LP, B, fin, fout, st, 0, lazy_in);
   }
   if (rc) return rc;
-  return enqueue_bcs(LP, fout, st);
+  return bc_out ? enqueue_bcs(LP, fout, st) : VS_OK;
+}
+
+// Boundaries can be deferred to the next step's load when they all sit on one axis and
+// the body's box (whose nodes the body kernel reads) touches none of their walls.
+static bool lazy_boundaries(const vs_lattice_plan* LP, const vs_body_plan* B) {
+  if (!LP->lazy_ok || LP->cfg.n_bc == 0 || !B) return false;
+  for (int k = 0; k < LP->cfg.n_bc; ++k)
+    if (loc_axis(LP->cfg.bc[k].loc) != 0) return false;
+  const int nn[3] = {LP->cfg.nx, LP->cfg.ny, LP->cfg.nz};
+  for (int k = 0; k < LP->cfg.n_bc; ++k) {
+    const int a = loc_axis(LP->cfg.bc[k].loc);
+    const int wall = loc_sign(LP->cfg.bc[k].loc) > 0 ? 0 : nn[a] - 1;
+    if (wall >= B->box[2 * a] && wall < B->box[2 * a + 1]) return false;
+  }
+  return true;
 }
 
 extern "C" {
@@ -1026,6 +1129,9 @@ int vs_lattice_plan_create(const vs_lattice_cfg* cfg, vs_lattice_plan** out) {
     ++gsize;
   }
   p->n_groups = cfg->n_bc ? gid + 1 : 0;
+  p->lazy_ok = p->n_groups == 1;
+  for (int k = 0; k < cfg->n_bc; ++k)
+    if (cfg->bc[k].kind == VS_BC_BB || cfg->bc[k].kind == VS_BC_SPECULAR) p->lazy_ok = 0;
   *out = p;
   return VS_OK;
 }
@@ -1104,7 +1210,9 @@ int vs_body_plan_create(const vs_body_cfg* cfg, const vs_lattice_plan* lattice, 
     }
   }
   {
-    cudaError_t es = cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking);
+    int prio_lo = 0, prio_hi = 0;
+    cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
+    cudaError_t es = cudaStreamCreateWithPriority(&b->side, cudaStreamNonBlocking, prio_hi);
     if (es == cudaSuccess) es = cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming);
     if (es == cudaSuccess) es = cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming);
     if (es != cudaSuccess) {
@@ -1302,11 +1410,13 @@ int vs_run(const vs_lattice_plan* lattice, vs_body_plan* body, void* f_a, void* 
            void* stream) {
   VS_REQUIRE(lattice && f_a && f_b && f_a != f_b && n_steps >= 0, "vs_run: bad arguments");
   const size_t hs = 3 * dsize(lattice->cfg.dtype);
+  const bool lazy = lazy_boundaries(lattice, body);
   for (int s = 0; s < n_steps; ++s) {
     void* src = (s % 2 == 0) ? f_a : f_b;
     void* dst = (s % 2 == 0) ? f_b : f_a;
     void* hist = force_hist ? (void*)((char*)force_hist + hs * s) : nullptr;
-    int rc = enqueue_step(lattice, body, src, dst, hist, as_stream(stream));
+    int rc = enqueue_step(lattice, body, src, dst, hist, as_stream(stream), lazy && s > 0,
+                          !lazy || s == n_steps - 1);
     if (rc) return rc;
   }
   return VS_OK;
