@@ -181,6 +181,10 @@ typedef struct vs_bc {
 } vs_bc;
 
 #define VS_MAX_BC 8
+/* grid kernel variants: one thread per node reading populations straight from global
+ * memory, or a persistent kernel staging row tiles through shared memory with bulk
+ * (TMA) copies; AUTO picks the plain kernel */
+enum { VS_GRID_AUTO = 0, VS_GRID_PLAIN = 1, VS_GRID_TMA = 2 };
 typedef struct vs_lattice_cfg {
   int q;         /* 9 or 19 */
   int dtype;     /* VS_F32 / VS_F64 */
@@ -193,11 +197,16 @@ typedef struct vs_lattice_cfg {
   double mrt_fop[19 * 19]; /* q*q forcing operator when forcing == VS_FORCE_GUO_MRT   */
   int n_bc;                /* boundaries applied in this order after streaming      */
   vs_bc bc[VS_MAX_BC];
+  int variant;             /* grid kernel: VS_GRID_AUTO, VS_GRID_PLAIN or VS_GRID_TMA */
 } vs_lattice_cfg;
 
 typedef struct vs_lattice_plan vs_lattice_plan;
 int vs_lattice_plan_create(const vs_lattice_cfg* cfg, vs_lattice_plan** out);
 int vs_lattice_plan_destroy(vs_lattice_plan* plan);
+/* Device status of the plan's grid kernels: VS_OK, or VS_ERR_TIMEOUT when a bounded wait
+ * for a bulk copy gave up (that launch left its nodes unwritten).  Synchronises the stream;
+ * reset != 0 clears the word. */
+int vs_lattice_status(const vs_lattice_plan* plan, int reset, void* stream);
 
 /* Immersed body advanced by the IB step (dyn.py + ib/mdf.py).  Markers follow a rigid
  * 2-DOF translation d (get_markers_coords_2dof); DOFs with free[k] = 0 stay at zero. */

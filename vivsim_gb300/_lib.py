@@ -20,6 +20,7 @@ VS_BC_NEE, VS_BC_NEBB, VS_BC_EQ, VS_BC_BB, VS_BC_SPECULAR = range(5)
 VS_WALL_GIVEN, VS_WALL_VELOCITY, VS_WALL_PRESSURE, VS_WALL_FORCE_CORRECTED = range(4)
 VS_KERNEL_PESKIN3, VS_KERNEL_PESKIN4, VS_KERNEL_COSINE4 = range(3)
 VS_MAX_BC = 8
+VS_GRID_AUTO, VS_GRID_PLAIN, VS_GRID_TMA = 0, 1, 2
 
 LOCS = {"left": VS_LEFT, "right": VS_RIGHT, "bottom": VS_BOTTOM, "top": VS_TOP, "back": VS_BACK,
         "front": VS_FRONT}
@@ -49,7 +50,7 @@ class vs_lattice_cfg(C.Structure):
     _fields_ = [("q", C.c_int), ("dtype", C.c_int), ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
                 ("collision", C.c_int), ("omega", C.c_double), ("mrt_op", C.c_double * 361),
                 ("forcing", C.c_int), ("g_uniform", C.c_double * 3), ("mrt_fop", C.c_double * 361),
-                ("n_bc", C.c_int), ("bc", vs_bc * VS_MAX_BC)]
+                ("n_bc", C.c_int), ("bc", vs_bc * VS_MAX_BC), ("variant", C.c_int)]
 
 
 class vs_body_cfg(C.Structure):
@@ -105,6 +106,7 @@ _SIGS = {
     "vs_run": (_i, [_p, _p, _p, _p, _i, _p, _p]),
     "vs_run_graph": (_i, [_p, _p, _p, _p, _i, _p, _p]),
     "vs_step_grid_only": (_i, [_p, _p, _p, _p, _p]),
+    "vs_lattice_status": (_i, [_p, _i, _p]),
 }
 
 _LIB = None

@@ -129,14 +129,14 @@ def periodic2d(n=8192, collision="kbc", U0=0.05, nu=0.01, seed=4):
 CASES = {"cavity": cavity, "viv2d": viv2d, "sphere3d": sphere3d, "periodic2d": periodic2d}
 
 
-def build_solver(case, device="cuda"):
+def build_solver(case, device="cuda", variant="auto"):
     """LatticeStep, RigidBody (or None) and Simulation for a case dict."""
     import torch
 
     from . import solver as S
     bcs = [S.boundary(k, loc, mode=m, **kw) for (k, loc, m, kw) in case["boundaries"]]
     step = S.LatticeStep(case["q"], case["shape"], case["collision"], case["omega"], forcing=case["forcing"],
-                         boundaries=bcs)
+                         boundaries=bcs, variant=variant)
     body = None
     if case["body"] is not None:
         b = case["body"]

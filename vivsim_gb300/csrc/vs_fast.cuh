@@ -3,9 +3,9 @@
 // Same mathematics as vs_common.cuh (and the reference), rearranged for instruction
 // throughput: divisions by the lattice constants become multiplications by exact
 // reciprocals (x / cs2 -> 3 x, x / cs2^2 -> 9 x), per-population divisions by feq use one
-// correctly rounded reciprocal each, and the velocity uses one reciprocal of rho.  Each
-// rearrangement changes a result by at most about one unit in the last place; the
-// per-operator kernels keep the reference's exact operation sequence.
+// hardware reciprocal each (float) and the velocity uses one reciprocal of rho.  Each
+// rearrangement changes a result by about one unit in the last place; the per-operator
+// kernels keep the reference's exact operation sequence.
 #pragma once
 
 #include "vs_common.cuh"
@@ -13,10 +13,16 @@
 namespace vs {
 namespace fast {
 
+// float: one MUFU reciprocal (rcp.approx, within an ulp of 1/x); double: correctly rounded
 template <typename T>
 __device__ __forceinline__ T rcp(T x) {
-  if constexpr (sizeof(T) == 4) return __frcp_rn(x);
-  else return __drcp_rn(x);
+  if constexpr (sizeof(T) == 4) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+  } else {
+    return __drcp_rn(x);
+  }
 }
 
 template <class L, typename T>

@@ -55,51 +55,12 @@ struct StepParams {
   T fop[L::Q * L::Q];            // MRT forcing operator
 };
 
-// One thread per node.  blockIdx.y = x; blockIdx.x = (y, chunk of the contiguous axis)
-// in 3-D or the chunk of y in 2-D; threads run along the contiguous axis, so every load
-// and store of a warp covers 32 consecutive addresses.  Wrap-around offsets of the push
-// are per-block uniform except along the contiguous axis.
+// Per-node work of the grid kernels: (lazy face boundaries,) moments, equilibrium,
+// collision, forcing, push streaming.  f holds the node's loaded populations.
 template <class L, typename T, int COLL, bool WALLS>
-__global__ void __launch_bounds__(256) k_step(const __grid_constant__ StepParams<L, T> P) {
+__device__ __forceinline__ void step_node(const StepParams<L, T>& P, int x, int y, int z, int p, T* f) {
   constexpr int Q = L::Q;
-  int x, y, z;
-  if (P.nreg == 0) {
-    x = blockIdx.y;
-    if constexpr (L::D == 2) {
-      y = blockIdx.x * blockDim.x + threadIdx.x;
-      if (y >= P.ny) return;
-      z = 0;
-    } else {
-      y = blockIdx.x / P.chunks;
-      z = (blockIdx.x - y * P.chunks) * blockDim.x + threadIdx.x;
-      if (z >= P.nz) return;
-    }
-  } else {
-    const int r = blockIdx.y;
-    const int g = (r >= P.rowstart[1]) + (r >= P.rowstart[2]);
-    const int* R = P.reg[g];
-    x = R[0] + (r - P.rowstart[g]);
-    if constexpr (L::D == 2) {
-      y = R[2] + blockIdx.x * blockDim.x + threadIdx.x;
-      if (y >= R[3]) return;
-      z = 0;
-    } else {
-      const int by = blockIdx.x / P.chunks;
-      y = R[2] + by;
-      z = R[4] + (blockIdx.x - by * P.chunks) * blockDim.x + threadIdx.x;
-      if (y >= R[3] || z >= R[5]) return;
-    }
-  }
-  if (P.skip_box && x >= P.box[0] && x < P.box[1] && y >= P.box[2] && y < P.box[3] && z >= P.box[4] &&
-      z < P.box[5])
-    return;
-  if (P.skip_walls && (x == 0 || x == P.nx - 1)) return;
   const int syz = P.ny * P.nz;
-  const int p = x * syz + y * P.nz + z;
-
-  T f[Q];
-#pragma unroll
-  for (int i = 0; i < Q; ++i) f[i] = __ldg(P.fin + (size_t)i * P.n + p);
 
   // the previous step's face boundaries, applied to the wall nodes as they are loaded
   // (all of them on the x faces, so they touch disjoint nodes and commute)
@@ -204,6 +165,184 @@ __global__ void __launch_bounds__(256) k_step(const __grid_constant__ StepParams
     const int d = (cx > 0 ? dxp : (cx < 0 ? dxm : 0)) + (cy > 0 ? dyp : (cy < 0 ? dym : 0)) +
                   (cz > 0 ? dzp : (cz < 0 ? dzm : 0));
     P.fout[(size_t)i * P.n + (p + d)] = f[i];
+  }
+}
+
+// One thread per node.  blockIdx.y = x; blockIdx.x = (y, chunk of the contiguous axis)
+// in 3-D or the chunk of y in 2-D; threads run along the contiguous axis, so every load
+// and store of a warp covers 32 consecutive addresses.  Wrap-around offsets of the push
+// are per-block uniform except along the contiguous axis.
+// With nreg > 0 the launch rows walk a list of regions instead of the whole grid.
+template <class L, typename T, int COLL, bool WALLS>
+__global__ void __launch_bounds__(256) k_step(const __grid_constant__ StepParams<L, T> P) {
+  constexpr int Q = L::Q;
+  int x, y, z;
+  if (P.nreg == 0) {
+    x = blockIdx.y;
+    if constexpr (L::D == 2) {
+      y = blockIdx.x * blockDim.x + threadIdx.x;
+      if (y >= P.ny) return;
+      z = 0;
+    } else {
+      y = blockIdx.x / P.chunks;
+      z = (blockIdx.x - y * P.chunks) * blockDim.x + threadIdx.x;
+      if (z >= P.nz) return;
+    }
+  } else {
+    const int r = blockIdx.y;
+    const int g = (r >= P.rowstart[1]) + (r >= P.rowstart[2]);
+    const int* R = P.reg[g];
+    x = R[0] + (r - P.rowstart[g]);
+    if constexpr (L::D == 2) {
+      y = R[2] + blockIdx.x * blockDim.x + threadIdx.x;
+      if (y >= R[3]) return;
+      z = 0;
+    } else {
+      const int by = blockIdx.x / P.chunks;
+      y = R[2] + by;
+      z = R[4] + (blockIdx.x - by * P.chunks) * blockDim.x + threadIdx.x;
+      if (y >= R[3] || z >= R[5]) return;
+    }
+  }
+  if (P.skip_box && x >= P.box[0] && x < P.box[1] && y >= P.box[2] && y < P.box[3] && z >= P.box[4] &&
+      z < P.box[5])
+    return;
+  if (P.skip_walls && (x == 0 || x == P.nx - 1)) return;
+
+  const int p = (x * P.ny + y) * P.nz + z;
+  T f[Q];
+#pragma unroll
+  for (int i = 0; i < Q; ++i) f[i] = __ldg(P.fin + (size_t)i * P.n + p);
+  step_node<L, T, COLL, WALLS>(P, x, y, z, p, f);
+}
+
+
+// ------------------------------------------------------------------ TMA-pipelined grid kernel
+// Persistent variant of k_step for the bulk of the grid.  A tile is TB consecutive nodes of
+// one row along the contiguous axis; CTA b processes tiles b, b + gridDim.x, ...  For every
+// tile, lane i < Q of warp 0 copies population i's TB contiguous values into a stage of a
+// shared-memory ring with cp.async.bulk (TMA); an mbarrier per stage counts the bytes.
+// NS stages are in flight per CTA, so the bytes in flight no longer scale with the
+// registers of a thread.  All waits are bounded: on a timeout the CTA records
+// VS_ERR_TIMEOUT in *P.status, drains its copies (bounded) and exits.
+namespace tma {
+
+__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+          smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+// true once the barrier has completed the phase with this parity; bounded spin
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, int limit) {
+  const unsigned a = smem_addr(bar);
+  for (int it = 0; it < limit; ++it) {
+    unsigned done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+}  // namespace tma
+
+constexpr int kTmaStages = 4;
+constexpr int kTmaWaitLimit = 1 << 22;  // try_wait suspends in hardware between polls
+
+template <class L, typename T, int COLL, int TB>
+__global__ void __launch_bounds__(TB) k_step_tma(const __grid_constant__ StepParams<L, T> P, int tiles,
+                                                 int tiles_per_row, int* status) {
+  constexpr int Q = L::Q;
+  constexpr unsigned STAGE_BYTES = Q * TB * sizeof(T);
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  T* buf = (T*)smem_raw;                                       // [NS][Q][TB]
+  uint64_t* full = (uint64_t*)(smem_raw + kTmaStages * STAGE_BYTES);
+  const int tid = threadIdx.x;
+  const int nl = L::D == 2 ? P.ny : P.nz;  // contiguous extent
+
+  auto tile_base = [&](int t) -> long long {
+    const int row = t / tiles_per_row, col = t - row * tiles_per_row;
+    return (long long)row * nl + (long long)col * TB;
+  };
+  auto issue = [&](int stage, int t) {  // called by warp 0
+    const int lane = tid & 31;
+    if (lane == 0) tma::mbar_expect_tx(&full[stage], STAGE_BYTES);
+    __syncwarp();
+    const long long base = tile_base(t);
+    for (int i = lane; i < Q; i += 32)
+      tma::bulk_load(buf + ((size_t)stage * Q + i) * TB, P.fin + (size_t)i * P.n + base, TB * sizeof(T),
+                     &full[stage]);
+  };
+
+  if (tid == 0) {
+    for (int s2 = 0; s2 < kTmaStages; ++s2) tma::mbar_init(&full[s2], 1);
+    tma::fence_init();
+  }
+  __syncthreads();
+  if (tid < 32)
+    for (int s2 = 0; s2 < kTmaStages; ++s2) {
+      const int t = blockIdx.x + s2 * gridDim.x;
+      if (t < tiles) issue(s2, t);
+    }
+
+  int k = 0;
+  for (int t = blockIdx.x; t < tiles; t += gridDim.x, ++k) {
+    const int stage = k % kTmaStages;
+    const unsigned parity = (unsigned)((k / kTmaStages) & 1);
+    const bool ok = tma::mbar_wait(&full[stage], parity, kTmaWaitLimit);
+    if (__syncthreads_or(!ok)) {
+      // some copy never completed: report, give the outstanding ones a bounded chance, leave
+      if (tid == 0) atomicExch(status, VS_ERR_TIMEOUT);
+      for (int j = 1; j < kTmaStages; ++j) {
+        const int tj = t + j * gridDim.x;
+        if (tj < tiles) tma::mbar_wait(&full[(k + j) % kTmaStages], (unsigned)(((k + j) / kTmaStages) & 1), 1 << 16);
+      }
+      return;
+    }
+    T f[Q];
+    const T* sb = buf + (size_t)stage * Q * TB;
+#pragma unroll
+    for (int i = 0; i < Q; ++i) f[i] = sb[i * TB + tid];
+    __syncthreads();  // the stage has been read by every thread: refill it
+    if (tid < 32) {
+      const int tn = t + kTmaStages * gridDim.x;
+      if (tn < tiles) issue(stage, tn);
+    }
+    const long long base = tile_base(t);
+    const int p = (int)base + tid;
+    int x, y, z;
+    if constexpr (L::D == 2) {
+      x = (int)(base / P.ny);
+      y = (int)(base - (long long)x * P.ny) + tid;
+      z = 0;
+    } else {
+      const int row = (int)(base / P.nz);
+      x = row / P.ny;
+      y = row - x * P.ny;
+      z = (int)(base - (long long)row * P.nz) + tid;
+    }
+    if (P.skip_box && x >= P.box[0] && x < P.box[1] && y >= P.box[2] && y < P.box[3] && z >= P.box[4] &&
+        z < P.box[5])
+      continue;
+    if (P.skip_walls && (x == 0 || x == P.nx - 1)) continue;
+    step_node<L, T, COLL, false>(P, x, y, z, p, f);
   }
 }
 
@@ -745,6 +884,9 @@ struct vs_lattice_plan {
   int bc_group[VS_MAX_BC];   // group id of each boundary op
   int n_groups;
   int lazy_ok;               // all boundaries in one launch group and none needs pre-stream data
+  int* d_status;             // device status word of the grid kernels (VS_ERR_TIMEOUT)
+  int tma_tb;                // tile width of the TMA grid kernel, 0 when it does not apply
+  int tma_grid;              // persistent CTAs of the TMA grid kernel
   // graph cache
   cudaGraphExec_t graph;
   const void* g_fa;
@@ -791,6 +933,7 @@ static void free_lattice(vs_lattice_plan* p) {
   for (int k = 0; k < VS_MAX_BC; ++k)
     if (p->pre_buf[k]) cudaFree(p->pre_buf[k]);
   if (p->graph) cudaGraphExecDestroy(p->graph);
+  if (p->d_status) cudaFree(p->d_status);
   delete p;
 }
 
@@ -952,6 +1095,50 @@ static int enqueue_body(vs_body_plan* B, const vs_lattice_plan* LP, const void* 
   });
 }
 
+
+template <class L, typename T, int COLL, int TB>
+static size_t tma_smem() {
+  return (size_t)kTmaStages * L::Q * TB * sizeof(T) + kTmaStages * sizeof(uint64_t);
+}
+
+// Persistent CTAs for the TMA kernel: resident CTAs per SM x SMs (set once per plan).
+template <class L, typename T, int COLL, int TB>
+static int tma_configure(int* grid_out) {
+  const size_t smem = tma_smem<L, T, COLL, TB>();
+  cudaError_t e = cudaFuncSetAttribute(k_step_tma<L, T, COLL, TB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e != cudaSuccess) return cuda_status(e, "tma attribute");
+  int per_sm = 0, dev = 0, sms = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_step_tma<L, T, COLL, TB>, TB, smem);
+  if (e == cudaSuccess) e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return cuda_status(e, "tma occupancy");
+  *grid_out = (per_sm > 0 ? per_sm : 1) * sms;
+  return VS_OK;
+}
+
+template <class L, typename T, int COLL, int TB>
+static int tma_launch(vs_lattice_plan* LP, const StepParams<L, T>& P, cudaStream_t st) {
+  if (LP->tma_grid == 0) {
+    int rc = tma_configure<L, T, COLL, TB>(&LP->tma_grid);
+    if (rc) return rc;
+  }
+  const int nl = L::D == 2 ? P.ny : P.nz;
+  const int tiles_per_row = nl / TB;
+  const int tiles = (int)(P.n / TB);
+  const int grid = tiles < LP->tma_grid ? tiles : LP->tma_grid;
+  k_step_tma<L, T, COLL, TB><<<grid, TB, tma_smem<L, T, COLL, TB>(), st>>>(P, tiles, tiles_per_row, LP->d_status);
+  return VS_OK;
+}
+
+template <class L, typename T, int COLL>
+static int tma_dispatch(vs_lattice_plan* LP, const StepParams<L, T>& P, cudaStream_t st) {
+  if constexpr (L::Q == 9) {
+    if (LP->tma_tb == 256) return tma_launch<L, T, COLL, 256>(LP, P, st);
+  }
+  return tma_launch<L, T, COLL, 128>(LP, P, st);
+}
+
 // mode 0: every node.
 // mode 1: every node except the body's box and, with lazy_walls, the x = 0 / nx-1 planes
 //         (nodes outside the box read no force window).
@@ -1007,6 +1194,20 @@ static int enqueue_grid(const vs_lattice_plan* LP, const vs_body_plan* B, const 
     P.chunks = (ext_last + tb - 1) / tb;
     const dim3 grid(L::D == 2 ? P.chunks : P.chunks * ext_mid, rows);
     const bool walls = mode == 2 && lazy_walls;
+    const bool aligned = ((uintptr_t)fin % 16) == 0;
+    if (mode != 2 && LP->tma_tb > 0 && aligned) {
+      vs_lattice_plan* mp = const_cast<vs_lattice_plan*>(LP);
+      int trc;
+      switch (c.collision) {
+        case VS_COLLIDE_BGK: trc = tma_dispatch<L, T, VS_COLLIDE_BGK>(mp, P, st); break;
+        case VS_COLLIDE_KBC: trc = tma_dispatch<L, T, VS_COLLIDE_KBC>(mp, P, st); break;
+        case VS_COLLIDE_REG: trc = tma_dispatch<L, T, VS_COLLIDE_REG>(mp, P, st); break;
+        default: trc = tma_dispatch<L, T, VS_COLLIDE_MRT>(mp, P, st); break;
+      }
+      if (trc) return trc;
+      VS_CHECK_LAUNCH("vs_step grid kernel (TMA)");
+      return VS_OK;
+    }
 #define VS_LAUNCH_STEP(K)                                                              \
   (walls ? k_step<L, T, K, true><<<grid, tb, 0, st>>>(P) : k_step<L, T, K, false><<<grid, tb, 0, st>>>(P))
     switch (c.collision) {
@@ -1082,6 +1283,7 @@ int vs_lattice_plan_create(const vs_lattice_cfg* cfg, vs_lattice_plan** out) {
              cfg->collision);
   VS_REQUIRE(cfg->forcing >= VS_FORCE_NONE && cfg->forcing <= VS_FORCE_GUO_MRT, "bad forcing %d", cfg->forcing);
   VS_REQUIRE(cfg->n_bc >= 0 && cfg->n_bc <= VS_MAX_BC, "n_bc must be 0..%d", VS_MAX_BC);
+  VS_REQUIRE(cfg->variant >= VS_GRID_AUTO && cfg->variant <= VS_GRID_TMA, "bad grid kernel variant %d", cfg->variant);
   const int dim = cfg->q == 9 ? 2 : 3;
   for (int k = 0; k < cfg->n_bc; ++k) {
     const vs_bc& b = cfg->bc[k];
@@ -1129,11 +1331,33 @@ int vs_lattice_plan_create(const vs_lattice_cfg* cfg, vs_lattice_plan** out) {
     ++gsize;
   }
   p->n_groups = cfg->n_bc ? gid + 1 : 0;
+  {
+    const int nl = cfg->q == 9 ? cfg->ny : nz;
+    p->tma_tb = cfg->variant != VS_GRID_TMA ? 0 : ((cfg->q == 9 && nl % 256 == 0) ? 256 : (nl % 128 == 0 ? 128 : 0));
+    cudaError_t e = cudaMalloc(&p->d_status, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(p->d_status, 0, sizeof(int));
+    if (e != cudaSuccess) {
+      free_lattice(p);
+      return cuda_status(e, "vs_lattice_plan_create status");
+    }
+  }
   p->lazy_ok = p->n_groups == 1;
   for (int k = 0; k < cfg->n_bc; ++k)
     if (cfg->bc[k].kind == VS_BC_BB || cfg->bc[k].kind == VS_BC_SPECULAR) p->lazy_ok = 0;
   *out = p;
   return VS_OK;
+}
+
+int vs_lattice_status(const vs_lattice_plan* plan, int reset, void* stream) {
+  VS_REQUIRE(plan, "vs_lattice_status: null plan");
+  int v = 0;
+  cudaStream_t st = as_stream(stream);
+  cudaError_t e = cudaMemcpyAsync(&v, plan->d_status, sizeof(int), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e == cudaSuccess && reset && v) e = cudaMemset(plan->d_status, 0, sizeof(int));
+  if (e != cudaSuccess) return cuda_status(e, "vs_lattice_status");
+  if (v) set_error("a grid kernel gave up waiting for its bulk copies (device status %d)", v);
+  return v;
 }
 
 int vs_lattice_plan_destroy(vs_lattice_plan* plan) {

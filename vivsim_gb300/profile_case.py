@@ -25,6 +25,7 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--graph", action="store_true")
     ap.add_argument("--grid-only", action="store_true")
+    ap.add_argument("--variant", choices=["auto", "plain", "tma"], default="auto")
     a = ap.parse_args()
     kw = {}
     if a.n is not None and a.case in ("periodic2d", "cavity"):
@@ -34,7 +35,7 @@ def main():
     case = configs.CASES[a.case](**kw)
     stream = torch.cuda.Stream()
     with torch.cuda.stream(stream):
-        step, body, sim = configs.build_solver(case)
+        step, body, sim = configs.build_solver(case, variant=a.variant)
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()

@@ -45,7 +45,7 @@ class LatticeStep:
     """Plan of the fused collide-force-stream-boundary step on one grid."""
 
     def __init__(self, q, shape, collision="bgk", omega=1.0, dtype=torch.float32, mrt_op=None, forcing="none",
-                 g=None, boundaries=()):
+                 g=None, boundaries=(), variant="auto"):
         if q not in (9, 19):
             raise ValueError("q must be 9 (D2Q9) or 19 (D3Q19)")
         self.q = q
@@ -86,6 +86,7 @@ class LatticeStep:
             s.loc = V.LOCS[b["loc"]]
             for name in ("rho", "ux", "uy", "uz", "gx", "gy", "gz"):
                 setattr(s, name, float(b[name]))
+        cfg.variant = {"auto": V.VS_GRID_AUTO, "plain": V.VS_GRID_PLAIN, "tma": V.VS_GRID_TMA}[variant]
         self.cfg = cfg
         handle = C.c_void_p()
         V.call("vs_lattice_plan_create", C.byref(cfg), C.byref(handle))
@@ -94,6 +95,10 @@ class LatticeStep:
     @property
     def n_nodes(self):
         return int(np.prod(self.shape))
+
+    def check(self, reset=True):
+        """Raise if a grid kernel of this plan reported a device-side error (synchronises)."""
+        V.call("vs_lattice_status", self.handle, 1 if reset else 0, V.stream())
 
     def close(self):
         if getattr(self, "handle", None) and self.handle.value:
