@@ -11,6 +11,9 @@
 //                  forcing from g, push-stream to the neighbours (1 write/population)
 //   [face kernels] the ordered boundary conditions on the streamed populations
 // The grid kernel carries all of the HBM traffic; the other two touch O(surface) nodes.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include <climits>
 #include <cmath>
 #include <new>
@@ -24,7 +27,9 @@
 namespace vs {
 
 // device window descriptor (int[8]): origin, extent, sticky status
-enum { META_OX = 0, META_OY, META_OZ, META_WX, META_WY, META_WZ, META_STATUS, META_N = 8 };
+// META_PX/PY: lower corner of the body's last stencil bounding box (2-D moving bodies
+// predict their next window from it)
+enum { META_OX = 0, META_OY, META_OZ, META_WX, META_WY, META_WZ, META_STATUS, META_PX, META_PY, META_N = 12 };
 
 // ------------------------------------------------------------------ grid kernel
 template <class L, typename T>
@@ -390,7 +395,10 @@ struct BodyParams {
   const T* ds_arr;
   T ds2_scalar;  // 2 * ds as the reference forms it: (T)ds * 2
   int M, kernel, n_iter;
-  int cap_x, cap_y;
+  int cap_x, cap_y;  // window region: (cap_x + 2) x (cap_y + 2) cells from the predicted corner
+  int row_len;       // staged row length (multiple of 16 bytes), the TMA box's inner extent
+  int bulk;          // stage the region with one tensor-map TMA copy
+  CUtensorMap map;   // f as a (ny, nx, 9) tensor, box (row_len, cap_x + 2, 9)
   int box[4];  // the window must stay inside x0..x1, y0..y1 (half-open)
   T* state;  // a[3], v[3], d[3], h[3]
   T* gw;
@@ -474,55 +482,50 @@ __device__ __forceinline__ T interp_group(const T* W, const int* slot, const T* 
   return acc;
 }
 
-// asynchronous 4- or 8-byte global -> shared copy (completes at cp_async_wait_all)
-template <typename T>
-__device__ __forceinline__ void cp_async(T* dst, const T* src) {
-  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-  if constexpr (sizeof(T) == 4)
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
-  else
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
-
 // One CTA advances one 2-D rigid body by one step: marker positions from the body
 // displacement, stencil weights, a counting-sort CSR of (node, pair) in shared memory,
 // interpolation of u from f at the touched nodes, the multi-direct-forcing iterations,
 // the force window for the grid kernel, the total force and the Newmark update.
 // Each touched node keeps its contributions in increasing (marker, stencil point) order,
 // the order of the reference's scatter-add; no floating-point atomics are used.
-// The populations of the whole window are copied to shared memory asynchronously as soon
-// as the window is known, so their latency hides behind the CSR construction.
+//
+// Latency layout: one global round trip up front (body state, last bounding-box corner,
+// marker coordinates).  The window region is predicted from the last corner (one node of
+// slack per side, the body moves less than a node per step), so stencil keys need no
+// block-wide bounding-box reduction, and the region's populations are staged into shared
+// memory by bulk copies (TMA) issued by warp 0 while the CSR is built.
 // The last MDF iteration only adds its force step: its spread and interpolation feed a
 // marker velocity that the reference computes and then discards (ib/mdf.py:57-64).
 template <typename T, int R>
-__global__ void __launch_bounds__(kBodyThreads) k_body2d(const BodyParams<T> B) {
+__global__ void __launch_bounds__(kBodyThreads) k_body2d(const __grid_constant__ BodyParams<T> B) {
   constexpr int WD = 2 * R, S = WD * WD;
   constexpr int LN = S >= 16 ? 4 : 1;
-  extern __shared__ __align__(16) unsigned char smem[];
+  constexpr int AL = 16 / sizeof(T);  // elements per 16 bytes
+  extern __shared__ __align__(128) unsigned char smem[];
   const int tid = threadIdx.x, nt = blockDim.x;
   const int M = B.M, P = M * S;
-  const int Bcap = B.cap_x * B.cap_y;
-  T* fwin = (T*)smem;             // window populations [9][Bcap]
-  T* wx = fwin + 9 * Bcap;        // per marker: 2R one-dimensional weights along x
+  const int EX = B.cap_x + 2, EY = B.cap_y + 2, NB = EX * EY, RL = B.row_len;
+  T* fwin = (T*)smem;             // staged populations [9][EX][RL]
+  T* wx = fwin + 9 * EX * RL;     // per marker: 2R one-dimensional weights along x
   T* wy = wx + WD * M;            //                              ... along y
   T* W = wy + WD * M;
   T* U = W + P;
   T* Fs = U + 2 * M;
   T* Ft = Fs + 2 * M;
-  T* nu = Ft + 2 * M;             // per touched node: u [2][Bcap]
-  T* nv = nu + 2 * Bcap;          // per touched node: 0.5 spread(F_step) [2][Bcap]
-  int* key = (int*)(nv + 2 * Bcap);  // pair -> window cell
-  int* slot = key + P;               // pair -> touched-node slot
-  int* sorted = slot + P;            // pairs grouped by touched node, in pair order
-  int* cnt = sorted + P;             // per cell: pair count, then scatter cursor
-  int* cslot = cnt + Bcap;           // per cell: touched slot or -1
-  int* tcell = cslot + Bcap;         // touched slot -> cell
-  int* tstart = tcell + Bcap;        // touched slot -> first sorted position (+ end)
-  int* fxy = tstart + Bcap + 1;      // per marker: floor(X), floor(Y)
-  int* misc = fxy + 2 * M;           // [0..3] bbox, [4..35] warp sums
+  T* nu = Ft + 2 * M;             // per touched node: u [2][NB]
+  T* nv = nu + 2 * NB;            // per touched node: 0.5 spread(F_step) [2][NB]
+  int* key = (int*)(nv + 2 * NB); // pair -> region cell
+  int* slot = key + P;            // pair -> touched-node slot
+  int* sorted = slot + P;         // pairs grouped by touched node, in pair order
+  int* cnt = sorted + P;          // per cell: pair count, then scatter cursor
+  int* cslot = cnt + NB;          // per cell: touched slot or -1
+  int* tcell = cslot + NB;        // touched slot -> cell
+  int* tstart = tcell + NB;       // touched slot -> first sorted position (+ end)
+  int* fxy = tstart + NB + 1;     // per marker: floor(X), floor(Y)
+  int* misc = fxy + 2 * M;        // [0..3] bbox, [4] out-of-region flag, [8..39] warp sums
+  uint64_t* bar = (uint64_t*)(((uintptr_t)(misc + 40) + 7) & ~(uintptr_t)7);
 
+  // one round trip: state, last corner, marker coordinates
   T a[2], v[2], d[2];
 #pragma unroll
   for (int c = 0; c < 2; ++c) {
@@ -530,10 +533,29 @@ __global__ void __launch_bounds__(kBodyThreads) k_body2d(const BodyParams<T> B) 
     v[c] = B.state[3 + c];
     d[c] = B.state[6 + c];
   }
+  const int ox = B.meta[META_PX] - 1, oy = B.meta[META_PY] - 1;  // region corner
+  const int ya = oy >= 0 ? oy - oy % AL : 0;                     // 16-byte aligned row start
+  const int64_t n = (int64_t)B.nx * B.ny;
+  const bool region_ok = ox >= B.box[0] && oy >= B.box[2] && ox + EX <= B.box[1] && oy + EY <= B.box[3];
+  const bool bulk = B.bulk && region_ok;
   if (tid == 0) {
-    misc[0] = INT_MAX; misc[1] = INT_MIN; misc[2] = INT_MAX; misc[3] = INT_MIN;
+    misc[0] = INT_MAX; misc[1] = INT_MIN; misc[2] = INT_MAX; misc[3] = INT_MIN; misc[4] = 0;
+    if (bulk) {
+      tma::mbar_init(bar, 1);
+      tma::fence_init();
+    }
   }
-  for (int k = tid; k < Bcap; k += nt) cnt[k] = 0;
+  if (bulk && tid == 0) {
+    // the region [ya, ya + RL) x [ox, ox + EX) x all 9 populations in one tensor copy;
+    // elements past the grid's edge arrive as zeros
+    tma::mbar_expect_tx(bar, (unsigned)(9 * EX * RL * sizeof(T)));
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];\n" ::"r"(tma::smem_addr(fwin)),
+        "l"(&B.map), "r"(ya), "r"(ox), "r"(0), "r"(tma::smem_addr(bar))
+        : "memory");
+  }
+  for (int k = tid; k < NB; k += nt) cnt[k] = 0;
   __syncthreads();
   // markers follow the body (dyn.py:68-81); the tensor-product stencil weight
   // kernel(sx - X) * kernel(sy - Y) (ib/stencil.py:44-47) is formed from the 2R one-dimensional
@@ -550,44 +572,47 @@ __global__ void __launch_bounds__(kBodyThreads) k_body2d(const BodyParams<T> B) 
     }
   }
   __syncthreads();
-  const int bx0 = misc[0] - R + 1, by0 = misc[2] - R + 1;
-  const int BW = misc[1] - misc[0] + WD, BH = misc[3] - misc[2] + WD;
-  const bool bad = BW > B.cap_x || BH > B.cap_y || bx0 < B.box[0] || by0 < B.box[2] || bx0 + BW > B.box[1] ||
-                   by0 + BH > B.box[3];
-  if (bad) {
+  // stencil (ib/stencil.py:7-51): weights and region-local node keys; pairs per cell
+  for (int p = tid; p < P; p += nt) {
+    const int m = p / S, k = p - m * S, ix = k / WD, iy = k % WD;
+    W[p] = wx[m * WD + ix] * wy[m * WD + iy];
+    const int cx = fxy[2 * m] + ix - R + 1 - ox, cy = fxy[2 * m + 1] + iy - R + 1 - oy;
+    if (cx < 0 || cx >= EX || cy < 0 || cy >= EY) {
+      misc[4] = 1;
+      key[p] = 0;
+      continue;
+    }
+    const int kk = cx * EY + cy;
+    key[p] = kk;
+    atomicAdd(&cnt[kk], 1);
+  }
+  __syncthreads();
+  if (misc[4] || !region_ok) {
+    // the body moved a node or more in one step, or its region left the box
+    if (bulk && tid == 0) tma::mbar_wait(bar, 0, kTmaWaitLimit);  // let the staged copies land
+    __syncthreads();
     if (tid == 0) {
       B.meta[META_STATUS] = VS_ERR_RANGE;
       B.meta[META_WX] = 0; B.meta[META_WY] = 0; B.meta[META_WZ] = 0;
     }
     return;
   }
-  const int NB = BW * BH;
-  const int64_t n = (int64_t)B.nx * B.ny;
-  // start copying the window's populations (consumed after the CSR is built)
-  for (int k = tid; k < NB; k += nt) {
-    const int64_t pn = (int64_t)(bx0 + k / BH) * B.ny + (by0 + k % BH);
-#pragma unroll
-    for (int i = 0; i < 9; ++i) cp_async(fwin + i * Bcap + k, B.fin + i * n + pn);
-  }
-  cp_async_commit();
-  // stencil (ib/stencil.py:7-51) with window-local node keys; pairs per cell
-  for (int p = tid; p < P; p += nt) {
-    const int m = p / S, k = p - m * S, ix = k / WD, iy = k % WD;
-    W[p] = wx[m * WD + ix] * wy[m * WD + iy];
-    const int kk = (fxy[2 * m] + ix - R + 1 - bx0) * BH + (fxy[2 * m + 1] + iy - R + 1 - by0);
-    key[p] = kk;
-    atomicAdd(&cnt[kk], 1);
-  }
-  __syncthreads();
-  const int NT = block_csr_scan(cnt, cslot, tcell, tstart, NB, misc + 4);
+  const int NT = block_csr_scan(cnt, cslot, tcell, tstart, NB, misc + 8);
   __syncthreads();
   for (int p = tid; p < P; p += nt) {
     const int kk = key[p];
     sorted[atomicAdd(&cnt[kk], 1)] = p;
     slot[p] = cslot[kk];
   }
-  cp_async_wait_all();
-  __syncthreads();
+  bool staged = true;
+  if (bulk) staged = tma::mbar_wait(bar, 0, kTmaWaitLimit);
+  if (__syncthreads_or(!staged)) {
+    if (tid == 0) {
+      B.meta[META_STATUS] = VS_ERR_TIMEOUT;
+      B.meta[META_WX] = 0; B.meta[META_WY] = 0; B.meta[META_WZ] = 0;
+    }
+    return;
+  }
   // order each node's pairs by pair id (= the reference's scatter order); u at the node
   for (int j = tid; j < NT; j += nt) {
     const int lo = tstart[j], hi = tstart[j + 1];
@@ -600,20 +625,26 @@ __global__ void __launch_bounds__(kBodyThreads) k_body2d(const BodyParams<T> B) 
       }
       sorted[q + 1] = val;
     }
-    const int k = tcell[j];
+    const int k = tcell[j], cx = k / EY, cy = k - cx * EY;
     T fl[9];
+    if (bulk) {
 #pragma unroll
-    for (int i = 0; i < 9; ++i) fl[i] = fwin[i * Bcap + k];
+      for (int i = 0; i < 9; ++i) fl[i] = fwin[(i * EX + cx) * RL + (oy - ya) + cy];
+    } else {
+      const int64_t pn = (int64_t)(ox + cx) * B.ny + (oy + cy);
+#pragma unroll
+      for (int i = 0; i < 9; ++i) fl[i] = __ldg(B.fin + i * n + pn);
+    }
     T r, uu[3];
     macro(L9{}, fl, r, uu);
     nu[j] = uu[0];
-    nu[Bcap + j] = uu[1];
+    nu[NB + j] = uu[1];
   }
   __syncthreads();
   // U = interpolate(u) and the first force step (ib/mdf.py:38-48); target = body velocity
   for (int t = tid; t < 2 * M * LN; t += nt) {
     const int q = t / LN, m = q >> 1, c = q & 1;
-    const T acc = interp_group<T, S, LN>(W, slot, nu + c * Bcap, m);
+    const T acc = interp_group<T, S, LN>(W, slot, nu + c * NB, m);
     if ((t & (LN - 1)) == 0) {
       U[q] = acc;
       const T d2 = B.ds_arr ? B.ds_arr[m] * T(2) : B.ds2_scalar;
@@ -637,13 +668,13 @@ __global__ void __launch_bounds__(kBodyThreads) k_body2d(const BodyParams<T> B) 
         a1 = i == lo ? t1 : a1 + t1;
       }
       nv[j] = a0 * T(0.5);
-      nv[Bcap + j] = a1 * T(0.5);
+      nv[NB + j] = a1 * T(0.5);
     }
     __syncthreads();
     // U += interpolate(0.5 spread); next force step (ib/mdf.py:41-52)
     for (int t = tid; t < 2 * M * LN; t += nt) {
       const int q = t / LN, m = q >> 1, c = q & 1;
-      const T acc = interp_group<T, S, LN>(W, slot, nv + c * Bcap, m);
+      const T acc = interp_group<T, S, LN>(W, slot, nv + c * NB, m);
       if ((t & (LN - 1)) == 0) {
         const T uq = U[q] + acc;
         U[q] = uq;
@@ -655,7 +686,7 @@ __global__ void __launch_bounds__(kBodyThreads) k_body2d(const BodyParams<T> B) 
     }
     __syncthreads();
   }
-  // g = spread(F_total) over the window (ib/mdf.py:60-62); zero where no marker reaches
+  // g = spread(F_total) over the region (ib/mdf.py:60-62); zero where no marker reaches
   for (int k = tid; k < NB; k += nt) {
     const int j = cslot[k];
     T a0 = T(0), a1 = T(0);
@@ -674,8 +705,10 @@ __global__ void __launch_bounds__(kBodyThreads) k_body2d(const BodyParams<T> B) 
     B.gw[NB + k] = a1;
   }
   if (tid == 0) {
-    B.meta[META_OX] = bx0; B.meta[META_OY] = by0; B.meta[META_OZ] = 0;
-    B.meta[META_WX] = BW; B.meta[META_WY] = BH; B.meta[META_WZ] = 1;
+    B.meta[META_OX] = ox; B.meta[META_OY] = oy; B.meta[META_OZ] = 0;
+    B.meta[META_WX] = EX; B.meta[META_WY] = EY; B.meta[META_WZ] = 1;
+    B.meta[META_PX] = misc[0] - R + 1;
+    B.meta[META_PY] = misc[2] - R + 1;
   }
   // total force h = sum_m(-F_total) (dyn.py:126-136) by warp 0 in a fixed tree, added
   // mass h += a A (vortex_induced_vibration.py:136), Newmark update (dyn.py:5-51)
@@ -714,11 +747,12 @@ __global__ void __launch_bounds__(kBodyThreads) k_body2d(const BodyParams<T> B) 
   }
 }
 
+// shared memory of k_body2d for M markers, radius R, region EX x EY, staged rows of RL
 template <typename T>
-static size_t body2d_smem(int M, int R, int Bcap) {
-  const int S = 4 * R * R, P = M * S;
-  return sizeof(T) * ((4 * (size_t)R + 6) * M + P + 13 * (size_t)Bcap) +
-         sizeof(int) * (3 * (size_t)P + 4 * (size_t)Bcap + 2 + 2 * (size_t)M + 40);
+static size_t body2d_smem(int M, int R, int EX, int EY, int RL) {
+  const size_t S = 4 * R * R, P = M * S, NB = (size_t)EX * EY;
+  return sizeof(T) * (9 * (size_t)EX * RL + (4 * (size_t)R + 6) * M + P + 4 * NB) +
+         sizeof(int) * (3 * P + 4 * NB + 1 + 2 * (size_t)M + 40) + 16;
 }
 
 template <typename T>
@@ -920,6 +954,10 @@ struct vs_body_plan {
   void* d_nv;       // 3 x U node force step
   void* d_mk;       // U, F_step, F_total: 3 x (3 M)
   size_t smem;
+  int row_len, bulk;  // 2-D body kernel: staged row length, bulk staging on/off
+  CUtensorMap maps[2]; // tensor maps of the last two population buffers seen
+  const void* map_ptr[2];
+  int map_next;
   double nm[9];  // k1, k2, c1, c2, dt, damping, stiffness, den, area
   int box[6];    // region the body's window never leaves (half-open x0,x1,y0,y1,z0,z1)
   cudaStream_t side;
@@ -1034,6 +1072,42 @@ static StepParams<L, T> make_step_params(const vs_lattice_plan* LP, const vs_bod
   return P;
 }
 
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no libcuda link)
+static PFN_cuTensorMapEncodeTiled_v12000 encode_tiled() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+  }
+  return fn;
+}
+
+// Tensor map of population buffer f (viewed as (ny, nx, 9)) with the body's region box.
+static const CUtensorMap* body_map(vs_body_plan* b, const vs_lattice_plan* L, const void* f) {
+  for (int k = 0; k < 2; ++k)
+    if (b->map_ptr[k] == f) return &b->maps[k];
+  PFN_cuTensorMapEncodeTiled_v12000 enc = encode_tiled();
+  if (!enc) return nullptr;
+  const int ts = L->cfg.dtype == VS_F64 ? 8 : 4;
+  const cuuint64_t dims[3] = {(cuuint64_t)L->cfg.ny, (cuuint64_t)L->cfg.nx, 9};
+  const cuuint64_t strides[2] = {(cuuint64_t)L->cfg.ny * ts, (cuuint64_t)L->n * ts};
+  const cuuint32_t box[3] = {(cuuint32_t)b->row_len, (cuuint32_t)(b->cap[0] + 2), 9};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  const int k = b->map_next;
+  CUresult r = enc(&b->maps[k], ts == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3,
+                   const_cast<void*>(f), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                   CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return nullptr;
+  b->map_ptr[k] = f;
+  b->map_next = 1 - k;
+  return &b->maps[k];
+}
+
 static int enqueue_body(vs_body_plan* B, const vs_lattice_plan* LP, const void* fin, void* force_hist,
                         cudaStream_t st) {
   const int dtype = B->cfg.dtype;
@@ -1053,6 +1127,15 @@ static int enqueue_body(vs_body_plan* B, const vs_lattice_plan* LP, const void* 
       P.n_iter = B->cfg.n_iter;
       P.cap_x = B->cap[0];
       P.cap_y = B->cap[1];
+      P.row_len = B->row_len;
+      P.bulk = 0;
+      if (B->bulk && ((uintptr_t)fin % 16) == 0) {
+        const CUtensorMap* m = body_map(B, LP, fin);
+        if (m) {
+          P.map = *m;
+          P.bulk = 1;
+        }
+      }
       for (int q = 0; q < 4; ++q) P.box[q] = B->box[q];
       P.state = (T*)B->d_state;
       P.gw = (T*)B->d_gw;
@@ -1426,7 +1509,7 @@ int vs_body_plan_create(const vs_body_cfg* cfg, const vs_lattice_plan* lattice, 
         continue;
       }
       const int lo_n = (int)floor(lo[d]) - cfg->radius + 1, hi_n = (int)floor(hi[d]) + cfg->radius + 1;
-      int margin = 2;
+      int margin = 4;
       if (cfg->moving && cfg->free_dof[d])
         margin += cfg->window_margin > 0 ? cfg->window_margin : (hi_n - lo_n);
       b->box[2 * d] = lo_n - margin < 0 ? 0 : lo_n - margin;
@@ -1470,7 +1553,9 @@ int vs_body_plan_create(const vs_body_cfg* cfg, const vs_lattice_plan* lattice, 
       return rc;
     }
   }
-  const int64_t cells = (int64_t)b->cap[0] * b->cap[1] * b->cap[2];
+  // force window: a 2-D body writes its predicted region, (cap + 2) nodes per axis
+  const int64_t cells = cfg->dim == 2 ? (int64_t)(b->cap[0] + 2) * (b->cap[1] + 2)
+                                      : (int64_t)b->cap[0] * b->cap[1] * b->cap[2];
   if ((e = cudaMalloc(&b->d_gw, ts * b->C * cells)) != cudaSuccess) return fail(e);
   if ((e = cudaMalloc(&b->d_meta, sizeof(int) * META_N)) != cudaSuccess) return fail(e);
   {
@@ -1489,20 +1574,38 @@ int vs_body_plan_create(const vs_body_cfg* cfg, const vs_lattice_plan* lattice, 
   b->nm[7] = cfg->mass + b->nm[2] * cfg->damping + b->nm[3] * cfg->stiffness;
   b->nm[8] = cfg->added_mass_area;
   if (cfg->dim == 2) {
-    const int Bcap = b->cap[0] * b->cap[1];
-    if ((int64_t)M * b->S >= 65536 || Bcap >= 65536) {
+    const int EX = b->cap[0] + 2, EY = b->cap[1] + 2;
+    if ((int64_t)M * b->S >= 65536 || (int64_t)EX * EY >= 65536) {
       free_body(b);
-      set_error("2-D body with %d markers (%d window cells) exceeds the single-CTA body kernel", M, Bcap);
+      set_error("2-D body with %d markers (%d x %d window) exceeds the single-CTA body kernel", M, EX, EY);
       return VS_ERR_UNSUPPORTED;
     }
-    b->smem = ts == 8 ? body2d_smem<double>(M, cfg->radius, Bcap) : body2d_smem<float>(M, cfg->radius, Bcap);
+    const int al = (int)(16 / ts);
+    b->row_len = ((EY + al - 1 + al - 1) / al) * al;  // region row plus alignment slack
+    b->bulk = lattice->cfg.ny % al == 0 && b->row_len <= 256 && EX <= 256;
     int dev = 0, optin = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    auto smem_of = [&](int rl) {
+      return ts == 8 ? body2d_smem<double>(M, cfg->radius, EX, EY, rl) : body2d_smem<float>(M, cfg->radius, EX, EY, rl);
+    };
+    b->smem = smem_of(b->bulk ? b->row_len : 0);
+    if ((int64_t)b->smem > optin && b->bulk) {  // fall back to direct loads without staging
+      b->bulk = 0;
+      b->smem = smem_of(0);
+    }
     if ((int64_t)b->smem > optin) {
       free_body(b);
       set_error("body of %d markers needs %zu bytes of shared memory (> %d available)", M, b->smem, optin);
       return VS_ERR_UNSUPPORTED;
+    }
+    if (!b->bulk) b->row_len = 0;
+    {
+      // last bounding-box corner before the first step
+      int meta0[META_N] = {0};
+      meta0[META_PX] = (int)floor(lo[0] + cfg->d0[0]) - cfg->radius + 1;
+      meta0[META_PY] = (int)floor(lo[1] + cfg->d0[1]) - cfg->radius + 1;
+      if ((e = cudaMemcpy(b->d_meta, meta0, sizeof(meta0), cudaMemcpyHostToDevice)) != cudaSuccess) return fail(e);
     }
     e = ts == 8 ? body2d_attr<double>(cfg->radius, (int)b->smem) : body2d_attr<float>(cfg->radius, (int)b->smem);
     if (e != cudaSuccess) return fail(e);
