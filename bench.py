@@ -35,11 +35,11 @@ BYTES_PER_UPDATE = {9: 72, 19: 152}  # f32: each population read once and writte
 def parse():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--workload", choices=["viv2d", "cavity", "sphere3d", "periodic2d"], default="viv2d")
-    ap.add_argument("--chunk", type=int, default=50, help="time steps per bench step")
+    ap.add_argument("--chunk", type=int, default=500, help="time steps per bench step")
     ap.add_argument("--no-extras", action="store_true", help="skip the HBM-bound roofline cases")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU-baseline sample budget")
     return ap.parse_args()
@@ -89,24 +89,42 @@ class ClockSampler:
         self.gpu = gpu_index
 
     def __enter__(self):
+        import threading
+        self.lines = []
+        self._first = threading.Event()
         try:
             self.proc = subprocess.Popen(
-                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200",
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "50",
                  "-i", str(self.gpu)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except (OSError, ValueError):
             self.proc = None
+            return self
+
+        def reader():
+            for ln in self.proc.stdout:
+                if ln.strip():
+                    self.lines.append(ln)
+                    self._first.set()
+            self._first.set()
+
+        self._thread = threading.Thread(target=reader, daemon=True)
+        self._thread.start()
+        self._first.wait(timeout=5.0)  # sampling is running before the timed region starts
+        self._start = len(self.lines)
         return self
 
     def __exit__(self, *a):
-        self.lines = []
         if self.proc is not None:
+            self._stop = len(self.lines)
             self.proc.terminate()
             try:
-                out, _ = self.proc.communicate(timeout=5)
+                self.proc.wait(timeout=5)
             except subprocess.TimeoutExpired:
                 self.proc.kill()
-                out, _ = self.proc.communicate()
-            self.lines = [ln for ln in out.splitlines() if ln.strip()]
+                self.proc.wait()
+            self._thread.join(timeout=5)
+            # samples taken while the timed region ran (plus the one just before it)
+            self.lines = self.lines[max(0, self._start - 1):max(self._stop, self._start)]
 
     def summary(self):
         sm, smax, reasons = [], None, set()
