@@ -140,6 +140,18 @@ int vs_ib_mdf(int dtype, const void* grid_u, int c, int64_t n_grid, const void* 
               const void* u_target, const void* ds, double ds_scalar, int n_iter, void* grid_force,
               void* marker_force, void* workspace, size_t workspace_bytes, void* stream);
 
+/* spread() like vs_ib_spread, for callers that may not allocate device memory while they
+ * run (an open CUDA graph capture, a host runtime that owns all device memory and passes
+ * no workspace).  No counterpart in the reference: vivsim's spread is a JAX scatter-add
+ * whose scratch XLA provides.  Scratch is a fixed 4 MiB device array of the library, one
+ * per device, looked up by the first call on each device (make that call before any
+ * stream capture); nothing is allocated.  Limit: m * s <= 65536 marker-stencil pairs
+ * (4096 markers of a 4x4 stencil), else VS_ERR_INVALID_ARG.  All calls on a device share
+ * the scratch, so calls that may overlap on the device (different streams, several host
+ * threads) race: issue them in order on one stream.  Results equal vs_ib_spread's. */
+int vs_ib_spread_noalloc(int dtype, const void* marker_values, const void* grid_in, void* grid_out, int c,
+                         int64_t n_grid, const void* W, const int32_t* I, int m, int s, void* stream);
+
 /* Read (and optionally clear) the IB status word: bit 0 is set when a stencil index fell
  * outside [0, n_grid) in an IB call (that contribution is dropped / read as zero).
  * Synchronous with respect to the device. */

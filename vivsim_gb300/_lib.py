@@ -89,6 +89,7 @@ _SIGS = {
     "vs_ib_workspace_bytes": (_z, [_i, _i]),
     "vs_ib_spread": (_i, [_i, _p, _p, _p, _i, _l, _p, _p, _i, _i, _p, _z, _p]),
     "vs_ib_mdf": (_i, [_i, _p, _i, _l, _p, _p, _i, _i, _p, _p, _d, _i, _p, _p, _p, _z, _p]),
+    "vs_ib_spread_noalloc": (_i, [_i, _p, _p, _p, _i, _l, _p, _p, _i, _i, _p]),
     "vs_ib_status": (_i, [C.POINTER(C.c_uint), _i]),
     "vs_newmark": (_i, [_i, _i, _p, _p, _p, _p, _d, _d, _d, _p, _p, _p, _d, _d, _d, _p, _p, _p, _p]),
     "vs_markers_coords_2dof": (_i, [_i, _p, _p, _i, _p, _p, _p, _p]),

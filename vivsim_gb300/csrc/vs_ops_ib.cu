@@ -8,6 +8,8 @@
 #include <cub/device/device_radix_sort.cuh>
 #include <cub/device/device_scan.cuh>
 
+#include <mutex>
+
 #include "vs_dispatch.cuh"
 #include "vs_ib.cuh"
 
@@ -617,6 +619,100 @@ int vs_torque_to_obj(int dtype, const void* x, const void* y, int m, double xc, 
     k_torque<T><<<1, 32, 0, as_stream(stream)>>>((const T*)x, (const T*)y, m, (T)xc, (T)yc, (const T*)d,
                                                  (const T*)h, (T*)out);
     VS_CHECK_LAUNCH("vs_torque_to_obj");
+    return VS_OK;
+  });
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------ spread without allocation
+// vs_ib_spread_noalloc serves callers that must not allocate device memory while they run:
+// a host loop that holds a CUDA graph capture open (an allocation would end or invalidate
+// the capture), a foreign runtime that owns every device allocation and hands out no
+// scratch (an XLA custom call registered without a workspace), or a latency-critical loop
+// that cannot afford a pool miss.  Its scratch is one file-scope device array, set up once
+// per device and shared by every call on that device.
+namespace vs {
+namespace {
+
+constexpr int64_t kNoAllocMaxPairs = 65536;              // m * s: 4096 markers of a 4x4 stencil
+constexpr size_t kNoAllocScratchBytes = (size_t)4 << 20;  // 4 MiB
+constexpr int kNoAllocMaxDevices = 64;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+
+// Address of this device's copy of g_noalloc_scratch.  The first call on a device looks it
+// up (loading this module on that device if it is not loaded yet) and caches it.
+int noalloc_scratch(void** out) {
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_status(e, "vs_ib_spread_noalloc: cudaGetDevice");
+  VS_REQUIRE(dev >= 0 && dev < kNoAllocMaxDevices, "vs_ib_spread_noalloc: device %d beyond %d", dev,
+             kNoAllocMaxDevices);
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_status(e, "vs_ib_spread_noalloc: cudaGetSymbolAddress");
+    if (!p) {
+      set_error("vs_ib_spread_noalloc: no device address for the scratch array");
+      return VS_ERR_CUDA;
+    }
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return VS_OK;
+}
+
+// Scratch the spread itself touches: the seven pair arrays and the CUB sort/scan storage
+// (the MDF tail that carve() also lays out is never dereferenced by a spread).
+size_t spread_scratch_bytes(int m, int s) {
+  const int64_t P = (int64_t)m * s;
+  return 7 * align256(sizeof(int32_t) * P) + align256(cub_sort_bytes(P));
+}
+
+}  // namespace
+}  // namespace vs
+
+extern "C" {
+
+int vs_ib_spread_noalloc(int dtype, const void* marker_values, const void* grid_in, void* grid_out, int c,
+                         int64_t n_grid, const void* W, const int32_t* I, int m, int s, void* stream) {
+  VS_REQUIRE(marker_values && grid_in && grid_out && W && I && c > 0 && m > 0 && s > 0 && n_grid > 0,
+             "vs_ib_spread_noalloc: bad arguments");
+  VS_REQUIRE((int64_t)m * s <= kNoAllocMaxPairs,
+             "vs_ib_spread_noalloc: %lld marker-stencil pairs exceed the fixed scratch limit of %lld; "
+             "use vs_ib_spread with a caller workspace",
+             (long long)m * s, (long long)kNoAllocMaxPairs);
+  VS_REQUIRE(n_grid < (1ll << 31), "vs_ib_spread_noalloc: grid too large for int32 indices");
+  VS_REQUIRE(dtype == VS_F32 || dtype == VS_F64, "vs_ib_spread_noalloc: bad dtype %d", dtype);
+  void* scratch = nullptr;
+  int rc = noalloc_scratch(&scratch);
+  if (rc) return rc;
+  const size_t need = spread_scratch_bytes(m, s);
+  VS_REQUIRE(need <= kNoAllocScratchBytes, "vs_ib_spread_noalloc: %zu scratch bytes needed, %zu available", need,
+             kNoAllocScratchBytes);
+  // Every scratch word the spread reads is written earlier in the same call (keys and ids
+  // by k_iota_keys, the sorted copies by the sort, heads and ids by k_heads and the scan),
+  // so nothing has to be cleared first.
+  return dispatch_t(dtype, [&](auto t) -> int {
+    using T = typename decltype(t)::type;
+    cudaStream_t st = as_stream(stream);
+    const int64_t P = (int64_t)m * s;
+    IbWorkspace w = carve(scratch, m, s);
+    if (grid_out != grid_in) {
+      k_copy<T><<<grid_for((int64_t)c * n_grid, 256), 256, 0, st>>>((const T*)grid_in, (T*)grid_out,
+                                                                    (int64_t)c * n_grid);
+    }
+    int rc2 = build_csr(I, P, n_grid, w, st);
+    if (rc2) return rc2;
+    k_segment_sum<T><<<grid_for(P, 256), 256, 0, st>>>(0, w.skeys, w.sids, w.head, w.uid, P, (const T*)marker_values,
+                                                       (const T*)W, c, s, (const T*)grid_out, (T*)grid_out, n_grid,
+                                                       nullptr, 0, T(1));
+    VS_CHECK_LAUNCH("vs_ib_spread_noalloc");
     return VS_OK;
   });
 }
