@@ -42,6 +42,7 @@ def parse():
     ap.add_argument("--chunk", type=int, default=500, help="time steps per bench step")
     ap.add_argument("--no-extras", action="store_true", help="skip the HBM-bound roofline cases")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU-baseline sample budget")
+    ap.add_argument("--batch-steps", type=int, default=5000, help="time steps of the batched-sweep comparison")
     return ap.parse_args()
 
 
@@ -203,6 +204,44 @@ def roofline(torch, case, step, body, sim, flush, peak, peak_kind, launches):
             "kernel_mlups": round(n / t / 1e6, 1)}
 
 
+def batched_vs_sequential(torch, steps, n_cases=64, seed=3):
+    """The uneven VIV sweep (vivsim_gb300.configs.viv_sweep): every case's loop run one
+    after the other with plain launches (vs_run), against all cases advanced together
+    (vs_batch_run, launch shape from the autotuner, graph replay).  Aggregate MLUPS."""
+    from vivsim_gb300 import configs, solver
+    cases = configs.viv_sweep(n_cases, seed)
+    nodes = sum(int(math.prod(c["shape"])) for c in cases)
+    seq = [configs.build_solver(c)[2] for c in cases]
+    for sim in seq:
+        sim.run(2)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for sim in seq:
+        sim.run(steps)
+    e1.record()
+    torch.cuda.synchronize()
+    t_seq = e0.elapsed_time(e1) / 1e3
+    del seq
+    bat = [configs.build_solver(c)[2] for c in cases]
+    batch = solver.Batch(bat)
+    tuned = batch.tune(trial_steps=32)
+    batch.run(steps)  # tables and graph for this buffer parity (untimed)
+    torch.cuda.synchronize()
+    e0.record()
+    batch.run(steps)
+    e1.record()
+    torch.cuda.synchronize()
+    t_bat = e0.elapsed_time(e1) / 1e3
+    m_seq, m_bat = nodes * steps / t_seq / 1e6, nodes * steps / t_bat / 1e6
+    return {"workload": f"viv_sweep_{n_cases}_cases_seed{seed}_d2q9_kbc", "cases": n_cases, "nodes": nodes,
+            "time_steps": steps, "sequential_plain_mlups": round(m_seq, 1), "batched_mlups": round(m_bat, 1),
+            "batched_over_sequential": round(m_bat / m_seq, 2),
+            "launch_shape": {"threads_per_block": batch.threads_per_block,
+                             "steps_per_graph": batch.steps_per_graph},
+            "tuning_ms_per_step": {f"{k[0]}x{k[1]}": round(v, 4) for k, v in tuned.items()}}
+
+
 def gb300_arm(args, world, rank, local):
     import numpy as np
     import torch
@@ -244,7 +283,9 @@ def gb300_arm(args, world, rank, local):
             secs = float(t.item())
             dist.barrier()
         mlups = n * args.chunk * args.steps * world / secs / 1e6
-        launches_per_step = (1 if body is not None else 0) + 1 + step_groups(case)
+        # with a body: body kernel, grid launch outside its box, box launch; the x-face
+        # boundaries of these cases run on the next step's load and once at the end of a chunk
+        launches_per_step = 3 if body is not None else 1 + step_groups(case)
         rl = roofline(torch, case, step, body, sim, flush, peak, peak_kind, 2 * args.chunk)
 
         # end to end through the public API with host buffers: H2D f, chunk, D2H f
@@ -264,6 +305,7 @@ def gb300_arm(args, world, rank, local):
         fbytes = int(f_host.numel() * f_host.element_size())
 
         extras = {}
+        extras_batch = None
         if not args.no_extras and rank == 0:
             del e2e_sim
             for name in ("sphere3d", "periodic2d"):
@@ -280,6 +322,8 @@ def gb300_arm(args, world, rank, local):
                     "roofline": roofline(torch, c2, st2, bd2, sm2, flush, peak, peak_kind, 10)}
                 del st2, bd2, sm2, c2
                 torch.cuda.empty_cache()
+            extras_batch = batched_vs_sequential(torch, args.batch_steps)
+            torch.cuda.empty_cache()
     if rank != 0:
         if dist is not None:
             dist.destroy_process_group()
@@ -305,10 +349,12 @@ def gb300_arm(args, world, rank, local):
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
         "roofline": rl,
         "roofline_hbm_bound": extras,
+        "batched_vs_sequential": extras_batch,
         "e2e": {"value": round(e2e_mlups, 1), "unit": "MLUPS", "h2d_bytes_per_step": fbytes,
                 "d2h_bytes_per_step": fbytes,
                 "path": "vivsim_gb300.solver.Simulation.run from pinned host populations"},
-        "gpu_launches": launches_per_step * args.chunk * args.steps,
+        "gpu_launches": (launches_per_step * args.chunk + (step_groups(case) if body is not None else 0))
+        * args.steps,
         "cpu_baseline": cpu,
         "clocks": clocks,
     }

@@ -242,11 +242,19 @@ typedef struct vs_body_cfg {
 } vs_body_cfg;
 
 typedef struct vs_body_plan vs_body_plan;
+/* A 2-D body whose markers share stencil nodes only with neighbours a few positions away in
+ * marker order (a curve of markers; checked once from the rigid marker set) uses the chain
+ * form of the body kernel; others use the general form (an in-shared-memory sort).  Both
+ * give the same results; VIVSIM_GB300_BODY_CSR=1 in the environment at plan creation
+ * selects the general form. */
 int vs_body_plan_create(const vs_body_cfg* cfg, const vs_lattice_plan* lattice, vs_body_plan** out);
 int vs_body_plan_destroy(vs_body_plan* plan);
 /* Copy the body state out: (a, v, d, h) as 4 x 3 doubles (device state, synchronises the stream). */
 int vs_body_get_state(const vs_body_plan* plan, double* state_host, void* stream);
 int vs_body_set_state(vs_body_plan* plan, const double* state_host, void* stream);
+/* Device address of the body state (a[3], v[3], d[3], h[3] in the plan dtype), for
+ * callers that copy or read it on the device between steps. */
+int vs_body_state_device(const vs_body_plan* plan, void** state);
 
 /* One step: f_out = step(f_in).  body may be NULL.  force_hist, when not NULL, receives
  * the body force h (3 values of the plan dtype) of this step.  f_out must not alias f_in. */
@@ -266,6 +274,61 @@ int vs_run_graph(vs_lattice_plan* lattice, vs_body_plan* body, void* f_a, void* 
  * dominant kernel can be timed on its own. */
 int vs_step_grid_only(const vs_lattice_plan* lattice, const vs_body_plan* body, const void* f_in, void* f_out,
                       void* stream);
+
+/* ================================================================ many cases ===
+ * A batch advances many independent cases (one lattice plan each, with an optional body
+ * plan) in lock step: every time step is one body launch (one CTA per 2-D body of the
+ * chain form), one grid launch over the nodes of all cases outside their bodies' boxes,
+ * and one launch over all boxes after the join, instead of three launches per case.
+ * The reference runs such sweeps as separate jitted loops (one per case); this has no
+ * single counterpart there.  Results equal vs_run of each case on its own.
+ * All cases share q, dtype and collision model; other bodies (3-D, general form) run
+ * their own kernels inside the batch.  The plans must stay alive while the batch is used. */
+typedef struct vs_batch_plan vs_batch_plan;
+int vs_batch_plan_create(vs_lattice_plan* const* lattices, vs_body_plan* const* bodies, int n_cases,
+                         vs_batch_plan** out);
+int vs_batch_plan_destroy(vs_batch_plan* plan);
+/* Launch shape: threads per block of the grid launches (32, 64, 128, 256) and the number
+ * of middle time steps captured per CUDA graph (0: no graph; rounded down to even). */
+int vs_batch_set_launch(vs_batch_plan* plan, int threads_per_block, int steps_per_graph);
+/* n_steps steps of every case; case k ping-pongs between f_a[k] (input) and f_b[k] as in
+ * vs_run.  Device parameter tables are built on the first call for a set of buffers (a
+ * synchronous upload); graphs need a non-default stream (else steps are launched one by
+ * one). */
+int vs_batch_run(vs_batch_plan* plan, void* const* f_a, void* const* f_b, int n_steps, void* stream);
+
+/* ================================================================== adjoint ===
+ * Gradients of a 2-D cylinder VIV objective by a hand-written discrete adjoint of the
+ * fused step: D2Q9 BGK, exact-difference forcing, MDF immersed boundary, a 1-DOF
+ * transverse spring (Newmark), equilibrium inflow ux = U0 at x = 0, pressure NEE
+ * outflow at x = nx-1, periodic y (examples/2d/vortex_induced_vibration.py:96-148 with
+ * BGK).  The reference obtains such gradients with jax.grad through its jitted loop; this
+ * has no single counterpart there.  Objective: J = mean over steps [obj_start, n_steps)
+ * of the x force on the body.  Parameters: U0 (inflow, initial state feq(1, (U0, 0)),
+ * and omega = 1 / (3 U0 D / Re + 0.5)), the spring stiffness, and the radial offsets of
+ * the markers (marker m at angle 2 pi m / n_markers, radius D/2 + offsets[m]; ds =
+ * pi D / n_markers).  Populations are checkpointed every checkpoint_every steps and
+ * each segment is recomputed before its reverse sweep. */
+typedef struct vs_adjoint_cfg {
+  int dtype;
+  int nx, ny;
+  double U0, D, Re, rho_out;
+  int n_markers;
+  double cx, cy;
+  const double* offsets_host; /* (n_markers,) */
+  int kernel, radius, n_iter;
+  double mass, stiffness, damping, added_mass_area;
+  int n_steps, checkpoint_every, obj_start;
+} vs_adjoint_cfg;
+typedef struct vs_adjoint_plan vs_adjoint_plan;
+int vs_adjoint_plan_create(const vs_adjoint_cfg* cfg, vs_adjoint_plan** out);
+int vs_adjoint_plan_destroy(vs_adjoint_plan* plan);
+/* Forward run from rest; J_out receives the objective.  keep_checkpoints != 0 stores
+ * what vs_adjoint_backward needs. */
+int vs_adjoint_forward(vs_adjoint_plan* plan, int keep_checkpoints, double* J_out, void* stream);
+/* Reverse sweep: seed * dJ/dU0, dJ/dstiffness and dJ/doffsets (n_markers). */
+int vs_adjoint_backward(vs_adjoint_plan* plan, double seed, double* grad_U0, double* grad_K, double* grad_offsets,
+                        void* stream);
 
 #ifdef __cplusplus
 }

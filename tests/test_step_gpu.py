@@ -209,6 +209,85 @@ def test_viv_oracle_larger(S):
     assert rel_err(st["h"][:2], h) <= 3e-4
 
 
+def _chain_width(X, R=2):
+    """Cyclic index distance bound of a rigid marker set (the plan's chain check)."""
+    M, K = len(X), 0
+    for i in range(M):
+        for j in range(i + 1, M):
+            if abs(X[i, 0] - X[j, 0]) < 2 * R + 1e-3 and abs(X[i, 1] - X[j, 1]) < 2 * R + 1e-3:
+                K = max(K, min(j - i, M - (j - i)))
+    return K
+
+
+def _viv_small(S, X, steps, graph=False):
+    nx, ny = 96, 64
+    rng = np.random.default_rng(3)
+    u = np.zeros((2, nx, ny), np.float32)
+    u[0] = 0.05
+    u[1] = 1e-3 * rng.standard_normal((nx, ny))
+    f0 = T(L2.get_equilibrium(np.ones((nx, ny), np.float32), u))
+    step = S.LatticeStep(9, (nx, ny), "kbc", 1.8, forcing="edm",
+                         boundaries=[S.boundary("equilibrium", "left", ux_wall=0.05),
+                                     S.boundary("nee", "right", mode="pressure")])
+    body = S.RigidBody(step, X, 0.94, moving=True, free_dof=(False, True), mass=500.0, stiffness=0.05,
+                       added_mass_area=113.0, v0=(0, 2e-3, 0))
+    sim = S.Simulation(step, f0, body)
+    hist = sim.run(steps, graph=graph, force_history=True)
+    return N(sim.f), body.state(), N(hist)
+
+
+def test_body_chain_form_equals_general_form(S, monkeypatch):
+    """The chain body kernel (neighbour search by marker index) and the general one (shared-
+    memory sort) sum every node in the same order: identical bits over 30 moving steps."""
+    th = np.linspace(0, 2 * np.pi, 40, endpoint=False)
+    X = np.stack([30 + 6 * np.cos(th), 32 + 6 * np.sin(th)], 1).astype(np.float32).astype(np.float64)
+    assert 2 * _chain_width(X) + 1 <= 31  # the chain form applies to this marker set
+    fa, sa, ha = _viv_small(S, X, 30)
+    monkeypatch.setenv("VIVSIM_GB300_BODY_CSR", "1")
+    fb, sb, hb = _viv_small(S, X, 30)
+    assert np.array_equal(fa, fb)
+    assert np.array_equal(ha, hb)
+    for k in ("a", "v", "d", "h"):
+        assert np.array_equal(sa[k], sb[k]), k
+
+
+def test_viv_shuffled_markers_general_form(S):
+    """Markers in random order (no chain bound: the general body kernel) against the oracle."""
+    nx, ny, D, U0, M = 64, 48, 12.0, 0.05, 38
+    om = L2.get_omega(U0 * D / 60.0)
+    th = np.linspace(0, 2 * np.pi, M, endpoint=False)
+    perm = np.random.default_rng(5).permutation(M)
+    X0 = (20.0 + 0.5 * D * np.cos(th)).astype(np.float32)[perm]
+    Y0 = (24.0 + 0.5 * D * np.sin(th)).astype(np.float32)[perm]
+    assert 2 * _chain_width(np.stack([X0, Y0], 1).astype(np.float64)) + 1 > 31
+    rng = np.random.default_rng(0)
+    u = np.zeros((2, nx, ny), np.float32)
+    u[0] = U0
+    u[1] = 1e-4 * rng.standard_normal((nx, ny))
+    f0 = L2.get_equilibrium(np.ones((nx, ny), np.float32), u)
+    area = math.pi * (D / 2) ** 2
+    mass = 10 * area
+    K = (2 * math.pi * U0 / (5 * D)) ** 2 * mass * 1.1
+    ds = math.pi * D / M
+    bcs = [("eq", "left", dict(ux_wall=U0)), ("pnee", "right", dict(rho_wall=1.0))]
+    body_o = recipes.Body2D(X0, Y0, ds, mass, K, 0.0, area, free=(False, True), n_iter=3,
+                            v=np.array([0, 1e-3], np.float32))
+    step = S.LatticeStep(9, (nx, ny), "kbc", om, forcing="edm",
+                         boundaries=[S.boundary("equilibrium", "left", ux_wall=U0),
+                                     S.boundary("nee", "right", mode="pressure", rho_wall=1.0)])
+    body = S.RigidBody(step, np.stack([X0, Y0], 1), ds, moving=True, free_dof=(False, True), mass=mass,
+                       stiffness=K, added_mass_area=area, v0=(0, 1e-3, 0))
+    sim = S.Simulation(step, T(f0), body)
+    f = f0
+    for _ in range(10):
+        f, h = recipes.ib_lbm_step_2d(f, body_o, "kbc", om, None, bcs)
+    sim.run(10)
+    assert rel_err(N(sim.f), f) <= 1e-5
+    st = body.state()
+    assert rel_err(st["d"][:2], body_o.d) <= 1e-4
+    assert rel_err(st["h"][:2], h) <= 3e-4
+
+
 def test_graph_replay_matches_eager_and_is_deterministic(S):
     nx, ny = 96, 64
     rng = np.random.default_rng(3)

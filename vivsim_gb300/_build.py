@@ -24,6 +24,7 @@ UNITS = {
     "vs_ops_lbm.cu": ["-fmad=false"],
     "vs_ops_ib.cu": ["-fmad=false"],
     "vs_step.cu": [],
+    "vs_adjoint.cu": [],
 }
 
 

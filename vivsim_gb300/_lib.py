@@ -65,6 +65,17 @@ class vs_body_cfg(C.Structure):
                 ("window_margin", C.c_int)]
 
 
+class vs_adjoint_cfg(C.Structure):
+    _fields_ = [("dtype", C.c_int), ("nx", C.c_int), ("ny", C.c_int),
+                ("U0", C.c_double), ("D", C.c_double), ("Re", C.c_double), ("rho_out", C.c_double),
+                ("n_markers", C.c_int), ("cx", C.c_double), ("cy", C.c_double),
+                ("offsets_host", C.POINTER(C.c_double)),
+                ("kernel", C.c_int), ("radius", C.c_int), ("n_iter", C.c_int),
+                ("mass", C.c_double), ("stiffness", C.c_double), ("damping", C.c_double),
+                ("added_mass_area", C.c_double),
+                ("n_steps", C.c_int), ("checkpoint_every", C.c_int), ("obj_start", C.c_int)]
+
+
 _i, _d, _p, _l, _z = C.c_int, C.c_double, C.c_void_p, C.c_int64, C.c_size_t
 _SIGS = {
     "vs_last_error": (C.c_char_p, []),
@@ -107,6 +118,15 @@ _SIGS = {
     "vs_run": (_i, [_p, _p, _p, _p, _i, _p, _p]),
     "vs_run_graph": (_i, [_p, _p, _p, _p, _i, _p, _p]),
     "vs_step_grid_only": (_i, [_p, _p, _p, _p, _p]),
+    "vs_body_state_device": (_i, [_p, C.POINTER(C.c_void_p)]),
+    "vs_batch_plan_create": (_i, [C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), _i, C.POINTER(C.c_void_p)]),
+    "vs_batch_plan_destroy": (_i, [_p]),
+    "vs_batch_set_launch": (_i, [_p, _i, _i]),
+    "vs_batch_run": (_i, [_p, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), _i, _p]),
+    "vs_adjoint_plan_create": (_i, [C.POINTER(vs_adjoint_cfg), C.POINTER(C.c_void_p)]),
+    "vs_adjoint_plan_destroy": (_i, [_p]),
+    "vs_adjoint_forward": (_i, [_p, _i, C.POINTER(_d), _p]),
+    "vs_adjoint_backward": (_i, [_p, _d, C.POINTER(_d), C.POINTER(_d), C.POINTER(_d), _p]),
     "vs_lattice_status": (_i, [_p, _i, _p]),
 }
 

@@ -126,6 +126,24 @@ def periodic2d(n=8192, collision="kbc", U0=0.05, nu=0.01, seed=4):
                 omega=omega_of(nu), forcing="none", boundaries=[], f0=equilibrium_d2q9(rho, u), body=None)
 
 
+def viv_sweep(n_cases=64, seed=3, heights=(64, 128, 256, 512), collision="kbc"):
+    """Independent cylinder VIV cases of uneven size: H uniform in `heights`, grid 2H x H,
+    D = H/12 at (H/2, H/2) (W/4, H/2 with W = 2H), round(pi D) markers, U_r ~ U[3, 8],
+    Re ~ U[50, 200], U0 = 0.05, mass ratio 10, KBC; boundaries as viv2d.  Draw order per
+    case from default_rng(seed): H, U_r, Re, then the case's perturbation seed."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n_cases):
+        H = int(heights[int(rng.integers(len(heights)))])
+        U_r = float(rng.uniform(3.0, 8.0))
+        Re = float(rng.uniform(50.0, 200.0))
+        s = int(rng.integers(1 << 31))
+        D = H / 12.0
+        out.append(viv2d(nx=2 * H, ny=H, collision=collision, D=D, center=(H / 2.0, H / 2.0),
+                         n_markers=int(round(math.pi * D)), Re=Re, U_r=U_r, seed=s))
+    return out
+
+
 CASES = {"cavity": cavity, "viv2d": viv2d, "sphere3d": sphere3d, "periodic2d": periodic2d}
 
 

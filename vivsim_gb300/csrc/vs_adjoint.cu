@@ -1,0 +1,922 @@
+// Discrete adjoint of the 2-D cylinder VIV step (D2Q9 BGK, exact-difference forcing,
+// multi-direct-forcing immersed boundary on a spring-mounted rigid cylinder, Newmark,
+// equilibrium inflow, pressure non-equilibrium-extrapolation outflow, periodic y).
+//
+// Forward step (examples/2d/vortex_induced_vibration.py:96-148, with BGK collision):
+//   rho, u = get_macroscopic(f);  f1 = (1 - w) f + w feq(rho, u)
+//   X = X0 + d;  W = kernel(node - X) (ib/stencil.py:7-51)
+//   U0 = interp(u);  k = 0..n_iter-1:  Fs_k = (v - U_k) 2 ds,  Ft += Fs_k,
+//                                     U_k+1 = U_k + interp(0.5 spread(Fs_k))   (ib/mdf.py)
+//   g = spread(Ft);  h = -sum Ft + a A;  Newmark (dyn.py:5-51) on the free DOFs
+//   f2 = f1 + guo(g, u) (lbm/forcing/edm.py);  f3 = stream(f2);  f' = nee_p(eq(f3))
+// The reverse sweep runs these in reverse with hand-derived transposes:
+//   k_adj_bc    the outflow boundary (its 9 x 18 local Jacobian by forward-mode dual numbers)
+//               and the inflow boundary (zeroes the wall adjoint, accumulates d/dU0)
+//   k_adj_body  one CTA: recomputes the body's forward MDF, then Newmark^T, spread^T =
+//               interpolation, the MDF iterations in reverse, interp^T = spread, and the
+//               derivative of the weights with respect to the marker positions
+//   k_adj_grid  per node: reverse streaming (pull) fused with the transposed Jacobian of
+//               collision + forcing, plus the d/domega reduction
+// f is checkpointed every `checkpoint_every` steps; each segment is recomputed forward
+// (keeping its states) before its reverse sweep, so memory is (steps / C + C) grids.
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "vs_boundary.cuh"
+#include "vs_dispatch.cuh"
+#include "vs_ib.cuh"
+
+namespace vs {
+namespace adj {
+
+// ------------------------------------------------------------------ dual numbers
+template <typename T>
+struct Dual {
+  T v, d;
+  __device__ Dual() : v(0), d(0) {}
+  __device__ Dual(T a, T b) : v(a), d(b) {}
+  template <typename U>
+  __device__ Dual(U a) : v((T)a), d(0) {}
+};
+template <typename T>
+__device__ __forceinline__ Dual<T> operator+(Dual<T> a, Dual<T> b) { return Dual<T>(a.v + b.v, a.d + b.d); }
+template <typename T>
+__device__ __forceinline__ Dual<T> operator-(Dual<T> a, Dual<T> b) { return Dual<T>(a.v - b.v, a.d - b.d); }
+template <typename T>
+__device__ __forceinline__ Dual<T> operator-(Dual<T> a) { return Dual<T>(-a.v, -a.d); }
+template <typename T>
+__device__ __forceinline__ Dual<T> operator*(Dual<T> a, Dual<T> b) {
+  return Dual<T>(a.v * b.v, a.d * b.v + a.v * b.d);
+}
+template <typename T>
+__device__ __forceinline__ Dual<T> operator/(Dual<T> a, Dual<T> b) {
+  const T q = a.v / b.v;
+  return Dual<T>(q, (a.d - q * b.d) / b.v);
+}
+
+// feq_i(rho, u) in the reference's form (lbm/basic.py:114-135), generic scalar S
+template <typename S, typename T>
+__device__ __forceinline__ void feq9(S rho, S ux, S uy, S* out) {
+  const S usq = ux * ux + uy * uy;
+#pragma unroll
+  for (int i = 0; i < 9; ++i) {
+    const S uc = ux * S((T)q9_cx(i)) + uy * S((T)q9_cy(i));
+    out[i] = (rho * S(q9_w<T>(i))) * (((S(1) + S(3) * uc) + S(4.5) * (uc * uc)) - S(1.5) * usq);
+  }
+}
+
+// boundary_pressure_nee at the right wall for one face node (lbm/boundary/nee.py:19-60,
+// _helpers.py:98-121, 200-217): wall populations w, neighbour populations nb -> out
+template <typename S, typename T>
+__device__ __forceinline__ void pnee_right(const S* w, const S* nb, T rho_w, S* out) {
+  constexpr int loc = VS_RIGHT;
+  const S num = rho_numerator(L9{}, loc, w);
+  const S nvs = S(1) - num / S(rho_w);
+  S u[2];
+  u[0] = S(loc_sign(loc)) * nvs;
+  pressure_tangential(L9{}, loc, nb, u);
+  S fw[9], fe[9], rn, un[2];
+  feq9<S, T>(S(rho_w), u[0], u[1], fw);
+  macro(L9{}, nb, rn, un);
+  feq9<S, T>(rn, un[0], un[1], fe);
+#pragma unroll
+  for (int i = 0; i < 9; ++i) out[i] = fw[i] + (nb[i] - fe[i]);
+}
+
+// post-collision populations of node (x, y) without body force (BGK)
+template <typename T>
+__device__ __forceinline__ void post_collide(const T* __restrict__ f, int64_t n, int ny, int x, int y, T omega,
+                                             T* out) {
+  const int64_t p = (int64_t)x * ny + y;
+  T fl[9], r, u[2], fe[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) fl[i] = f[i * n + p];
+  macro(L9{}, fl, r, u);
+  feq9<T, T>(r, u[0], u[1], fe);
+#pragma unroll
+  for (int i = 0; i < 9; ++i) out[i] = (T(1) - omega) * fl[i] + omega * fe[i];
+}
+
+template <typename T>
+struct GridArgs {
+  const T* f;   // populations at the start of the step (9, nx, ny)
+  T* lam;       // in: adjoint of the step's output; k_adj_bc rewrites its wall columns
+  T* lam_out;   // out: adjoint of f
+  const T* g;   // body force of the step on the full grid (2, nx, ny), zero off the stencils
+  const T* lu;  // adjoint of u from the immersed boundary (2, nx, ny)
+  int nx, ny;
+  T omega, U0, rho_out;
+  double* acc;  // [0] d/dU0 (boundaries), [1] d/domega
+};
+
+__device__ __forceinline__ int wrap(int a, int n) { return a < 0 ? a + n : (a >= n ? a - n : a); }
+
+// block sum of v into *acc (one atomic per block; the order of the atomics varies, the
+// per-block partial sums do not)
+template <int NT>
+__device__ __forceinline__ void block_accumulate(double v, double* acc) {
+  __shared__ double red[NT / 32];
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0;
+    for (int k = 0; k < NT / 32; ++k) s += red[k];
+    if (s != 0.0) atomicAdd(acc, s);
+  }
+}
+
+// Boundary adjoint, one thread per face row y.  Forward order: f_a = eq_left(f3),
+// f' = nee_p_right(f_a); reverse: right wall and neighbour columns, then the left wall.
+template <typename T>
+__global__ void __launch_bounds__(128) k_adj_bc(GridArgs<T> A) {
+  const int y = blockIdx.x * blockDim.x + threadIdx.x;
+  double dU0 = 0.0;
+  if (y < A.ny) {
+    const int nx = A.nx, ny = A.ny;
+    const int64_t n = (int64_t)nx * ny;
+    // streamed populations (before the boundaries) at the wall and its neighbour
+    T w[9], nb[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+      T src[9];
+      post_collide(A.f, n, ny, wrap(nx - 1 - q9_cx(i), nx), wrap(y - q9_cy(i), ny), A.omega, src);
+      w[i] = src[i];
+      post_collide(A.f, n, ny, nx - 2 - q9_cx(i), wrap(y - q9_cy(i), ny), A.omega, src);
+      nb[i] = src[i];
+    }
+    const int64_t pw = (int64_t)(nx - 1) * ny + y, pn = (int64_t)(nx - 2) * ny + y;
+    T lout[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) lout[i] = A.lam[i * n + pw];
+    T lw[9], ln[9];
+    for (int k = 0; k < 18; ++k) {
+      Dual<T> dw[9], dn[9], o[9];
+#pragma unroll
+      for (int i = 0; i < 9; ++i) {
+        dw[i] = Dual<T>(w[i], (T)(k == i));
+        dn[i] = Dual<T>(nb[i], (T)(k == 9 + i));
+      }
+      pnee_right<Dual<T>, T>(dw, dn, A.rho_out, o);
+      T s = T(0);
+#pragma unroll
+      for (int i = 0; i < 9; ++i) s += lout[i] * o[i].d;
+      if (k < 9) lw[k] = s;
+      else ln[k - 9] = s;
+    }
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+      A.lam[i * n + pw] = lw[i];  // the wall values were replaced: only the new path remains
+      A.lam[i * n + pn] = A.lam[i * n + pn] + ln[i];
+    }
+    // left wall: f = feq(1, (U0, 0)) replaced every population (lbm/boundary/eq.py:25-56)
+    const int64_t p0 = y;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+      const T cx = (T)q9_cx(i);
+      const T dfeq = q9_w<T>(i) * ((T(3) * cx + T(9) * (cx * A.U0) * cx) - T(3) * A.U0);
+      dU0 += (double)(A.lam[i * n + p0] * dfeq);
+      A.lam[i * n + p0] = T(0);
+    }
+  }
+  block_accumulate<128>(dU0, A.acc + 0);
+}
+
+// Grid adjoint, one thread per node: pull the streamed adjoint, then the transposed
+// Jacobian of BGK collision + exact-difference forcing at this node.
+template <typename T>
+__global__ void __launch_bounds__(256) k_adj_grid(GridArgs<T> A) {
+  const int nx = A.nx, ny = A.ny;
+  const int64_t n = (int64_t)nx * ny;
+  const int x = blockIdx.y, y = blockIdx.x * blockDim.x + threadIdx.x;
+  double dw = 0.0;
+  if (y < ny) {
+    const int64_t p = (int64_t)x * ny + y;
+    T f[9], l2[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+      f[i] = A.f[i * n + p];
+      l2[i] = A.lam[i * n + (int64_t)wrap(x + q9_cx(i), nx) * ny + wrap(y + q9_cy(i), ny)];
+    }
+    T r, u[2], fe[9];
+    macro(L9{}, f, r, u);
+    feq9<T, T>(r, u[0], u[1], fe);
+    const T g0 = A.g[p], g1 = A.g[n + p];
+    // lambda_u from the forcing term: d/du_a of w_i (3 (c_i - u).g + 9 (c_i.u)(c_i.g))
+    T lu0 = A.lu[p], lu1 = A.lu[n + p];
+    T lrho = T(0);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+      const T cx = (T)q9_cx(i), cy = (T)q9_cy(i), wi = q9_w<T>(i);
+      const T cu = cx * u[0] + cy * u[1], cg = cx * g0 + cy * g1;
+      lu0 += l2[i] * wi * (T(-3) * g0 + T(9) * cg * cx);
+      lu1 += l2[i] * wi * (T(-3) * g1 + T(9) * cg * cy);
+      // collision: omega feq_i(rho, u)
+      const T lf = A.omega * l2[i];
+      lrho += lf * fe[i] / r;
+      const T rw = r * wi;
+      lu0 += lf * rw * ((T(3) * cx + T(9) * cu * cx) - T(3) * u[0]);
+      lu1 += lf * rw * ((T(3) * cy + T(9) * cu * cy) - T(3) * u[1]);
+      dw += (double)(l2[i] * (fe[i] - f[i]));
+    }
+#pragma unroll
+    for (int j = 0; j < 9; ++j) {
+      const T cx = (T)q9_cx(j), cy = (T)q9_cy(j);
+      A.lam_out[j * n + p] = (T(1) - A.omega) * l2[j] + lrho + (lu0 * (cx - u[0]) + lu1 * (cy - u[1])) / r;
+    }
+  }
+  block_accumulate<256>(dw, A.acc + 1);
+}
+
+// d/dU0 of the initial state f = feq(1, (U0, 0)) everywhere
+template <typename T>
+__global__ void __launch_bounds__(256) k_adj_initial(const T* __restrict__ lam, int64_t n, T U0, double* acc) {
+  double s = 0.0;
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+      const T cx = (T)q9_cx(i);
+      s += (double)(lam[i * n + p] * (q9_w<T>(i) * ((T(3) * cx + T(9) * (cx * U0) * cx) - T(3) * U0)));
+    }
+  }
+  block_accumulate<256>(s, acc);
+}
+
+// ------------------------------------------------------------------ body adjoint
+template <typename T>
+struct BodyArgs {
+  const T* f;       // populations at the start of the step
+  const T* lam;     // adjoint of the streamed populations (after k_adj_bc)
+  T* g;             // out: forward body force at the stencil nodes (2, nx, ny)
+  T* lu;            // out: adjoint of u at the stencil nodes (2, nx, ny)
+  const T* state;   // body state at the start of the step: a[3], v[3], d[3], h[3]
+  T* lstate;        // in: adjoint of the state after the step (a, v, d: 3 each); out: before
+  const T* X0;      // (M) marker x, (M) marker y
+  int nx, ny, M, kernel, n_iter;
+  T ds2;            // 2 ds
+  T wobj;           // weight of this step's x force in the objective
+  T k1, k2, c1, c2, dt, damp, stiff, den, area;
+  int free_dof[2];
+  double* dK;       // d/dstiffness
+  double* dX;       // (2 M): d/dX0, d/dY0
+};
+
+constexpr int kAdjBodyThreads = 512;
+
+// derivative of the delta kernels (ib/kernels.py), d phi / d r
+template <typename T>
+__device__ __forceinline__ T ddelta(int kernel, T r) {
+  const T a = fabs(r), sg = r < T(0) ? T(-1) : T(1);
+  if (kernel == VS_KERNEL_PESKIN4) {
+    if (a >= T(2)) return T(0);
+    if (a < T(1)) {
+      const T q = sqrt((T(1) + T(4) * a) - T(4) * (a * a));
+      return sg * T(0.125) * (T(-2) + (T(2) - T(4) * a) / q);
+    }
+    const T q = sqrt((T(-7) + T(12) * a) - T(4) * (a * a));
+    return sg * T(0.125) * (T(-2) - (T(6) - T(4) * a) / q);
+  }
+  if (kernel == VS_KERNEL_PESKIN3) {
+    if (a >= T(1.5)) return T(0);
+    if (a < T(0.5)) return sg * (-(T(3) * a) / sqrt(T(1) - T(3) * (a * a))) / T(3);
+    return sg * (T(-3) - (T(3) - T(3) * a) / sqrt((T(-2) + T(6) * a) - T(3) * (a * a))) / T(6);
+  }
+  if (a >= T(2)) return T(0);
+  const T k = (T)3.14159265358979323846 * T(0.5);
+  return sg * T(-0.25) * k * sin(k * a);
+}
+
+// Node sum over the pairs that reach the node of pair (m, s): sum_p W_p F[m_p] (both
+// components), the pairs found by scanning every marker (M is small for this body).
+template <typename T, int WD>
+__device__ __forceinline__ void node_sum(int nx_, int ny_, int M, const int* fxy, const T* W, const T* F, T& s0,
+                                         T& s1) {
+  constexpr int S = WD * WD;
+  s0 = T(0);
+  s1 = T(0);
+  for (int i = 0; i < M; ++i) {
+    const unsigned dx = (unsigned)(nx_ - fxy[2 * i]), dy = (unsigned)(ny_ - fxy[2 * i + 1]);
+    if (dx < (unsigned)WD && dy < (unsigned)WD) {
+      const T w = W[i * S + dx * WD + dy];
+      s0 += F[2 * i] * w;
+      s1 += F[2 * i + 1] * w;
+    }
+  }
+}
+
+template <typename T, int R>
+__global__ void __launch_bounds__(kAdjBodyThreads) k_adj_body(BodyArgs<T> A) {
+  constexpr int WD = 2 * R, S = WD * WD;
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int M = A.M, P = M * S, NI = A.n_iter > 0 ? A.n_iter : 0, NF = NI > 0 ? NI : 1;
+  const int nx = A.nx, ny = A.ny;
+  const int64_t n = (int64_t)nx * ny;
+  T* W = (T*)smem;             // [P] weights
+  T* dWx = W + P;              // [P] dW/dX of the marker
+  T* dWy = dWx + P;            // [P] dW/dY
+  T* lW = dWy + P;             // [P] adjoint of the weight
+  T* un = lW + P;              // [2P] u at the pair's node
+  T* lg = un + 2 * P;          // [2P] adjoint of g at the pair's node
+  T* nmu = lg + 2 * P;         // [2P] nodeval(mu) at the pair's node
+  T* Fs = nmu + 2 * P;         // [NF][2M] force steps; in reverse their adjoints
+  T* Ft = Fs + 2 * M * NF;     // [2M]
+  T* U = Ft + 2 * M;           // [2M]
+  T* mu = U + 2 * M;           // [2M] adjoint of U_k
+  T* lFt = mu + 2 * M;         // [2M] adjoint of Ft
+  T* red = lFt + 2 * M;        // [8] a, v, d, h adjoints
+  int* fxy = (int*)(red + 8);  // [2M] stencil corners
+
+  const T a[2] = {A.state[0], A.state[1]}, v[2] = {A.state[3], A.state[4]}, d[2] = {A.state[6], A.state[7]};
+  // markers (dyn.py:68-81), weights and their position derivatives, u and lambda_g at the nodes
+  for (int p = tid; p < P; p += nt) {
+    const int m = p / S, s = p - m * S, ix = s / WD, iy = s - ix * WD;
+    const T xm = A.X0[m] + d[0], ym = A.X0[M + m] + d[1];
+    const int fx = ifloor(xm), fy = ifloor(ym);
+    if (s == 0) {
+      fxy[2 * m] = fx - R + 1;
+      fxy[2 * m + 1] = fy - R + 1;
+    }
+    const T rx = (T)(fx + ix - R + 1) - xm, ry = (T)(fy + iy - R + 1) - ym;
+    const T px = delta(A.kernel, rx), py = delta(A.kernel, ry);
+    W[p] = px * py;
+    dWx[p] = -ddelta(A.kernel, rx) * py;
+    dWy[p] = -px * ddelta(A.kernel, ry);
+    lW[p] = T(0);
+    const int gx = fx + ix - R + 1, gy = fy + iy - R + 1;
+    // a forward run that succeeded kept every stencil inside the grid; clamp so that a
+    // caller's inconsistent state cannot read outside it
+    const int gxc = min(max(gx, 0), nx - 1), gyc = min(max(gy, 0), ny - 1);
+    const int64_t q = (int64_t)gxc * ny + gyc;
+    T fl[9], r, uu[2];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) fl[i] = A.f[i * n + q];
+    macro(L9{}, fl, r, uu);
+    un[2 * p] = uu[0];
+    un[2 * p + 1] = uu[1];
+    // lambda_g = sum_i lambda2_i d guo_i / d g, lambda2 pulled from the streamed adjoint
+    T l0 = T(0), l1 = T(0);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+      const T cx = (T)q9_cx(i), cy = (T)q9_cy(i), wi = q9_w<T>(i);
+      const T l = A.lam[i * n + (int64_t)wrap(gxc + q9_cx(i), nx) * ny + wrap(gyc + q9_cy(i), ny)];
+      const T cu = cx * uu[0] + cy * uu[1];
+      l0 += l * wi * (T(3) * (cx - uu[0]) + T(9) * cu * cx);
+      l1 += l * wi * (T(3) * (cy - uu[1]) + T(9) * cu * cy);
+    }
+    lg[2 * p] = l0;
+    lg[2 * p + 1] = l1;
+  }
+  __syncthreads();
+  // forward MDF (ib/mdf.py:38-64), every force step kept
+  for (int q = tid; q < 2 * M; q += nt) {
+    const int m = q >> 1, c = q & 1;
+    T acc = T(0);
+    for (int s = 0; s < S; ++s) acc += W[m * S + s] * un[2 * (m * S + s) + c];
+    U[q] = acc;
+    const T fs = (v[c] - acc) * A.ds2;
+    Fs[q] = fs;
+    Ft[q] = NI > 0 ? fs : T(0);
+  }
+  __syncthreads();
+  for (int k = 0; k + 1 < NI; ++k) {
+    const T* F = Fs + 2 * M * k;
+    for (int p = tid; p < P; p += nt) {  // spread(F_k) at each pair's node
+      const int m = p / S, s = p - m * S, ix = s / WD, iy = s - ix * WD;
+      node_sum<T, WD>(fxy[2 * m] + ix, fxy[2 * m + 1] + iy, M, fxy, W, F, nmu[2 * p], nmu[2 * p + 1]);
+    }
+    __syncthreads();
+    for (int q = tid; q < 2 * M; q += nt) {
+      const int m = q >> 1, c = q & 1;
+      T acc = T(0);
+      for (int s = 0; s < S; ++s) acc += W[m * S + s] * (T(0.5) * nmu[2 * (m * S + s) + c]);
+      const T uq = U[q] + acc;
+      U[q] = uq;
+      const T fs = (v[c] - uq) * A.ds2;
+      Fs[2 * M * (k + 1) + q] = fs;
+      Ft[q] = Ft[q] + fs;
+    }
+    __syncthreads();
+  }
+  // g = spread(Ft) at the stencil nodes, for the grid adjoint's forcing Jacobian
+  for (int p = tid; p < P; p += nt) {
+    const int m = p / S, s = p - m * S, ix = s / WD, iy = s - ix * WD;
+    const int gx = fxy[2 * m] + ix, gy = fxy[2 * m + 1] + iy;
+    T s0, s1;
+    node_sum<T, WD>(gx, gy, M, fxy, W, Ft, s0, s1);
+    if (gx < 0 || gx >= nx || gy < 0 || gy >= ny) continue;
+    const int64_t q = (int64_t)gx * ny + gy;
+    A.g[q] = s0;
+    A.g[n + q] = s1;
+  }
+  // h = -sum Ft + a A (dyn.py:126-136, vortex_induced_vibration.py:136) and the Newmark
+  // transpose (dyn.py:5-51); the objective weights h_x
+  if (tid == 0) {
+    T h[2];
+    for (int c = 0; c < 2; ++c) {
+      T acc = T(0);
+      for (int m = 0; m < M; ++m) acc += -Ft[2 * m + c];
+      h[c] = acc + a[c] * A.area;
+    }
+    double dK = 0.0;
+    for (int c = 0; c < 2; ++c) {
+      const T la1 = A.lstate[c], lv1 = A.lstate[3 + c], ld1 = A.lstate[6 + c];
+      T la, lv, ld, lh;
+      if (A.free_dof[c]) {
+        const T v1 = v[c] + A.k1 * a[c];
+        const T v2 = (d[c] + A.dt * v[c]) + A.k2 * a[c];
+        const T an = ((h[c] - A.damp * v1) - A.stiff * v2) / A.den;
+        const T lan = la1 + A.c1 * lv1 + A.c2 * ld1;  // a' feeds v' = c1 a' + v1, d' = c2 a' + v2
+        const T lv1_ = lv1 - lan * A.damp / A.den;
+        const T lv2_ = ld1 - lan * A.stiff / A.den;
+        lh = lan / A.den;
+        dK += (double)(lan * ((-v2 - an * A.c2) / A.den));  // den = m + c1 c + c2 k
+        la = A.k1 * lv1_ + A.k2 * lv2_;
+        lv = lv1_ + A.dt * lv2_;
+        ld = lv2_;
+      } else {
+        la = la1;
+        lv = lv1;
+        ld = ld1;
+        lh = T(0);
+      }
+      if (c == 0) lh += A.wobj;
+      red[c] = la + A.area * lh;
+      red[2 + c] = lv;
+      red[4 + c] = ld;
+      red[6 + c] = lh;
+    }
+    if (dK != 0.0) atomicAdd(A.dK, dK);
+  }
+  __syncthreads();
+  // lambda_Ft = interp(lambda_g) - lambda_h; mu_NI-1 = 0
+  for (int q = tid; q < 2 * M; q += nt) {
+    const int m = q >> 1, c = q & 1;
+    T acc = T(0);
+    for (int s = 0; s < S; ++s) acc += W[m * S + s] * lg[2 * (m * S + s) + c];
+    lFt[q] = acc - red[6 + c];
+    mu[q] = T(0);
+  }
+  __syncthreads();
+  // MDF in reverse: for k = NI-1 .. 0
+  //   lambda_Fs_k = lambda_Ft + [k < NI-1] 0.5 interp(nodeval(mu_k+1))
+  //   lambda_W   += [k < NI-1] 0.5 (mu_k+1,m . nodeval(Fs_k) + Fs_k,m . nodeval(mu_k+1))
+  //   mu_k = mu_k+1 - 2 ds lambda_Fs_k
+  for (int k = NI - 1; k >= 0; --k) {
+    T* F = Fs + 2 * M * k;
+    if (k + 1 < NI) {
+      for (int p = tid; p < P; p += nt) {
+        const int m = p / S, s = p - m * S, ix = s / WD, iy = s - ix * WD;
+        const int gx = fxy[2 * m] + ix, gy = fxy[2 * m + 1] + iy;
+        T m0, m1, f0, f1;
+        node_sum<T, WD>(gx, gy, M, fxy, W, mu, m0, m1);
+        node_sum<T, WD>(gx, gy, M, fxy, W, F, f0, f1);
+        nmu[2 * p] = m0;
+        nmu[2 * p + 1] = m1;
+        lW[p] += T(0.5) * ((mu[2 * m] * f0 + mu[2 * m + 1] * f1) + (F[2 * m] * m0 + F[2 * m + 1] * m1));
+      }
+      __syncthreads();
+    }
+    for (int q = tid; q < 2 * M; q += nt) {
+      const int m = q >> 1, c = q & 1;
+      T acc = T(0);
+      if (k + 1 < NI)
+        for (int s = 0; s < S; ++s) acc += W[m * S + s] * (T(0.5) * nmu[2 * (m * S + s) + c]);
+      const T lfs = lFt[q] + acc;
+      F[q] = lfs;  // the forward force step is no longer needed
+      mu[q] = mu[q] - A.ds2 * lfs;
+    }
+    __syncthreads();
+  }
+  // lambda_v: every force step targets the body velocity
+  if (tid < 2) {
+    T acc = T(0);
+    for (int k = 0; k < NI; ++k)
+      for (int m = 0; m < M; ++m) acc += A.ds2 * Fs[2 * M * k + 2 * m + tid];
+    red[2 + tid] += acc;
+  }
+  // interp^T: lambda_u at the nodes = nodeval(mu_0); weight adjoints of U0 = interp(u)
+  // and of g = spread(Ft)
+  for (int p = tid; p < P; p += nt) {
+    const int m = p / S, s = p - m * S, ix = s / WD, iy = s - ix * WD;
+    const int gx = fxy[2 * m] + ix, gy = fxy[2 * m + 1] + iy;
+    T n0, n1;
+    node_sum<T, WD>(gx, gy, M, fxy, W, mu, n0, n1);
+    if (gx >= 0 && gx < nx && gy >= 0 && gy < ny) {
+      const int64_t q = (int64_t)gx * ny + gy;
+      A.lu[q] = n0;
+      A.lu[n + q] = n1;
+    }
+    lW[p] += (mu[2 * m] * un[2 * p] + mu[2 * m + 1] * un[2 * p + 1]) +
+             (Ft[2 * m] * lg[2 * p] + Ft[2 * m + 1] * lg[2 * p + 1]);
+  }
+  __syncthreads();
+  // marker positions: X = X0 + d
+  for (int m = tid; m < M; m += nt) {
+    T gx_ = T(0), gy_ = T(0);
+    for (int s = 0; s < S; ++s) {
+      gx_ += lW[m * S + s] * dWx[m * S + s];
+      gy_ += lW[m * S + s] * dWy[m * S + s];
+    }
+    lFt[2 * m] = gx_;
+    lFt[2 * m + 1] = gy_;
+    atomicAdd(A.dX + m, (double)gx_);
+    atomicAdd(A.dX + M + m, (double)gy_);
+  }
+  __syncthreads();
+  if (tid < 2) {
+    T acc = T(0);
+    for (int m = 0; m < M; ++m) acc += lFt[2 * m + tid];
+    A.lstate[tid] = red[tid];
+    A.lstate[3 + tid] = red[2 + tid];
+    A.lstate[6 + tid] = red[4 + tid] + acc;
+  }
+}
+
+template <typename T>
+static size_t adj_body_smem(int M, int R, int n_iter) {
+  const size_t S = 4 * R * R, P = M * S, NF = n_iter > 0 ? n_iter : 1;
+  return sizeof(T) * (4 * P + 6 * P + 2 * M * NF + 8 * (size_t)M + 8) + sizeof(int) * 2 * M + 16;
+}
+
+}  // namespace adj
+}  // namespace vs
+
+// ------------------------------------------------------------------ plan
+struct vs_adjoint_plan {
+  vs_adjoint_cfg cfg;
+  vs_lattice_plan* lat = nullptr;
+  vs_body_plan* body = nullptr;
+  int64_t n = 0;
+  int M = 0, S = 0, C = 0, n_ck = 0;
+  size_t ts = 4;
+  double omega = 0, ds = 0;
+  std::vector<double> theta;       // marker angles
+  void* d_f0 = nullptr;            // initial populations
+  void* d_fa = nullptr;
+  void* d_fb = nullptr;
+  void* d_ck = nullptr;            // checkpoints: n_ck x (9 n)
+  void* d_ck_state = nullptr;      // n_ck x 12
+  void* d_seg = nullptr;           // (C + 1) x (9 n): one recomputed segment
+  void* d_seg_state = nullptr;     // (C + 1) x 12
+  void* d_lam[2] = {nullptr, nullptr};
+  void* d_g = nullptr;             // 2 n
+  void* d_lu = nullptr;            // 2 n
+  void* d_lstate = nullptr;        // 12
+  void* d_X0 = nullptr;            // 2 M
+  void* d_hist = nullptr;          // n_steps x 3
+  double* d_acc = nullptr;         // [0] dU0 (boundary), [1] domega, [2] dK, [3] dU0 (initial state), [4..] dX0, dY0
+  int have_ck = 0;
+  size_t body_smem = 0;
+};
+
+namespace vs {
+namespace adj {
+
+static void free_plan(vs_adjoint_plan* p) {
+  if (p->body) vs_body_plan_destroy(p->body);
+  if (p->lat) vs_lattice_plan_destroy(p->lat);
+  void* bufs[] = {p->d_f0, p->d_fa, p->d_fb, p->d_ck, p->d_ck_state, p->d_seg, p->d_seg_state, p->d_lam[0],
+                  p->d_lam[1], p->d_g, p->d_lu, p->d_lstate, p->d_X0, p->d_hist, p->d_acc};
+  for (void* b : bufs)
+    if (b) cudaFree(b);
+  delete p;
+}
+
+template <typename T>
+static void host_equilibrium(double U0, int64_t n, std::vector<T>& f) {
+  f.resize(9 * n);
+  for (int i = 0; i < 9; ++i) {
+    const double cx = q9_cx(i);
+    const double w = (double)(float)(i == 0 ? 4.0 / 9 : (i <= 4 ? 1.0 / 9 : 1.0 / 36));
+    const T uc = (T)(cx * U0), usq = (T)U0 * (T)U0;
+    const T v = ((T)1 * (T)w) * ((((T)1 + (T)3 * uc) + (T)4.5 * (uc * uc)) - (T)1.5 * usq);
+    for (int64_t p = 0; p < n; ++p) f[i * n + p] = v;
+  }
+}
+
+template <typename T>
+static int backward_t(vs_adjoint_plan* P, cudaStream_t st) {
+  const vs_adjoint_cfg& c = P->cfg;
+  const int64_t n = P->n;
+  const int N = c.n_steps, C = P->C;
+  const size_t fb = sizeof(T) * 9 * n;
+  cudaError_t e = cudaMemsetAsync(P->d_acc, 0, sizeof(double) * (4 + 2 * P->M), st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(P->d_lam[0], 0, fb, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(P->d_lstate, 0, sizeof(T) * 12, st);
+  if (e != cudaSuccess) return cuda_status(e, "vs_adjoint_backward");
+  int cur = 0;
+  void* state_dev = nullptr;
+  int rc = vs_body_state_device(P->body, &state_dev);
+  if (rc) return rc;
+  const double k1 = 0.5, k2 = 0.25, c1 = 0.5, c2 = 0.25;  // Newmark beta 1/4, gamma 1/2, dt 1
+  const double den = c.mass + c1 * c.damping + c2 * c.stiffness;
+  for (int sg = P->n_ck - 1; sg >= 0; --sg) {
+    const int s0 = sg * C, len = (N - s0) < C ? (N - s0) : C;
+    // restore the checkpoint and recompute the segment, keeping every state
+    T* seg = (T*)P->d_seg;
+    T* sst = (T*)P->d_seg_state;
+    e = cudaMemcpyAsync(seg, (const char*)P->d_ck + (size_t)sg * fb, fb, cudaMemcpyDeviceToDevice, st);
+    if (e != cudaSuccess) return cuda_status(e, "vs_adjoint_backward restore");
+    {
+      T hs[12];
+      double hd[12];
+      e = cudaMemcpyAsync(hs, (const char*)P->d_ck_state + (size_t)sg * 12 * sizeof(T), sizeof(hs),
+                          cudaMemcpyDeviceToHost, st);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+      if (e != cudaSuccess) return cuda_status(e, "vs_adjoint_backward state");
+      for (int i = 0; i < 12; ++i) hd[i] = (double)hs[i];
+      rc = vs_body_set_state(P->body, hd, st);
+      if (rc) return rc;
+    }
+    for (int j = 0; j < len; ++j) {
+      e = cudaMemcpyAsync(sst + 12 * j, state_dev, sizeof(T) * 12, cudaMemcpyDeviceToDevice, st);
+      if (e != cudaSuccess) return cuda_status(e, "vs_adjoint_backward state copy");
+      rc = vs_step(P->lat, P->body, seg + (size_t)j * 9 * n, seg + (size_t)(j + 1) * 9 * n, nullptr, st);
+      if (rc) return rc;
+    }
+    // reverse sweep over the segment
+    for (int j = len - 1; j >= 0; --j) {
+      const int step = s0 + j;
+      const T* fj = seg + (size_t)j * 9 * n;
+      e = cudaMemsetAsync(P->d_g, 0, sizeof(T) * 2 * n, st);
+      if (e == cudaSuccess) e = cudaMemsetAsync(P->d_lu, 0, sizeof(T) * 2 * n, st);
+      if (e != cudaSuccess) return cuda_status(e, "vs_adjoint_backward memset");
+      GridArgs<T> G{};
+      G.f = fj;
+      G.lam = (T*)P->d_lam[cur];
+      G.lam_out = (T*)P->d_lam[1 - cur];
+      G.g = (const T*)P->d_g;
+      G.lu = (const T*)P->d_lu;
+      G.nx = c.nx;
+      G.ny = c.ny;
+      G.omega = (T)P->omega;
+      G.U0 = (T)c.U0;
+      G.rho_out = (T)c.rho_out;
+      G.acc = P->d_acc;
+      k_adj_bc<T><<<grid_for(c.ny, 128), 128, 0, st>>>(G);
+      BodyArgs<T> B{};
+      B.f = fj;
+      B.lam = (const T*)P->d_lam[cur];
+      B.g = (T*)P->d_g;
+      B.lu = (T*)P->d_lu;
+      B.state = sst + 12 * j;
+      B.lstate = (T*)P->d_lstate;
+      B.X0 = (const T*)P->d_X0;
+      B.nx = c.nx;
+      B.ny = c.ny;
+      B.M = P->M;
+      B.kernel = c.kernel;
+      B.n_iter = c.n_iter;
+      B.ds2 = (T)P->ds * T(2);
+      B.wobj = step >= c.obj_start ? (T)(1.0 / (double)(N - c.obj_start)) : T(0);
+      B.k1 = (T)k1; B.k2 = (T)k2; B.c1 = (T)c1; B.c2 = (T)c2; B.dt = T(1);
+      B.damp = (T)c.damping; B.stiff = (T)c.stiffness; B.den = (T)den; B.area = (T)c.added_mass_area;
+      B.free_dof[0] = 0;
+      B.free_dof[1] = 1;
+      B.dK = P->d_acc + 2;
+      B.dX = P->d_acc + 4;
+      switch (c.radius) {
+        case 1: k_adj_body<T, 1><<<1, kAdjBodyThreads, P->body_smem, st>>>(B); break;
+        case 2: k_adj_body<T, 2><<<1, kAdjBodyThreads, P->body_smem, st>>>(B); break;
+        default: k_adj_body<T, 3><<<1, kAdjBodyThreads, P->body_smem, st>>>(B); break;
+      }
+      k_adj_grid<T><<<dim3(grid_for(c.ny, 256), c.nx), 256, 0, st>>>(G);
+      VS_CHECK_LAUNCH("vs_adjoint_backward kernels");
+      cur = 1 - cur;
+    }
+  }
+  k_adj_initial<T><<<256, 256, 0, st>>>((const T*)P->d_lam[cur], n, (T)c.U0, P->d_acc + 3);
+  VS_CHECK_LAUNCH("vs_adjoint_backward initial state");
+  return VS_OK;
+}
+
+}  // namespace adj
+}  // namespace vs
+
+using namespace vs;
+using namespace vs::adj;
+
+extern "C" {
+
+int vs_adjoint_plan_create(const vs_adjoint_cfg* cfg, vs_adjoint_plan** out) {
+  VS_REQUIRE(cfg && out, "vs_adjoint_plan_create: null argument");
+  VS_REQUIRE(cfg->dtype == VS_F32 || cfg->dtype == VS_F64, "vs_adjoint_plan_create: bad dtype");
+  VS_REQUIRE(cfg->nx >= 16 && cfg->ny >= 16, "vs_adjoint_plan_create: grid too small");
+  VS_REQUIRE(cfg->n_markers >= 3 && cfg->offsets_host, "vs_adjoint_plan_create: markers and offsets needed");
+  VS_REQUIRE(cfg->n_steps >= 1 && cfg->checkpoint_every >= 1, "vs_adjoint_plan_create: steps / checkpoints");
+  VS_REQUIRE(cfg->obj_start >= 0 && cfg->obj_start < cfg->n_steps, "vs_adjoint_plan_create: objective window");
+  VS_REQUIRE(cfg->radius >= 1 && cfg->radius <= 3, "vs_adjoint_plan_create: radius 1..3");
+  VS_REQUIRE(cfg->U0 > 0 && cfg->D > 0 && cfg->Re > 0, "vs_adjoint_plan_create: U0, D, Re must be positive");
+  vs_adjoint_plan* P = new (std::nothrow) vs_adjoint_plan();
+  if (!P) {
+    set_error("out of host memory");
+    return VS_ERR_INVALID_ARG;
+  }
+  P->cfg = *cfg;
+  P->cfg.offsets_host = nullptr;
+  P->n = (int64_t)cfg->nx * cfg->ny;
+  P->M = cfg->n_markers;
+  P->S = 4 * cfg->radius * cfg->radius;
+  P->C = cfg->checkpoint_every;
+  P->n_ck = (cfg->n_steps + P->C - 1) / P->C;
+  P->ts = cfg->dtype == VS_F64 ? 8 : 4;
+  const double nu = cfg->U0 * cfg->D / cfg->Re;
+  P->omega = 1.0 / (3.0 * nu + 0.5);
+  P->ds = M_PI * cfg->D / cfg->n_markers;
+  auto fail = [&](int rc) {
+    free_plan(P);
+    return rc;
+  };
+  // markers on the circle, radius D/2 + offset
+  const int M = P->M;
+  std::vector<double> X(M), Y(M);
+  P->theta.resize(M);
+  double rmax = 0;
+  for (int m = 0; m < M; ++m) {
+    P->theta[m] = 2 * M_PI * m / M;
+    const double r = 0.5 * cfg->D + cfg->offsets_host[m];
+    rmax = r > rmax ? r : rmax;
+    X[m] = cfg->cx + r * cos(P->theta[m]);
+    Y[m] = cfg->cy + r * sin(P->theta[m]);
+  }
+  if (cfg->cx - rmax - cfg->radius - 2 < 4 || cfg->cx + rmax + cfg->radius + 2 > cfg->nx - 5) {
+    set_error("vs_adjoint_plan_create: the body's stencils must stay clear of the x = 0 / nx-1 boundaries");
+    return fail(VS_ERR_INVALID_ARG);
+  }
+  // the forward step: fused lattice + body plans
+  vs_lattice_cfg lc;
+  memset(&lc, 0, sizeof(lc));
+  lc.q = 9;
+  lc.dtype = cfg->dtype;
+  lc.nx = cfg->nx;
+  lc.ny = cfg->ny;
+  lc.nz = 1;
+  lc.collision = VS_COLLIDE_BGK;
+  lc.omega = P->omega;
+  lc.forcing = VS_FORCE_EDM;
+  lc.n_bc = 2;
+  lc.bc[0].kind = VS_BC_EQ;
+  lc.bc[0].mode = VS_WALL_GIVEN;
+  lc.bc[0].loc = VS_LEFT;
+  lc.bc[0].rho = 1.0;
+  lc.bc[0].ux = cfg->U0;
+  lc.bc[1].kind = VS_BC_NEE;
+  lc.bc[1].mode = VS_WALL_PRESSURE;
+  lc.bc[1].loc = VS_RIGHT;
+  lc.bc[1].rho = cfg->rho_out;
+  lc.variant = VS_GRID_PLAIN;
+  int rc = vs_lattice_plan_create(&lc, &P->lat);
+  if (rc) return fail(rc);
+  vs_body_cfg bc;
+  memset(&bc, 0, sizeof(bc));
+  bc.dim = 2;
+  bc.dtype = cfg->dtype;
+  bc.n_markers = M;
+  bc.x0_host = X.data();
+  bc.y0_host = Y.data();
+  bc.ds_scalar = P->ds;
+  bc.kernel = cfg->kernel;
+  bc.radius = cfg->radius;
+  bc.n_iter = cfg->n_iter;
+  bc.moving = 1;
+  bc.free_dof[1] = 1;
+  bc.mass = cfg->mass;
+  bc.stiffness = cfg->stiffness;
+  bc.damping = cfg->damping;
+  bc.added_mass_area = cfg->added_mass_area;
+  rc = vs_body_plan_create(&bc, P->lat, &P->body);
+  if (rc) return fail(rc);
+  const size_t ts = P->ts, fbytes = ts * 9 * P->n;
+  cudaError_t e = cudaSuccess;
+  auto alloc = [&](void** p, size_t bytes) {
+    if (e == cudaSuccess) e = cudaMalloc(p, bytes);
+  };
+  alloc(&P->d_f0, fbytes);
+  alloc(&P->d_fa, fbytes);
+  alloc(&P->d_fb, fbytes);
+  alloc(&P->d_ck, fbytes * P->n_ck);
+  alloc(&P->d_ck_state, ts * 12 * P->n_ck);
+  alloc(&P->d_seg, fbytes * (P->C + 1));
+  alloc(&P->d_seg_state, ts * 12 * (P->C + 1));
+  alloc(&P->d_lam[0], fbytes);
+  alloc(&P->d_lam[1], fbytes);
+  alloc(&P->d_g, ts * 2 * P->n);
+  alloc(&P->d_lu, ts * 2 * P->n);
+  alloc(&P->d_lstate, ts * 12);
+  alloc(&P->d_X0, ts * 2 * M);
+  alloc(&P->d_hist, ts * 3 * cfg->n_steps);
+  alloc((void**)&P->d_acc, sizeof(double) * (4 + 2 * M));
+  if (e != cudaSuccess) return fail(cuda_status(e, "vs_adjoint_plan_create"));
+  rc = dispatch_t(cfg->dtype, [&](auto t) -> int {
+    using T = typename decltype(t)::type;
+    std::vector<T> f0, x0(2 * M);
+    host_equilibrium<T>(cfg->U0, P->n, f0);
+    for (int m = 0; m < M; ++m) {
+      x0[m] = (T)X[m];
+      x0[M + m] = (T)Y[m];
+    }
+    cudaError_t e2 = cudaMemcpy(P->d_f0, f0.data(), fbytes, cudaMemcpyHostToDevice);
+    if (e2 == cudaSuccess) e2 = cudaMemcpy(P->d_X0, x0.data(), ts * 2 * M, cudaMemcpyHostToDevice);
+    if (e2 != cudaSuccess) return cuda_status(e2, "vs_adjoint_plan_create upload");
+    P->body_smem = adj_body_smem<T>(M, cfg->radius, cfg->n_iter);
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if ((int64_t)P->body_smem > optin) {
+      set_error("vs_adjoint_plan_create: %d markers need %zu bytes of shared memory", M, P->body_smem);
+      return VS_ERR_UNSUPPORTED;
+    }
+    switch (cfg->radius) {
+      case 1: e2 = cudaFuncSetAttribute(k_adj_body<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin); break;
+      case 2: e2 = cudaFuncSetAttribute(k_adj_body<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin); break;
+      default: e2 = cudaFuncSetAttribute(k_adj_body<T, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin); break;
+    }
+    return cuda_status(e2, "vs_adjoint_plan_create attribute");
+  });
+  if (rc) return fail(rc);
+  *out = P;
+  return VS_OK;
+}
+
+int vs_adjoint_plan_destroy(vs_adjoint_plan* plan) {
+  if (plan) free_plan(plan);
+  return VS_OK;
+}
+
+int vs_adjoint_forward(vs_adjoint_plan* P, int keep_checkpoints, double* J_out, void* stream) {
+  VS_REQUIRE(P, "vs_adjoint_forward: null plan");
+  cudaStream_t st = as_stream(stream);
+  const vs_adjoint_cfg& c = P->cfg;
+  const size_t ts = P->ts, fbytes = ts * 9 * P->n;
+  double zero[12] = {0};
+  int rc = vs_body_set_state(P->body, zero, stream);
+  if (rc) return rc;
+  cudaError_t e = cudaMemcpyAsync(P->d_fa, P->d_f0, fbytes, cudaMemcpyDeviceToDevice, st);
+  if (e != cudaSuccess) return cuda_status(e, "vs_adjoint_forward");
+  void* state_dev = nullptr;
+  rc = vs_body_state_device(P->body, &state_dev);
+  if (rc) return rc;
+  void* fa = P->d_fa;
+  void* fbuf = P->d_fb;
+  for (int s = 0, k = 0; s < c.n_steps; s += P->C, ++k) {
+    const int len = (c.n_steps - s) < P->C ? (c.n_steps - s) : P->C;
+    if (keep_checkpoints) {
+      e = cudaMemcpyAsync((char*)P->d_ck + (size_t)k * fbytes, fa, fbytes, cudaMemcpyDeviceToDevice, st);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync((char*)P->d_ck_state + (size_t)k * 12 * ts, state_dev, 12 * ts, cudaMemcpyDeviceToDevice,
+                            st);
+      if (e != cudaSuccess) return cuda_status(e, "vs_adjoint_forward checkpoint");
+    }
+    rc = vs_run(P->lat, P->body, fa, fbuf, len, (char*)P->d_hist + (size_t)s * 3 * ts, stream);
+    if (rc) return rc;
+    if (len % 2 == 1) {
+      void* t = fa;
+      fa = fbuf;
+      fbuf = t;
+    }
+  }
+  std::vector<unsigned char> h(ts * 3 * c.n_steps);
+  e = cudaMemcpyAsync(h.data(), P->d_hist, h.size(), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_status(e, "vs_adjoint_forward history");
+  double J = 0;
+  for (int s = c.obj_start; s < c.n_steps; ++s)
+    J += ts == 8 ? ((double*)h.data())[3 * s] : (double)((float*)h.data())[3 * s];
+  J /= (double)(c.n_steps - c.obj_start);
+  if (J_out) *J_out = J;
+  P->have_ck = keep_checkpoints ? 1 : 0;
+  double st_h[12];
+  return vs_body_get_state(P->body, st_h, stream);  // surfaces a body that left its window
+}
+
+int vs_adjoint_backward(vs_adjoint_plan* P, double seed, double* grad_U0, double* grad_K, double* grad_offsets,
+                        void* stream) {
+  VS_REQUIRE(P, "vs_adjoint_backward: null plan");
+  VS_REQUIRE(P->have_ck, "vs_adjoint_backward: run vs_adjoint_forward with keep_checkpoints first");
+  cudaStream_t st = as_stream(stream);
+  const int rc = dispatch_t(P->cfg.dtype, [&](auto t) -> int {
+    return backward_t<typename decltype(t)::type>(P, st);
+  });
+  if (rc) return rc;
+  const int M = P->M;
+  std::vector<double> acc(4 + 2 * M);
+  cudaError_t e = cudaMemcpyAsync(acc.data(), P->d_acc, sizeof(double) * acc.size(), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_status(e, "vs_adjoint_backward result");
+  const vs_adjoint_cfg& c = P->cfg;
+  const double domega = -3.0 * (c.D / c.Re) * P->omega * P->omega;
+  if (grad_U0) *grad_U0 = seed * (acc[0] + acc[3] + acc[1] * domega);
+  if (grad_K) *grad_K = seed * acc[2];
+  if (grad_offsets)
+    for (int m = 0; m < M; ++m)
+      grad_offsets[m] = seed * (acc[4 + m] * cos(P->theta[m]) + acc[4 + M + m] * sin(P->theta[m]));
+  double st_h[12];
+  return vs_body_get_state(P->body, st_h, stream);
+}
+
+}  // extern "C"

@@ -32,6 +32,24 @@ int cuda_status(cudaError_t e, const char* where);
 
 inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
+// Correctly rounded products and sums that the compiler never contracts into an FMA, for
+// the immersed-boundary arithmetic whose results must not depend on contraction choices.
+template <typename T>
+__device__ __forceinline__ T mul_rn(T a, T b) {
+  if constexpr (sizeof(T) == 4) return __fmul_rn(a, b);
+  else return __dmul_rn(a, b);
+}
+template <typename T>
+__device__ __forceinline__ T add_rn(T a, T b) {
+  if constexpr (sizeof(T) == 4) return __fadd_rn(a, b);
+  else return __dadd_rn(a, b);
+}
+template <typename T>
+__device__ __forceinline__ T sub_rn(T a, T b) {
+  if constexpr (sizeof(T) == 4) return __fsub_rn(a, b);
+  else return __dsub_rn(a, b);
+}
+
 inline unsigned grid_for(int64_t n, int block) {
   int64_t g = (n + block - 1) / block;
   return (unsigned)(g < 1 ? 1 : g);

@@ -7,28 +7,35 @@
 
 namespace vs {
 
+// The kernels are written with uncontracted operations (mul_rn / add_rn / sub_rn), so the
+// fused body kernels and the per-operator kernels compute identical weights.
+
 // Peskin 3-point, vivsim/ib/kernels.py:4-22
 template <typename T>
 __device__ __forceinline__ T delta_peskin3(T r) {
   const T a = fabs(r);
   if (a > T(1.5)) return T(0);
-  if (a < T(0.5)) return (T(1) + sqrt(T(1) - T(3) * (a * a))) / T(3);
-  return ((T(5) - T(3) * a) - sqrt((T(-2) + T(6) * a) - T(3) * (a * a))) / T(6);
+  const T aa = mul_rn(a, a);
+  if (a < T(0.5)) return add_rn(T(1), sqrt(sub_rn(T(1), mul_rn(T(3), aa)))) / T(3);
+  return sub_rn(sub_rn(T(5), mul_rn(T(3), a)), sqrt(sub_rn(add_rn(T(-2), mul_rn(T(6), a)), mul_rn(T(3), aa)))) /
+         T(6);
 }
 // Peskin 4-point, vivsim/ib/kernels.py:25-43
 template <typename T>
 __device__ __forceinline__ T delta_peskin4(T r) {
   const T a = fabs(r);
   if (a > T(2)) return T(0);
-  if (a < T(1)) return ((T(3) - T(2) * a) + sqrt((T(1) + T(4) * a) - T(4) * (a * a))) * T(0.125);
-  return ((T(5) - T(2) * a) - sqrt((T(-7) + T(12) * a) - T(4) * (a * a))) * T(0.125);
+  const T aa4 = mul_rn(T(4), mul_rn(a, a));
+  if (a < T(1))
+    return mul_rn(add_rn(sub_rn(T(3), mul_rn(T(2), a)), sqrt(sub_rn(add_rn(T(1), mul_rn(T(4), a)), aa4))), T(0.125));
+  return mul_rn(sub_rn(sub_rn(T(5), mul_rn(T(2), a)), sqrt(sub_rn(add_rn(T(-7), mul_rn(T(12), a)), aa4))), T(0.125));
 }
 // Cosine 4-point, vivsim/ib/kernels.py:46-61
 template <typename T>
 __device__ __forceinline__ T delta_cosine4(T r) {
   const T a = fabs(r);
   if (a > T(2)) return T(0);
-  return (T(1) + cos(((T)3.14159265358979323846 * a) * T(0.5))) * T(0.25);
+  return mul_rn(add_rn(T(1), cos(mul_rn(mul_rn((T)3.14159265358979323846, a), T(0.5)))), T(0.25));
 }
 template <typename T>
 __device__ __forceinline__ T delta(int kernel, T r) {

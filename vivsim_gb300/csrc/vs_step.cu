@@ -16,6 +16,7 @@
 
 #include <climits>
 #include <cmath>
+#include <cstdlib>
 #include <new>
 #include <vector>
 
@@ -38,6 +39,7 @@ struct StepParams {
   T* fout;
   int nx, ny, nz, n;
   int chunks;                    // blocks along the contiguous axis (3-D)
+  int gx;                        // blocks per launch row (the launch's grid.x)
   int nreg;                      // 0: the whole grid; else the union of reg[0..nreg)
   int reg[3][6];                 // regions x0, x1, y0, y1, z0, z1 (half-open)
   int rowstart[4];               // first launch row (x plane) of each region
@@ -178,34 +180,36 @@ __device__ __forceinline__ void step_node(const StepParams<L, T>& P, int x, int 
 // and store of a warp covers 32 consecutive addresses.  Wrap-around offsets of the push
 // are per-block uniform except along the contiguous axis.
 // With nreg > 0 the launch rows walk a list of regions instead of the whole grid.
+// One block of the grid kernel: block (bx, by) of the launch geometry set up by
+// enqueue_grid (bx: chunk along the contiguous axis [x (y, chunk) in 3-D], by: row).
 template <class L, typename T, int COLL, bool WALLS>
-__global__ void __launch_bounds__(256) k_step(const __grid_constant__ StepParams<L, T> P) {
+__device__ __forceinline__ void step_block(const StepParams<L, T>& P, int bx, int by) {
   constexpr int Q = L::Q;
   int x, y, z;
   if (P.nreg == 0) {
-    x = blockIdx.y;
+    x = by;
     if constexpr (L::D == 2) {
-      y = blockIdx.x * blockDim.x + threadIdx.x;
+      y = bx * blockDim.x + threadIdx.x;
       if (y >= P.ny) return;
       z = 0;
     } else {
-      y = blockIdx.x / P.chunks;
-      z = (blockIdx.x - y * P.chunks) * blockDim.x + threadIdx.x;
+      y = bx / P.chunks;
+      z = (bx - y * P.chunks) * blockDim.x + threadIdx.x;
       if (z >= P.nz) return;
     }
   } else {
-    const int r = blockIdx.y;
+    const int r = by;
     const int g = (r >= P.rowstart[1]) + (r >= P.rowstart[2]);
     const int* R = P.reg[g];
     x = R[0] + (r - P.rowstart[g]);
     if constexpr (L::D == 2) {
-      y = R[2] + blockIdx.x * blockDim.x + threadIdx.x;
+      y = R[2] + bx * blockDim.x + threadIdx.x;
       if (y >= R[3]) return;
       z = 0;
     } else {
-      const int by = blockIdx.x / P.chunks;
-      y = R[2] + by;
-      z = R[4] + (blockIdx.x - by * P.chunks) * blockDim.x + threadIdx.x;
+      const int cy = bx / P.chunks;
+      y = R[2] + cy;
+      z = R[4] + (bx - cy * P.chunks) * blockDim.x + threadIdx.x;
       if (y >= R[3] || z >= R[5]) return;
     }
   }
@@ -219,6 +223,23 @@ __global__ void __launch_bounds__(256) k_step(const __grid_constant__ StepParams
 #pragma unroll
   for (int i = 0; i < Q; ++i) f[i] = __ldg(P.fin + (size_t)i * P.n + p);
   step_node<L, T, COLL, WALLS>(P, x, y, z, p, f);
+}
+
+template <class L, typename T, int COLL, bool WALLS>
+__global__ void __launch_bounds__(256) k_step(const __grid_constant__ StepParams<L, T> P) {
+  step_block<L, T, COLL, WALLS>(P, blockIdx.x, blockIdx.y);
+}
+
+// Grid kernel over many independent lattices in one launch: block b works on lattice
+// blk[b].x, as block blk[b].y of that lattice's own launch geometry (chunks x rows,
+// row-major), with that lattice's parameters.
+template <class L, typename T, int COLL, bool WALLS>
+__global__ void __launch_bounds__(256) k_step_batch(const StepParams<L, T>* __restrict__ Ps,
+                                                    const int2* __restrict__ blk) {
+  const int2 cb = blk[blockIdx.x];
+  const StepParams<L, T>& P = Ps[cb.x];
+  const int by = cb.y / P.gx;
+  step_block<L, T, COLL, WALLS>(P, cb.y - by * P.gx, by);
 }
 
 
@@ -395,6 +416,7 @@ struct BodyParams {
   const T* ds_arr;
   T ds2_scalar;  // 2 * ds as the reference forms it: (T)ds * 2
   int M, kernel, n_iter;
+  int chain_k;       // chain kernel: markers share stencil nodes only within +-chain_k (cyclic)
   int cap_x, cap_y;  // window region: (cap_x + 2) x (cap_y + 2) cells from the predicted corner
   int row_len;       // staged row length (multiple of 16 bytes), the TMA box's inner extent
   int bulk;          // stage the region with one tensor-map TMA copy
@@ -470,8 +492,8 @@ __device__ __forceinline__ T interp_group(const T* W, const int* slot, const T* 
 #pragma unroll
   for (int j = 0; j < PER; ++j) {
     const int s = sub * PER + j;
-    const T t = W[m * S + s] * nodes[slot[m * S + s]];
-    acc = j == 0 ? t : acc + t;
+    const T t = mul_rn(W[m * S + s], nodes[slot[m * S + s]]);
+    acc = j == 0 ? t : add_rn(acc, t);
   }
   if constexpr (LN > 1) {
     const unsigned lane = threadIdx.x & 31;
@@ -524,6 +546,18 @@ __global__ void __launch_bounds__(kBodyThreads) k_body2d(const __grid_constant__
   int* fxy = tstart + NB + 1;     // per marker: floor(X), floor(Y)
   int* misc = fxy + 2 * M;        // [0..3] bbox, [4] out-of-region flag, [8..39] warp sums
   uint64_t* bar = (uint64_t*)(((uintptr_t)(misc + 40) + 7) & ~(uintptr_t)7);
+  {
+    // the layout must fit the dynamic shared memory this launch received
+    unsigned have;
+    asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(have));
+    if ((size_t)((const unsigned char*)(bar + 1) - smem) > have) {
+      if (tid == 0) {
+        B.meta[META_STATUS] = VS_ERR_INVALID_ARG;
+        B.meta[META_WX] = 0; B.meta[META_WY] = 0; B.meta[META_WZ] = 0;
+      }
+      return;
+    }
+  }
 
   // one round trip: state, last corner, marker coordinates
   T a[2], v[2], d[2];
@@ -648,7 +682,7 @@ __global__ void __launch_bounds__(kBodyThreads) k_body2d(const __grid_constant__
     if ((t & (LN - 1)) == 0) {
       U[q] = acc;
       const T d2 = B.ds_arr ? B.ds_arr[m] * T(2) : B.ds2_scalar;
-      const T fs = (v[c] - acc) * d2;
+      const T fs = mul_rn(v[c] - acc, d2);
       Fs[q] = fs;
       Ft[q] = B.n_iter > 0 ? fs : T(0);
     }
@@ -663,9 +697,9 @@ __global__ void __launch_bounds__(kBodyThreads) k_body2d(const __grid_constant__
         const int p = sorted[i];
         const int m = p / S;
         const T w = W[p];
-        const T t0 = Fs[2 * m] * w, t1 = Fs[2 * m + 1] * w;
-        a0 = i == lo ? t0 : a0 + t0;
-        a1 = i == lo ? t1 : a1 + t1;
+        const T t0 = mul_rn(Fs[2 * m], w), t1 = mul_rn(Fs[2 * m + 1], w);
+        a0 = i == lo ? t0 : add_rn(a0, t0);
+        a1 = i == lo ? t1 : add_rn(a1, t1);
       }
       nv[j] = a0 * T(0.5);
       nv[NB + j] = a1 * T(0.5);
@@ -679,7 +713,7 @@ __global__ void __launch_bounds__(kBodyThreads) k_body2d(const __grid_constant__
         const T uq = U[q] + acc;
         U[q] = uq;
         const T d2 = B.ds_arr ? B.ds_arr[m] * T(2) : B.ds2_scalar;
-        const T fs = (v[c] - uq) * d2;
+        const T fs = mul_rn(v[c] - uq, d2);
         Fs[q] = fs;
         Ft[q] = Ft[q] + fs;
       }
@@ -696,9 +730,9 @@ __global__ void __launch_bounds__(kBodyThreads) k_body2d(const __grid_constant__
         const int p = sorted[i];
         const int m = p / S;
         const T w = W[p];
-        const T t0 = Ft[2 * m] * w, t1 = Ft[2 * m + 1] * w;
-        a0 = i == lo ? t0 : a0 + t0;
-        a1 = i == lo ? t1 : a1 + t1;
+        const T t0 = mul_rn(Ft[2 * m], w), t1 = mul_rn(Ft[2 * m + 1], w);
+        a0 = i == lo ? t0 : add_rn(a0, t0);
+        a1 = i == lo ? t1 : add_rn(a1, t1);
       }
     }
     B.gw[k] = a0;
@@ -725,14 +759,15 @@ __global__ void __launch_bounds__(kBodyThreads) k_body2d(const __grid_constant__
     const T h0 = __shfl_sync(0xffffffffu, h[0], 0), h1 = __shfl_sync(0xffffffffu, h[1], 0);
     if (tid < 2) {
       const int c = tid;
-      const T hh = (c == 0 ? h0 : h1) + a[c] * B.area;
-      T an = a[c], vn = v[c], dn = d[c];
+      const T ac = c == 0 ? a[0] : a[1], vc = c == 0 ? v[0] : v[1], dc = c == 0 ? d[0] : d[1];
+      const T hh = add_rn(c == 0 ? h0 : h1, mul_rn(ac, B.area));
+      T an = ac, vn = vc, dn = dc;
       if (B.free_dof[c]) {
-        const T v1 = v[c] + B.k1 * a[c];
-        const T v2 = (d[c] + B.dt * v[c]) + B.k2 * a[c];
-        an = ((hh - B.damp * v1) - B.stiff * v2) / B.den;
-        vn = B.c1 * an + v1;
-        dn = B.c2 * an + v2;
+        const T v1 = add_rn(vc, mul_rn(B.k1, ac));
+        const T v2 = add_rn(add_rn(dc, mul_rn(B.dt, vc)), mul_rn(B.k2, ac));
+        an = sub_rn(sub_rn(hh, mul_rn(B.damp, v1)), mul_rn(B.stiff, v2)) / B.den;
+        vn = add_rn(mul_rn(B.c1, an), v1);
+        dn = add_rn(mul_rn(B.c2, an), v2);
       }
       B.state[c] = an;
       B.state[3 + c] = vn;
@@ -771,6 +806,378 @@ static void body2d_launch(int R, size_t smem, cudaStream_t st, const BodyParams<
     case 2: k_body2d<T, 2><<<1, kBodyThreads, smem, st>>>(P); break;
     default: k_body2d<T, 3><<<1, kBodyThreads, smem, st>>>(P); break;
   }
+}
+
+// ------------------------------------------------------------------ 2-D body kernel, chain form
+// For most immersed boundaries the markers are ordered along a curve, and two markers
+// whose stencils can share a node are at most K positions apart in that (cyclic) order.
+// The markers of a rigid body only translate, so K is a property of the marker set that
+// the plan computes once on the host (markers i, j can share a node under some
+// translation iff |x_i - x_j| < 2R and |y_i - y_j| < 2R).  The node of pair (j, s) then
+// receives contributions only from markers j-K..j+K; which of them reach it follows from
+// their stencil corners by index arithmetic, and taking them in increasing marker index is
+// the reference's scatter order (each marker reaches a node through at most one stencil
+// point).  So every pair recomputes its own node's spread value: no sort, no per-node
+// lists, one block-wide barrier per MDF iteration.  Results equal those of k_body2d.
+__device__ __forceinline__ void chain_range(int j, int K, int M, int& a0, int& nA, int& b0, int& nc) {
+  if (2 * K + 1 >= M) {
+    a0 = 0; nA = M; b0 = 0; nc = M;
+    return;
+  }
+  nc = 2 * K + 1;
+  const int lo = j - K, hi = j + K;
+  if (lo < 0) {         // {0..hi} then {lo+M..M-1}
+    a0 = 0; nA = hi + 1; b0 = lo + M;
+  } else if (hi >= M) { // {0..hi-M} then {lo..M-1}
+    a0 = 0; nA = hi - M + 1; b0 = lo;
+  } else {
+    a0 = lo; nA = nc; b0 = 0;
+  }
+}
+
+// sum over the contributors in `msk` of F[i] * W[i, s_i] for the node (nx, ny), both
+// components, first term not added to zero (as the ordered segment sums do)
+template <typename T, int WD>
+__device__ __forceinline__ void chain_node_sum(unsigned msk, int a0, int nA, int b0, int nx, int ny, const int* fxy,
+                                               const T* W, const T* F, T& s0, T& s1) {
+  constexpr int S = WD * WD;
+  bool first = true;
+  s0 = T(0);
+  s1 = T(0);
+  while (msk) {
+    const int b = __ffs(msk) - 1;
+    msk &= msk - 1;
+    const int i = b < nA ? a0 + b : b0 + (b - nA);
+    const int k = (nx - fxy[2 * i]) * WD + (ny - fxy[2 * i + 1]);
+    const T w = W[i * S + k];
+    const T t0 = mul_rn(F[2 * i], w), t1 = mul_rn(F[2 * i + 1], w);
+    s0 = first ? t0 : add_rn(s0, t0);
+    s1 = first ? t1 : add_rn(s1, t1);
+    first = false;
+  }
+}
+
+template <typename T, int LN>
+__device__ __forceinline__ T group_sum(T acc) {
+  if constexpr (LN > 1) {
+    const unsigned lane = threadIdx.x & 31;
+    const unsigned mask = ((1u << LN) - 1u) << (lane & ~(unsigned)(LN - 1));
+#pragma unroll
+    for (int o = LN / 2; o >= 1; o >>= 1) acc = acc + __shfl_down_sync(mask, acc, o, LN);
+  }
+  return acc;
+}
+
+template <typename T, int R>
+__device__ __forceinline__ void body2d_chain(const BodyParams<T>& B) {
+  constexpr int WD = 2 * R, S = WD * WD;
+  constexpr int LN = S >= 16 ? 4 : 1;  // lanes per marker
+  constexpr int PER = S / LN;          // stencil points per lane, contiguous
+  constexpr int AL = 16 / sizeof(T);
+  extern __shared__ __align__(128) unsigned char smem[];
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int M = B.M, P = M * S, K = B.chain_k;
+  const int EX = B.cap_x + 2, EY = B.cap_y + 2, NB = EX * EY, RL = B.row_len;
+  T* fwin = (T*)smem;          // staged populations [9][EX][RL]
+  T* W = fwin + 9 * EX * RL;   // [P] stencil weights
+  T* U = W + P;                // [2M] marker velocity
+  T* Fa = U + 2 * M;           // [2M] force step, ping
+  T* Fb = Fa + 2 * M;          // [2M] force step, pong
+  T* Ft = Fb + 2 * M;          // [2M] total force
+  int* fxy = (int*)(Ft + 2 * M);               // [2M] stencil corner (floor - R + 1)
+  unsigned* cmask = (unsigned*)(fxy + 2 * M);  // [P] contributors of each pair's node
+  int* misc = (int*)(cmask + P);               // [0..3] min/max floor x, y; [4] out-of-region
+  uint64_t* bar = (uint64_t*)(((uintptr_t)(misc + 8) + 7) & ~(uintptr_t)7);
+  {
+    // the layout must fit the dynamic shared memory this launch received
+    unsigned have;
+    asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(have));
+    if ((size_t)((const unsigned char*)(bar + 1) - smem) > have) {
+      if (tid == 0) {
+        B.meta[META_STATUS] = VS_ERR_INVALID_ARG;
+        B.meta[META_WX] = 0; B.meta[META_WY] = 0; B.meta[META_WZ] = 0;
+      }
+      return;
+    }
+  }
+
+  T a[2], v[2], d[2];
+#pragma unroll
+  for (int c = 0; c < 2; ++c) {
+    a[c] = B.state[c];
+    v[c] = B.state[3 + c];
+    d[c] = B.state[6 + c];
+  }
+  const int ox = B.meta[META_PX] - 1, oy = B.meta[META_PY] - 1;  // predicted region corner
+  const int ya = oy >= 0 ? oy - oy % AL : 0;
+  const int64_t n = (int64_t)B.nx * B.ny;
+  const bool region_ok = ox >= B.box[0] && oy >= B.box[2] && ox + EX <= B.box[1] && oy + EY <= B.box[3];
+  const bool bulk = B.bulk && region_ok;
+  if (tid == 0) {
+    misc[0] = INT_MAX; misc[1] = INT_MIN; misc[2] = INT_MAX; misc[3] = INT_MIN; misc[4] = 0;
+    if (bulk) {
+      tma::mbar_init(bar, 1);
+      tma::fence_init();
+      tma::mbar_expect_tx(bar, (unsigned)(9 * EX * RL * sizeof(T)));
+      asm volatile(
+          "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, "
+          "%4}], [%5];\n" ::"r"(tma::smem_addr(fwin)),
+          "l"(&B.map), "r"(ya), "r"(ox), "r"(0), "r"(tma::smem_addr(bar))
+          : "memory");
+    }
+  }
+  // the force window starts at zero; cells no marker reaches stay zero
+  if (region_ok)
+    for (int k = tid; k < 2 * NB; k += nt) B.gw[k] = T(0);
+  __syncthreads();
+  // markers follow the body (dyn.py:68-81); stencil weights kernel(sx - X) * kernel(sy - Y)
+  // (ib/stencil.py:7-51), one thread per (marker, lane), PER stencil points each
+  for (int t = tid; t < M * LN; t += nt) {
+    const int m = t / LN, sub = t - m * LN;
+    const T xm = B.X0[m] + d[0], ym = B.Y0[m] + d[1];
+    const int fx = ifloor(xm), fy = ifloor(ym);
+    if (sub == 0) {
+      fxy[2 * m] = fx - R + 1;
+      fxy[2 * m + 1] = fy - R + 1;
+      atomicMin(&misc[0], fx); atomicMax(&misc[1], fx);
+      atomicMin(&misc[2], fy); atomicMax(&misc[3], fy);
+    }
+    bool out = false;
+#pragma unroll
+    for (int j = 0; j < PER; ++j) {
+      const int s = sub * PER + j, ix = s / WD, iy = s - ix * WD;
+      W[m * S + s] = delta(B.kernel, (T)(fx + ix - R + 1) - xm) * delta(B.kernel, (T)(fy + iy - R + 1) - ym);
+      const int cx = fx + ix - R + 1 - ox, cy = fy + iy - R + 1 - oy;
+      out |= cx < 0 || cx >= EX || cy < 0 || cy >= EY;
+    }
+    if (out) misc[4] = 1;
+  }
+  __syncthreads();
+  if (misc[4] || !region_ok) {
+    // the body moved a node or more in one step, or its region left the box
+    if (bulk && tid == 0) tma::mbar_wait(bar, 0, kTmaWaitLimit);
+    __syncthreads();
+    if (tid == 0) {
+      B.meta[META_STATUS] = VS_ERR_RANGE;
+      B.meta[META_WX] = 0; B.meta[META_WY] = 0; B.meta[META_WZ] = 0;
+    }
+    return;
+  }
+  bool staged = true;
+  if (bulk) staged = tma::mbar_wait(bar, 0, kTmaWaitLimit);
+  if (__syncthreads_or(!staged)) {
+    if (tid == 0) {
+      B.meta[META_STATUS] = VS_ERR_TIMEOUT;
+      B.meta[META_WX] = 0; B.meta[META_WY] = 0; B.meta[META_WZ] = 0;
+    }
+    return;
+  }
+  // contributors of each pair's node; u there; U = interpolate(u) and the first force
+  // step (ib/mdf.py:38-48) with the body velocity as target
+  for (int t = tid; t < M * LN; t += nt) {
+    const int m = t / LN, sub = t - m * LN;
+    int a0, nA, b0, nc;
+    chain_range(m, K, M, a0, nA, b0, nc);
+    const int bx = fxy[2 * m], by = fxy[2 * m + 1];
+    T acc0 = T(0), acc1 = T(0);
+#pragma unroll
+    for (int j = 0; j < PER; ++j) {
+      const int s = sub * PER + j, ix = s / WD, iy = s - ix * WD;
+      const int nx = bx + ix, ny = by + iy;
+      unsigned msk = 0;
+      for (int b = 0; b < nc; ++b) {
+        const int i = b < nA ? a0 + b : b0 + (b - nA);
+        const unsigned dx = (unsigned)(nx - fxy[2 * i]), dy = (unsigned)(ny - fxy[2 * i + 1]);
+        if (dx < (unsigned)WD && dy < (unsigned)WD) msk |= 1u << b;
+      }
+      cmask[m * S + s] = msk;
+      const int cx = nx - ox, cy = ny - oy;
+      T fl[9];
+      if (bulk) {
+#pragma unroll
+        for (int i = 0; i < 9; ++i) fl[i] = fwin[(i * EX + cx) * RL + (oy - ya) + cy];
+      } else {
+        const int64_t pn = (int64_t)nx * B.ny + ny;
+#pragma unroll
+        for (int i = 0; i < 9; ++i) fl[i] = __ldg(B.fin + i * n + pn);
+      }
+      T r, uu[3];
+      macro(L9{}, fl, r, uu);
+      const T w = W[m * S + s];
+      const T t0 = mul_rn(w, uu[0]), t1 = mul_rn(w, uu[1]);
+      acc0 = j == 0 ? t0 : add_rn(acc0, t0);
+      acc1 = j == 0 ? t1 : add_rn(acc1, t1);
+    }
+    acc0 = group_sum<T, LN>(acc0);
+    acc1 = group_sum<T, LN>(acc1);
+    if (sub == 0) {
+      const T d2 = B.ds_arr ? B.ds_arr[m] * T(2) : B.ds2_scalar;
+      const T acc[2] = {acc0, acc1};
+#pragma unroll
+      for (int c = 0; c < 2; ++c) {
+        U[2 * m + c] = acc[c];
+        const T fs = mul_rn(v[c] - acc[c], d2);
+        Fa[2 * m + c] = fs;
+        Ft[2 * m + c] = B.n_iter > 0 ? fs : T(0);
+      }
+    }
+  }
+  __syncthreads();
+  // MDF iterations (ib/mdf.py:41-52): U += interpolate(0.5 spread(F_step)); next force step
+  T* Fcur = Fa;
+  T* Fnext = Fb;
+  for (int it = 0; it + 1 < B.n_iter; ++it) {
+    for (int t = tid; t < M * LN; t += nt) {
+      const int m = t / LN, sub = t - m * LN;
+      int a0, nA, b0, nc;
+      chain_range(m, K, M, a0, nA, b0, nc);
+      const int bx = fxy[2 * m], by = fxy[2 * m + 1];
+      T acc0 = T(0), acc1 = T(0);
+#pragma unroll
+      for (int j = 0; j < PER; ++j) {
+        const int s = sub * PER + j, ix = s / WD, iy = s - ix * WD;
+        T n0, n1;
+        chain_node_sum<T, WD>(cmask[m * S + s], a0, nA, b0, bx + ix, by + iy, fxy, W, Fcur, n0, n1);
+        const T w = W[m * S + s];
+        const T t0 = mul_rn(w, n0 * T(0.5)), t1 = mul_rn(w, n1 * T(0.5));
+        acc0 = j == 0 ? t0 : add_rn(acc0, t0);
+        acc1 = j == 0 ? t1 : add_rn(acc1, t1);
+      }
+      acc0 = group_sum<T, LN>(acc0);
+      acc1 = group_sum<T, LN>(acc1);
+      if (sub == 0) {
+        const T d2 = B.ds_arr ? B.ds_arr[m] * T(2) : B.ds2_scalar;
+        const T acc[2] = {acc0, acc1};
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+          const T uq = U[2 * m + c] + acc[c];
+          U[2 * m + c] = uq;
+          const T fs = mul_rn(v[c] - uq, d2);
+          Fnext[2 * m + c] = fs;
+          Ft[2 * m + c] = Ft[2 * m + c] + fs;
+        }
+      }
+    }
+    __syncthreads();
+    T* tmp = Fcur;
+    Fcur = Fnext;
+    Fnext = tmp;
+  }
+  // g = spread(F_total) (ib/mdf.py:60-62): every pair writes its node's sum; pairs that
+  // share a node compute the same value in the same order
+  for (int t = tid; t < M * LN; t += nt) {
+    const int m = t / LN, sub = t - m * LN;
+    int a0, nA, b0, nc;
+    chain_range(m, K, M, a0, nA, b0, nc);
+    const int bx = fxy[2 * m], by = fxy[2 * m + 1];
+#pragma unroll
+    for (int j = 0; j < PER; ++j) {
+      const int s = sub * PER + j, ix = s / WD, iy = s - ix * WD;
+      T g0, g1;
+      chain_node_sum<T, WD>(cmask[m * S + s], a0, nA, b0, bx + ix, by + iy, fxy, W, Ft, g0, g1);
+      const int k = (bx + ix - ox) * EY + (by + iy - oy);
+      B.gw[k] = g0;
+      B.gw[NB + k] = g1;
+    }
+  }
+  if (tid == 0) {
+    B.meta[META_OX] = ox; B.meta[META_OY] = oy; B.meta[META_OZ] = 0;
+    B.meta[META_WX] = EX; B.meta[META_WY] = EY; B.meta[META_WZ] = 1;
+    B.meta[META_PX] = misc[0] - R + 1;
+    B.meta[META_PY] = misc[2] - R + 1;
+  }
+  // total force h = sum_m(-F_total) (dyn.py:126-136) in a fixed tree by warp 0, added mass
+  // h += a A (vortex_induced_vibration.py:136), Newmark update (dyn.py:5-51)
+  if (tid < 32) {
+    T h[2];
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      T acc = T(0);
+      for (int m = tid; m < M; m += 32) acc = m == tid ? -Ft[2 * m + c] : acc + (-Ft[2 * m + c]);
+#pragma unroll
+      for (int o = 16; o >= 1; o >>= 1) acc = acc + __shfl_down_sync(0xffffffffu, acc, o);
+      h[c] = acc;
+    }
+    const T h0 = __shfl_sync(0xffffffffu, h[0], 0), h1 = __shfl_sync(0xffffffffu, h[1], 0);
+    if (tid < 2) {
+      const int c = tid;
+      const T ac = c == 0 ? a[0] : a[1], vc = c == 0 ? v[0] : v[1], dc = c == 0 ? d[0] : d[1];
+      const T hh = add_rn(c == 0 ? h0 : h1, mul_rn(ac, B.area));
+      T an = ac, vn = vc, dn = dc;
+      if (B.free_dof[c]) {
+        const T v1 = add_rn(vc, mul_rn(B.k1, ac));
+        const T v2 = add_rn(add_rn(dc, mul_rn(B.dt, vc)), mul_rn(B.k2, ac));
+        an = sub_rn(sub_rn(hh, mul_rn(B.damp, v1)), mul_rn(B.stiff, v2)) / B.den;
+        vn = add_rn(mul_rn(B.c1, an), v1);
+        dn = add_rn(mul_rn(B.c2, an), v2);
+      }
+      B.state[c] = an;
+      B.state[3 + c] = vn;
+      B.state[6 + c] = dn;
+      B.state[9 + c] = hh;
+      if (B.force_hist) B.force_hist[c] = hh;
+    }
+    if (tid == 2) {
+      B.state[9 + 2] = T(0);
+      if (B.force_hist) B.force_hist[2] = T(0);
+    }
+  }
+}
+
+template <typename T, int R>
+__global__ void __launch_bounds__(kBodyThreads) k_body2d_chain(const __grid_constant__ BodyParams<T> B) {
+  body2d_chain<T, R>(B);
+}
+
+// many bodies, one CTA each (each of its own lattice)
+template <typename T, int R>
+__global__ void __launch_bounds__(kBodyThreads) k_body2d_chain_batch(const BodyParams<T>* __restrict__ Bs) {
+  body2d_chain<T, R>(Bs[blockIdx.x]);
+}
+
+template <typename T>
+static size_t body2d_chain_smem(int M, int R, int EX, int RL) {
+  const size_t S = 4 * R * R, P = M * S;
+  return sizeof(T) * (9 * (size_t)EX * RL + P + 8 * (size_t)M) + sizeof(int) * (2 * (size_t)M + P + 8) + 16;
+}
+
+template <typename T>
+static cudaError_t body2d_chain_attr(int R, int smem) {
+  switch (R) {
+    case 1: return cudaFuncSetAttribute(k_body2d_chain<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    case 2: return cudaFuncSetAttribute(k_body2d_chain<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    default: return cudaFuncSetAttribute(k_body2d_chain<T, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  }
+}
+
+template <typename T>
+static void body2d_chain_launch(int R, size_t smem, cudaStream_t st, const BodyParams<T>& P) {
+  switch (R) {
+    case 1: k_body2d_chain<T, 1><<<1, kBodyThreads, smem, st>>>(P); break;
+    case 2: k_body2d_chain<T, 2><<<1, kBodyThreads, smem, st>>>(P); break;
+    default: k_body2d_chain<T, 3><<<1, kBodyThreads, smem, st>>>(P); break;
+  }
+}
+
+static bool getenv_flag(const char* name) {
+  const char* v = getenv(name);
+  return v && v[0] && !(v[0] == '0' && v[1] == 0);
+}
+
+// Chain width of a rigid 2-D marker set (coordinates in the plan precision): the largest
+// cyclic index distance between two markers whose stencils can share a node under some
+// translation, i.e. |dx| < 2R and |dy| < 2R (with a small margin for rounding).
+static int chain_width(const double* x, const double* y, int M, int R) {
+  const double lim = 2.0 * R + 1e-3;
+  int K = 0;
+  for (int i = 0; i < M; ++i)
+    for (int j = i + 1; j < M; ++j) {
+      if (fabs(x[i] - x[j]) < lim && fabs(y[i] - y[j]) < lim) {
+        const int dd = j - i, cyc = dd < M - dd ? dd : M - dd;
+        K = cyc > K ? cyc : K;
+      }
+    }
+  return K;
 }
 
 // ------------------------------------------------------------------ body kernels (3-D fixed)
@@ -816,8 +1223,8 @@ __global__ void k_static_marker(int first, int use_step, const T* __restrict__ W
     const int id = pair_uid[q];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      const T t = w * nodes[c * U + id];
-      acc[c] = firstterm ? t : acc[c] + t;
+      const T t = mul_rn(w, nodes[c * U + id]);
+      acc[c] = firstterm ? t : add_rn(acc[c], t);
     }
     firstterm = false;
   }
@@ -832,7 +1239,7 @@ __global__ void k_static_marker(int first, int use_step, const T* __restrict__ W
       const int64_t q = (int64_t)m * 3 + c;
       const T u = first ? acc[c] : Ua[q] + acc[c];
       Ua[q] = u;
-      const T fs = (state[3 + c] - u) * d2;
+      const T fs = mul_rn(state[3 + c] - u, d2);
       Fs[q] = fs;
       Ft[q] = first ? (use_step ? fs : T(0)) : Ft[q] + fs;
     }
@@ -856,8 +1263,8 @@ __global__ void k_static_spread(const int32_t* __restrict__ seg, const int32_t* 
       const T w = W[p];
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        const T t = F[m * 3 + c] * w;
-        a[c] = i == lo ? t : a[c] + t;
+        const T t = mul_rn(F[m * 3 + c], w);
+        a[c] = i == lo ? t : add_rn(a[c], t);
       }
     }
     if (gw) {
@@ -955,11 +1362,13 @@ struct vs_body_plan {
   void* d_mk;       // U, F_step, F_total: 3 x (3 M)
   size_t smem;
   int row_len, bulk;  // 2-D body kernel: staged row length, bulk staging on/off
+  int chain, chain_k; // 2-D body kernel: chain form and its width
   CUtensorMap maps[2]; // tensor maps of the last two population buffers seen
   const void* map_ptr[2];
   int map_next;
   double nm[9];  // k1, k2, c1, c2, dt, damping, stiffness, den, area
   int box[6];    // region the body's window never leaves (half-open x0,x1,y0,y1,z0,z1)
+  double lo_t[2];  // 2-D: smallest marker x and y, rounded to the plan precision
   cudaStream_t side;
   cudaEvent_t ev_fork, ev_join;
 };
@@ -1108,43 +1517,56 @@ static const CUtensorMap* body_map(vs_body_plan* b, const vs_lattice_plan* L, co
   return &b->maps[k];
 }
 
+// Parameters of the 2-D body kernel for one step reading populations fin.  allow_bulk: the
+// window may be staged by a tensor-map TMA copy (the map travels in the parameters).
+template <typename T>
+static BodyParams<T> body_params2d(vs_body_plan* B, const vs_lattice_plan* LP, const void* fin, void* force_hist,
+                                   bool allow_bulk) {
+  BodyParams<T> P{};
+  P.fin = (const T*)fin;
+  P.nx = LP->cfg.nx;
+  P.ny = LP->cfg.ny;
+  P.X0 = (const T*)B->d_X0;
+  P.Y0 = (const T*)B->d_X0 + B->M;
+  P.ds_arr = (const T*)B->d_ds;
+  P.ds2_scalar = (T)B->cfg.ds_scalar * T(2);
+  P.M = B->M;
+  P.kernel = B->cfg.kernel;
+  P.n_iter = B->cfg.n_iter;
+  P.cap_x = B->cap[0];
+  P.cap_y = B->cap[1];
+  // without staging the kernel's shared memory holds no window rows (its size is
+  // computed for row_len 0 then)
+  P.row_len = allow_bulk ? B->row_len : 0;
+  P.bulk = 0;
+  if (allow_bulk && B->bulk && ((uintptr_t)fin % 16) == 0) {
+    const CUtensorMap* m = body_map(B, LP, fin);
+    if (m) {
+      P.map = *m;
+      P.bulk = 1;
+    }
+  }
+  for (int q = 0; q < 4; ++q) P.box[q] = B->box[q];
+  P.state = (T*)B->d_state;
+  P.gw = (T*)B->d_gw;
+  P.meta = B->d_meta;
+  P.force_hist = (T*)force_hist;
+  for (int c = 0; c < 3; ++c) P.free_dof[c] = B->cfg.free_dof[c];
+  P.k1 = (T)B->nm[0]; P.k2 = (T)B->nm[1]; P.c1 = (T)B->nm[2]; P.c2 = (T)B->nm[3]; P.dt = (T)B->nm[4];
+  P.damp = (T)B->nm[5]; P.stiff = (T)B->nm[6]; P.den = (T)B->nm[7]; P.area = (T)B->nm[8];
+  P.chain_k = B->chain_k;
+  return P;
+}
+
 static int enqueue_body(vs_body_plan* B, const vs_lattice_plan* LP, const void* fin, void* force_hist,
                         cudaStream_t st) {
   const int dtype = B->cfg.dtype;
   if (B->dim == 2) {
     return dispatch_t(dtype, [&](auto t) -> int {
       using T = typename decltype(t)::type;
-      BodyParams<T> P{};
-      P.fin = (const T*)fin;
-      P.nx = LP->cfg.nx;
-      P.ny = LP->cfg.ny;
-      P.X0 = (const T*)B->d_X0;
-      P.Y0 = (const T*)B->d_X0 + B->M;
-      P.ds_arr = (const T*)B->d_ds;
-      P.ds2_scalar = (T)B->cfg.ds_scalar * T(2);
-      P.M = B->M;
-      P.kernel = B->cfg.kernel;
-      P.n_iter = B->cfg.n_iter;
-      P.cap_x = B->cap[0];
-      P.cap_y = B->cap[1];
-      P.row_len = B->row_len;
-      P.bulk = 0;
-      if (B->bulk && ((uintptr_t)fin % 16) == 0) {
-        const CUtensorMap* m = body_map(B, LP, fin);
-        if (m) {
-          P.map = *m;
-          P.bulk = 1;
-        }
-      }
-      for (int q = 0; q < 4; ++q) P.box[q] = B->box[q];
-      P.state = (T*)B->d_state;
-      P.gw = (T*)B->d_gw;
-      P.meta = B->d_meta;
-      P.force_hist = (T*)force_hist;
-      for (int c = 0; c < 3; ++c) P.free_dof[c] = B->cfg.free_dof[c];
-      P.k1 = (T)B->nm[0]; P.k2 = (T)B->nm[1]; P.c1 = (T)B->nm[2]; P.c2 = (T)B->nm[3]; P.dt = (T)B->nm[4];
-      P.damp = (T)B->nm[5]; P.stiff = (T)B->nm[6]; P.den = (T)B->nm[7]; P.area = (T)B->nm[8];
-      body2d_launch<T>(B->cfg.radius, B->smem, st, P);
+      const BodyParams<T> P = body_params2d<T>(B, LP, fin, force_hist, true);
+      if (B->chain) body2d_chain_launch<T>(B->cfg.radius, B->smem, st, P);
+      else body2d_launch<T>(B->cfg.radius, B->smem, st, P);
       VS_CHECK_LAUNCH("vs_step body kernel");
       return VS_OK;
     });
@@ -1227,55 +1649,68 @@ static int tma_dispatch(vs_lattice_plan* LP, const StepParams<L, T>& P, cudaStre
 //         (nodes outside the box read no force window).
 // mode 2: the body's box and, with lazy_walls, the x = 0 / nx-1 planes, whose populations
 //         first get the previous step's face boundaries.
+// Fills the grid-kernel parameters and launch geometry; false when there is no node to do.
+// tb_force > 0 fixes the threads per block (the batched launches use one block size).
+template <class L, typename T>
+static bool grid_setup(const vs_lattice_plan* LP, const vs_body_plan* B, const void* fin, void* fout, int mode,
+                       bool lazy_walls, int tb_force, StepParams<L, T>& P, dim3& grid, int& tb) {
+  const vs_lattice_cfg& c = LP->cfg;
+  P = make_step_params<L, T>(LP, B, fin, fout);
+  P.nreg = 0;
+  P.skip_box = mode == 1 && B;
+  P.skip_walls = mode == 1 && lazy_walls;
+  for (int q = 0; q < 6; ++q) P.box[q] = B ? B->box[q] : 0;
+  P.n_lazy = 0;
+  if (mode == 1) {  // outside the box no node reads the force window
+    P.gw = nullptr;
+    P.meta = nullptr;
+  }
+  int rows = c.nx, ext_last = L::D == 2 ? c.ny : c.nz, ext_mid = c.ny;
+  if (mode == 2) {
+    int nr = 0;
+    auto add = [&](const int* R) {
+      for (int q = 0; q < 6; ++q) P.reg[nr][q] = R[q];
+      ++nr;
+    };
+    if (B) add(B->box);
+    if (lazy_walls) {
+      int w0[6] = {0, 1, 0, c.ny, 0, c.nz}, w1[6] = {c.nx - 1, c.nx, 0, c.ny, 0, c.nz};
+      if (!B || B->box[0] > 0) add(w0);
+      if (!B || B->box[1] < c.nx) add(w1);
+      for (int k = 0; k < c.n_bc && k < 2; ++k) P.lazy[P.n_lazy++] = wall_args_from_bc<T>(c.bc[k], LP, k);
+    }
+    P.nreg = nr;
+    rows = 0;
+    ext_last = 0;
+    ext_mid = 0;
+    for (int g = 0; g < nr; ++g) {
+      P.rowstart[g] = rows;
+      rows += P.reg[g][1] - P.reg[g][0];
+      const int el = L::D == 2 ? P.reg[g][3] - P.reg[g][2] : P.reg[g][5] - P.reg[g][4];
+      ext_last = el > ext_last ? el : ext_last;
+      ext_mid = P.reg[g][3] - P.reg[g][2] > ext_mid ? P.reg[g][3] - P.reg[g][2] : ext_mid;
+    }
+    for (int g = nr; g < 4; ++g) P.rowstart[g] = 1 << 30;
+    if (nr == 0) return false;
+  }
+  // threads along the contiguous axis (y in 2-D, z in 3-D)
+  tb = tb_force > 0 ? tb_force : (ext_last >= 256 ? 256 : (ext_last >= 128 ? 128 : ((ext_last + 31) / 32) * 32));
+  P.chunks = (ext_last + tb - 1) / tb;
+  grid = dim3(L::D == 2 ? P.chunks : P.chunks * ext_mid, rows);
+  P.gx = (int)grid.x;
+  return true;
+}
+
 static int enqueue_grid(const vs_lattice_plan* LP, const vs_body_plan* B, const void* fin, void* fout,
                         cudaStream_t st, int mode = 0, bool lazy_walls = false) {
   const vs_lattice_cfg& c = LP->cfg;
   int rc = dispatch(c.q, c.dtype, [&](auto l, auto t) -> int {
     using L = decltype(l);
     using T = typename decltype(t)::type;
-    StepParams<L, T> P = make_step_params<L, T>(LP, B, fin, fout);
-    P.nreg = 0;
-    P.skip_box = mode == 1 && B;
-    P.skip_walls = mode == 1 && lazy_walls;
-    for (int q = 0; q < 6; ++q) P.box[q] = B ? B->box[q] : 0;
-    P.n_lazy = 0;
-    if (mode == 1) {  // outside the box no node reads the force window
-      P.gw = nullptr;
-      P.meta = nullptr;
-    }
-    int rows = c.nx, ext_last = L::D == 2 ? c.ny : c.nz, ext_mid = c.ny;
-    if (mode == 2) {
-      int nr = 0;
-      auto add = [&](const int* R) {
-        for (int q = 0; q < 6; ++q) P.reg[nr][q] = R[q];
-        ++nr;
-      };
-      if (B) add(B->box);
-      if (lazy_walls) {
-        int w0[6] = {0, 1, 0, c.ny, 0, c.nz}, w1[6] = {c.nx - 1, c.nx, 0, c.ny, 0, c.nz};
-        if (!B || B->box[0] > 0) add(w0);
-        if (!B || B->box[1] < c.nx) add(w1);
-        for (int k = 0; k < c.n_bc && k < 2; ++k) P.lazy[P.n_lazy++] = wall_args_from_bc<T>(c.bc[k], LP, k);
-      }
-      P.nreg = nr;
-      rows = 0;
-      ext_last = 0;
-      ext_mid = 0;
-      rows = 0;
-      for (int g = 0; g < nr; ++g) {
-        P.rowstart[g] = rows;
-        rows += P.reg[g][1] - P.reg[g][0];
-        const int el = L::D == 2 ? P.reg[g][3] - P.reg[g][2] : P.reg[g][5] - P.reg[g][4];
-        ext_last = el > ext_last ? el : ext_last;
-        ext_mid = P.reg[g][3] - P.reg[g][2] > ext_mid ? P.reg[g][3] - P.reg[g][2] : ext_mid;
-      }
-      for (int g = nr; g < 4; ++g) P.rowstart[g] = 1 << 30;
-      if (nr == 0) return VS_OK;
-    }
-    // threads along the contiguous axis (y in 2-D, z in 3-D)
-    const int tb = ext_last >= 256 ? 256 : (ext_last >= 128 ? 128 : ((ext_last + 31) / 32) * 32);
-    P.chunks = (ext_last + tb - 1) / tb;
-    const dim3 grid(L::D == 2 ? P.chunks : P.chunks * ext_mid, rows);
+    StepParams<L, T> P;
+    dim3 grid;
+    int tb = 0;
+    if (!grid_setup<L, T>(LP, B, fin, fout, mode, lazy_walls, 0, P, grid, tb)) return VS_OK;
     const bool walls = mode == 2 && lazy_walls;
     const bool aligned = ((uintptr_t)fin % 16) == 0;
     if (mode != 2 && LP->tma_tb > 0 && aligned) {
@@ -1497,6 +1932,7 @@ int vs_body_plan_create(const vs_body_cfg* cfg, const vs_lattice_plan* lattice, 
       else put(m * 3 + d, v);
     }
   for (int d = 0; d < cfg->dim; ++d) b->cap[d] = (int)(floor(hi[d]) - floor(lo[d])) + w + 2;
+  for (int d = 0; d < 2; ++d) b->lo_t[d] = ts == 8 ? lo[d] : (double)(float)lo[d];
   if (cfg->dim == 2) b->cap[2] = 1;
   {
     // region the window can reach: the initial stencil box, widened along free DOFs by the
@@ -1586,7 +2022,19 @@ int vs_body_plan_create(const vs_body_cfg* cfg, const vs_lattice_plan* lattice, 
     int dev = 0, optin = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    {
+      // chain form when the marker order bounds node sharing (markers rounded to the plan precision)
+      std::vector<double> xr(M), yr(M);
+      for (int m = 0; m < M; ++m) {
+        xr[m] = ts == 8 ? cfg->x0_host[m] : (double)(float)cfg->x0_host[m];
+        yr[m] = ts == 8 ? cfg->y0_host[m] : (double)(float)cfg->y0_host[m];
+      }
+      b->chain_k = chain_width(xr.data(), yr.data(), M, cfg->radius);
+      b->chain = (M <= 32 || 2 * b->chain_k + 1 <= 31) && !getenv_flag("VIVSIM_GB300_BODY_CSR");
+    }
     auto smem_of = [&](int rl) {
+      if (b->chain)
+        return ts == 8 ? body2d_chain_smem<double>(M, cfg->radius, EX, rl) : body2d_chain_smem<float>(M, cfg->radius, EX, rl);
       return ts == 8 ? body2d_smem<double>(M, cfg->radius, EX, EY, rl) : body2d_smem<float>(M, cfg->radius, EX, EY, rl);
     };
     b->smem = smem_of(b->bulk ? b->row_len : 0);
@@ -1607,7 +2055,13 @@ int vs_body_plan_create(const vs_body_cfg* cfg, const vs_lattice_plan* lattice, 
       meta0[META_PY] = (int)floor(lo[1] + cfg->d0[1]) - cfg->radius + 1;
       if ((e = cudaMemcpy(b->d_meta, meta0, sizeof(meta0), cudaMemcpyHostToDevice)) != cudaSuccess) return fail(e);
     }
-    e = ts == 8 ? body2d_attr<double>(cfg->radius, (int)b->smem) : body2d_attr<float>(cfg->radius, (int)b->smem);
+    // the limit is a property of the kernel function, shared by every plan: raise it to the
+    // device maximum once rather than to this plan's size (a smaller later plan would
+    // otherwise invalidate the launches of a larger one)
+    if (b->chain)
+      e = ts == 8 ? body2d_chain_attr<double>(cfg->radius, optin) : body2d_chain_attr<float>(cfg->radius, optin);
+    else
+      e = ts == 8 ? body2d_attr<double>(cfg->radius, optin) : body2d_attr<float>(cfg->radius, optin);
     if (e != cudaSuccess) return fail(e);
   } else {
     // fixed 3-D body: stencil once over a fixed window around the markers
@@ -1699,8 +2153,25 @@ int vs_body_set_state(vs_body_plan* plan, const double* state_host, void* stream
   }
   cudaStream_t st = as_stream(stream);
   cudaError_t e = cudaMemcpyAsync(plan->d_state, buf, ts * 12, cudaMemcpyHostToDevice, st);
+  int corner[2];
+  if (plan->dim == 2 && plan->d_meta) {
+    // the 2-D body kernel predicts its window from the last stencil corner: restart that
+    // prediction from the new displacement (floor of the smallest marker coordinate)
+    for (int d = 0; d < 2; ++d) {
+      const double x = ts == 8 ? plan->lo_t[d] + state_host[6 + d] : (double)((float)plan->lo_t[d] + (float)state_host[6 + d]);
+      corner[d] = (int)floor(x) - plan->cfg.radius + 1;
+    }
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(plan->d_meta + META_PX, corner, sizeof(corner), cudaMemcpyHostToDevice, st);
+  }
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   return cuda_status(e, "vs_body_set_state");
+}
+
+int vs_body_state_device(const vs_body_plan* plan, void** state) {
+  VS_REQUIRE(plan && state, "vs_body_state_device: null argument");
+  *state = plan->d_state;
+  return VS_OK;
 }
 
 int vs_body_get_state(const vs_body_plan* plan, double* state_host, void* stream) {
@@ -1782,6 +2253,357 @@ int vs_run_graph(vs_lattice_plan* lattice, vs_body_plan* body, void* f_a, void* 
     lattice->g_stream = st;
   }
   return cuda_status(cudaGraphLaunch(lattice->graph, st), "vs_run_graph launch");
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------ many cases per launch
+// A batch advances many independent cases (each a lattice plan with an optional body plan)
+// in lock step: per time step ONE body launch (one CTA per body, chain form), ONE grid
+// launch over the nodes of every case outside its body's box (a flattened block list:
+// block b works on case blk[b].x as block blk[b].y of that case's own geometry), and ONE
+// launch over every box (+ lazy walls) after the join.  Per-case parameters sit in device
+// arrays, built once for a pair of population buffer sets.  The middle time steps can be
+// replayed from a CUDA graph of `steps_per_graph` steps.
+struct vs_batch_plan {
+  int n = 0;
+  std::vector<vs_lattice_plan*> L;
+  std::vector<vs_body_plan*> B;
+  std::vector<int> lazy;        // per case: face boundaries deferred to the next step's load
+  std::vector<int> chain_bodies, other_bodies;  // case indices
+  int q = 0, dtype = 0, collision = 0, radius = 0;
+  int tb = 128;                 // threads per block of the grid launches
+  int spg = 64;                 // default steps per graph
+  size_t body_smem = 0;
+  std::vector<const void*> fa, fb;  // buffers the device parameters were built for
+  int built_tb = 0;
+  void* d_main[2][2] = {};      // [parity][first step] StepParams per case
+  void* d_reg[2][2] = {};       // [parity][first step] StepParams per chain-body case
+  int2* d_blk_main = nullptr;
+  int2* d_blk_reg[2] = {};
+  int n_blk_main = 0, n_blk_reg[2] = {0, 0};
+  void* d_body[2] = {};         // [parity] BodyParams per chain body
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  int g_steps = 0;
+  cudaStream_t g_stream = nullptr;
+};
+
+namespace vs {
+
+static void batch_free_params(vs_batch_plan* bp) {
+  for (int p = 0; p < 2; ++p) {
+    for (int f = 0; f < 2; ++f) {
+      if (bp->d_main[p][f]) cudaFree(bp->d_main[p][f]);
+      if (bp->d_reg[p][f]) cudaFree(bp->d_reg[p][f]);
+      bp->d_main[p][f] = bp->d_reg[p][f] = nullptr;
+    }
+    if (bp->d_body[p]) cudaFree(bp->d_body[p]);
+    bp->d_body[p] = nullptr;
+    if (bp->d_blk_reg[p]) cudaFree(bp->d_blk_reg[p]);
+    bp->d_blk_reg[p] = nullptr;
+  }
+  if (bp->d_blk_main) cudaFree(bp->d_blk_main);
+  bp->d_blk_main = nullptr;
+  if (bp->graph) cudaGraphExecDestroy(bp->graph);
+  bp->graph = nullptr;
+  bp->fa.clear();
+  bp->fb.clear();
+}
+
+template <typename V>
+static cudaError_t upload(void** dst, const std::vector<V>& v) {
+  if (v.empty()) return cudaSuccess;
+  cudaError_t e = cudaMalloc(dst, sizeof(V) * v.size());
+  if (e == cudaSuccess) e = cudaMemcpy(*dst, v.data(), sizeof(V) * v.size(), cudaMemcpyHostToDevice);
+  return e;
+}
+
+template <class L, typename T>
+static int batch_build(vs_batch_plan* bp, void* const* fa, void* const* fb) {
+  batch_free_params(bp);
+  std::vector<StepParams<L, T>> main[2][2], reg[2][2];
+  std::vector<int2> bm, br[2];
+  std::vector<BodyParams<T>> body[2];
+  for (int p = 0; p < 2; ++p)
+    for (int first = 0; first < 2; ++first) {
+      for (int k = 0; k < bp->n; ++k) {
+        const void* fin = p == 0 ? fa[k] : fb[k];
+        void* fout = p == 0 ? fb[k] : fa[k];
+        const bool lazy_in = !first && bp->lazy[k];
+        StepParams<L, T> P;
+        dim3 g;
+        int tb = 0;
+        const bool chain_body = bp->B[k] && bp->B[k]->dim == 2 && bp->B[k]->chain;
+        if (bp->B[k] && !chain_body) {
+          // a body outside the batched form runs its own kernels; its whole grid then
+          // goes after the join (it reads the force window)
+          if (grid_setup<L, T>(bp->L[k], bp->B[k], fin, fout, 0, false, bp->tb, P, g, tb)) {
+            const int idx = (int)reg[p][first].size();
+            reg[p][first].push_back(P);
+            if (p == 0)
+              for (int j = 0; j < (int)(g.x * g.y); ++j) br[first].push_back(make_int2(idx, j));
+          }
+          continue;
+        }
+        const vs_body_plan* Bk = bp->B[k];
+        if (grid_setup<L, T>(bp->L[k], Bk, fin, fout, Bk ? 1 : 0, lazy_in, bp->tb, P, g, tb)) {
+          const int idx = (int)main[p][first].size();
+          main[p][first].push_back(P);
+          if (p == 0 && first == 1)
+            for (int j = 0; j < (int)(g.x * g.y); ++j) bm.push_back(make_int2(idx, j));
+        }
+        if (!chain_body) continue;
+        if (grid_setup<L, T>(bp->L[k], Bk, fin, fout, 2, lazy_in, bp->tb, P, g, tb)) {
+          const int idx = (int)reg[p][first].size();
+          reg[p][first].push_back(P);
+          if (p == 0)
+            for (int j = 0; j < (int)(g.x * g.y); ++j) br[first].push_back(make_int2(idx, j));
+        }
+        if (first == 0) body[p].push_back(body_params2d<T>(bp->B[k], bp->L[k], fin, nullptr, false));
+      }
+    }
+  cudaError_t e = cudaSuccess;
+  for (int p = 0; p < 2 && e == cudaSuccess; ++p) {
+    for (int f = 0; f < 2 && e == cudaSuccess; ++f) {
+      e = upload(&bp->d_main[p][f], main[p][f]);
+      if (e == cudaSuccess) e = upload(&bp->d_reg[p][f], reg[p][f]);
+    }
+    if (e == cudaSuccess) e = upload(&bp->d_body[p], body[p]);
+    if (e == cudaSuccess) e = upload((void**)&bp->d_blk_reg[p], br[p]);
+    bp->n_blk_reg[p] = (int)br[p].size();
+  }
+  if (e == cudaSuccess) e = upload((void**)&bp->d_blk_main, bm);
+  bp->n_blk_main = (int)bm.size();
+  if (e != cudaSuccess) {
+    batch_free_params(bp);
+    return cuda_status(e, "vs_batch_run parameters");
+  }
+  bp->fa.assign(fa, fa + bp->n);
+  bp->fb.assign(fb, fb + bp->n);
+  bp->built_tb = bp->tb;
+  return VS_OK;
+}
+
+template <class L, typename T, int COLL>
+static int batch_step_t(vs_batch_plan* bp, int s, int n_steps, void* const* fa, void* const* fb, cudaStream_t st) {
+  const int p = s & 1, first = s == 0 ? 1 : 0;
+  const int nb = (int)bp->chain_bodies.size();
+  const bool fork = nb > 0 || !bp->other_bodies.empty();
+  cudaError_t e = cudaSuccess;
+  if (fork) {
+    e = cudaEventRecord(bp->ev_fork, st);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(bp->side, bp->ev_fork, 0);
+    if (e != cudaSuccess) return cuda_status(e, "vs_batch fork");
+    if (nb > 0) {
+      const BodyParams<T>* bpar = (const BodyParams<T>*)bp->d_body[p];
+      switch (bp->radius) {
+        case 1: k_body2d_chain_batch<T, 1><<<nb, kBodyThreads, bp->body_smem, bp->side>>>(bpar); break;
+        case 2: k_body2d_chain_batch<T, 2><<<nb, kBodyThreads, bp->body_smem, bp->side>>>(bpar); break;
+        default: k_body2d_chain_batch<T, 3><<<nb, kBodyThreads, bp->body_smem, bp->side>>>(bpar); break;
+      }
+    }
+    // bodies outside the batched form: their own kernel(s), full grid in the main launch
+    for (int k : bp->other_bodies) {
+      const int rc = enqueue_body(bp->B[k], bp->L[k], p == 0 ? fa[k] : fb[k], nullptr, bp->side);
+      if (rc) return rc;
+    }
+  }
+  if (bp->n_blk_main > 0)
+    k_step_batch<L, T, COLL, false><<<bp->n_blk_main, bp->tb, 0, st>>>(
+        (const StepParams<L, T>*)bp->d_main[p][first], bp->d_blk_main);
+  if (fork) {
+    e = cudaEventRecord(bp->ev_join, bp->side);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(st, bp->ev_join, 0);
+    if (e != cudaSuccess) return cuda_status(e, "vs_batch join");
+  }
+  if (bp->n_blk_reg[first] > 0)
+    k_step_batch<L, T, COLL, true><<<bp->n_blk_reg[first], bp->tb, 0, st>>>(
+        (const StepParams<L, T>*)bp->d_reg[p][first], bp->d_blk_reg[first]);
+  VS_CHECK_LAUNCH("vs_batch step");
+  for (int k = 0; k < bp->n; ++k) {
+    if (bp->lazy[k] && s != n_steps - 1) continue;
+    const int rc = enqueue_bcs(bp->L[k], p == 0 ? fb[k] : fa[k], st);
+    if (rc) return rc;
+  }
+  return VS_OK;
+}
+
+static int batch_step(vs_batch_plan* bp, int s, int n_steps, void* const* fa, void* const* fb, cudaStream_t st) {
+  return dispatch(bp->q, bp->dtype, [&](auto l, auto t) -> int {
+    using L = decltype(l);
+    using T = typename decltype(t)::type;
+    switch (bp->collision) {
+      case VS_COLLIDE_BGK: return batch_step_t<L, T, VS_COLLIDE_BGK>(bp, s, n_steps, fa, fb, st);
+      case VS_COLLIDE_KBC: return batch_step_t<L, T, VS_COLLIDE_KBC>(bp, s, n_steps, fa, fb, st);
+      case VS_COLLIDE_REG: return batch_step_t<L, T, VS_COLLIDE_REG>(bp, s, n_steps, fa, fb, st);
+      default: return batch_step_t<L, T, VS_COLLIDE_MRT>(bp, s, n_steps, fa, fb, st);
+    }
+  });
+}
+
+static void batch_destroy(vs_batch_plan* bp) {
+  batch_free_params(bp);
+  if (bp->ev_fork) cudaEventDestroy(bp->ev_fork);
+  if (bp->ev_join) cudaEventDestroy(bp->ev_join);
+  if (bp->side) cudaStreamDestroy(bp->side);
+  delete bp;
+}
+
+}  // namespace vs
+
+extern "C" {
+
+int vs_batch_plan_create(vs_lattice_plan* const* lattices, vs_body_plan* const* bodies, int n_cases,
+                         vs_batch_plan** out) {
+  VS_REQUIRE(lattices && out && n_cases > 0, "vs_batch_plan_create: bad arguments");
+  vs_batch_plan* bp = new (std::nothrow) vs_batch_plan();
+  if (!bp) {
+    set_error("out of host memory");
+    return VS_ERR_INVALID_ARG;
+  }
+  auto fail = [&](int rc) {
+    batch_destroy(bp);
+    return rc;
+  };
+  bp->n = n_cases;
+  for (int k = 0; k < n_cases; ++k) {
+    vs_lattice_plan* Lk = lattices[k];
+    vs_body_plan* Bk = bodies ? bodies[k] : nullptr;
+    if (!Lk) {
+      set_error("vs_batch_plan_create: case %d has no lattice plan", k);
+      return fail(VS_ERR_INVALID_ARG);
+    }
+    if (k == 0) {
+      bp->q = Lk->cfg.q;
+      bp->dtype = Lk->cfg.dtype;
+      bp->collision = Lk->cfg.collision;
+    } else if (Lk->cfg.q != bp->q || Lk->cfg.dtype != bp->dtype || Lk->cfg.collision != bp->collision) {
+      set_error("vs_batch_plan_create: case %d differs in lattice, dtype or collision from case 0", k);
+      return fail(VS_ERR_UNSUPPORTED);
+    }
+    bp->L.push_back(Lk);
+    bp->B.push_back(Bk);
+    const bool batched_body = Bk && Bk->dim == 2 && Bk->chain;
+    bp->lazy.push_back(batched_body && lazy_boundaries(Lk, Bk) ? 1 : 0);
+    if (batched_body) {
+      if (bp->chain_bodies.empty()) bp->radius = Bk->cfg.radius;
+      if (Bk->cfg.radius != bp->radius) {
+        set_error("vs_batch_plan_create: bodies with different stencil radii");
+        return fail(VS_ERR_UNSUPPORTED);
+      }
+      bp->chain_bodies.push_back(k);
+      const size_t sm = bp->dtype == VS_F64 ? body2d_chain_smem<double>(Bk->M, Bk->cfg.radius, Bk->cap[0] + 2, 0)
+                                            : body2d_chain_smem<float>(Bk->M, Bk->cfg.radius, Bk->cap[0] + 2, 0);
+      bp->body_smem = sm > bp->body_smem ? sm : bp->body_smem;
+    } else if (Bk) {
+      bp->other_bodies.push_back(k);
+    }
+  }
+  for (size_t i = 0; i < bp->B.size(); ++i)
+    for (size_t j = i + 1; j < bp->B.size(); ++j)
+      if ((bp->B[i] && bp->B[i] == bp->B[j]) || bp->L[i] == bp->L[j]) {
+        set_error("vs_batch_plan_create: cases %zu and %zu share a plan", i, j);
+        return fail(VS_ERR_INVALID_ARG);
+      }
+  if (!bp->chain_bodies.empty()) {
+    cudaError_t e = bp->dtype == VS_F64 ? cudaSuccess : cudaSuccess;
+    auto attr = [&](auto fn) {
+      int dev = 0, optin = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+      if ((int64_t)bp->body_smem > optin) return cudaErrorInvalidValue;
+      return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    };
+    if (bp->dtype == VS_F64)
+      e = bp->radius == 1 ? attr(k_body2d_chain_batch<double, 1>)
+                          : (bp->radius == 2 ? attr(k_body2d_chain_batch<double, 2>) : attr(k_body2d_chain_batch<double, 3>));
+    else
+      e = bp->radius == 1 ? attr(k_body2d_chain_batch<float, 1>)
+                          : (bp->radius == 2 ? attr(k_body2d_chain_batch<float, 2>) : attr(k_body2d_chain_batch<float, 3>));
+    if (e != cudaSuccess) return fail(cuda_status(e, "vs_batch_plan_create body kernel"));
+  }
+  if (!bp->chain_bodies.empty() || !bp->other_bodies.empty()) {
+    int prio_lo = 0, prio_hi = 0;
+    cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
+    cudaError_t e = cudaStreamCreateWithPriority(&bp->side, cudaStreamNonBlocking, prio_hi);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&bp->ev_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&bp->ev_join, cudaEventDisableTiming);
+    if (e != cudaSuccess) return fail(cuda_status(e, "vs_batch_plan_create stream"));
+  }
+  *out = bp;
+  return VS_OK;
+}
+
+int vs_batch_plan_destroy(vs_batch_plan* plan) {
+  if (plan) batch_destroy(plan);
+  return VS_OK;
+}
+
+int vs_batch_set_launch(vs_batch_plan* plan, int threads_per_block, int steps_per_graph) {
+  VS_REQUIRE(plan, "vs_batch_set_launch: null plan");
+  VS_REQUIRE(threads_per_block == 32 || threads_per_block == 64 || threads_per_block == 128 ||
+                 threads_per_block == 256,
+             "vs_batch_set_launch: threads_per_block must be 32, 64, 128 or 256");
+  VS_REQUIRE(steps_per_graph >= 0, "vs_batch_set_launch: steps_per_graph must be >= 0");
+  plan->tb = threads_per_block;
+  plan->spg = steps_per_graph;
+  return VS_OK;
+}
+
+int vs_batch_run(vs_batch_plan* plan, void* const* f_a, void* const* f_b, int n_steps, void* stream) {
+  VS_REQUIRE(plan && f_a && f_b && n_steps >= 0, "vs_batch_run: bad arguments");
+  for (int k = 0; k < plan->n; ++k)
+    VS_REQUIRE(f_a[k] && f_b[k] && f_a[k] != f_b[k], "vs_batch_run: case %d needs two distinct buffers", k);
+  if (n_steps == 0) return VS_OK;
+  cudaStream_t st = as_stream(stream);
+  bool same = plan->built_tb == plan->tb && (int)plan->fa.size() == plan->n;
+  for (int k = 0; same && k < plan->n; ++k) same = plan->fa[k] == f_a[k] && plan->fb[k] == f_b[k];
+  if (!same) {
+    const int rc = dispatch(plan->q, plan->dtype, [&](auto l, auto t) -> int {
+      return batch_build<decltype(l), typename decltype(t)::type>(plan, f_a, f_b);
+    });
+    if (rc) return rc;
+  }
+  // first step, then whole graphs of G middle steps (G even: every replay starts on an odd
+  // step, so one graph serves all), then the remaining steps one by one
+  const int G = (plan->spg / 2) * 2;
+  int s = 0;
+  int rc = batch_step(plan, s++, n_steps, f_a, f_b, st);
+  if (rc) return rc;
+  if (G > 0 && st != nullptr && n_steps - 1 - s >= G) {
+    if (!plan->graph || plan->g_steps != G || plan->g_stream != st) {
+      if (plan->graph) cudaGraphExecDestroy(plan->graph);
+      plan->graph = nullptr;
+      cudaGraph_t g = nullptr;
+      cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+      if (e != cudaSuccess) return cuda_status(e, "vs_batch_run capture");
+      int crc = VS_OK;
+      for (int j = 0; j < G && crc == VS_OK; ++j) crc = batch_step(plan, 1 + j, 1 << 30, f_a, f_b, st);
+      e = cudaStreamEndCapture(st, &g);
+      if (crc) {
+        if (g) cudaGraphDestroy(g);
+        return crc;
+      }
+      if (e != cudaSuccess) return cuda_status(e, "vs_batch_run end capture");
+      e = cudaGraphInstantiate(&plan->graph, g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) return cuda_status(e, "vs_batch_run instantiate");
+      plan->g_steps = G;
+      plan->g_stream = st;
+    }
+    while (n_steps - 1 - s >= G) {
+      cudaError_t e = cudaGraphLaunch(plan->graph, st);
+      if (e != cudaSuccess) return cuda_status(e, "vs_batch_run graph launch");
+      s += G;
+    }
+  }
+  for (; s < n_steps; ++s) {
+    rc = batch_step(plan, s, n_steps, f_a, f_b, st);
+    if (rc) return rc;
+  }
+  return VS_OK;
 }
 
 }  // extern "C"

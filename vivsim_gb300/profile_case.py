@@ -36,6 +36,8 @@ def main():
     stream = torch.cuda.Stream()
     with torch.cuda.stream(stream):
         step, body, sim = configs.build_solver(case, variant=a.variant)
+        if a.graph and not a.grid_only:
+            sim.run(a.steps, graph=True)  # capture (untimed)
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()

@@ -210,3 +210,69 @@ class Simulation:
         if n_steps % 2 == 1:
             self._cur_is_a = not self._cur_is_a
         return hist
+
+
+class Batch:
+    """Many independent simulations advanced together: per time step one body launch, one
+    grid launch over all cases and one launch over all body boxes (vs_batch_run)."""
+
+    def __init__(self, sims, threads_per_block=128, steps_per_graph=64):
+        self.sims = list(sims)
+        n = len(self.sims)
+        if n == 0:
+            raise ValueError("a batch needs at least one simulation")
+        lat = (C.c_void_p * n)(*[s.step.handle.value for s in self.sims])
+        bod = (C.c_void_p * n)(*[(s.body.handle.value if s.body is not None else None) for s in self.sims])
+        h = C.c_void_p()
+        V.call("vs_batch_plan_create", lat, bod, n, C.byref(h))
+        self.handle = h
+        self.set_launch(threads_per_block, steps_per_graph)
+
+    def set_launch(self, threads_per_block=128, steps_per_graph=64):
+        V.call("vs_batch_set_launch", self.handle, int(threads_per_block), int(steps_per_graph))
+        self.threads_per_block, self.steps_per_graph = int(threads_per_block), int(steps_per_graph)
+
+    def tune(self, trial_steps=64, candidates=None):
+        """Pick the launch shape (threads per block, steps per graph) with the shortest time
+        for `trial_steps` steps; each candidate runs twice (the first run builds its tables
+        and graph) and the second is timed with CUDA events.  Advances the simulations by
+        2 * trial_steps * len(candidates) steps.  Returns {(tb, spg): ms per step}."""
+        if candidates is None:
+            candidates = [(tb, spg) for tb in (64, 128, 256) for spg in (16, 64)]
+        times = {}
+        for tb, spg in candidates:
+            self.set_launch(tb, spg)
+            self.run(trial_steps)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            self.run(trial_steps)
+            e1.record()
+            torch.cuda.synchronize()
+            times[(tb, spg)] = e0.elapsed_time(e1) / trial_steps
+        best = min(times, key=times.get)
+        self.set_launch(*best)
+        return times
+
+    def run(self, n_steps):
+        if n_steps <= 0:
+            return
+        n = len(self.sims)
+        cur = [(s._a if s._cur_is_a else s._b) for s in self.sims]
+        oth = [(s._b if s._cur_is_a else s._a) for s in self.sims]
+        fa = (C.c_void_p * n)(*[V.ptr(t) for t in cur])
+        fb = (C.c_void_p * n)(*[V.ptr(t) for t in oth])
+        V.call("vs_batch_run", self.handle, fa, fb, int(n_steps), V.stream())
+        if n_steps % 2 == 1:
+            for s in self.sims:
+                s._cur_is_a = not s._cur_is_a
+
+    def close(self):
+        if getattr(self, "handle", None) and self.handle.value:
+            V.lib().vs_batch_plan_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
