@@ -43,6 +43,7 @@ def parse():
     ap.add_argument("--no-extras", action="store_true", help="skip the HBM-bound roofline cases")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU-baseline sample budget")
     ap.add_argument("--batch-steps", type=int, default=5000, help="time steps of the batched-sweep comparison")
+    ap.add_argument("--adjoint-steps", type=int, default=4000, help="time steps of the adjoint timing")
     return ap.parse_args()
 
 
@@ -242,6 +243,36 @@ def batched_vs_sequential(torch, steps, n_cases=64, seed=3):
             "tuning_ms_per_step": {f"{k[0]}x{k[1]}": round(v, 4) for k, v in tuned.items()}}
 
 
+def adjoint_over_forward(torch, steps):
+    """Differentiable cylinder (D2Q9 BGK 512 x 256, D = 20, 64 markers, 1-DOF spring,
+    checkpoint every 100 steps, objective = mean drag over the second half): time of the
+    forward run alone vs the forward run with checkpoints plus the reverse sweep."""
+    import numpy as np
+    from vivsim_gb300 import adjoint
+    off = np.random.default_rng(2).normal(0.0, 0.1, 64)
+    plan = adjoint.CylinderDrag(nx=512, ny=256, D=20.0, Re=100.0, n_markers=64, offsets=off, n_steps=steps,
+                                checkpoint_every=100, obj_start=steps // 2)
+    plan.forward(keep_checkpoints=True)
+    plan.backward()  # captures the graphs (untimed)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    J = plan.forward(keep_checkpoints=False)
+    t_fwd = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    plan.forward(keep_checkpoints=True)
+    t_fck = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    gU0, gK, goff = plan.backward()
+    t_bwd = time.perf_counter() - t0
+    plan.close()
+    return {"workload": f"diff_cylinder_d2q9_bgk_512x256_m64_{steps}steps_ckpt100", "objective": J,
+            "forward_s": round(t_fwd, 4), "forward_with_checkpoints_s": round(t_fck, 4),
+            "reverse_s": round(t_bwd, 4), "adjoint_over_forward": round(t_bwd / t_fwd, 3),
+            "gradient_over_forward": round((t_fck + t_bwd) / t_fwd, 3),
+            "grad_U0": gU0, "grad_stiffness": gK, "grad_offsets_norm": float(np.linalg.norm(goff)),
+            "timing": "host wall clock around synchronising calls (each call ends with a stream sync)"}
+
+
 def gb300_arm(args, world, rank, local):
     import numpy as np
     import torch
@@ -306,6 +337,7 @@ def gb300_arm(args, world, rank, local):
 
         extras = {}
         extras_batch = None
+        extras_adj = None
         if not args.no_extras and rank == 0:
             del e2e_sim
             for name in ("sphere3d", "periodic2d"):
@@ -323,6 +355,8 @@ def gb300_arm(args, world, rank, local):
                 del st2, bd2, sm2, c2
                 torch.cuda.empty_cache()
             extras_batch = batched_vs_sequential(torch, args.batch_steps)
+            torch.cuda.empty_cache()
+            extras_adj = adjoint_over_forward(torch, args.adjoint_steps)
             torch.cuda.empty_cache()
     if rank != 0:
         if dist is not None:
@@ -350,6 +384,7 @@ def gb300_arm(args, world, rank, local):
         "roofline": rl,
         "roofline_hbm_bound": extras,
         "batched_vs_sequential": extras_batch,
+        "adjoint": extras_adj,
         "e2e": {"value": round(e2e_mlups, 1), "unit": "MLUPS", "h2d_bytes_per_step": fbytes,
                 "d2h_bytes_per_step": fbytes,
                 "path": "vivsim_gb300.solver.Simulation.run from pinned host populations"},

@@ -255,6 +255,9 @@ int vs_body_set_state(vs_body_plan* plan, const double* state_host, void* stream
 /* Device address of the body state (a[3], v[3], d[3], h[3] in the plan dtype), for
  * callers that copy or read it on the device between steps. */
 int vs_body_state_device(const vs_body_plan* plan, void** state);
+/* vs_body_set_state from a device copy of the 12 values, enqueued on the stream (no host
+ * synchronisation; capturable into a CUDA graph). */
+int vs_body_set_state_device(vs_body_plan* plan, const void* state, void* stream);
 
 /* One step: f_out = step(f_in).  body may be NULL.  force_hist, when not NULL, receives
  * the body force h (3 values of the plan dtype) of this step.  f_out must not alias f_in. */

@@ -119,6 +119,7 @@ _SIGS = {
     "vs_run_graph": (_i, [_p, _p, _p, _p, _i, _p, _p]),
     "vs_step_grid_only": (_i, [_p, _p, _p, _p, _p]),
     "vs_body_state_device": (_i, [_p, C.POINTER(C.c_void_p)]),
+    "vs_body_set_state_device": (_i, [_p, _p, _p]),
     "vs_batch_plan_create": (_i, [C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), _i, C.POINTER(C.c_void_p)]),
     "vs_batch_plan_destroy": (_i, [_p]),
     "vs_batch_set_launch": (_i, [_p, _i, _i]),

@@ -104,8 +104,8 @@ struct GridArgs {
   const T* f;   // populations at the start of the step (9, nx, ny)
   T* lam;       // in: adjoint of the step's output; k_adj_bc rewrites its wall columns
   T* lam_out;   // out: adjoint of f
-  const T* g;   // body force of the step on the full grid (2, nx, ny), zero off the stencils
-  const T* lu;  // adjoint of u from the immersed boundary (2, nx, ny)
+  T* g;         // body force of the step on the full grid (2, nx, ny), zero off the stencils
+  T* lu;        // adjoint of u from the immersed boundary (2, nx, ny); both reset to zero here
   int nx, ny;
   T omega, U0, rho_out;
   double* acc;  // [0] d/dU0 (boundaries), [1] d/domega
@@ -208,6 +208,13 @@ __global__ void __launch_bounds__(256) k_adj_grid(GridArgs<T> A) {
     const T g0 = A.g[p], g1 = A.g[n + p];
     // lambda_u from the forcing term: d/du_a of w_i (3 (c_i - u).g + 9 (c_i.u)(c_i.g))
     T lu0 = A.lu[p], lu1 = A.lu[n + p];
+    // leave the body fields zero for the next (earlier) step, which writes only its stencils
+    if (g0 != T(0) || g1 != T(0) || lu0 != T(0) || lu1 != T(0)) {
+      A.g[p] = T(0);
+      A.g[n + p] = T(0);
+      A.lu[p] = T(0);
+      A.lu[n + p] = T(0);
+    }
     T lrho = T(0);
 #pragma unroll
     for (int i = 0; i < 9; ++i) {
@@ -258,7 +265,9 @@ struct BodyArgs {
   const T* X0;      // (M) marker x, (M) marker y
   int nx, ny, M, kernel, n_iter;
   T ds2;            // 2 ds
-  T wobj;           // weight of this step's x force in the objective
+  T wobj;           // weight of the x force in the objective, for steps >= obj_start
+  const int* seg_start;  // first step of the segment (device), so a graph can replay it
+  int j, obj_start;      // this step's index in its segment
   T k1, k2, c1, c2, dt, damp, stiff, den, area;
   int free_dof[2];
   double* dK;       // d/dstiffness
@@ -290,20 +299,23 @@ __device__ __forceinline__ T ddelta(int kernel, T r) {
   return sg * T(-0.25) * k * sin(k * a);
 }
 
-// Node sum over the pairs that reach the node of pair (m, s): sum_p W_p F[m_p] (both
-// components), the pairs found by scanning every marker (M is small for this body).
+// Node sum over the pairs that reach the node (nx_, ny_) of a pair: sum_p W_p F[m_p] (both
+// components), the contributing markers given by the pair's bit mask (NW 64-bit words,
+// bit i = marker i), taken in increasing marker order.
 template <typename T, int WD>
-__device__ __forceinline__ void node_sum(int nx_, int ny_, int M, const int* fxy, const T* W, const T* F, T& s0,
-                                         T& s1) {
+__device__ __forceinline__ void node_sum(int nx_, int ny_, const unsigned long long* mask, int NW, const int* fxy,
+                                         const T* W, const T* F, T& s0, T& s1) {
   constexpr int S = WD * WD;
   s0 = T(0);
   s1 = T(0);
-  for (int i = 0; i < M; ++i) {
-    const unsigned dx = (unsigned)(nx_ - fxy[2 * i]), dy = (unsigned)(ny_ - fxy[2 * i + 1]);
-    if (dx < (unsigned)WD && dy < (unsigned)WD) {
-      const T w = W[i * S + dx * WD + dy];
-      s0 += F[2 * i] * w;
-      s1 += F[2 * i + 1] * w;
+  for (int w = 0; w < NW; ++w) {
+    unsigned long long b = mask[w];
+    while (b) {
+      const int i = w * 64 + __ffsll((long long)b) - 1;
+      b &= b - 1;
+      const T wt = W[i * S + (nx_ - fxy[2 * i]) * WD + (ny_ - fxy[2 * i + 1])];
+      s0 += F[2 * i] * wt;
+      s1 += F[2 * i + 1] * wt;
     }
   }
 }
@@ -329,7 +341,16 @@ __global__ void __launch_bounds__(kAdjBodyThreads) k_adj_body(BodyArgs<T> A) {
   T* mu = U + 2 * M;           // [2M] adjoint of U_k
   T* lFt = mu + 2 * M;         // [2M] adjoint of Ft
   T* red = lFt + 2 * M;        // [8] a, v, d, h adjoints
-  int* fxy = (int*)(red + 8);  // [2M] stencil corners
+  const int NW = (M + 63) / 64;
+  unsigned long long* cm = (unsigned long long*)(((uintptr_t)(red + 8) + 7) & ~(uintptr_t)7);  // [P][NW]
+  int* fxy = (int*)(cm + (size_t)P * NW);  // [2M] stencil corners
+  {
+    unsigned have;
+    asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(have));
+    if ((size_t)((const unsigned char*)(fxy + 2 * M) - smem) > have) return;  // host sizing error: no work
+  }
+  const int step = *A.seg_start + A.j;
+  const T wobj = step >= A.obj_start ? A.wobj : T(0);
 
   const T a[2] = {A.state[0], A.state[1]}, v[2] = {A.state[3], A.state[4]}, d[2] = {A.state[6], A.state[7]};
   // markers (dyn.py:68-81), weights and their position derivatives, u and lambda_g at the nodes
@@ -372,6 +393,20 @@ __global__ void __launch_bounds__(kAdjBodyThreads) k_adj_body(BodyArgs<T> A) {
     lg[2 * p + 1] = l1;
   }
   __syncthreads();
+  // contributors of each pair's node
+  for (int p = tid; p < P; p += nt) {
+    const int m = p / S, s = p - m * S, ix = s / WD, iy = s - ix * WD;
+    const int gx = fxy[2 * m] + ix, gy = fxy[2 * m + 1] + iy;
+    for (int w = 0; w < NW; ++w) {
+      unsigned long long b = 0;
+      for (int i = w * 64; i < M && i < w * 64 + 64; ++i) {
+        const unsigned dx = (unsigned)(gx - fxy[2 * i]), dy = (unsigned)(gy - fxy[2 * i + 1]);
+        if (dx < (unsigned)WD && dy < (unsigned)WD) b |= 1ull << (i - w * 64);
+      }
+      cm[(size_t)p * NW + w] = b;
+    }
+  }
+  __syncthreads();
   // forward MDF (ib/mdf.py:38-64), every force step kept
   for (int q = tid; q < 2 * M; q += nt) {
     const int m = q >> 1, c = q & 1;
@@ -387,7 +422,8 @@ __global__ void __launch_bounds__(kAdjBodyThreads) k_adj_body(BodyArgs<T> A) {
     const T* F = Fs + 2 * M * k;
     for (int p = tid; p < P; p += nt) {  // spread(F_k) at each pair's node
       const int m = p / S, s = p - m * S, ix = s / WD, iy = s - ix * WD;
-      node_sum<T, WD>(fxy[2 * m] + ix, fxy[2 * m + 1] + iy, M, fxy, W, F, nmu[2 * p], nmu[2 * p + 1]);
+      node_sum<T, WD>(fxy[2 * m] + ix, fxy[2 * m + 1] + iy, cm + (size_t)p * NW, NW, fxy, W, F, nmu[2 * p],
+                      nmu[2 * p + 1]);
     }
     __syncthreads();
     for (int q = tid; q < 2 * M; q += nt) {
@@ -407,7 +443,7 @@ __global__ void __launch_bounds__(kAdjBodyThreads) k_adj_body(BodyArgs<T> A) {
     const int m = p / S, s = p - m * S, ix = s / WD, iy = s - ix * WD;
     const int gx = fxy[2 * m] + ix, gy = fxy[2 * m + 1] + iy;
     T s0, s1;
-    node_sum<T, WD>(gx, gy, M, fxy, W, Ft, s0, s1);
+    node_sum<T, WD>(gx, gy, cm + (size_t)p * NW, NW, fxy, W, Ft, s0, s1);
     if (gx < 0 || gx >= nx || gy < 0 || gy >= ny) continue;
     const int64_t q = (int64_t)gx * ny + gy;
     A.g[q] = s0;
@@ -444,7 +480,7 @@ __global__ void __launch_bounds__(kAdjBodyThreads) k_adj_body(BodyArgs<T> A) {
         ld = ld1;
         lh = T(0);
       }
-      if (c == 0) lh += A.wobj;
+      if (c == 0) lh += wobj;
       red[c] = la + A.area * lh;
       red[2 + c] = lv;
       red[4 + c] = ld;
@@ -473,8 +509,8 @@ __global__ void __launch_bounds__(kAdjBodyThreads) k_adj_body(BodyArgs<T> A) {
         const int m = p / S, s = p - m * S, ix = s / WD, iy = s - ix * WD;
         const int gx = fxy[2 * m] + ix, gy = fxy[2 * m + 1] + iy;
         T m0, m1, f0, f1;
-        node_sum<T, WD>(gx, gy, M, fxy, W, mu, m0, m1);
-        node_sum<T, WD>(gx, gy, M, fxy, W, F, f0, f1);
+        node_sum<T, WD>(gx, gy, cm + (size_t)p * NW, NW, fxy, W, mu, m0, m1);
+        node_sum<T, WD>(gx, gy, cm + (size_t)p * NW, NW, fxy, W, F, f0, f1);
         nmu[2 * p] = m0;
         nmu[2 * p + 1] = m1;
         lW[p] += T(0.5) * ((mu[2 * m] * f0 + mu[2 * m + 1] * f1) + (F[2 * m] * m0 + F[2 * m + 1] * m1));
@@ -505,7 +541,7 @@ __global__ void __launch_bounds__(kAdjBodyThreads) k_adj_body(BodyArgs<T> A) {
     const int m = p / S, s = p - m * S, ix = s / WD, iy = s - ix * WD;
     const int gx = fxy[2 * m] + ix, gy = fxy[2 * m + 1] + iy;
     T n0, n1;
-    node_sum<T, WD>(gx, gy, M, fxy, W, mu, n0, n1);
+    node_sum<T, WD>(gx, gy, cm + (size_t)p * NW, NW, fxy, W, mu, n0, n1);
     if (gx >= 0 && gx < nx && gy >= 0 && gy < ny) {
       const int64_t q = (int64_t)gx * ny + gy;
       A.lu[q] = n0;
@@ -539,8 +575,8 @@ __global__ void __launch_bounds__(kAdjBodyThreads) k_adj_body(BodyArgs<T> A) {
 
 template <typename T>
 static size_t adj_body_smem(int M, int R, int n_iter) {
-  const size_t S = 4 * R * R, P = M * S, NF = n_iter > 0 ? n_iter : 1;
-  return sizeof(T) * (4 * P + 6 * P + 2 * M * NF + 8 * (size_t)M + 8) + sizeof(int) * 2 * M + 16;
+  const size_t S = 4 * R * R, P = M * S, NF = n_iter > 0 ? n_iter : 1, NW = (M + 63) / 64;
+  return sizeof(T) * (4 * P + 6 * P + 2 * M * NF + 8 * (size_t)M + 8) + 8 + 8 * P * NW + sizeof(int) * 2 * M + 16;
 }
 
 }  // namespace adj
@@ -561,8 +597,14 @@ struct vs_adjoint_plan {
   void* d_fb = nullptr;
   void* d_ck = nullptr;            // checkpoints: n_ck x (9 n)
   void* d_ck_state = nullptr;      // n_ck x 12
-  void* d_seg = nullptr;           // (C + 1) x (9 n): one recomputed segment
-  void* d_seg_state = nullptr;     // (C + 1) x 12
+  void* d_seg[2] = {nullptr, nullptr};        // (C + 1) x (9 n): recomputed segments (two in flight)
+  void* d_seg_state[2] = {nullptr, nullptr};  // (C + 1) x 12
+  int* d_seg_start = nullptr;      // [2] first step of the segment in each buffer
+  cudaStream_t rec = nullptr;      // recompute stream (runs the next segment's forward)
+  cudaStream_t aux = nullptr;      // boundary adjoint, concurrent with the body adjoint
+  cudaEvent_t ev_rec[2] = {}, ev_rev[2] = {}, ev_f = nullptr, ev_b = nullptr;
+  cudaGraphExec_t g_rec[2] = {}, g_rev[2] = {};
+  cudaStream_t g_stream = nullptr;
   void* d_lam[2] = {nullptr, nullptr};
   void* d_g = nullptr;             // 2 n
   void* d_lu = nullptr;            // 2 n
@@ -580,10 +622,21 @@ namespace adj {
 static void free_plan(vs_adjoint_plan* p) {
   if (p->body) vs_body_plan_destroy(p->body);
   if (p->lat) vs_lattice_plan_destroy(p->lat);
-  void* bufs[] = {p->d_f0, p->d_fa, p->d_fb, p->d_ck, p->d_ck_state, p->d_seg, p->d_seg_state, p->d_lam[0],
-                  p->d_lam[1], p->d_g, p->d_lu, p->d_lstate, p->d_X0, p->d_hist, p->d_acc};
+  void* bufs[] = {p->d_f0,  p->d_fa,       p->d_fb,     p->d_ck,        p->d_ck_state, p->d_seg[0],
+                  p->d_seg[1], p->d_seg_state[0], p->d_seg_state[1], p->d_lam[0], p->d_lam[1], p->d_g,
+                  p->d_lu,  p->d_lstate,  p->d_X0,     p->d_hist,      p->d_acc,      p->d_seg_start};
   for (void* b : bufs)
     if (b) cudaFree(b);
+  for (int k = 0; k < 2; ++k) {
+    if (p->g_rec[k]) cudaGraphExecDestroy(p->g_rec[k]);
+    if (p->g_rev[k]) cudaGraphExecDestroy(p->g_rev[k]);
+    if (p->ev_rec[k]) cudaEventDestroy(p->ev_rec[k]);
+    if (p->ev_rev[k]) cudaEventDestroy(p->ev_rev[k]);
+  }
+  if (p->ev_f) cudaEventDestroy(p->ev_f);
+  if (p->ev_b) cudaEventDestroy(p->ev_b);
+  if (p->rec) cudaStreamDestroy(p->rec);
+  if (p->aux) cudaStreamDestroy(p->aux);
   delete p;
 }
 
@@ -599,96 +652,191 @@ static void host_equilibrium(double U0, int64_t n, std::vector<T>& f) {
   }
 }
 
+__global__ void k_set_int(int* p, int v) { *p = v; }
+
+// Forward recomputation of segment sg into buffer b (states kept), on stream `st`:
+// the restore (checkpoint copy, device-side body state) and then `len` fused steps.
+template <typename T>
+static int recompute_steps(vs_adjoint_plan* P, int b, int len, cudaStream_t st) {
+  const int64_t n = P->n;
+  T* seg = (T*)P->d_seg[b];
+  T* sst = (T*)P->d_seg_state[b];
+  void* state_dev = nullptr;
+  int rc = vs_body_state_device(P->body, &state_dev);
+  if (rc) return rc;
+  for (int j = 0; j < len; ++j) {
+    cudaError_t e = cudaMemcpyAsync(sst + 12 * j, state_dev, sizeof(T) * 12, cudaMemcpyDeviceToDevice, st);
+    if (e != cudaSuccess) return cuda_status(e, "vs_adjoint_backward state copy");
+    rc = vs_step(P->lat, P->body, seg + (size_t)j * 9 * n, seg + (size_t)(j + 1) * 9 * n, nullptr, st);
+    if (rc) return rc;
+  }
+  return VS_OK;
+}
+
+// Reverse sweep over `len` steps of buffer b (steps seg_start[b] + len-1 .. seg_start[b]),
+// starting from adjoint buffer `cur`; returns the final buffer index through *cur.
+template <typename T>
+static int reverse_steps(vs_adjoint_plan* P, int b, int len, int* cur, cudaStream_t st) {
+  const vs_adjoint_cfg& c = P->cfg;
+  const int64_t n = P->n;
+  const T* seg = (const T*)P->d_seg[b];
+  const T* sst = (const T*)P->d_seg_state[b];
+  const double k1 = 0.5, k2 = 0.25, c1 = 0.5, c2 = 0.25;  // Newmark beta 1/4, gamma 1/2, dt 1
+  const double den = c.mass + c1 * c.damping + c2 * c.stiffness;
+  for (int j = len - 1; j >= 0; --j) {
+    const T* fj = seg + (size_t)j * 9 * n;
+    GridArgs<T> G{};
+    G.f = fj;
+    G.lam = (T*)P->d_lam[*cur];
+    G.lam_out = (T*)P->d_lam[1 - *cur];
+    G.g = (T*)P->d_g;
+    G.lu = (T*)P->d_lu;
+    G.nx = c.nx;
+    G.ny = c.ny;
+    G.omega = (T)P->omega;
+    G.U0 = (T)c.U0;
+    G.rho_out = (T)c.rho_out;
+    G.acc = P->d_acc;
+    // the boundary adjoint touches the x = 0, nx-2, nx-1 columns only, the body adjoint
+    // reads the stencils (kept clear of them): run them side by side
+    cudaError_t e = cudaEventRecord(P->ev_f, st);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(P->aux, P->ev_f, 0);
+    if (e != cudaSuccess) return cuda_status(e, "vs_adjoint_backward fork");
+    k_adj_bc<T><<<grid_for(c.ny, 128), 128, 0, P->aux>>>(G);
+    BodyArgs<T> B{};
+    B.f = fj;
+    B.lam = (const T*)P->d_lam[*cur];
+    B.g = (T*)P->d_g;
+    B.lu = (T*)P->d_lu;
+    B.state = sst + 12 * j;
+    B.lstate = (T*)P->d_lstate;
+    B.X0 = (const T*)P->d_X0;
+    B.nx = c.nx;
+    B.ny = c.ny;
+    B.M = P->M;
+    B.kernel = c.kernel;
+    B.n_iter = c.n_iter;
+    B.ds2 = (T)P->ds * T(2);
+    B.wobj = (T)(1.0 / (double)(c.n_steps - c.obj_start));
+    B.seg_start = P->d_seg_start + b;
+    B.j = j;
+    B.obj_start = c.obj_start;
+    B.k1 = (T)k1; B.k2 = (T)k2; B.c1 = (T)c1; B.c2 = (T)c2; B.dt = T(1);
+    B.damp = (T)c.damping; B.stiff = (T)c.stiffness; B.den = (T)den; B.area = (T)c.added_mass_area;
+    B.free_dof[0] = 0;
+    B.free_dof[1] = 1;
+    B.dK = P->d_acc + 2;
+    B.dX = P->d_acc + 4;
+    switch (c.radius) {
+      case 1: k_adj_body<T, 1><<<1, kAdjBodyThreads, P->body_smem, st>>>(B); break;
+      case 2: k_adj_body<T, 2><<<1, kAdjBodyThreads, P->body_smem, st>>>(B); break;
+      default: k_adj_body<T, 3><<<1, kAdjBodyThreads, P->body_smem, st>>>(B); break;
+    }
+    e = cudaEventRecord(P->ev_b, P->aux);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(st, P->ev_b, 0);
+    if (e != cudaSuccess) return cuda_status(e, "vs_adjoint_backward join");
+    k_adj_grid<T><<<dim3(grid_for(c.ny, 256), c.nx), 256, 0, st>>>(G);
+    VS_CHECK_LAUNCH("vs_adjoint_backward kernels");
+    *cur = 1 - *cur;
+  }
+  return VS_OK;
+}
+
+// Captures fn(stream) into *g once (replayed afterwards).
+template <class F>
+static int capture(cudaGraphExec_t* g, cudaStream_t st, F&& fn) {
+  if (*g) return VS_OK;
+  cudaGraph_t gr = nullptr;
+  cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return cuda_status(e, "vs_adjoint capture");
+  const int rc = fn();
+  e = cudaStreamEndCapture(st, &gr);
+  if (rc) {
+    if (gr) cudaGraphDestroy(gr);
+    return rc;
+  }
+  if (e != cudaSuccess) return cuda_status(e, "vs_adjoint end capture");
+  e = cudaGraphInstantiate(g, gr, 0);
+  cudaGraphDestroy(gr);
+  return cuda_status(e, "vs_adjoint instantiate");
+}
+
+// Reverse sweep.  Segments are recomputed on P->rec one ahead of the reverse sweep on st
+// (double-buffered), so the forward recomputation of segment sg-1 overlaps the adjoint of
+// segment sg.  Full segments of an even length replay CUDA graphs.
 template <typename T>
 static int backward_t(vs_adjoint_plan* P, cudaStream_t st) {
   const vs_adjoint_cfg& c = P->cfg;
   const int64_t n = P->n;
   const int N = c.n_steps, C = P->C;
   const size_t fb = sizeof(T) * 9 * n;
+  if (P->g_stream != st) {  // graphs are tied to the stream they were captured for
+    for (int k = 0; k < 2; ++k) {
+      if (P->g_rec[k]) cudaGraphExecDestroy(P->g_rec[k]);
+      if (P->g_rev[k]) cudaGraphExecDestroy(P->g_rev[k]);
+      P->g_rec[k] = P->g_rev[k] = nullptr;
+    }
+    P->g_stream = st;
+  }
   cudaError_t e = cudaMemsetAsync(P->d_acc, 0, sizeof(double) * (4 + 2 * P->M), st);
   if (e == cudaSuccess) e = cudaMemsetAsync(P->d_lam[0], 0, fb, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(P->d_lstate, 0, sizeof(T) * 12, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(P->d_g, 0, sizeof(T) * 2 * n, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(P->d_lu, 0, sizeof(T) * 2 * n, st);
+  if (e == cudaSuccess) e = cudaEventRecord(P->ev_f, st);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(P->rec, P->ev_f, 0);
   if (e != cudaSuccess) return cuda_status(e, "vs_adjoint_backward");
-  int cur = 0;
-  void* state_dev = nullptr;
-  int rc = vs_body_state_device(P->body, &state_dev);
+  const bool graphs = C % 2 == 0 && st != nullptr;
+  bool rev_pending[2] = {false, false};
+  auto launch_recompute = [&](int sg) -> int {
+    const int b = sg & 1, s0 = sg * C, len = (N - s0) < C ? (N - s0) : C;
+    cudaStream_t rs = P->rec;
+    cudaError_t e2 = cudaSuccess;
+    if (rev_pending[b]) e2 = cudaStreamWaitEvent(rs, P->ev_rev[b], 0);  // buffer b free again
+    if (e2 == cudaSuccess)
+      e2 = cudaMemcpyAsync(P->d_seg[b], (const char*)P->d_ck + (size_t)sg * fb, fb, cudaMemcpyDeviceToDevice, rs);
+    if (e2 != cudaSuccess) return cuda_status(e2, "vs_adjoint_backward restore");
+    int rc = vs_body_set_state_device(P->body, (const char*)P->d_ck_state + (size_t)sg * 12 * sizeof(T), rs);
+    if (rc) return rc;
+    k_set_int<<<1, 1, 0, rs>>>(P->d_seg_start + b, s0);
+    if (graphs && len == C) {
+      rc = capture(&P->g_rec[b], rs, [&]() { return recompute_steps<T>(P, b, C, rs); });
+      if (rc) return rc;
+      e2 = cudaGraphLaunch(P->g_rec[b], rs);
+      if (e2 != cudaSuccess) return cuda_status(e2, "vs_adjoint_backward recompute graph");
+    } else {
+      rc = recompute_steps<T>(P, b, len, rs);
+      if (rc) return rc;
+    }
+    e2 = cudaEventRecord(P->ev_rec[b], rs);
+    return e2 == cudaSuccess ? VS_OK : cuda_status(e2, "vs_adjoint_backward event");
+  };
+  int rc = launch_recompute(P->n_ck - 1);
   if (rc) return rc;
-  const double k1 = 0.5, k2 = 0.25, c1 = 0.5, c2 = 0.25;  // Newmark beta 1/4, gamma 1/2, dt 1
-  const double den = c.mass + c1 * c.damping + c2 * c.stiffness;
+  int cur = 0;
   for (int sg = P->n_ck - 1; sg >= 0; --sg) {
-    const int s0 = sg * C, len = (N - s0) < C ? (N - s0) : C;
-    // restore the checkpoint and recompute the segment, keeping every state
-    T* seg = (T*)P->d_seg;
-    T* sst = (T*)P->d_seg_state;
-    e = cudaMemcpyAsync(seg, (const char*)P->d_ck + (size_t)sg * fb, fb, cudaMemcpyDeviceToDevice, st);
-    if (e != cudaSuccess) return cuda_status(e, "vs_adjoint_backward restore");
-    {
-      T hs[12];
-      double hd[12];
-      e = cudaMemcpyAsync(hs, (const char*)P->d_ck_state + (size_t)sg * 12 * sizeof(T), sizeof(hs),
-                          cudaMemcpyDeviceToHost, st);
-      if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-      if (e != cudaSuccess) return cuda_status(e, "vs_adjoint_backward state");
-      for (int i = 0; i < 12; ++i) hd[i] = (double)hs[i];
-      rc = vs_body_set_state(P->body, hd, st);
+    const int b = sg & 1, s0 = sg * C, len = (N - s0) < C ? (N - s0) : C;
+    e = cudaStreamWaitEvent(st, P->ev_rec[b], 0);
+    if (e != cudaSuccess) return cuda_status(e, "vs_adjoint_backward wait");
+    if (sg > 0) {
+      rc = launch_recompute(sg - 1);  // overlaps the reverse sweep below
       if (rc) return rc;
     }
-    for (int j = 0; j < len; ++j) {
-      e = cudaMemcpyAsync(sst + 12 * j, state_dev, sizeof(T) * 12, cudaMemcpyDeviceToDevice, st);
-      if (e != cudaSuccess) return cuda_status(e, "vs_adjoint_backward state copy");
-      rc = vs_step(P->lat, P->body, seg + (size_t)j * 9 * n, seg + (size_t)(j + 1) * 9 * n, nullptr, st);
+    if (graphs && len == C && cur == 0) {
+      rc = capture(&P->g_rev[b], st, [&]() {
+        int cc = 0;
+        return reverse_steps<T>(P, b, C, &cc, st);
+      });
+      if (rc) return rc;
+      e = cudaGraphLaunch(P->g_rev[b], st);
+      if (e != cudaSuccess) return cuda_status(e, "vs_adjoint_backward reverse graph");
+    } else {
+      rc = reverse_steps<T>(P, b, len, &cur, st);
       if (rc) return rc;
     }
-    // reverse sweep over the segment
-    for (int j = len - 1; j >= 0; --j) {
-      const int step = s0 + j;
-      const T* fj = seg + (size_t)j * 9 * n;
-      e = cudaMemsetAsync(P->d_g, 0, sizeof(T) * 2 * n, st);
-      if (e == cudaSuccess) e = cudaMemsetAsync(P->d_lu, 0, sizeof(T) * 2 * n, st);
-      if (e != cudaSuccess) return cuda_status(e, "vs_adjoint_backward memset");
-      GridArgs<T> G{};
-      G.f = fj;
-      G.lam = (T*)P->d_lam[cur];
-      G.lam_out = (T*)P->d_lam[1 - cur];
-      G.g = (const T*)P->d_g;
-      G.lu = (const T*)P->d_lu;
-      G.nx = c.nx;
-      G.ny = c.ny;
-      G.omega = (T)P->omega;
-      G.U0 = (T)c.U0;
-      G.rho_out = (T)c.rho_out;
-      G.acc = P->d_acc;
-      k_adj_bc<T><<<grid_for(c.ny, 128), 128, 0, st>>>(G);
-      BodyArgs<T> B{};
-      B.f = fj;
-      B.lam = (const T*)P->d_lam[cur];
-      B.g = (T*)P->d_g;
-      B.lu = (T*)P->d_lu;
-      B.state = sst + 12 * j;
-      B.lstate = (T*)P->d_lstate;
-      B.X0 = (const T*)P->d_X0;
-      B.nx = c.nx;
-      B.ny = c.ny;
-      B.M = P->M;
-      B.kernel = c.kernel;
-      B.n_iter = c.n_iter;
-      B.ds2 = (T)P->ds * T(2);
-      B.wobj = step >= c.obj_start ? (T)(1.0 / (double)(N - c.obj_start)) : T(0);
-      B.k1 = (T)k1; B.k2 = (T)k2; B.c1 = (T)c1; B.c2 = (T)c2; B.dt = T(1);
-      B.damp = (T)c.damping; B.stiff = (T)c.stiffness; B.den = (T)den; B.area = (T)c.added_mass_area;
-      B.free_dof[0] = 0;
-      B.free_dof[1] = 1;
-      B.dK = P->d_acc + 2;
-      B.dX = P->d_acc + 4;
-      switch (c.radius) {
-        case 1: k_adj_body<T, 1><<<1, kAdjBodyThreads, P->body_smem, st>>>(B); break;
-        case 2: k_adj_body<T, 2><<<1, kAdjBodyThreads, P->body_smem, st>>>(B); break;
-        default: k_adj_body<T, 3><<<1, kAdjBodyThreads, P->body_smem, st>>>(B); break;
-      }
-      k_adj_grid<T><<<dim3(grid_for(c.ny, 256), c.nx), 256, 0, st>>>(G);
-      VS_CHECK_LAUNCH("vs_adjoint_backward kernels");
-      cur = 1 - cur;
-    }
+    e = cudaEventRecord(P->ev_rev[b], st);
+    if (e != cudaSuccess) return cuda_status(e, "vs_adjoint_backward event");
+    rev_pending[b] = true;
   }
   k_adj_initial<T><<<256, 256, 0, st>>>((const T*)P->d_lam[cur], n, (T)c.U0, P->d_acc + 3);
   VS_CHECK_LAUNCH("vs_adjoint_backward initial state");
@@ -801,8 +949,17 @@ int vs_adjoint_plan_create(const vs_adjoint_cfg* cfg, vs_adjoint_plan** out) {
   alloc(&P->d_fb, fbytes);
   alloc(&P->d_ck, fbytes * P->n_ck);
   alloc(&P->d_ck_state, ts * 12 * P->n_ck);
-  alloc(&P->d_seg, fbytes * (P->C + 1));
-  alloc(&P->d_seg_state, ts * 12 * (P->C + 1));
+  for (int k = 0; k < 2; ++k) {
+    alloc(&P->d_seg[k], fbytes * (P->C + 1));
+    alloc(&P->d_seg_state[k], ts * 12 * (P->C + 1));
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&P->ev_rec[k], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&P->ev_rev[k], cudaEventDisableTiming);
+  }
+  alloc((void**)&P->d_seg_start, sizeof(int) * 2);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&P->rec, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&P->aux, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&P->ev_f, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&P->ev_b, cudaEventDisableTiming);
   alloc(&P->d_lam[0], fbytes);
   alloc(&P->d_lam[1], fbytes);
   alloc(&P->d_g, ts * 2 * P->n);

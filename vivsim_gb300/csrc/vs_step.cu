@@ -1306,6 +1306,15 @@ __global__ void k_compact_csr(const int32_t* __restrict__ skeys, const int32_t* 
     }
 }
 
+// body state from a device copy; a 2-D body's window prediction restarts from the new
+// displacement (floor of the smallest marker coordinate, as vs_body_set_state does)
+template <typename T>
+__global__ void k_set_state(T* state, const T* src, int* meta, double lo0, double lo1, int R) {
+  const int i = threadIdx.x;
+  if (i < 12) state[i] = src[i];
+  if (meta && i < 2) meta[META_PX + i] = (int)floor((i == 0 ? (T)lo0 : (T)lo1) + src[6 + i]) - R + 1;
+}
+
 template <typename T>
 __global__ void k_fill(T* p, T v, int64_t n) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
@@ -2166,6 +2175,18 @@ int vs_body_set_state(vs_body_plan* plan, const double* state_host, void* stream
   }
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   return cuda_status(e, "vs_body_set_state");
+}
+
+int vs_body_set_state_device(vs_body_plan* plan, const void* state, void* stream) {
+  VS_REQUIRE(plan && state, "vs_body_set_state_device: null argument");
+  return dispatch_t(plan->cfg.dtype, [&](auto t) -> int {
+    using T = typename decltype(t)::type;
+    k_set_state<T><<<1, 32, 0, as_stream(stream)>>>((T*)plan->d_state, (const T*)state,
+                                                    plan->dim == 2 ? plan->d_meta : nullptr, plan->lo_t[0],
+                                                    plan->lo_t[1], plan->cfg.radius);
+    VS_CHECK_LAUNCH("vs_body_set_state_device");
+    return VS_OK;
+  });
 }
 
 int vs_body_state_device(const vs_body_plan* plan, void** state) {
