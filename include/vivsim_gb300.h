@@ -246,7 +246,8 @@ typedef struct vs_body_plan vs_body_plan;
  * marker order (a curve of markers; checked once from the rigid marker set) uses the chain
  * form of the body kernel; others use the general form (an in-shared-memory sort).  Both
  * give the same results; VIVSIM_GB300_BODY_CSR=1 in the environment at plan creation
- * selects the general form. */
+ * selects the general form.  The chain form runs over a cluster of up to 8 CTAs that also
+ * update the body's box (VIVSIM_GB300_BODY_SINGLE=1: one CTA and a separate box launch). */
 int vs_body_plan_create(const vs_body_cfg* cfg, const vs_lattice_plan* lattice, vs_body_plan** out);
 int vs_body_plan_destroy(vs_body_plan* plan);
 /* Copy the body state out: (a, v, d, h) as 4 x 3 doubles (device state, synchronises the stream). */

@@ -237,18 +237,27 @@ def _viv_small(S, X, steps, graph=False):
 
 
 def test_body_chain_form_equals_general_form(S, monkeypatch):
-    """The chain body kernel (neighbour search by marker index) and the general one (shared-
-    memory sort) sum every node in the same order: identical bits over 30 moving steps."""
+    """The body kernel's cluster form, its single-CTA chain form (neighbour search by marker
+    index) and the general form (shared-memory sort) sum every node in the same order:
+    identical bits over 30 moving steps."""
     th = np.linspace(0, 2 * np.pi, 40, endpoint=False)
     X = np.stack([30 + 6 * np.cos(th), 32 + 6 * np.sin(th)], 1).astype(np.float32).astype(np.float64)
     assert 2 * _chain_width(X) + 1 <= 31  # the chain form applies to this marker set
-    fa, sa, ha = _viv_small(S, X, 30)
-    monkeypatch.setenv("VIVSIM_GB300_BODY_CSR", "1")
-    fb, sb, hb = _viv_small(S, X, 30)
-    assert np.array_equal(fa, fb)
-    assert np.array_equal(ha, hb)
-    for k in ("a", "v", "d", "h"):
-        assert np.array_equal(sa[k], sb[k]), k
+    fa, sa, ha = _viv_small(S, X, 30)  # cluster form (body + box in one launch)
+    for env in ("VIVSIM_GB300_BODY_SINGLE", "VIVSIM_GB300_BODY_CSR"):
+        monkeypatch.setenv(env, "1")
+        fb, sb, hb = _viv_small(S, X, 30)
+        assert np.array_equal(fa, fb), env
+        assert np.array_equal(ha, hb), env
+        for k in ("a", "v", "d", "h"):
+            assert np.array_equal(sa[k], sb[k]), (env, k)
+    # and through graph replay
+    monkeypatch.delenv("VIVSIM_GB300_BODY_SINGLE")
+    monkeypatch.delenv("VIVSIM_GB300_BODY_CSR")
+    with torch.cuda.stream(torch.cuda.Stream()):
+        fg, sg, hg = _viv_small(S, X, 30, graph=True)
+        torch.cuda.synchronize()
+    assert np.array_equal(fa, fg)
 
 
 def test_viv_shuffled_markers_general_form(S):

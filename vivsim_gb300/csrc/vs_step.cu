@@ -11,6 +11,7 @@
 //                  forcing from g, push-stream to the neighbours (1 write/population)
 //   [face kernels] the ordered boundary conditions on the streamed populations
 // The grid kernel carries all of the HBM traffic; the other two touch O(surface) nodes.
+#include <cooperative_groups.h>
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
@@ -30,7 +31,12 @@ namespace vs {
 // device window descriptor (int[8]): origin, extent, sticky status
 // META_PX/PY: lower corner of the body's last stencil bounding box (2-D moving bodies
 // predict their next window from it)
-enum { META_OX = 0, META_OY, META_OZ, META_WX, META_WY, META_WZ, META_STATUS, META_PX, META_PY, META_N = 12 };
+// META_PX2/PY2: a second prediction slot; the cluster-form body reads one slot while the
+// concurrent grid kernel reads the same slot for the box it skips, and writes the other
+enum {
+  META_OX = 0, META_OY, META_OZ, META_WX, META_WY, META_WZ, META_STATUS, META_PX, META_PY, META_PX2, META_PY2,
+  META_N = 12
+};
 
 // ------------------------------------------------------------------ grid kernel
 template <class L, typename T>
@@ -46,6 +52,8 @@ struct StepParams {
   int skip_box;                  // nodes inside box[] are left to another launch
   int box[6];
   int skip_walls;                // the x = 0 and x = nx-1 planes are left to another launch
+  const int* dyn_meta;           // non-null: the skipped box is the body's predicted window,
+  int dyn_slot, dyn_ext[2];      //   read from this prediction slot, extent dyn_ext
   CollideParams<T> cp;
   int forcing;
   int has_g0;
@@ -216,6 +224,10 @@ __device__ __forceinline__ void step_block(const StepParams<L, T>& P, int bx, in
   if (P.skip_box && x >= P.box[0] && x < P.box[1] && y >= P.box[2] && y < P.box[3] && z >= P.box[4] &&
       z < P.box[5])
     return;
+  if (P.dyn_meta) {
+    const int bx = P.dyn_meta[P.dyn_slot ? META_PX2 : META_PX] - 1, by = P.dyn_meta[P.dyn_slot ? META_PY2 : META_PY] - 1;
+    if (x >= bx && x < bx + P.dyn_ext[0] && y >= by && y < by + P.dyn_ext[1]) return;
+  }
   if (P.skip_walls && (x == 0 || x == P.nx - 1)) return;
 
   const int p = (x * P.ny + y) * P.nz + z;
@@ -417,6 +429,7 @@ struct BodyParams {
   T ds2_scalar;  // 2 * ds as the reference forms it: (T)ds * 2
   int M, kernel, n_iter;
   int chain_k;       // chain kernel: markers share stencil nodes only within +-chain_k (cyclic)
+  int pred_slot;     // cluster kernel: prediction slot to read (the other one is written)
   int cap_x, cap_y;  // window region: (cap_x + 2) x (cap_y + 2) cells from the predicted corner
   int row_len;       // staged row length (multiple of 16 bytes), the TMA box's inner extent
   int bulk;          // stage the region with one tensor-map TMA copy
@@ -743,6 +756,8 @@ __global__ void __launch_bounds__(kBodyThreads) k_body2d(const __grid_constant__
     B.meta[META_WX] = EX; B.meta[META_WY] = EY; B.meta[META_WZ] = 1;
     B.meta[META_PX] = misc[0] - R + 1;
     B.meta[META_PY] = misc[2] - R + 1;
+    B.meta[META_PX2] = misc[0] - R + 1;
+    B.meta[META_PY2] = misc[2] - R + 1;
   }
   // total force h = sum_m(-F_total) (dyn.py:126-136) by warp 0 in a fixed tree, added
   // mass h += a A (vortex_induced_vibration.py:136), Newmark update (dyn.py:5-51)
@@ -1085,6 +1100,8 @@ __device__ __forceinline__ void body2d_chain(const BodyParams<T>& B) {
     B.meta[META_WX] = EX; B.meta[META_WY] = EY; B.meta[META_WZ] = 1;
     B.meta[META_PX] = misc[0] - R + 1;
     B.meta[META_PY] = misc[2] - R + 1;
+    B.meta[META_PX2] = misc[0] - R + 1;
+    B.meta[META_PY2] = misc[2] - R + 1;
   }
   // total force h = sum_m(-F_total) (dyn.py:126-136) in a fixed tree by warp 0, added mass
   // h += a A (vortex_induced_vibration.py:136), Newmark update (dyn.py:5-51)
@@ -1133,6 +1150,262 @@ __global__ void __launch_bounds__(kBodyThreads) k_body2d_chain(const __grid_cons
 template <typename T, int R>
 __global__ void __launch_bounds__(kBodyThreads) k_body2d_chain_batch(const BodyParams<T>* __restrict__ Bs) {
   body2d_chain<T, R>(Bs[blockIdx.x]);
+}
+
+// ------------------------------------------------------------------ 2-D body, cluster form
+// The chain form spread over a thread-block cluster of CL CTAs (distributed shared memory),
+// one stencil pair per thread, followed by the box update that waits for the body force.
+// CTA r owns markers [r M / CL, (r+1) M / CL); it recomputes the positions of all markers
+// and the weights of its own markers and their +-K neighbours, so only the per-iteration
+// force steps travel between CTAs: each CTA writes its markers' values into every CTA's
+// replica (st.shared::cluster) before a cluster barrier.  The sums use the chain form's
+// order (4 stencil points per lane-group, then (0 + 2) + (1 + 3); the total force in
+// warp 0's tree on the replicated totals), so the results equal the single-CTA kernels'.
+// After the body, all CTAs of the cluster update the body's box and the lazy face planes
+// (the work of the post-join box launch), so one time step is this kernel beside the
+// grid kernel over the rest of the grid.
+constexpr int kClusterThreads = 256;
+
+template <typename T, int R, int COLL>
+__global__ void __launch_bounds__(kClusterThreads) k_body2d_cluster(const __grid_constant__ BodyParams<T> B,
+                                                                   const __grid_constant__ StepParams<L9, T> SP) {
+  namespace cg = cooperative_groups;
+  constexpr int WD = 2 * R, S = WD * WD;
+  cg::cluster_group cluster = cg::this_cluster();
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int CL = (int)cluster.num_blocks(), rank = (int)cluster.block_rank();
+  const int M = B.M, K = B.chain_k;
+  const int EX = B.cap_x + 2, EY = B.cap_y + 2, NB = EX * EY;
+  const int m0 = (int)((int64_t)rank * M / CL), m1 = (int)((int64_t)(rank + 1) * M / CL);
+  T* W = (T*)smem;              // [M S] (own markers and their neighbours filled)
+  T* Fa = W + M * S;            // [2M] force step replica, ping
+  T* Fb = Fa + 2 * M;           // [2M] pong
+  T* Ft = Fb + 2 * M;           // [2M] total force replica
+  T* U = Ft + 2 * M;            // [2M] own markers' velocity
+  T* prod = U + 2 * M;          // [2 nt] interpolation products (generic radius)
+  int* fxy = (int*)(prod + 2 * nt);  // [2M]
+  unsigned* cm = (unsigned*)(fxy + 2 * M);  // [nt] contributor mask of the thread's pair
+  int* flags = (int*)(cm + nt);      // [4]: [0] a pair of this CTA left the predicted region
+  // every CTA of the cluster must be running before any distributed shared memory access:
+  // arrive now, wait just before the first remote store
+  asm volatile("barrier.cluster.arrive.relaxed.aligned;\n" ::: "memory");
+
+  T a[2], v[2], d[2];
+#pragma unroll
+  for (int c = 0; c < 2; ++c) {
+    a[c] = B.state[c];
+    v[c] = B.state[3 + c];
+    d[c] = B.state[6 + c];
+  }
+  const int slot = B.pred_slot;
+  const int ox = B.meta[slot ? META_PX2 : META_PX] - 1, oy = B.meta[slot ? META_PY2 : META_PY] - 1;
+  const bool region_ok = ox >= B.box[0] && oy >= B.box[2] && ox + EX <= B.box[1] && oy + EY <= B.box[3];
+  if (tid == 0) flags[0] = 0;
+  __syncthreads();
+  // the force window starts at zero (split over the cluster)
+  if (region_ok)
+    for (int k = rank * nt + tid; k < 2 * NB; k += CL * nt) B.gw[k] = T(0);
+  // every marker's stencil corner; weights of the own markers and their +-K neighbours
+  for (int m = tid; m < M; m += nt) {
+    fxy[2 * m] = ifloor(B.X0[m] + d[0]) - R + 1;
+    fxy[2 * m + 1] = ifloor(B.Y0[m] + d[1]) - R + 1;
+  }
+  const int own = m1 - m0;
+  const int span = own + 2 * K < M ? own + 2 * K : M;
+  for (int t = tid; t < span * S; t += nt) {
+    const int k = t / S, s = t - k * S, ix = s / WD, iy = s - ix * WD;
+    int m = span == M ? k : m0 - K + k;
+    m = m < 0 ? m + M : (m >= M ? m - M : m);
+    const T xm = B.X0[m] + d[0], ym = B.Y0[m] + d[1];
+    const int fx = ifloor(xm), fy = ifloor(ym);
+    W[m * S + s] = delta(B.kernel, (T)(fx + ix - R + 1) - xm) * delta(B.kernel, (T)(fy + iy - R + 1) - ym);
+  }
+  __syncthreads();
+  // the thread's own pair: contributors, u at its node, U0 = interp(u), first force step
+  const int lp = tid, m = m0 + lp / S, s = lp - (lp / S) * S;
+  const bool has_pair = lp < own * S;
+  int a0 = 0, nA = 0, b0 = 0, nc = 0, nxp = 0, nyp = 0;
+  unsigned msk = 0;
+  T uu[2] = {T(0), T(0)};
+  if (has_pair) {
+    chain_range(m, K, M, a0, nA, b0, nc);
+    const int ix = s / WD, iy = s - ix * WD;
+    nxp = fxy[2 * m] + ix;
+    nyp = fxy[2 * m + 1] + iy;
+    for (int b = 0; b < nc; ++b) {
+      const int i = b < nA ? a0 + b : b0 + (b - nA);
+      const unsigned dx = (unsigned)(nxp - fxy[2 * i]), dy = (unsigned)(nyp - fxy[2 * i + 1]);
+      if (dx < (unsigned)WD && dy < (unsigned)WD) msk |= 1u << b;
+    }
+    const int cx = nxp - ox, cy = nyp - oy;
+    if (cx < 0 || cx >= EX || cy < 0 || cy >= EY) {
+      atomicOr(flags, 1);
+    } else {
+      const int64_t n = (int64_t)B.nx * B.ny, pn = (int64_t)nxp * B.ny + nyp;
+      T fl[9], r;
+#pragma unroll
+      for (int i = 0; i < 9; ++i) fl[i] = __ldg(B.fin + i * n + pn);
+      macro(L9{}, fl, r, uu);
+    }
+  }
+  cm[tid] = msk;
+  // U0 = interp(u) per own marker, force step 0
+  auto interp = [&](T p0, T p1, T* acc) {
+    // sum of the S products of one marker in the chain form's order
+    if constexpr (S == 16) {
+      const unsigned lane = threadIdx.x & 31, base = lane & ~15u;
+      const unsigned gm = 0xffffu << base;
+      T q[2] = {p0, p1};
+#pragma unroll
+      for (int c = 0; c < 2; ++c) {
+        const T v1 = __shfl_down_sync(gm, q[c], 1, 16), v2 = __shfl_down_sync(gm, q[c], 2, 16),
+                v3 = __shfl_down_sync(gm, q[c], 3, 16);
+        const T Lq = add_rn(add_rn(add_rn(q[c], v1), v2), v3);  // lanes 4k: their 4 stencil points
+        const T L1 = __shfl_down_sync(gm, Lq, 4, 16), L2 = __shfl_down_sync(gm, Lq, 8, 16),
+                L3 = __shfl_down_sync(gm, Lq, 12, 16);
+        acc[c] = add_rn(add_rn(Lq, L2), add_rn(L1, L3));
+      }
+    } else {
+      prod[2 * tid] = p0;
+      prod[2 * tid + 1] = p1;
+      __syncthreads();
+      if (has_pair && s == 0)
+        for (int c = 0; c < 2; ++c) {
+          T z = prod[2 * tid + c];
+          for (int k = 1; k < S; ++k) z = add_rn(z, prod[2 * (tid + k) + c]);
+          acc[c] = z;
+        }
+      __syncthreads();
+    }
+  };
+  const T wself = has_pair ? W[m * S + s] : T(0);
+  const T d2 = has_pair ? (B.ds_arr ? B.ds_arr[m] * T(2) : B.ds2_scalar) : T(0);
+  asm volatile("barrier.cluster.wait.aligned;\n" ::: "memory");
+  {
+    T acc[2];
+    interp(mul_rn(wself, uu[0]), mul_rn(wself, uu[1]), acc);
+    if (has_pair && s == 0) {
+#pragma unroll
+      for (int c = 0; c < 2; ++c) {
+        U[2 * m + c] = acc[c];
+        const T fs = mul_rn(v[c] - acc[c], d2);
+        Ft[2 * m + c] = B.n_iter > 0 ? fs : T(0);
+        for (int r = 0; r < CL; ++r) *cluster.map_shared_rank(Fa + 2 * m + c, r) = fs;
+      }
+    }
+  }
+  cluster.sync();
+  int bad = 0;
+  for (int r = 0; r < CL; ++r) bad |= *cluster.map_shared_rank(flags, r);
+  const bool ok = region_ok && bad == 0;
+  T* Fcur = Fa;
+  T* Fnext = Fb;
+  if (ok) {
+    for (int it = 0; it + 1 < B.n_iter; ++it) {
+      T n0 = T(0), n1 = T(0);
+      if (has_pair) chain_node_sum<T, WD>(msk, a0, nA, b0, nxp, nyp, fxy, W, Fcur, n0, n1);
+      T acc[2];
+      interp(mul_rn(wself, n0 * T(0.5)), mul_rn(wself, n1 * T(0.5)), acc);
+      if (has_pair && s == 0) {
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+          const T uq = U[2 * m + c] + acc[c];
+          U[2 * m + c] = uq;
+          const T fs = mul_rn(v[c] - uq, d2);
+          Ft[2 * m + c] = Ft[2 * m + c] + fs;
+          for (int r = 0; r < CL; ++r) *cluster.map_shared_rank(Fnext + 2 * m + c, r) = fs;
+        }
+      }
+      cluster.sync();
+      T* tmp = Fcur;
+      Fcur = Fnext;
+      Fnext = tmp;
+    }
+    // totals to every replica
+    if (has_pair && s == 0)
+      for (int c = 0; c < 2; ++c)
+        for (int r = 0; r < CL; ++r)
+          if (r != rank) *cluster.map_shared_rank(Ft + 2 * m + c, r) = Ft[2 * m + c];
+    cluster.sync();
+    // g = spread(F_total): each pair writes its node's sum
+    if (has_pair) {
+      T g0, g1;
+      chain_node_sum<T, WD>(msk, a0, nA, b0, nxp, nyp, fxy, W, Ft, g0, g1);
+      const int k = (nxp - ox) * EY + (nyp - oy);
+      B.gw[k] = g0;
+      B.gw[NB + k] = g1;
+    }
+    if (rank == 0 && tid < 32) {
+      // h = sum_m(-F_total) in warp 0's fixed tree, added mass, Newmark (as the chain form)
+      T h[2];
+#pragma unroll
+      for (int c = 0; c < 2; ++c) {
+        T acc = T(0);
+        for (int mm = tid; mm < M; mm += 32) acc = mm == tid ? -Ft[2 * mm + c] : acc + (-Ft[2 * mm + c]);
+#pragma unroll
+        for (int o = 16; o >= 1; o >>= 1) acc = acc + __shfl_down_sync(0xffffffffu, acc, o);
+        h[c] = acc;
+      }
+      const T h0 = __shfl_sync(0xffffffffu, h[0], 0), h1 = __shfl_sync(0xffffffffu, h[1], 0);
+      if (tid < 2) {
+        const int c = tid;
+        const T ac = c == 0 ? a[0] : a[1], vc = c == 0 ? v[0] : v[1], dc = c == 0 ? d[0] : d[1];
+        const T hh = add_rn(c == 0 ? h0 : h1, mul_rn(ac, B.area));
+        T an = ac, vn = vc, dn = dc;
+        if (B.free_dof[c]) {
+          const T v1 = add_rn(vc, mul_rn(B.k1, ac));
+          const T v2 = add_rn(add_rn(dc, mul_rn(B.dt, vc)), mul_rn(B.k2, ac));
+          an = sub_rn(sub_rn(hh, mul_rn(B.damp, v1)), mul_rn(B.stiff, v2)) / B.den;
+          vn = add_rn(mul_rn(B.c1, an), v1);
+          dn = add_rn(mul_rn(B.c2, an), v2);
+        }
+        B.state[c] = an;
+        B.state[3 + c] = vn;
+        B.state[6 + c] = dn;
+        B.state[9 + c] = hh;
+        if (B.force_hist) B.force_hist[c] = hh;
+      }
+      if (tid == 2) {
+        B.state[9 + 2] = T(0);
+        if (B.force_hist) B.force_hist[2] = T(0);
+      }
+      if (tid == 0) {
+        int mnx = INT_MAX, mny = INT_MAX;
+        for (int mm = 0; mm < M; ++mm) {
+          mnx = min(mnx, fxy[2 * mm]);
+          mny = min(mny, fxy[2 * mm + 1]);
+        }
+        B.meta[META_OX] = ox; B.meta[META_OY] = oy; B.meta[META_OZ] = 0;
+        B.meta[META_WX] = EX; B.meta[META_WY] = EY; B.meta[META_WZ] = 1;
+        B.meta[slot ? META_PX : META_PX2] = mnx;  // the next step reads the other slot
+        B.meta[slot ? META_PY : META_PY2] = mny;
+      }
+    }
+  } else if (rank == 0 && tid == 0) {
+    B.meta[META_STATUS] = VS_ERR_RANGE;
+    B.meta[META_WX] = 0; B.meta[META_WY] = 0; B.meta[META_WZ] = 0;
+  }
+  // the body force of every CTA and the window descriptor are in place
+  cluster.sync();
+  // the nodes of the predicted window, which the concurrent grid launch skips (the same
+  // slot gives it the same window); lazy face planes are another launch's
+  for (int k = rank * nt + tid; k < NB; k += CL * nt) {
+    const int x = ox + k / EY, y = oy + k % EY;
+    if (x < 0 || x >= SP.nx || y < 0 || y >= SP.ny || (SP.skip_walls && (x == 0 || x == SP.nx - 1))) continue;
+    const int p = x * SP.ny + y;
+    T f[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) f[i] = __ldg(SP.fin + (size_t)i * SP.n + p);
+    step_node<L9, T, COLL, false>(SP, x, y, 0, p, f);
+  }
+}
+
+template <typename T>
+static size_t body2d_cluster_smem(int M, int R) {
+  const size_t S = 4 * R * R;
+  return sizeof(T) * (M * S + 8 * (size_t)M + 2 * kClusterThreads) + sizeof(int) * (2 * (size_t)M + kClusterThreads + 4) +
+         16;
 }
 
 template <typename T>
@@ -1312,7 +1585,11 @@ template <typename T>
 __global__ void k_set_state(T* state, const T* src, int* meta, double lo0, double lo1, int R) {
   const int i = threadIdx.x;
   if (i < 12) state[i] = src[i];
-  if (meta && i < 2) meta[META_PX + i] = (int)floor((i == 0 ? (T)lo0 : (T)lo1) + src[6 + i]) - R + 1;
+  if (meta && i < 2) {
+    const int c = (int)floor((i == 0 ? (T)lo0 : (T)lo1) + src[6 + i]) - R + 1;
+    meta[META_PX + i] = c;
+    meta[META_PX2 + i] = c;
+  }
 }
 
 template <typename T>
@@ -1372,6 +1649,9 @@ struct vs_body_plan {
   size_t smem;
   int row_len, bulk;  // 2-D body kernel: staged row length, bulk staging on/off
   int chain, chain_k; // 2-D body kernel: chain form and its width
+  int cluster, cl_size;  // 2-D body kernel: cluster form (with the box update) and its CTAs
+  int parity;            // cluster form: prediction slot of the next step
+  size_t cl_smem;
   CUtensorMap maps[2]; // tensor maps of the last two population buffers seen
   const void* map_ptr[2];
   int map_next;
@@ -1658,34 +1938,43 @@ static int tma_dispatch(vs_lattice_plan* LP, const StepParams<L, T>& P, cudaStre
 //         (nodes outside the box read no force window).
 // mode 2: the body's box and, with lazy_walls, the x = 0 / nx-1 planes, whose populations
 //         first get the previous step's face boundaries.
+// mode 3: only the x = 0 / nx-1 planes, with the previous step's face boundaries on load.
+// mode 4: every node except the body's predicted window (read on the device from
+//         prediction slot `slot`) and, with lazy_walls, the x = 0 / nx-1 planes.
 // Fills the grid-kernel parameters and launch geometry; false when there is no node to do.
 // tb_force > 0 fixes the threads per block (the batched launches use one block size).
 template <class L, typename T>
 static bool grid_setup(const vs_lattice_plan* LP, const vs_body_plan* B, const void* fin, void* fout, int mode,
-                       bool lazy_walls, int tb_force, StepParams<L, T>& P, dim3& grid, int& tb) {
+                       bool lazy_walls, int tb_force, StepParams<L, T>& P, dim3& grid, int& tb, int slot = 0) {
   const vs_lattice_cfg& c = LP->cfg;
   P = make_step_params<L, T>(LP, B, fin, fout);
   P.nreg = 0;
   P.skip_box = mode == 1 && B;
-  P.skip_walls = mode == 1 && lazy_walls;
+  P.skip_walls = (mode == 1 || mode == 4) && lazy_walls;
   for (int q = 0; q < 6; ++q) P.box[q] = B ? B->box[q] : 0;
   P.n_lazy = 0;
-  if (mode == 1) {  // outside the box no node reads the force window
+  if (mode == 4 && B) {
+    P.dyn_meta = B->d_meta;
+    P.dyn_slot = slot;
+    P.dyn_ext[0] = B->cap[0] + 2;
+    P.dyn_ext[1] = B->cap[1] + 2;
+  }
+  if (mode == 1 || mode == 4) {  // outside the box no node reads the force window
     P.gw = nullptr;
     P.meta = nullptr;
   }
   int rows = c.nx, ext_last = L::D == 2 ? c.ny : c.nz, ext_mid = c.ny;
-  if (mode == 2) {
+  if (mode == 2 || mode == 3) {
     int nr = 0;
     auto add = [&](const int* R) {
       for (int q = 0; q < 6; ++q) P.reg[nr][q] = R[q];
       ++nr;
     };
-    if (B) add(B->box);
+    if (B && mode == 2) add(B->box);
     if (lazy_walls) {
       int w0[6] = {0, 1, 0, c.ny, 0, c.nz}, w1[6] = {c.nx - 1, c.nx, 0, c.ny, 0, c.nz};
-      if (!B || B->box[0] > 0) add(w0);
-      if (!B || B->box[1] < c.nx) add(w1);
+      if (!B || mode == 3 || B->box[0] > 0) add(w0);
+      if (!B || mode == 3 || B->box[1] < c.nx) add(w1);
       for (int k = 0; k < c.n_bc && k < 2; ++k) P.lazy[P.n_lazy++] = wall_args_from_bc<T>(c.bc[k], LP, k);
     }
     P.nreg = nr;
@@ -1711,7 +2000,7 @@ static bool grid_setup(const vs_lattice_plan* LP, const vs_body_plan* B, const v
 }
 
 static int enqueue_grid(const vs_lattice_plan* LP, const vs_body_plan* B, const void* fin, void* fout,
-                        cudaStream_t st, int mode = 0, bool lazy_walls = false) {
+                        cudaStream_t st, int mode = 0, bool lazy_walls = false, int slot = 0) {
   const vs_lattice_cfg& c = LP->cfg;
   int rc = dispatch(c.q, c.dtype, [&](auto l, auto t) -> int {
     using L = decltype(l);
@@ -1719,10 +2008,10 @@ static int enqueue_grid(const vs_lattice_plan* LP, const vs_body_plan* B, const 
     StepParams<L, T> P;
     dim3 grid;
     int tb = 0;
-    if (!grid_setup<L, T>(LP, B, fin, fout, mode, lazy_walls, 0, P, grid, tb)) return VS_OK;
-    const bool walls = mode == 2 && lazy_walls;
+    if (!grid_setup<L, T>(LP, B, fin, fout, mode, lazy_walls, 0, P, grid, tb, slot)) return VS_OK;
+    const bool walls = (mode == 2 || mode == 3) && lazy_walls;
     const bool aligned = ((uintptr_t)fin % 16) == 0;
-    if (mode != 2 && LP->tma_tb > 0 && aligned) {
+    if ((mode == 0 || mode == 1) && LP->tma_tb > 0 && aligned) {
       vs_lattice_plan* mp = const_cast<vs_lattice_plan*>(LP);
       int trc;
       switch (c.collision) {
@@ -1756,10 +2045,100 @@ static int enqueue_grid(const vs_lattice_plan* LP, const vs_body_plan* B, const 
 // written by exactly one source node, so the two grid launches never write the same word.
 // lazy_in: fin holds the previous step's populations before its face boundaries (they
 // are applied on load); bc_out: run the face kernels on fout (else the next step will).
+// Cluster form: the body kernel also updates the box and the lazy face planes, so the
+// step is that one launch beside the grid launch over the rest of the grid.
+template <typename T, int R, int COLL>
+static cudaError_t launch_cluster_t(vs_body_plan* B, const BodyParams<T>& P, const StepParams<L9, T>& SP,
+                                    cudaStream_t st) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)B->cl_size);
+  cfg.blockDim = dim3(kClusterThreads);
+  cfg.dynamicSmemBytes = B->cl_smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = (unsigned)B->cl_size;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k_body2d_cluster<T, R, COLL>, P, SP);
+}
+
+template <typename T, int R>
+static cudaError_t cluster_attr_t(int coll, int smem) {
+  switch (coll) {
+    case VS_COLLIDE_BGK:
+      return cudaFuncSetAttribute(k_body2d_cluster<T, R, VS_COLLIDE_BGK>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    case VS_COLLIDE_KBC:
+      return cudaFuncSetAttribute(k_body2d_cluster<T, R, VS_COLLIDE_KBC>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    case VS_COLLIDE_REG:
+      return cudaFuncSetAttribute(k_body2d_cluster<T, R, VS_COLLIDE_REG>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    default:
+      return cudaFuncSetAttribute(k_body2d_cluster<T, R, VS_COLLIDE_MRT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  }
+}
+
+static cudaError_t cluster_attr(int dtype, int R, int coll, int smem) {
+  if (dtype == VS_F64)
+    return R == 1 ? cluster_attr_t<double, 1>(coll, smem)
+                  : (R == 2 ? cluster_attr_t<double, 2>(coll, smem) : cluster_attr_t<double, 3>(coll, smem));
+  return R == 1 ? cluster_attr_t<float, 1>(coll, smem)
+                : (R == 2 ? cluster_attr_t<float, 2>(coll, smem) : cluster_attr_t<float, 3>(coll, smem));
+}
+
+static int enqueue_cluster_body(vs_body_plan* B, const vs_lattice_plan* LP, const void* fin, void* fout,
+                                void* force_hist, bool lazy_in, cudaStream_t st) {
+  return dispatch_t(B->cfg.dtype, [&](auto t) -> int {
+    using T = typename decltype(t)::type;
+    BodyParams<T> P = body_params2d<T>(B, LP, fin, force_hist, false);
+    P.pred_slot = B->parity;
+    StepParams<L9, T> SP;
+    dim3 grid;
+    int tb = 0;
+    grid_setup<L9, T>(LP, B, fin, fout, 2, false, 0, SP, grid, tb);  // the force window and the node physics
+    SP.nreg = 0;
+    SP.skip_walls = lazy_in ? 1 : 0;
+    cudaError_t e;
+    auto go = [&](auto rt) {
+      constexpr int R = decltype(rt)::value;
+      switch (LP->cfg.collision) {
+        case VS_COLLIDE_BGK: return launch_cluster_t<T, R, VS_COLLIDE_BGK>(B, P, SP, st);
+        case VS_COLLIDE_KBC: return launch_cluster_t<T, R, VS_COLLIDE_KBC>(B, P, SP, st);
+        case VS_COLLIDE_REG: return launch_cluster_t<T, R, VS_COLLIDE_REG>(B, P, SP, st);
+        default: return launch_cluster_t<T, R, VS_COLLIDE_MRT>(B, P, SP, st);
+      }
+    };
+    switch (B->cfg.radius) {
+      case 1: e = go(std::integral_constant<int, 1>{}); break;
+      case 2: e = go(std::integral_constant<int, 2>{}); break;
+      default: e = go(std::integral_constant<int, 3>{}); break;
+    }
+    if (e != cudaSuccess) return cuda_status(e, "vs_step cluster body kernel");
+    return VS_OK;
+  });
+}
+
 static int enqueue_step(const vs_lattice_plan* LP, vs_body_plan* B, const void* fin, void* fout, void* force_hist,
                         cudaStream_t st, bool lazy_in = false, bool bc_out = true) {
   int rc;
-  if (B) {
+  if (B && B->cluster) {
+    cudaError_t e = cudaEventRecord(B->ev_fork, st);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(B->side, B->ev_fork, 0);
+    if (e != cudaSuccess) return cuda_status(e, "vs_step fork");
+    rc = enqueue_cluster_body(B, LP, fin, fout, force_hist, lazy_in, B->side);
+    if (rc) return rc;
+    rc = enqueue_grid(LP, B, fin, fout, st, 4, lazy_in, B->parity);
+    if (rc) return rc;
+    if (lazy_in) {
+      rc = enqueue_grid(LP, B, fin, fout, st, 3, true);
+      if (rc) return rc;
+    }
+    e = cudaEventRecord(B->ev_join, B->side);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(st, B->ev_join, 0);
+    if (e != cudaSuccess) return cuda_status(e, "vs_step join");
+    B->parity ^= 1;
+  } else if (B) {
     cudaError_t e = cudaEventRecord(B->ev_fork, st);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(B->side, B->ev_fork, 0);
     if (e != cudaSuccess) return cuda_status(e, "vs_step fork");
@@ -2062,6 +2441,8 @@ int vs_body_plan_create(const vs_body_cfg* cfg, const vs_lattice_plan* lattice, 
       int meta0[META_N] = {0};
       meta0[META_PX] = (int)floor(lo[0] + cfg->d0[0]) - cfg->radius + 1;
       meta0[META_PY] = (int)floor(lo[1] + cfg->d0[1]) - cfg->radius + 1;
+      meta0[META_PX2] = meta0[META_PX];
+      meta0[META_PY2] = meta0[META_PY];
       if ((e = cudaMemcpy(b->d_meta, meta0, sizeof(meta0), cudaMemcpyHostToDevice)) != cudaSuccess) return fail(e);
     }
     // the limit is a property of the kernel function, shared by every plan: raise it to the
@@ -2072,6 +2453,24 @@ int vs_body_plan_create(const vs_body_cfg* cfg, const vs_lattice_plan* lattice, 
     else
       e = ts == 8 ? body2d_attr<double>(cfg->radius, optin) : body2d_attr<float>(cfg->radius, optin);
     if (e != cudaSuccess) return fail(e);
+    // cluster form: one pair per thread over up to 8 CTAs, each holding a contiguous share
+    // of the markers (ceil(M / CL) markers' pairs per CTA)
+    b->cluster = 0;
+    if (b->chain && !getenv_flag("VIVSIM_GB300_BODY_SINGLE")) {
+      int cl_ok = 0;
+      cudaDeviceGetAttribute(&cl_ok, cudaDevAttrClusterLaunch, dev);
+      int c = 1;
+      while (c <= 8 && ((M + c - 1) / c) * b->S > kClusterThreads) ++c;
+      if (cl_ok && c <= 8 && c <= M) {
+        b->cl_size = c;
+        b->cl_smem = ts == 8 ? body2d_cluster_smem<double>(M, cfg->radius) : body2d_cluster_smem<float>(M, cfg->radius);
+        if ((int64_t)b->cl_smem <= optin) {
+          e = cluster_attr(cfg->dtype, cfg->radius, lattice->cfg.collision, optin);
+          if (e != cudaSuccess) return fail(e);
+          b->cluster = 1;
+        }
+      }
+    }
   } else {
     // fixed 3-D body: stencil once over a fixed window around the markers
     const int nn[3] = {lattice->cfg.nx, lattice->cfg.ny, lattice->cfg.nz};
@@ -2172,6 +2571,8 @@ int vs_body_set_state(vs_body_plan* plan, const double* state_host, void* stream
     }
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(plan->d_meta + META_PX, corner, sizeof(corner), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(plan->d_meta + META_PX2, corner, sizeof(corner), cudaMemcpyHostToDevice, st);
   }
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   return cuda_status(e, "vs_body_set_state");
