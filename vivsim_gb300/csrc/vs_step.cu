@@ -1164,7 +1164,8 @@ __global__ void __launch_bounds__(kBodyThreads) k_body2d_chain_batch(const BodyP
 // After the body, all CTAs of the cluster update the body's box and the lazy face planes
 // (the work of the post-join box launch), so one time step is this kernel beside the
 // grid kernel over the rest of the grid.
-constexpr int kClusterThreads = 256;
+constexpr int kClusterPairs = 256;    // stencil pairs a CTA holds (one per thread)
+constexpr int kClusterThreads = 384;  // launch bound; a plan uses enough threads for its window
 
 template <typename T, int R, int COLL>
 __global__ void __launch_bounds__(kClusterThreads) k_body2d_cluster(const __grid_constant__ BodyParams<T> B,
@@ -1172,7 +1173,7 @@ __global__ void __launch_bounds__(kClusterThreads) k_body2d_cluster(const __grid
   namespace cg = cooperative_groups;
   constexpr int WD = 2 * R, S = WD * WD;
   cg::cluster_group cluster = cg::this_cluster();
-  extern __shared__ __align__(16) unsigned char smem[];
+  extern __shared__ __align__(128) unsigned char smem[];
   const int tid = threadIdx.x, nt = blockDim.x;
   const int CL = (int)cluster.num_blocks(), rank = (int)cluster.block_rank();
   const int M = B.M, K = B.chain_k;
@@ -1186,7 +1187,7 @@ __global__ void __launch_bounds__(kClusterThreads) k_body2d_cluster(const __grid
   T* prod = U + 2 * M;          // [2 nt] interpolation products (generic radius)
   int* fxy = (int*)(prod + 2 * nt);  // [2M]
   unsigned* cm = (unsigned*)(fxy + 2 * M);  // [nt] contributor mask of the thread's pair
-  int* flags = (int*)(cm + nt);      // [4]: [0] a pair of this CTA left the predicted region
+  int* flags = (int*)(cm + nt);      // [0] a pair of this CTA left the predicted region, [1..2] min corner
   // every CTA of the cluster must be running before any distributed shared memory access:
   // arrive now, wait just before the first remote store
   asm volatile("barrier.cluster.arrive.relaxed.aligned;\n" ::: "memory");
@@ -1201,56 +1202,89 @@ __global__ void __launch_bounds__(kClusterThreads) k_body2d_cluster(const __grid
   const int slot = B.pred_slot;
   const int ox = B.meta[slot ? META_PX2 : META_PX] - 1, oy = B.meta[slot ? META_PY2 : META_PY] - 1;
   const bool region_ok = ox >= B.box[0] && oy >= B.box[2] && ox + EX <= B.box[1] && oy + EY <= B.box[3];
-  if (tid == 0) flags[0] = 0;
-  __syncthreads();
-  // the force window starts at zero (split over the cluster)
-  if (region_ok)
-    for (int k = rank * nt + tid; k < 2 * NB; k += CL * nt) B.gw[k] = T(0);
-  // every marker's stencil corner; weights of the own markers and their +-K neighbours
-  for (int m = tid; m < M; m += nt) {
-    fxy[2 * m] = ifloor(B.X0[m] + d[0]) - R + 1;
-    fxy[2 * m + 1] = ifloor(B.Y0[m] + d[1]) - R + 1;
+  const int64_t n = (int64_t)SP.nx * SP.ny;
+  // Prefetch: the populations of this thread's first window node (read at the end) and
+  // of its own pair's node are both known now and f_in does not change during the step.
+  const int kw = rank * nt + tid;
+  int wx = 0, wy = 0, wp = -1;
+  T fw[9];
+  if (kw < NB) {
+    wx = ox + kw / EY;
+    wy = oy + kw % EY;
+    if (wx >= 0 && wx < SP.nx && wy >= 0 && wy < SP.ny && !(SP.skip_walls && (wx == 0 || wx == SP.nx - 1))) {
+      wp = wx * SP.ny + wy;
+#pragma unroll
+      for (int i = 0; i < 9; ++i) fw[i] = __ldg(SP.fin + (size_t)i * n + wp);
+    }
   }
   const int own = m1 - m0;
+  const int lp = tid, m = m0 + lp / S, s = lp - (lp / S) * S;
+  const bool has_pair = lp < own * S;
+  int nxp = 0, nyp = 0;
+  bool in_region = true;
+  T fl[9];
+  if (has_pair) {
+    const int ix = s / WD, iy = s - ix * WD;
+    nxp = ifloor(B.X0[m] + d[0]) - R + 1 + ix;
+    nyp = ifloor(B.Y0[m] + d[1]) - R + 1 + iy;
+    const int cx = nxp - ox, cy = nyp - oy;
+    in_region = cx >= 0 && cx < EX && cy >= 0 && cy < EY;
+    if (in_region) {
+      const int64_t pn = (int64_t)nxp * SP.ny + nyp;
+#pragma unroll
+      for (int i = 0; i < 9; ++i) fl[i] = __ldg(B.fin + i * n + pn);
+    }
+  }
+  if (tid == 0) {
+    flags[0] = 0;
+    flags[1] = INT_MAX;
+    flags[2] = INT_MAX;
+  }
+  if (rank == 0 && tid == 0) {  // window descriptor for the force lookup (grid kernels read it after the body)
+    B.meta[META_OX] = ox; B.meta[META_OY] = oy; B.meta[META_OZ] = 0;
+    B.meta[META_WX] = EX; B.meta[META_WY] = EY; B.meta[META_WZ] = 1;
+  }
+  // the force window starts at zero (split over the cluster)
+  if (region_ok)
+    for (int k = kw; k < 2 * NB; k += CL * nt) B.gw[k] = T(0);
+  __syncthreads();
+  // every marker's stencil corner (and their minimum, the next prediction); weights of the
+  // own markers and their +-K neighbours
+  for (int mm = tid; mm < M; mm += nt) {
+    const int cx = ifloor(B.X0[mm] + d[0]) - R + 1, cy = ifloor(B.Y0[mm] + d[1]) - R + 1;
+    fxy[2 * mm] = cx;
+    fxy[2 * mm + 1] = cy;
+    atomicMin(&flags[1], cx);
+    atomicMin(&flags[2], cy);
+  }
+  if (has_pair && !in_region) atomicOr(&flags[0], 1);
   const int span = own + 2 * K < M ? own + 2 * K : M;
   for (int t = tid; t < span * S; t += nt) {
-    const int k = t / S, s = t - k * S, ix = s / WD, iy = s - ix * WD;
-    int m = span == M ? k : m0 - K + k;
-    m = m < 0 ? m + M : (m >= M ? m - M : m);
-    const T xm = B.X0[m] + d[0], ym = B.Y0[m] + d[1];
+    const int k = t / S, s2 = t - k * S, ix = s2 / WD, iy = s2 - ix * WD;
+    int mm = span == M ? k : m0 - K + k;
+    mm = mm < 0 ? mm + M : (mm >= M ? mm - M : mm);
+    const T xm = B.X0[mm] + d[0], ym = B.Y0[mm] + d[1];
     const int fx = ifloor(xm), fy = ifloor(ym);
-    W[m * S + s] = delta(B.kernel, (T)(fx + ix - R + 1) - xm) * delta(B.kernel, (T)(fy + iy - R + 1) - ym);
+    W[mm * S + s2] = delta(B.kernel, (T)(fx + ix - R + 1) - xm) * delta(B.kernel, (T)(fy + iy - R + 1) - ym);
   }
   __syncthreads();
   // the thread's own pair: contributors, u at its node, U0 = interp(u), first force step
-  const int lp = tid, m = m0 + lp / S, s = lp - (lp / S) * S;
-  const bool has_pair = lp < own * S;
-  int a0 = 0, nA = 0, b0 = 0, nc = 0, nxp = 0, nyp = 0;
+  int a0 = 0, nA = 0, b0 = 0, nc = 0;
   unsigned msk = 0;
   T uu[2] = {T(0), T(0)};
   if (has_pair) {
     chain_range(m, K, M, a0, nA, b0, nc);
-    const int ix = s / WD, iy = s - ix * WD;
-    nxp = fxy[2 * m] + ix;
-    nyp = fxy[2 * m + 1] + iy;
     for (int b = 0; b < nc; ++b) {
       const int i = b < nA ? a0 + b : b0 + (b - nA);
       const unsigned dx = (unsigned)(nxp - fxy[2 * i]), dy = (unsigned)(nyp - fxy[2 * i + 1]);
       if (dx < (unsigned)WD && dy < (unsigned)WD) msk |= 1u << b;
     }
-    const int cx = nxp - ox, cy = nyp - oy;
-    if (cx < 0 || cx >= EX || cy < 0 || cy >= EY) {
-      atomicOr(flags, 1);
-    } else {
-      const int64_t n = (int64_t)B.nx * B.ny, pn = (int64_t)nxp * B.ny + nyp;
-      T fl[9], r;
-#pragma unroll
-      for (int i = 0; i < 9; ++i) fl[i] = __ldg(B.fin + i * n + pn);
+    if (in_region) {
+      T r;
       macro(L9{}, fl, r, uu);
     }
   }
   cm[tid] = msk;
-  // U0 = interp(u) per own marker, force step 0
   auto interp = [&](T p0, T p1, T* acc) {
     // sum of the S products of one marker in the chain form's order
     if constexpr (S == 16) {
@@ -1279,21 +1313,44 @@ __global__ void __launch_bounds__(kClusterThreads) k_body2d_cluster(const __grid
       __syncthreads();
     }
   };
+  // the marker's two values (held by its lane s == 0) into every CTA's replica at dst:
+  // with 16-lane groups, lane r of the group stores to CTA r
+  auto publish = [&](T* dst, T v0, T v1, bool skip_self) {
+    if constexpr (S == 16) {
+      const unsigned lane = threadIdx.x & 31, base = lane & ~15u;
+      const unsigned gm = 0xffffu << base;
+      v0 = __shfl_sync(gm, v0, 0, 16);
+      v1 = __shfl_sync(gm, v1, 0, 16);
+      if (has_pair && s < CL && !(skip_self && s == rank)) {
+        T* r = cluster.map_shared_rank(dst + 2 * m, s);
+        r[0] = v0;
+        r[1] = v1;
+      }
+    } else {
+      if (has_pair && s == 0)
+        for (int r = 0; r < CL; ++r)
+          if (!(skip_self && r == rank)) {
+            T* q = cluster.map_shared_rank(dst + 2 * m, r);
+            q[0] = v0;
+            q[1] = v1;
+          }
+    }
+  };
   const T wself = has_pair ? W[m * S + s] : T(0);
   const T d2 = has_pair ? (B.ds_arr ? B.ds_arr[m] * T(2) : B.ds2_scalar) : T(0);
   asm volatile("barrier.cluster.wait.aligned;\n" ::: "memory");
   {
-    T acc[2];
+    T acc[2] = {T(0), T(0)}, fs[2] = {T(0), T(0)};
     interp(mul_rn(wself, uu[0]), mul_rn(wself, uu[1]), acc);
     if (has_pair && s == 0) {
 #pragma unroll
       for (int c = 0; c < 2; ++c) {
         U[2 * m + c] = acc[c];
-        const T fs = mul_rn(v[c] - acc[c], d2);
-        Ft[2 * m + c] = B.n_iter > 0 ? fs : T(0);
-        for (int r = 0; r < CL; ++r) *cluster.map_shared_rank(Fa + 2 * m + c, r) = fs;
+        fs[c] = mul_rn(v[c] - acc[c], d2);
+        Ft[2 * m + c] = B.n_iter > 0 ? fs[c] : T(0);
       }
     }
+    publish(Fa, fs[0], fs[1], false);
   }
   cluster.sync();
   int bad = 0;
@@ -1305,29 +1362,30 @@ __global__ void __launch_bounds__(kClusterThreads) k_body2d_cluster(const __grid
     for (int it = 0; it + 1 < B.n_iter; ++it) {
       T n0 = T(0), n1 = T(0);
       if (has_pair) chain_node_sum<T, WD>(msk, a0, nA, b0, nxp, nyp, fxy, W, Fcur, n0, n1);
-      T acc[2];
+      T acc[2] = {T(0), T(0)}, fs[2] = {T(0), T(0)}, ft[2] = {T(0), T(0)};
       interp(mul_rn(wself, n0 * T(0.5)), mul_rn(wself, n1 * T(0.5)), acc);
       if (has_pair && s == 0) {
 #pragma unroll
         for (int c = 0; c < 2; ++c) {
           const T uq = U[2 * m + c] + acc[c];
           U[2 * m + c] = uq;
-          const T fs = mul_rn(v[c] - uq, d2);
-          Ft[2 * m + c] = Ft[2 * m + c] + fs;
-          for (int r = 0; r < CL; ++r) *cluster.map_shared_rank(Fnext + 2 * m + c, r) = fs;
+          fs[c] = mul_rn(v[c] - uq, d2);
+          ft[c] = Ft[2 * m + c] + fs[c];
+          Ft[2 * m + c] = ft[c];
         }
       }
+      if (it + 2 < B.n_iter) publish(Fnext, fs[0], fs[1], false);
+      else publish(Ft, ft[0], ft[1], true);  // the last iteration sends the totals
       cluster.sync();
       T* tmp = Fcur;
       Fcur = Fnext;
       Fnext = tmp;
     }
-    // totals to every replica
-    if (has_pair && s == 0)
-      for (int c = 0; c < 2; ++c)
-        for (int r = 0; r < CL; ++r)
-          if (r != rank) *cluster.map_shared_rank(Ft + 2 * m + c, r) = Ft[2 * m + c];
-    cluster.sync();
+    if (B.n_iter <= 1) {  // no iteration carried the totals: send them now
+      const T t0 = has_pair ? Ft[2 * m] : T(0), t1 = has_pair ? Ft[2 * m + 1] : T(0);
+      publish(Ft, t0, t1, true);
+      cluster.sync();
+    }
     // g = spread(F_total): each pair writes its node's sum
     if (has_pair) {
       T g0, g1;
@@ -1336,61 +1394,53 @@ __global__ void __launch_bounds__(kClusterThreads) k_body2d_cluster(const __grid
       B.gw[k] = g0;
       B.gw[NB + k] = g1;
     }
-    if (rank == 0 && tid < 32) {
-      // h = sum_m(-F_total) in warp 0's fixed tree, added mass, Newmark (as the chain form)
-      T h[2];
-#pragma unroll
-      for (int c = 0; c < 2; ++c) {
-        T acc = T(0);
-        for (int mm = tid; mm < M; mm += 32) acc = mm == tid ? -Ft[2 * mm + c] : acc + (-Ft[2 * mm + c]);
-#pragma unroll
-        for (int o = 16; o >= 1; o >>= 1) acc = acc + __shfl_down_sync(0xffffffffu, acc, o);
-        h[c] = acc;
-      }
-      const T h0 = __shfl_sync(0xffffffffu, h[0], 0), h1 = __shfl_sync(0xffffffffu, h[1], 0);
-      if (tid < 2) {
-        const int c = tid;
-        const T ac = c == 0 ? a[0] : a[1], vc = c == 0 ? v[0] : v[1], dc = c == 0 ? d[0] : d[1];
-        const T hh = add_rn(c == 0 ? h0 : h1, mul_rn(ac, B.area));
-        T an = ac, vn = vc, dn = dc;
-        if (B.free_dof[c]) {
-          const T v1 = add_rn(vc, mul_rn(B.k1, ac));
-          const T v2 = add_rn(add_rn(dc, mul_rn(B.dt, vc)), mul_rn(B.k2, ac));
-          an = sub_rn(sub_rn(hh, mul_rn(B.damp, v1)), mul_rn(B.stiff, v2)) / B.den;
-          vn = add_rn(mul_rn(B.c1, an), v1);
-          dn = add_rn(mul_rn(B.c2, an), v2);
-        }
-        B.state[c] = an;
-        B.state[3 + c] = vn;
-        B.state[6 + c] = dn;
-        B.state[9 + c] = hh;
-        if (B.force_hist) B.force_hist[c] = hh;
-      }
-      if (tid == 2) {
-        B.state[9 + 2] = T(0);
-        if (B.force_hist) B.force_hist[2] = T(0);
-      }
-      if (tid == 0) {
-        int mnx = INT_MAX, mny = INT_MAX;
-        for (int mm = 0; mm < M; ++mm) {
-          mnx = min(mnx, fxy[2 * mm]);
-          mny = min(mny, fxy[2 * mm + 1]);
-        }
-        B.meta[META_OX] = ox; B.meta[META_OY] = oy; B.meta[META_OZ] = 0;
-        B.meta[META_WX] = EX; B.meta[META_WY] = EY; B.meta[META_WZ] = 1;
-        B.meta[slot ? META_PX : META_PX2] = mnx;  // the next step reads the other slot
-        B.meta[slot ? META_PY : META_PY2] = mny;
-      }
-    }
   } else if (rank == 0 && tid == 0) {
     B.meta[META_STATUS] = VS_ERR_RANGE;
     B.meta[META_WX] = 0; B.meta[META_WY] = 0; B.meta[META_WZ] = 0;
   }
-  // the body force of every CTA and the window descriptor are in place
+  // the body force of every CTA (and the window descriptor) are in place
   cluster.sync();
+  if (ok && rank == 0 && tid < 32) {
+    // h = sum_m(-F_total) in warp 0's fixed tree, added mass, Newmark (as the chain form)
+    T h[2];
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      T acc = T(0);
+      for (int mm = tid; mm < M; mm += 32) acc = mm == tid ? -Ft[2 * mm + c] : acc + (-Ft[2 * mm + c]);
+#pragma unroll
+      for (int o = 16; o >= 1; o >>= 1) acc = acc + __shfl_down_sync(0xffffffffu, acc, o);
+      h[c] = acc;
+    }
+    const T h0 = __shfl_sync(0xffffffffu, h[0], 0), h1 = __shfl_sync(0xffffffffu, h[1], 0);
+    if (tid < 2) {
+      const int c = tid;
+      const T ac = c == 0 ? a[0] : a[1], vc = c == 0 ? v[0] : v[1], dc = c == 0 ? d[0] : d[1];
+      const T hh = add_rn(c == 0 ? h0 : h1, mul_rn(ac, B.area));
+      T an = ac, vn = vc, dn = dc;
+      if (B.free_dof[c]) {
+        const T v1 = add_rn(vc, mul_rn(B.k1, ac));
+        const T v2 = add_rn(add_rn(dc, mul_rn(B.dt, vc)), mul_rn(B.k2, ac));
+        an = sub_rn(sub_rn(hh, mul_rn(B.damp, v1)), mul_rn(B.stiff, v2)) / B.den;
+        vn = add_rn(mul_rn(B.c1, an), v1);
+        dn = add_rn(mul_rn(B.c2, an), v2);
+      }
+      B.state[c] = an;
+      B.state[3 + c] = vn;
+      B.state[6 + c] = dn;
+      B.state[9 + c] = hh;
+      if (B.force_hist) B.force_hist[c] = hh;
+    }
+    if (tid == 2) {
+      B.state[9 + 2] = T(0);
+      if (B.force_hist) B.force_hist[2] = T(0);
+      B.meta[slot ? META_PX : META_PX2] = flags[1];  // the next step reads the other slot
+      B.meta[slot ? META_PY : META_PY2] = flags[2];
+    }
+  }
   // the nodes of the predicted window, which the concurrent grid launch skips (the same
   // slot gives it the same window); lazy face planes are another launch's
-  for (int k = rank * nt + tid; k < NB; k += CL * nt) {
+  if (wp >= 0) step_node<L9, T, COLL, false>(SP, wx, wy, 0, wp, fw);
+  for (int k = kw + CL * nt; k < NB; k += CL * nt) {
     const int x = ox + k / EY, y = oy + k % EY;
     if (x < 0 || x >= SP.nx || y < 0 || y >= SP.ny || (SP.skip_walls && (x == 0 || x == SP.nx - 1))) continue;
     const int p = x * SP.ny + y;
@@ -1402,9 +1452,9 @@ __global__ void __launch_bounds__(kClusterThreads) k_body2d_cluster(const __grid
 }
 
 template <typename T>
-static size_t body2d_cluster_smem(int M, int R) {
+static size_t body2d_cluster_smem(int M, int R, int nt) {
   const size_t S = 4 * R * R;
-  return sizeof(T) * (M * S + 8 * (size_t)M + 2 * kClusterThreads) + sizeof(int) * (2 * (size_t)M + kClusterThreads + 4) +
+  return sizeof(T) * (M * S + 8 * (size_t)M + 2 * (size_t)nt) + sizeof(int) * (2 * (size_t)M + (size_t)nt + 4) +
          16;
 }
 
@@ -1650,6 +1700,7 @@ struct vs_body_plan {
   int row_len, bulk;  // 2-D body kernel: staged row length, bulk staging on/off
   int chain, chain_k; // 2-D body kernel: chain form and its width
   int cluster, cl_size;  // 2-D body kernel: cluster form (with the box update) and its CTAs
+  int cl_threads;        // threads per CTA of the cluster form
   int parity;            // cluster form: prediction slot of the next step
   size_t cl_smem;
   CUtensorMap maps[2]; // tensor maps of the last two population buffers seen
@@ -1660,6 +1711,8 @@ struct vs_body_plan {
   double lo_t[2];  // 2-D: smallest marker x and y, rounded to the plan precision
   cudaStream_t side;
   cudaEvent_t ev_fork, ev_join;
+  cudaStream_t side2;    // cluster form: the lazy face planes, beside the grid launch
+  cudaEvent_t ev_join2;
 };
 
 static size_t dsize(int dtype) { return dtype == VS_F64 ? 8 : 4; }
@@ -1682,6 +1735,8 @@ static void free_body(vs_body_plan* b) {
   if (b->ev_fork) cudaEventDestroy(b->ev_fork);
   if (b->ev_join) cudaEventDestroy(b->ev_join);
   if (b->side) cudaStreamDestroy(b->side);
+  if (b->ev_join2) cudaEventDestroy(b->ev_join2);
+  if (b->side2) cudaStreamDestroy(b->side2);
   delete b;
 }
 
@@ -1959,7 +2014,7 @@ static bool grid_setup(const vs_lattice_plan* LP, const vs_body_plan* B, const v
     P.dyn_ext[0] = B->cap[0] + 2;
     P.dyn_ext[1] = B->cap[1] + 2;
   }
-  if (mode == 1 || mode == 4) {  // outside the box no node reads the force window
+  if (mode == 1 || mode == 3 || mode == 4) {  // outside the box no node reads the force window
     P.gw = nullptr;
     P.meta = nullptr;
   }
@@ -2052,7 +2107,7 @@ static cudaError_t launch_cluster_t(vs_body_plan* B, const BodyParams<T>& P, con
                                     cudaStream_t st) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)B->cl_size);
-  cfg.blockDim = dim3(kClusterThreads);
+  cfg.blockDim = dim3((unsigned)B->cl_threads);
   cfg.dynamicSmemBytes = B->cl_smem;
   cfg.stream = st;
   cudaLaunchAttribute attr[1];
@@ -2128,14 +2183,19 @@ static int enqueue_step(const vs_lattice_plan* LP, vs_body_plan* B, const void* 
     if (e != cudaSuccess) return cuda_status(e, "vs_step fork");
     rc = enqueue_cluster_body(B, LP, fin, fout, force_hist, lazy_in, B->side);
     if (rc) return rc;
+    if (lazy_in) {  // the face planes on a third stream, beside the grid launch
+      e = cudaStreamWaitEvent(B->side2, B->ev_fork, 0);
+      if (e != cudaSuccess) return cuda_status(e, "vs_step fork");
+      rc = enqueue_grid(LP, B, fin, fout, B->side2, 3, true);
+      if (rc) return rc;
+      e = cudaEventRecord(B->ev_join2, B->side2);
+      if (e != cudaSuccess) return cuda_status(e, "vs_step join");
+    }
     rc = enqueue_grid(LP, B, fin, fout, st, 4, lazy_in, B->parity);
     if (rc) return rc;
-    if (lazy_in) {
-      rc = enqueue_grid(LP, B, fin, fout, st, 3, true);
-      if (rc) return rc;
-    }
     e = cudaEventRecord(B->ev_join, B->side);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(st, B->ev_join, 0);
+    if (e == cudaSuccess && lazy_in) e = cudaStreamWaitEvent(st, B->ev_join2, 0);
     if (e != cudaSuccess) return cuda_status(e, "vs_step join");
     B->parity ^= 1;
   } else if (B) {
@@ -2346,6 +2406,8 @@ int vs_body_plan_create(const vs_body_cfg* cfg, const vs_lattice_plan* lattice, 
     cudaError_t es = cudaStreamCreateWithPriority(&b->side, cudaStreamNonBlocking, prio_hi);
     if (es == cudaSuccess) es = cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming);
     if (es == cudaSuccess) es = cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming);
+    if (es == cudaSuccess) es = cudaStreamCreateWithPriority(&b->side2, cudaStreamNonBlocking, prio_hi);
+    if (es == cudaSuccess) es = cudaEventCreateWithFlags(&b->ev_join2, cudaEventDisableTiming);
     if (es != cudaSuccess) {
       free_body(b);
       return cuda_status(es, "vs_body_plan_create stream");
@@ -2460,10 +2522,18 @@ int vs_body_plan_create(const vs_body_cfg* cfg, const vs_lattice_plan* lattice, 
       int cl_ok = 0;
       cudaDeviceGetAttribute(&cl_ok, cudaDevAttrClusterLaunch, dev);
       int c = 1;
-      while (c <= 8 && ((M + c - 1) / c) * b->S > kClusterThreads) ++c;
+      while (c <= 8 && ((M + c - 1) / c) * b->S > kClusterPairs) ++c;
+      // threads: the CTA's pairs, and enough for one window node each
+      const int NB = (b->cap[0] + 2) * (b->cap[1] + 2);
+      int th = ((M + c - 1) / c) * b->S;
+      th = th > (NB + c - 1) / c ? th : (NB + c - 1) / c;
+      th = ((th + 31) / 32) * 32;
+      th = th < kClusterThreads ? th : kClusterThreads;
       if (cl_ok && c <= 8 && c <= M) {
         b->cl_size = c;
-        b->cl_smem = ts == 8 ? body2d_cluster_smem<double>(M, cfg->radius) : body2d_cluster_smem<float>(M, cfg->radius);
+        b->cl_threads = th;
+        b->cl_smem = ts == 8 ? body2d_cluster_smem<double>(M, cfg->radius, th)
+                             : body2d_cluster_smem<float>(M, cfg->radius, th);
         if ((int64_t)b->cl_smem <= optin) {
           e = cluster_attr(cfg->dtype, cfg->radius, lattice->cfg.collision, optin);
           if (e != cudaSuccess) return fail(e);
