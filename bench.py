@@ -273,6 +273,22 @@ def adjoint_over_forward(torch, steps):
             "timing": "host wall clock around synchronising calls (each call ends with a stream sync)"}
 
 
+def job_seconds(torch, dist, secs, device):
+    """The job's time: the maximum over ranks of each rank's timed-region seconds."""
+    if dist is None:
+        return secs
+    t = torch.tensor([secs], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.barrier()
+    return float(t.item())
+
+
+def aggregate_rate(units_per_rank, world, secs):
+    """Whole-job rate in millions of units per second: every rank (replica) processed
+    units_per_rank within the job's time."""
+    return units_per_rank * world / secs / 1e6
+
+
 def gb300_arm(args, world, rank, local):
     import numpy as np
     import torch
@@ -308,12 +324,8 @@ def gb300_arm(args, world, rank, local):
         with ClockSampler(gpu_id) as clk:
             secs = time_chunks(torch, run, args.steps, args.warmup, flush)
         torch.cuda.synchronize()
-        if dist is not None:
-            t = torch.tensor([secs], device="cuda", dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            secs = float(t.item())
-            dist.barrier()
-        mlups = n * args.chunk * args.steps * world / secs / 1e6
+        secs = job_seconds(torch, dist, secs, "cuda")
+        mlups = aggregate_rate(n * args.chunk * args.steps, world, secs)
         # with a body: body kernel, grid launch outside its box, box launch; the x-face
         # boundaries of these cases run on the next step's load and once at the end of a chunk
         launches_per_step = 3 if body is not None else 1 + step_groups(case)

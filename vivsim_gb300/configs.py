@@ -147,14 +147,15 @@ def viv_sweep(n_cases=64, seed=3, heights=(64, 128, 256, 512), collision="kbc"):
 CASES = {"cavity": cavity, "viv2d": viv2d, "sphere3d": sphere3d, "periodic2d": periodic2d}
 
 
-def build_solver(case, device="cuda", variant="auto"):
-    """LatticeStep, RigidBody (or None) and Simulation for a case dict."""
+def build_solver(case, device="cuda", variant="auto", dtype=None):
+    """LatticeStep, RigidBody (or None) and Simulation for a case dict (float32 unless
+    dtype says otherwise)."""
     import torch
 
     from . import solver as S
     bcs = [S.boundary(k, loc, mode=m, **kw) for (k, loc, m, kw) in case["boundaries"]]
     step = S.LatticeStep(case["q"], case["shape"], case["collision"], case["omega"], forcing=case["forcing"],
-                         boundaries=bcs, variant=variant)
+                         boundaries=bcs, variant=variant, dtype=dtype or torch.float32)
     body = None
     if case["body"] is not None:
         b = case["body"]

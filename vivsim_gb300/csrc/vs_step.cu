@@ -45,7 +45,8 @@ struct StepParams {
   T* fout;
   int nx, ny, nz, n;
   int chunks;                    // blocks along the contiguous axis (3-D)
-  int gx;                        // blocks per launch row (the launch's grid.x)
+  int gx;                        // blocks per launch row of the one-block-per-chunk geometry
+  int npt;                       // chunks per block (k_step): grid.x = ceil(gx / npt)
   int nreg;                      // 0: the whole grid; else the union of reg[0..nreg)
   int reg[3][6];                 // regions x0, x1, y0, y1, z0, z1 (half-open)
   int rowstart[4];               // first launch row (x plane) of each region
@@ -239,7 +240,15 @@ __device__ __forceinline__ void step_block(const StepParams<L, T>& P, int bx, in
 
 template <class L, typename T, int COLL, bool WALLS>
 __global__ void __launch_bounds__(256) k_step(const __grid_constant__ StepParams<L, T> P) {
-  step_block<L, T, COLL, WALLS>(P, blockIdx.x, blockIdx.y);
+  if (P.npt <= 1) {
+    step_block<L, T, COLL, WALLS>(P, blockIdx.x, blockIdx.y);
+    return;
+  }
+  for (int k = 0; k < P.npt; ++k) {
+    const int bx = blockIdx.x * P.npt + k;
+    if (bx >= P.gx) break;
+    step_block<L, T, COLL, WALLS>(P, bx, blockIdx.y);
+  }
 }
 
 // Grid kernel over many independent lattices in one launch: block b works on lattice
@@ -1185,7 +1194,8 @@ __global__ void __launch_bounds__(kClusterThreads) k_body2d_cluster(const __grid
   T* Ft = Fb + 2 * M;           // [2M] total force replica
   T* U = Ft + 2 * M;            // [2M] own markers' velocity
   T* prod = U + 2 * M;          // [2 nt] interpolation products (generic radius)
-  int* fxy = (int*)(prod + 2 * nt);  // [2M]
+  T* xs = prod + 2 * nt;        // [2M] marker positions X0 + d, Y0 + d
+  int* fxy = (int*)(xs + 2 * M);     // [2M]
   unsigned* cm = (unsigned*)(fxy + 2 * M);  // [nt] contributor mask of the thread's pair
   int* flags = (int*)(cm + nt);      // [0] a pair of this CTA left the predicted region, [1..2] min corner
   // every CTA of the cluster must be running before any distributed shared memory access:
@@ -1235,6 +1245,11 @@ __global__ void __launch_bounds__(kClusterThreads) k_body2d_cluster(const __grid
       for (int i = 0; i < 9; ++i) fl[i] = __ldg(B.fin + i * n + pn);
     }
   }
+  // all marker positions in one round trip (the own pair's above is the same load)
+  for (int mm = tid; mm < M; mm += nt) {
+    xs[mm] = B.X0[mm] + d[0];
+    xs[M + mm] = B.Y0[mm] + d[1];
+  }
   if (tid == 0) {
     flags[0] = 0;
     flags[1] = INT_MAX;
@@ -1250,12 +1265,21 @@ __global__ void __launch_bounds__(kClusterThreads) k_body2d_cluster(const __grid
   __syncthreads();
   // every marker's stencil corner (and their minimum, the next prediction); weights of the
   // own markers and their +-K neighbours
-  for (int mm = tid; mm < M; mm += nt) {
-    const int cx = ifloor(B.X0[mm] + d[0]) - R + 1, cy = ifloor(B.Y0[mm] + d[1]) - R + 1;
-    fxy[2 * mm] = cx;
-    fxy[2 * mm + 1] = cy;
-    atomicMin(&flags[1], cx);
-    atomicMin(&flags[2], cy);
+  const int Mw = ((M + 31) / 32) * 32;  // whole warps (nt is a multiple of 32): a warp-wide minimum
+  for (int m2 = tid; m2 < Mw; m2 += nt) {
+    int cx = INT_MAX, cy = INT_MAX;
+    if (m2 < M) {
+      cx = ifloor(xs[m2]) - R + 1;
+      cy = ifloor(xs[M + m2]) - R + 1;
+      fxy[2 * m2] = cx;
+      fxy[2 * m2 + 1] = cy;
+    }
+    cx = __reduce_min_sync(0xffffffffu, cx);
+    cy = __reduce_min_sync(0xffffffffu, cy);
+    if ((tid & 31) == 0 && cx != INT_MAX) {
+      atomicMin(&flags[1], cx);
+      atomicMin(&flags[2], cy);
+    }
   }
   if (has_pair && !in_region) atomicOr(&flags[0], 1);
   const int span = own + 2 * K < M ? own + 2 * K : M;
@@ -1263,7 +1287,7 @@ __global__ void __launch_bounds__(kClusterThreads) k_body2d_cluster(const __grid
     const int k = t / S, s2 = t - k * S, ix = s2 / WD, iy = s2 - ix * WD;
     int mm = span == M ? k : m0 - K + k;
     mm = mm < 0 ? mm + M : (mm >= M ? mm - M : mm);
-    const T xm = B.X0[mm] + d[0], ym = B.Y0[mm] + d[1];
+    const T xm = xs[mm], ym = xs[M + mm];
     const int fx = ifloor(xm), fy = ifloor(ym);
     W[mm * S + s2] = delta(B.kernel, (T)(fx + ix - R + 1) - xm) * delta(B.kernel, (T)(fy + iy - R + 1) - ym);
   }
@@ -1454,7 +1478,7 @@ __global__ void __launch_bounds__(kClusterThreads) k_body2d_cluster(const __grid
 template <typename T>
 static size_t body2d_cluster_smem(int M, int R, int nt) {
   const size_t S = 4 * R * R;
-  return sizeof(T) * (M * S + 8 * (size_t)M + 2 * (size_t)nt) + sizeof(int) * (2 * (size_t)M + (size_t)nt + 4) +
+  return sizeof(T) * (M * S + 10 * (size_t)M + 2 * (size_t)nt) + sizeof(int) * (2 * (size_t)M + (size_t)nt + 4) +
          16;
 }
 
@@ -1663,6 +1687,7 @@ struct vs_lattice_plan {
   int lazy_ok;               // all boundaries in one launch group and none needs pre-stream data
   int* d_status;             // device status word of the grid kernels (VS_ERR_TIMEOUT)
   int tma_tb;                // tile width of the TMA grid kernel, 0 when it does not apply
+  int npt;                   // row chunks per block of the plain grid kernel
   int tma_grid;              // persistent CTAs of the TMA grid kernel
   // graph cache
   cudaGraphExec_t graph;
@@ -2051,6 +2076,7 @@ static bool grid_setup(const vs_lattice_plan* LP, const vs_body_plan* B, const v
   P.chunks = (ext_last + tb - 1) / tb;
   grid = dim3(L::D == 2 ? P.chunks : P.chunks * ext_mid, rows);
   P.gx = (int)grid.x;
+  P.npt = 1;
   return true;
 }
 
@@ -2065,6 +2091,10 @@ static int enqueue_grid(const vs_lattice_plan* LP, const vs_body_plan* B, const 
     int tb = 0;
     if (!grid_setup<L, T>(LP, B, fin, fout, mode, lazy_walls, 0, P, grid, tb, slot)) return VS_OK;
     const bool walls = (mode == 2 || mode == 3) && lazy_walls;
+    if ((mode == 0 || mode == 1 || mode == 4) && LP->npt > 1) {  // several chunks per block
+      P.npt = LP->npt;
+      grid.x = (unsigned)((P.gx + P.npt - 1) / P.npt);
+    }
     const bool aligned = ((uintptr_t)fin % 16) == 0;
     if ((mode == 0 || mode == 1) && LP->tma_tb > 0 && aligned) {
       vs_lattice_plan* mp = const_cast<vs_lattice_plan*>(LP);
@@ -2300,6 +2330,9 @@ int vs_lattice_plan_create(const vs_lattice_cfg* cfg, vs_lattice_plan** out) {
   {
     const int nl = cfg->q == 9 ? cfg->ny : nz;
     p->tma_tb = cfg->variant != VS_GRID_TMA ? 0 : ((cfg->q == 9 && nl % 256 == 0) ? 256 : (nl % 128 == 0 ? 128 : 0));
+    const char* e_npt = getenv("VIVSIM_GB300_NPT");
+    p->npt = e_npt ? atoi(e_npt) : 1;
+    p->npt = p->npt < 1 ? 1 : (p->npt > 16 ? 16 : p->npt);
     cudaError_t e = cudaMalloc(&p->d_status, sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(p->d_status, 0, sizeof(int));
     if (e != cudaSuccess) {
