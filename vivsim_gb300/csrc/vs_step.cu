@@ -45,8 +45,7 @@ struct StepParams {
   T* fout;
   int nx, ny, nz, n;
   int chunks;                    // blocks along the contiguous axis (3-D)
-  int gx;                        // blocks per launch row of the one-block-per-chunk geometry
-  int npt;                       // chunks per block (k_step): grid.x = ceil(gx / npt)
+  int gx;                        // blocks per launch row (the launch's grid.x)
   int nreg;                      // 0: the whole grid; else the union of reg[0..nreg)
   int reg[3][6];                 // regions x0, x1, y0, y1, z0, z1 (half-open)
   int rowstart[4];               // first launch row (x plane) of each region
@@ -240,15 +239,7 @@ __device__ __forceinline__ void step_block(const StepParams<L, T>& P, int bx, in
 
 template <class L, typename T, int COLL, bool WALLS>
 __global__ void __launch_bounds__(256) k_step(const __grid_constant__ StepParams<L, T> P) {
-  if (P.npt <= 1) {
-    step_block<L, T, COLL, WALLS>(P, blockIdx.x, blockIdx.y);
-    return;
-  }
-  for (int k = 0; k < P.npt; ++k) {
-    const int bx = blockIdx.x * P.npt + k;
-    if (bx >= P.gx) break;
-    step_block<L, T, COLL, WALLS>(P, bx, blockIdx.y);
-  }
+  step_block<L, T, COLL, WALLS>(P, blockIdx.x, blockIdx.y);
 }
 
 // Grid kernel over many independent lattices in one launch: block b works on lattice
@@ -1687,7 +1678,6 @@ struct vs_lattice_plan {
   int lazy_ok;               // all boundaries in one launch group and none needs pre-stream data
   int* d_status;             // device status word of the grid kernels (VS_ERR_TIMEOUT)
   int tma_tb;                // tile width of the TMA grid kernel, 0 when it does not apply
-  int npt;                   // row chunks per block of the plain grid kernel
   int tma_grid;              // persistent CTAs of the TMA grid kernel
   // graph cache
   cudaGraphExec_t graph;
@@ -2076,7 +2066,6 @@ static bool grid_setup(const vs_lattice_plan* LP, const vs_body_plan* B, const v
   P.chunks = (ext_last + tb - 1) / tb;
   grid = dim3(L::D == 2 ? P.chunks : P.chunks * ext_mid, rows);
   P.gx = (int)grid.x;
-  P.npt = 1;
   return true;
 }
 
@@ -2091,10 +2080,6 @@ static int enqueue_grid(const vs_lattice_plan* LP, const vs_body_plan* B, const 
     int tb = 0;
     if (!grid_setup<L, T>(LP, B, fin, fout, mode, lazy_walls, 0, P, grid, tb, slot)) return VS_OK;
     const bool walls = (mode == 2 || mode == 3) && lazy_walls;
-    if ((mode == 0 || mode == 1 || mode == 4) && LP->npt > 1) {  // several chunks per block
-      P.npt = LP->npt;
-      grid.x = (unsigned)((P.gx + P.npt - 1) / P.npt);
-    }
     const bool aligned = ((uintptr_t)fin % 16) == 0;
     if ((mode == 0 || mode == 1) && LP->tma_tb > 0 && aligned) {
       vs_lattice_plan* mp = const_cast<vs_lattice_plan*>(LP);
@@ -2330,9 +2315,6 @@ int vs_lattice_plan_create(const vs_lattice_cfg* cfg, vs_lattice_plan** out) {
   {
     const int nl = cfg->q == 9 ? cfg->ny : nz;
     p->tma_tb = cfg->variant != VS_GRID_TMA ? 0 : ((cfg->q == 9 && nl % 256 == 0) ? 256 : (nl % 128 == 0 ? 128 : 0));
-    const char* e_npt = getenv("VIVSIM_GB300_NPT");
-    p->npt = e_npt ? atoi(e_npt) : 1;
-    p->npt = p->npt < 1 ? 1 : (p->npt > 16 ? 16 : p->npt);
     cudaError_t e = cudaMalloc(&p->d_status, sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(p->d_status, 0, sizeof(int));
     if (e != cudaSuccess) {
