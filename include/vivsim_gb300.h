@@ -210,6 +210,9 @@ typedef struct vs_lattice_cfg {
   int n_bc;                /* boundaries applied in this order after streaming      */
   vs_bc bc[VS_MAX_BC];
   int variant;             /* grid kernel: VS_GRID_AUTO, VS_GRID_PLAIN or VS_GRID_TMA */
+  const uint8_t* obstacle_mask; /* device, one byte per node or NULL: obstacle_bounce_back after
+                                    the face boundaries (lbm/boundary/bb.py:98-110); the plan
+                                    keeps the pointer, the caller keeps the memory alive */
 } vs_lattice_cfg;
 
 typedef struct vs_lattice_plan vs_lattice_plan;
@@ -300,6 +303,34 @@ int vs_batch_set_launch(vs_batch_plan* plan, int threads_per_block, int steps_pe
  * synchronous upload); graphs need a non-default stream (else steps are launched one by
  * one). */
 int vs_batch_run(vs_batch_plan* plan, void* const* f_a, void* const* f_b, int n_steps, void* stream);
+
+/* ============================================================== diagnostics ===
+ * vivsim/post.py on the device.  Derivatives as jnp.gradient: central differences
+ * inside, one-sided at the two ends of each axis (no periodic wrap).  The velocity is
+ * read from u (d, nx, ny[, nz]) or, when u is NULL, computed from the populations f
+ * (get_macroscopic), which saves the separate moments pass. */
+enum {
+  VS_POST_VELOCITY_MAGNITUDE = 0,    /* post.py:6-14    (n)            */
+  VS_POST_VELOCITY_GRADIENT = 1,     /* post.py:17-29   (d, d, n)      */
+  VS_POST_VORTICITY = 2,             /* post.py:32-54   (1 | 3, n)     */
+  VS_POST_VORTICITY_MAGNITUDE = 3,   /* post.py:57-68   (n)            */
+  VS_POST_DIVERGENCE = 4,            /* post.py:72-83   (n)            */
+  VS_POST_STRAIN_RATE = 5,           /* post.py:86-95   (d, d, n)      */
+  VS_POST_STRAIN_RATE_MAGNITUDE = 6, /* post.py:98-107  (n)            */
+  VS_POST_KINETIC_ENERGY = 7,        /* post.py:110-118 (n)            */
+  VS_POST_ENSTROPHY = 8,             /* post.py:144-155 (n)            */
+  VS_POST_Q_CRITERION = 9,           /* post.py:172-186 (n)            */
+  VS_POST_MEAN_KINETIC_ENERGY = 10,  /* post.py:121-129: sum into *sum_dev */
+  VS_POST_MEAN_ENSTROPHY = 11        /* post.py:158-167: sum into *sum_dev */
+};
+/* One field of the list above into out; for the two means, the sum over the nodes lands
+ * in the device double *sum_dev (divide by the node count for the mean). */
+int vs_post(int q, int dtype, int what, const void* u, const void* f, int nx, int ny, int nz, void* out,
+            double* sum_dev, void* stream);
+/* pressure(rho, cs2) = rho * cs2 — post.py:132-141 */
+int vs_post_pressure(int dtype, const void* rho, int64_t n, double cs2, void* out, void* stream);
+/* Components of a vs_post field (leading dimension of out). */
+int vs_post_components(int q, int what);
 
 /* ================================================================== adjoint ===
  * Gradients of a 2-D cylinder VIV objective by a hand-written discrete adjoint of the

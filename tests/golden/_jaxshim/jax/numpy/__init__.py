@@ -312,6 +312,10 @@ def pad(x, pad_width, mode="constant"):
     return _wrap(_np.pad(_canon(x), pad_width, mode=mode))
 
 
+def swapaxes(x, axis1, axis2):
+    return _wrap(_np.swapaxes(_canon(x), axis1, axis2))
+
+
 def moveaxis(x, source, destination):
     return _wrap(_np.moveaxis(_canon(x), source, destination))
 

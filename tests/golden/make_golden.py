@@ -248,7 +248,29 @@ def generate(mode, jax, jnp, lbm, lbm3d, ib, ib3d, dyn):
     # --------------------------------------------------------------- recipes
     recipes_2d(put, jnp, lbm, ib, dyn, dt, rng)
     recipes_3d(put, jnp, lbm3d, ib3d, dt, rng)
+    post_golden(put, jnp, dt)
     return G
+
+
+POST_FIELDS = ("velocity_magnitude", "velocity_gradient", "vorticity", "vorticity_magnitude", "divergence",
+               "strain_rate", "strain_rate_magnitude", "kinetic_energy", "mean_kinetic_energy", "enstrophy",
+               "mean_enstrophy", "q_criterion")
+
+
+def post_golden(put, jnp, dt):
+    """vivsim/post.py on random 2-D and 3-D velocity fields (its own seed, so the other
+    vectors do not move)."""
+    from vivsim import post
+    rng = np.random.default_rng(777)
+    u2 = rng.normal(0.0, 0.05, (2, 12, 10)).astype(dt)
+    u3 = rng.normal(0.0, 0.05, (3, 8, 7, 6)).astype(dt)
+    rho = (1 + 0.01 * rng.normal(0.0, 1.0, (12, 10))).astype(dt)
+    for tag, u in (("p2", u2), ("p3", u3)):
+        put(f"{tag}.u", u)
+        for name in POST_FIELDS:
+            put(f"{tag}.{name}", getattr(post, name)(jnp.asarray(u)))
+    put("p.rho", rho)
+    put("p.pressure", post.pressure(jnp.asarray(rho)))
 
 
 def recipes_2d(put, jnp, lbm, ib, dyn, dt, rng):

@@ -277,3 +277,19 @@ def test_recipe_sphere(mode, coll):
         if step in (1, 4):
             check(mode, h, f"sph.{coll}.h{step}", 1e-4 if mode == "f32" else 1e-10)
     check(mode, f, f"sph.{coll}.f4", TOL_RECIPE[mode])
+
+
+POST_FIELDS = ("velocity_magnitude", "velocity_gradient", "vorticity", "vorticity_magnitude", "divergence",
+               "strain_rate", "strain_rate_magnitude", "kinetic_energy", "mean_kinetic_energy", "enstrophy",
+               "mean_enstrophy", "q_criterion")
+
+
+def test_post_oracle(mode):
+    from oracle import post
+    G = golden(mode)
+    for tag in ("p2", "p3"):
+        u = G[f"{tag}.u"]
+        for name in POST_FIELDS:
+            err = rel_err(np.asarray(getattr(post, name)(u)), G[f"{tag}.{name}"])
+            assert err <= TOL[mode], f"{tag}.{name}: {err:.3e}"
+    assert rel_err(post.pressure(G["p.rho"]), G["p.pressure"]) <= TOL[mode]

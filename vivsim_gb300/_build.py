@@ -25,6 +25,7 @@ UNITS = {
     "vs_ops_ib.cu": ["-fmad=false"],
     "vs_step.cu": [],
     "vs_adjoint.cu": [],
+    "vs_post.cu": [],
 }
 
 

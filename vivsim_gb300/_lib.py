@@ -50,7 +50,8 @@ class vs_lattice_cfg(C.Structure):
     _fields_ = [("q", C.c_int), ("dtype", C.c_int), ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
                 ("collision", C.c_int), ("omega", C.c_double), ("mrt_op", C.c_double * 361),
                 ("forcing", C.c_int), ("g_uniform", C.c_double * 3), ("mrt_fop", C.c_double * 361),
-                ("n_bc", C.c_int), ("bc", vs_bc * VS_MAX_BC), ("variant", C.c_int)]
+                ("n_bc", C.c_int), ("bc", vs_bc * VS_MAX_BC), ("variant", C.c_int),
+                ("obstacle_mask", C.c_void_p)]
 
 
 class vs_body_cfg(C.Structure):
@@ -124,6 +125,9 @@ _SIGS = {
     "vs_batch_plan_destroy": (_i, [_p]),
     "vs_batch_set_launch": (_i, [_p, _i, _i]),
     "vs_batch_run": (_i, [_p, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), _i, _p]),
+    "vs_post": (_i, [_i, _i, _i, _p, _p, _i, _i, _i, _p, _p, _p]),
+    "vs_post_pressure": (_i, [_i, _p, _l, _d, _p, _p]),
+    "vs_post_components": (_i, [_i, _i]),
     "vs_adjoint_plan_create": (_i, [C.POINTER(vs_adjoint_cfg), C.POINTER(C.c_void_p)]),
     "vs_adjoint_plan_destroy": (_i, [_p]),
     "vs_adjoint_forward": (_i, [_p, _i, C.POINTER(_d), _p]),

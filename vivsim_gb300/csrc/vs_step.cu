@@ -52,6 +52,8 @@ struct StepParams {
   int skip_box;                  // nodes inside box[] are left to another launch
   int box[6];
   int skip_walls;                // the x = 0 and x = nx-1 planes are left to another launch
+  const uint8_t* mask;           // obstacle cells (one byte per node) or null
+  int mask_load;                 // apply the previous step's obstacle bounce-back on load
   const int* dyn_meta;           // non-null: the skipped box is the body's predicted window,
   int dyn_slot, dyn_ext[2];      //   read from this prediction slot, extent dyn_ext
   CollideParams<T> cp;
@@ -95,6 +97,19 @@ __device__ __forceinline__ void step_node(const StepParams<L, T>& P, int x, int 
     bc_node<L, T>(A, 0, f, nb, nullptr, out);
 #pragma unroll
     for (int i = 0; i < Q; ++i) f[i] = out[i];
+  }
+  // the previous step's obstacle bounce-back (lbm/boundary/bb.py:98-110), which follows its
+  // face boundaries: an obstacle cell's populations swap with their opposites
+  if (P.mask_load && P.mask[p]) {
+#pragma unroll
+    for (int i = 0; i < Q; ++i) {
+      const int o = L::opp(i);
+      if (o > i) {
+        const T t = f[i];
+        f[i] = f[o];
+        f[o] = t;
+      }
+    }
   }
 
   T rho, u[3] = {T(0), T(0), T(0)};
@@ -248,8 +263,19 @@ __global__ void __launch_bounds__(256) k_step(const __grid_constant__ StepParams
 template <class L, typename T, int COLL, bool WALLS>
 __global__ void __launch_bounds__(256) k_step_batch(const StepParams<L, T>* __restrict__ Ps,
                                                     const int2* __restrict__ blk) {
+  // the case's parameters, staged in shared memory once per block (every thread reads them)
+  __shared__ __align__(16) unsigned char sp[sizeof(StepParams<L, T>)];
   const int2 cb = blk[blockIdx.x];
-  const StepParams<L, T>& P = Ps[cb.x];
+  {
+    // array elements are 8-byte aligned (the struct holds pointers); copy in 8-byte words
+    static_assert(alignof(StepParams<L, T>) >= 8 && sizeof(StepParams<L, T>) % 8 == 0, "copy granularity");
+    const unsigned long long* src = (const unsigned long long*)(Ps + cb.x);
+    unsigned long long* dst = (unsigned long long*)sp;
+    constexpr int N8 = (int)(sizeof(StepParams<L, T>) / 8);
+    for (int i = threadIdx.x; i < N8; i += blockDim.x) dst[i] = src[i];
+  }
+  __syncthreads();
+  const StepParams<L, T>& P = *(const StepParams<L, T>*)sp;
   const int by = cb.y / P.gx;
   step_block<L, T, COLL, WALLS>(P, cb.y - by * P.gx, by);
 }
@@ -1644,6 +1670,23 @@ __global__ void k_compact_csr(const int32_t* __restrict__ skeys, const int32_t* 
     }
 }
 
+// obstacle bounce-back in place (the last step of a run: its output must be complete)
+template <class L, typename T>
+__global__ void k_mask_bb(T* f, const uint8_t* __restrict__ mask, int64_t n) {
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+    if (!mask[p]) continue;
+#pragma unroll
+    for (int i = 0; i < L::Q; ++i) {
+      const int o = L::opp(i);
+      if (o > i) {
+        const T t = f[i * n + p];
+        f[i * n + p] = f[o * n + p];
+        f[o * n + p] = t;
+      }
+    }
+  }
+}
+
 // body state from a device copy; a 2-D body's window prediction restarts from the new
 // displacement (floor of the smallest marker coordinate, as vs_body_set_state does)
 template <typename T>
@@ -1678,6 +1721,7 @@ struct vs_lattice_plan {
   int lazy_ok;               // all boundaries in one launch group and none needs pre-stream data
   int* d_status;             // device status word of the grid kernels (VS_ERR_TIMEOUT)
   int tma_tb;                // tile width of the TMA grid kernel, 0 when it does not apply
+  int bb_load;               // set per step: the input still lacks the obstacle bounce-back
   int tma_grid;              // persistent CTAs of the TMA grid kernel
   // graph cache
   cudaGraphExec_t graph;
@@ -1825,6 +1869,8 @@ static StepParams<L, T> make_step_params(const vs_lattice_plan* LP, const vs_bod
   P.guo_scale = (T)(1.0 - 0.5 * c.omega);
   P.gw = B ? (const T*)B->d_gw : nullptr;
   P.meta = B ? B->d_meta : nullptr;
+  P.mask = c.obstacle_mask;
+  P.mask_load = c.obstacle_mask && LP->bb_load ? 1 : 0;
   P.n_pre = 0;
   for (int k = 0; k < c.n_bc; ++k) {
     if (c.bc[k].kind == VS_BC_BB || c.bc[k].kind == VS_BC_SPECULAR) {
@@ -2190,8 +2236,10 @@ static int enqueue_cluster_body(vs_body_plan* B, const vs_lattice_plan* LP, cons
 }
 
 static int enqueue_step(const vs_lattice_plan* LP, vs_body_plan* B, const void* fin, void* fout, void* force_hist,
-                        cudaStream_t st, bool lazy_in = false, bool bc_out = true) {
+                        cudaStream_t st, bool lazy_in = false, bool bc_out = true, bool bb_in = false,
+                        bool bb_out = true) {
   int rc;
+  const_cast<vs_lattice_plan*>(LP)->bb_load = bb_in ? 1 : 0;  // read by make_step_params below
   if (B && B->cluster) {
     cudaError_t e = cudaEventRecord(B->ev_fork, st);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(B->side, B->ev_fork, 0);
@@ -2229,7 +2277,18 @@ static int enqueue_step(const vs_lattice_plan* LP, vs_body_plan* B, const void* 
     rc = enqueue_grid(LP, B, fin, fout, st, 0, lazy_in);
   }
   if (rc) return rc;
-  return bc_out ? enqueue_bcs(LP, fout, st) : VS_OK;
+  if (bc_out) {
+    rc = enqueue_bcs(LP, fout, st);
+    if (rc) return rc;
+  }
+  if (!bb_out || !LP->cfg.obstacle_mask) return VS_OK;
+  return dispatch(LP->cfg.q, LP->cfg.dtype, [&](auto l, auto t) -> int {
+    using L = decltype(l);
+    using T = typename decltype(t)::type;
+    k_mask_bb<L, T><<<grid_for(LP->n, 256), 256, 0, st>>>((T*)fout, LP->cfg.obstacle_mask, LP->n);
+    VS_CHECK_LAUNCH("vs_step obstacle bounce-back");
+    return VS_OK;
+  });
 }
 
 // Boundaries can be deferred to the next step's load when they all sit on one axis and
@@ -2408,7 +2467,9 @@ int vs_body_plan_create(const vs_body_cfg* cfg, const vs_lattice_plan* lattice, 
         continue;
       }
       const int lo_n = (int)floor(lo[d]) - cfg->radius + 1, hi_n = (int)floor(hi[d]) + cfg->radius + 1;
-      int margin = 4;
+      // a fixed 3-D body's force window is exactly its stencil box; a 2-D body's predicted
+      // window reaches one node below and three above the stencil box
+      int margin = cfg->dim == 3 && !cfg->moving ? 0 : 4;
       if (cfg->moving && cfg->free_dof[d])
         margin += cfg->window_margin > 0 ? cfg->window_margin : (hi_n - lo_n);
       b->box[2 * d] = lo_n - margin < 0 ? 0 : lo_n - margin;
@@ -2720,8 +2781,9 @@ int vs_run(const vs_lattice_plan* lattice, vs_body_plan* body, void* f_a, void* 
     void* src = (s % 2 == 0) ? f_a : f_b;
     void* dst = (s % 2 == 0) ? f_b : f_a;
     void* hist = force_hist ? (void*)((char*)force_hist + hs * s) : nullptr;
-    int rc = enqueue_step(lattice, body, src, dst, hist, as_stream(stream), lazy && s > 0,
-                          !lazy || s == n_steps - 1);
+    // obstacle bounce-back: deferred to the next step's load, applied at the end of the run
+    int rc = enqueue_step(lattice, body, src, dst, hist, as_stream(stream), lazy && s > 0, !lazy || s == n_steps - 1,
+                          s > 0, s == n_steps - 1);
     if (rc) return rc;
   }
   return VS_OK;
@@ -2981,6 +3043,10 @@ int vs_batch_plan_create(vs_lattice_plan* const* lattices, vs_body_plan* const* 
     if (!Lk) {
       set_error("vs_batch_plan_create: case %d has no lattice plan", k);
       return fail(VS_ERR_INVALID_ARG);
+    }
+    if (Lk->cfg.obstacle_mask) {
+      set_error("vs_batch_plan_create: case %d has an obstacle mask (not supported in a batch)", k);
+      return fail(VS_ERR_UNSUPPORTED);
     }
     if (k == 0) {
       bp->q = Lk->cfg.q;

@@ -45,7 +45,7 @@ class LatticeStep:
     """Plan of the fused collide-force-stream-boundary step on one grid."""
 
     def __init__(self, q, shape, collision="bgk", omega=1.0, dtype=torch.float32, mrt_op=None, forcing="none",
-                 g=None, boundaries=(), variant="auto"):
+                 g=None, boundaries=(), variant="auto", obstacle_mask=None):
         if q not in (9, 19):
             raise ValueError("q must be 9 (D2Q9) or 19 (D3Q19)")
         self.q = q
@@ -87,6 +87,14 @@ class LatticeStep:
             for name in ("rho", "ux", "uy", "uz", "gx", "gy", "gz"):
                 setattr(s, name, float(b[name]))
         cfg.variant = {"auto": V.VS_GRID_AUTO, "plain": V.VS_GRID_PLAIN, "tma": V.VS_GRID_TMA}[variant]
+        self._mask = None
+        if obstacle_mask is not None:  # obstacle_bounce_back after the face boundaries, every step
+            m = obstacle_mask if isinstance(obstacle_mask, torch.Tensor) else torch.as_tensor(obstacle_mask)
+            if tuple(m.shape) != self.shape:
+                raise ValueError(f"obstacle_mask must have shape {self.shape}")
+            V.require_cuda(m)
+            self._mask = m.to(torch.uint8).contiguous()
+            cfg.obstacle_mask = V.ptr(self._mask)
         self.cfg = cfg
         handle = C.c_void_p()
         V.call("vs_lattice_plan_create", C.byref(cfg), C.byref(handle))
