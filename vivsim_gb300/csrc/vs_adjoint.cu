@@ -268,13 +268,14 @@ struct BodyArgs {
   T wobj;           // weight of the x force in the objective, for steps >= obj_start
   const int* seg_start;  // first step of the segment (device), so a graph can replay it
   int j, obj_start;      // this step's index in its segment
+  int chain_k;           // markers share stencil nodes only within +-chain_k in marker order (0: any)
   T k1, k2, c1, c2, dt, damp, stiff, den, area;
   int free_dof[2];
   double* dK;       // d/dstiffness
   double* dX;       // (2 M): d/dX0, d/dY0
 };
 
-constexpr int kAdjBodyThreads = 512;
+constexpr int kAdjBodyThreads = 1024;
 
 // derivative of the delta kernels (ib/kernels.py), d phi / d r
 template <typename T>
@@ -397,13 +398,14 @@ __global__ void __launch_bounds__(kAdjBodyThreads) k_adj_body(BodyArgs<T> A) {
   for (int p = tid; p < P; p += nt) {
     const int m = p / S, s = p - m * S, ix = s / WD, iy = s - ix * WD;
     const int gx = fxy[2 * m] + ix, gy = fxy[2 * m + 1] + iy;
-    for (int w = 0; w < NW; ++w) {
-      unsigned long long b = 0;
-      for (int i = w * 64; i < M && i < w * 64 + 64; ++i) {
-        const unsigned dx = (unsigned)(gx - fxy[2 * i]), dy = (unsigned)(gy - fxy[2 * i + 1]);
-        if (dx < (unsigned)WD && dy < (unsigned)WD) b |= 1ull << (i - w * 64);
-      }
-      cm[(size_t)p * NW + w] = b;
+    for (int w = 0; w < NW; ++w) cm[(size_t)p * NW + w] = 0ull;
+    // candidates: the whole marker set, or the cyclic neighbourhood m-K..m+K
+    const int K = A.chain_k, nc = (K > 0 && 2 * K + 1 < M) ? 2 * K + 1 : M;
+    for (int b = 0; b < nc; ++b) {
+      int i = nc == M ? b : m - K + b;
+      i = i < 0 ? i + M : (i >= M ? i - M : i);
+      const unsigned dx = (unsigned)(gx - fxy[2 * i]), dy = (unsigned)(gy - fxy[2 * i + 1]);
+      if (dx < (unsigned)WD && dy < (unsigned)WD) cm[(size_t)p * NW + (i >> 6)] |= 1ull << (i & 63);
     }
   }
   __syncthreads();
@@ -451,13 +453,20 @@ __global__ void __launch_bounds__(kAdjBodyThreads) k_adj_body(BodyArgs<T> A) {
   }
   // h = -sum Ft + a A (dyn.py:126-136, vortex_induced_vibration.py:136) and the Newmark
   // transpose (dyn.py:5-51); the objective weights h_x
-  if (tid == 0) {
-    T h[2];
+  T hsum[2] = {T(0), T(0)};
+  if (tid < 32) {  // sum of -Ft over the markers, warp 0 in a fixed tree
+#pragma unroll
     for (int c = 0; c < 2; ++c) {
       T acc = T(0);
-      for (int m = 0; m < M; ++m) acc += -Ft[2 * m + c];
-      h[c] = acc + a[c] * A.area;
+      for (int m = tid; m < M; m += 32) acc += -Ft[2 * m + c];
+#pragma unroll
+      for (int o = 16; o >= 1; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+      hsum[c] = acc;
     }
+  }
+  if (tid == 0) {
+    T h[2];
+    for (int c = 0; c < 2; ++c) h[c] = hsum[c] + a[c] * A.area;
     double dK = 0.0;
     for (int c = 0; c < 2; ++c) {
       const T la1 = A.lstate[c], lv1 = A.lstate[3 + c], ld1 = A.lstate[6 + c];
@@ -529,11 +538,16 @@ __global__ void __launch_bounds__(kAdjBodyThreads) k_adj_body(BodyArgs<T> A) {
     __syncthreads();
   }
   // lambda_v: every force step targets the body velocity
-  if (tid < 2) {
-    T acc = T(0);
-    for (int k = 0; k < NI; ++k)
-      for (int m = 0; m < M; ++m) acc += A.ds2 * Fs[2 * M * k + 2 * m + tid];
-    red[2 + tid] += acc;
+  if (tid < 32) {  // warp 0, fixed tree
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      T acc = T(0);
+      for (int k = 0; k < NI; ++k)
+        for (int m = tid; m < M; m += 32) acc += A.ds2 * Fs[2 * M * k + 2 * m + c];
+#pragma unroll
+      for (int o = 16; o >= 1; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+      if (tid == 0) red[2 + c] += acc;
+    }
   }
   // interp^T: lambda_u at the nodes = nodeval(mu_0); weight adjoints of U0 = interp(u)
   // and of g = spread(Ft)
@@ -564,12 +578,19 @@ __global__ void __launch_bounds__(kAdjBodyThreads) k_adj_body(BodyArgs<T> A) {
     atomicAdd(A.dX + M + m, (double)gy_);
   }
   __syncthreads();
-  if (tid < 2) {
-    T acc = T(0);
-    for (int m = 0; m < M; ++m) acc += lFt[2 * m + tid];
-    A.lstate[tid] = red[tid];
-    A.lstate[3 + tid] = red[2 + tid];
-    A.lstate[6 + tid] = red[4 + tid] + acc;
+  if (tid < 32) {
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      T acc = T(0);
+      for (int m = tid; m < M; m += 32) acc += lFt[2 * m + c];
+#pragma unroll
+      for (int o = 16; o >= 1; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+      if (tid == 0) {
+        A.lstate[c] = red[c];
+        A.lstate[3 + c] = red[2 + c];
+        A.lstate[6 + c] = red[4 + c] + acc;
+      }
+    }
   }
 }
 
@@ -614,6 +635,7 @@ struct vs_adjoint_plan {
   double* d_acc = nullptr;         // [0] dU0 (boundary), [1] domega, [2] dK, [3] dU0 (initial state), [4..] dX0, dY0
   int have_ck = 0;
   size_t body_smem = 0;
+  int chain_k = 0;  // see BodyArgs::chain_k
 };
 
 namespace vs {
@@ -719,6 +741,7 @@ static int reverse_steps(vs_adjoint_plan* P, int b, int len, int* cur, cudaStrea
     B.ds2 = (T)P->ds * T(2);
     B.wobj = (T)(1.0 / (double)(c.n_steps - c.obj_start));
     B.seg_start = P->d_seg_start + b;
+    B.chain_k = P->chain_k;
     B.j = j;
     B.obj_start = c.obj_start;
     B.k1 = (T)k1; B.k2 = (T)k2; B.c1 = (T)c1; B.c2 = (T)c2; B.dt = T(1);
@@ -891,6 +914,19 @@ int vs_adjoint_plan_create(const vs_adjoint_cfg* cfg, vs_adjoint_plan** out) {
     rmax = r > rmax ? r : rmax;
     X[m] = cfg->cx + r * cos(P->theta[m]);
     Y[m] = cfg->cy + r * sin(P->theta[m]);
+  }
+  {
+    // cyclic index distance bound between markers that can share a stencil node under a
+    // translation (|dx| < 2R and |dy| < 2R); 0 when it does not pay
+    const double lim = 2.0 * cfg->radius + 1e-3;
+    int K = 0;
+    for (int i = 0; i < M; ++i)
+      for (int j = i + 1; j < M; ++j)
+        if (fabs(X[i] - X[j]) < lim && fabs(Y[i] - Y[j]) < lim) {
+          const int dd = j - i, cyc = dd < M - dd ? dd : M - dd;
+          K = cyc > K ? cyc : K;
+        }
+    P->chain_k = 2 * K + 1 < M ? K : 0;
   }
   if (cfg->cx - rmax - cfg->radius - 2 < 4 || cfg->cx + rmax + cfg->radius + 2 > cfg->nx - 5) {
     set_error("vs_adjoint_plan_create: the body's stencils must stay clear of the x = 0 / nx-1 boundaries");

@@ -263,19 +263,8 @@ __global__ void __launch_bounds__(256) k_step(const __grid_constant__ StepParams
 template <class L, typename T, int COLL, bool WALLS>
 __global__ void __launch_bounds__(256) k_step_batch(const StepParams<L, T>* __restrict__ Ps,
                                                     const int2* __restrict__ blk) {
-  // the case's parameters, staged in shared memory once per block (every thread reads them)
-  __shared__ __align__(16) unsigned char sp[sizeof(StepParams<L, T>)];
   const int2 cb = blk[blockIdx.x];
-  {
-    // array elements are 8-byte aligned (the struct holds pointers); copy in 8-byte words
-    static_assert(alignof(StepParams<L, T>) >= 8 && sizeof(StepParams<L, T>) % 8 == 0, "copy granularity");
-    const unsigned long long* src = (const unsigned long long*)(Ps + cb.x);
-    unsigned long long* dst = (unsigned long long*)sp;
-    constexpr int N8 = (int)(sizeof(StepParams<L, T>) / 8);
-    for (int i = threadIdx.x; i < N8; i += blockDim.x) dst[i] = src[i];
-  }
-  __syncthreads();
-  const StepParams<L, T>& P = *(const StepParams<L, T>*)sp;
+  const StepParams<L, T>& P = Ps[cb.x];  // read through L1 (staging it in shared memory cost registers)
   const int by = cb.y / P.gx;
   step_block<L, T, COLL, WALLS>(P, cb.y - by * P.gx, by);
 }
