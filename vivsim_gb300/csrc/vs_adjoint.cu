@@ -109,6 +109,7 @@ struct GridArgs {
   int nx, ny;
   T omega, U0, rho_out;
   double* acc;  // [0] d/dU0 (boundaries), [1] d/domega
+  double* acc_w;  // per-block partial sums of d/domega (one slot per grid-adjoint block)
 };
 
 __device__ __forceinline__ int wrap(int a, int n) { return a < 0 ? a + n : (a >= n ? a - n : a); }
@@ -130,60 +131,66 @@ __device__ __forceinline__ void block_accumulate(double v, double* acc) {
   }
 }
 
-// Boundary adjoint, one thread per face row y.  Forward order: f_a = eq_left(f3),
-// f' = nee_p_right(f_a); reverse: right wall and neighbour columns, then the left wall.
+// Boundary adjoint.  Forward order: f_a = eq_left(f3), f' = nee_p_right(f_a); reverse: the
+// right wall and neighbour columns, then the left wall.  A block handles kRows face rows:
+// phase 1 rebuilds the streamed wall and neighbour populations (one thread per row and
+// population), phase 2 evaluates the 18 Jacobian columns of the outflow boundary by
+// forward-mode dual numbers (one thread per row and input), phase 3 writes the adjoints.
+constexpr int kRows = 8;
+
 template <typename T>
-__global__ void __launch_bounds__(128) k_adj_bc(GridArgs<T> A) {
-  const int y = blockIdx.x * blockDim.x + threadIdx.x;
-  double dU0 = 0.0;
-  if (y < A.ny) {
-    const int nx = A.nx, ny = A.ny;
-    const int64_t n = (int64_t)nx * ny;
-    // streamed populations (before the boundaries) at the wall and its neighbour
-    T w[9], nb[9];
-#pragma unroll
-    for (int i = 0; i < 9; ++i) {
-      T src[9];
-      post_collide(A.f, n, ny, wrap(nx - 1 - q9_cx(i), nx), wrap(y - q9_cy(i), ny), A.omega, src);
-      w[i] = src[i];
-      post_collide(A.f, n, ny, nx - 2 - q9_cx(i), wrap(y - q9_cy(i), ny), A.omega, src);
-      nb[i] = src[i];
-    }
-    const int64_t pw = (int64_t)(nx - 1) * ny + y, pn = (int64_t)(nx - 2) * ny + y;
-    T lout[9];
-#pragma unroll
-    for (int i = 0; i < 9; ++i) lout[i] = A.lam[i * n + pw];
-    T lw[9], ln[9];
-    for (int k = 0; k < 18; ++k) {
-      Dual<T> dw[9], dn[9], o[9];
-#pragma unroll
-      for (int i = 0; i < 9; ++i) {
-        dw[i] = Dual<T>(w[i], (T)(k == i));
-        dn[i] = Dual<T>(nb[i], (T)(k == 9 + i));
-      }
-      pnee_right<Dual<T>, T>(dw, dn, A.rho_out, o);
-      T s = T(0);
-#pragma unroll
-      for (int i = 0; i < 9; ++i) s += lout[i] * o[i].d;
-      if (k < 9) lw[k] = s;
-      else ln[k - 9] = s;
-    }
-#pragma unroll
-    for (int i = 0; i < 9; ++i) {
-      A.lam[i * n + pw] = lw[i];  // the wall values were replaced: only the new path remains
-      A.lam[i * n + pn] = A.lam[i * n + pn] + ln[i];
-    }
-    // left wall: f = feq(1, (U0, 0)) replaced every population (lbm/boundary/eq.py:25-56)
-    const int64_t p0 = y;
-#pragma unroll
-    for (int i = 0; i < 9; ++i) {
-      const T cx = (T)q9_cx(i);
-      const T dfeq = q9_w<T>(i) * ((T(3) * cx + T(9) * (cx * A.U0) * cx) - T(3) * A.U0);
-      dU0 += (double)(A.lam[i * n + p0] * dfeq);
-      A.lam[i * n + p0] = T(0);
-    }
+__global__ void __launch_bounds__(kRows * 18) k_adj_bc(GridArgs<T> A) {
+  __shared__ T w[kRows][9], nb[kRows][9], lo[kRows][9], col[kRows][18];
+  const int nx = A.nx, ny = A.ny;
+  const int64_t n = (int64_t)nx * ny;
+  const int r = threadIdx.x / 18, k = threadIdx.x % 18;
+  const int y = blockIdx.x * kRows + r;
+  const bool live = y < ny;
+  if (live && k < 9) {
+    // streamed population k at the wall (x = nx-1) and at its neighbour (x = nx-2)
+    T src[9];
+    post_collide(A.f, n, ny, wrap(nx - 1 - q9_cx(k), nx), wrap(y - q9_cy(k), ny), A.omega, src);
+    w[r][k] = src[k];
+    post_collide(A.f, n, ny, nx - 2 - q9_cx(k), wrap(y - q9_cy(k), ny), A.omega, src);
+    nb[r][k] = src[k];
+    lo[r][k] = A.lam[k * n + (int64_t)(nx - 1) * ny + y];
   }
-  block_accumulate<128>(dU0, A.acc + 0);
+  __syncthreads();
+  if (live) {
+    Dual<T> dw[9], dn[9], o[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+      dw[i] = Dual<T>(w[r][i], (T)(k == i));
+      dn[i] = Dual<T>(nb[r][i], (T)(k == 9 + i));
+    }
+    pnee_right<Dual<T>, T>(dw, dn, A.rho_out, o);
+    T sum = T(0);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) sum += lo[r][i] * o[i].d;
+    col[r][k] = sum;
+  }
+  __syncthreads();
+  double dU0 = 0.0;
+  if (live && k < 9) {
+    const int64_t pw = (int64_t)(nx - 1) * ny + y, pn = (int64_t)(nx - 2) * ny + y;
+    A.lam[k * n + pw] = col[r][k];  // the wall values were replaced: only the new path remains
+    A.lam[k * n + pn] = A.lam[k * n + pn] + col[r][9 + k];
+    // left wall: f = feq(1, (U0, 0)) replaced every population (lbm/boundary/eq.py:25-56)
+    const T cx = (T)q9_cx(k);
+    const T dfeq = q9_w<T>(k) * ((T(3) * cx + T(9) * (cx * A.U0) * cx) - T(3) * A.U0);
+    const int64_t p0 = k * n + y;
+    dU0 = (double)(A.lam[p0] * dfeq);
+    A.lam[p0] = T(0);
+  }
+  // block sum of the inflow term (rows x populations) in a fixed order
+  __shared__ double red[kRows * 18];
+  red[threadIdx.x] = dU0;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double sum = 0.0;
+    for (int i = 0; i < kRows * 18; ++i) sum += red[i];
+    if (sum != 0.0) atomicAdd(A.acc + 0, sum);
+  }
 }
 
 // Grid adjoint, one thread per node: pull the streamed adjoint, then the transposed
@@ -236,7 +243,19 @@ __global__ void __launch_bounds__(256) k_adj_grid(GridArgs<T> A) {
       A.lam_out[j * n + p] = (T(1) - A.omega) * l2[j] + lrho + (lu0 * (cx - u[0]) + lu1 * (cy - u[1])) / r;
     }
   }
-  block_accumulate<256>(dw, A.acc + 1);
+  {
+    // per-block partial of d/domega in its own slot (no contention; summed at the end)
+    __shared__ double red[8];
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) dw += __shfl_down_sync(0xffffffffu, dw, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = dw;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double sum = 0;
+      for (int k = 0; k < (int)(blockDim.x >> 5); ++k) sum += red[k];
+      A.acc_w[blockIdx.y * gridDim.x + blockIdx.x] += sum;
+    }
+  }
 }
 
 // d/dU0 of the initial state f = feq(1, (U0, 0)) everywhere
@@ -633,6 +652,8 @@ struct vs_adjoint_plan {
   void* d_X0 = nullptr;            // 2 M
   void* d_hist = nullptr;          // n_steps x 3
   double* d_acc = nullptr;         // [0] dU0 (boundary), [1] domega, [2] dK, [3] dU0 (initial state), [4..] dX0, dY0
+  double* d_acc_w = nullptr;       // per-block partial sums of d/domega (grid adjoint)
+  int n_accw = 0;
   int have_ck = 0;
   size_t body_smem = 0;
   int chain_k = 0;  // see BodyArgs::chain_k
@@ -644,6 +665,7 @@ namespace adj {
 static void free_plan(vs_adjoint_plan* p) {
   if (p->body) vs_body_plan_destroy(p->body);
   if (p->lat) vs_lattice_plan_destroy(p->lat);
+  if (p->d_acc_w) cudaFree(p->d_acc_w);
   void* bufs[] = {p->d_f0,  p->d_fa,       p->d_fb,     p->d_ck,        p->d_ck_state, p->d_seg[0],
                   p->d_seg[1], p->d_seg_state[0], p->d_seg_state[1], p->d_lam[0], p->d_lam[1], p->d_g,
                   p->d_lu,  p->d_lstate,  p->d_X0,     p->d_hist,      p->d_acc,      p->d_seg_start};
@@ -719,12 +741,13 @@ static int reverse_steps(vs_adjoint_plan* P, int b, int len, int* cur, cudaStrea
     G.U0 = (T)c.U0;
     G.rho_out = (T)c.rho_out;
     G.acc = P->d_acc;
+    G.acc_w = P->d_acc_w;
     // the boundary adjoint touches the x = 0, nx-2, nx-1 columns only, the body adjoint
     // reads the stencils (kept clear of them): run them side by side
     cudaError_t e = cudaEventRecord(P->ev_f, st);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(P->aux, P->ev_f, 0);
     if (e != cudaSuccess) return cuda_status(e, "vs_adjoint_backward fork");
-    k_adj_bc<T><<<grid_for(c.ny, 128), 128, 0, P->aux>>>(G);
+    k_adj_bc<T><<<(c.ny + kRows - 1) / kRows, kRows * 18, 0, P->aux>>>(G);
     BodyArgs<T> B{};
     B.f = fj;
     B.lam = (const T*)P->d_lam[*cur];
@@ -802,6 +825,7 @@ static int backward_t(vs_adjoint_plan* P, cudaStream_t st) {
     P->g_stream = st;
   }
   cudaError_t e = cudaMemsetAsync(P->d_acc, 0, sizeof(double) * (4 + 2 * P->M), st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(P->d_acc_w, 0, sizeof(double) * P->n_accw, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(P->d_lam[0], 0, fb, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(P->d_lstate, 0, sizeof(T) * 12, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(P->d_g, 0, sizeof(T) * 2 * n, st);
@@ -1004,6 +1028,8 @@ int vs_adjoint_plan_create(const vs_adjoint_cfg* cfg, vs_adjoint_plan** out) {
   alloc(&P->d_X0, ts * 2 * M);
   alloc(&P->d_hist, ts * 3 * cfg->n_steps);
   alloc((void**)&P->d_acc, sizeof(double) * (4 + 2 * M));
+  P->n_accw = (int)grid_for(cfg->ny, 256) * cfg->nx;
+  alloc((void**)&P->d_acc_w, sizeof(double) * P->n_accw);
   if (e != cudaSuccess) return fail(cuda_status(e, "vs_adjoint_plan_create"));
   rc = dispatch_t(cfg->dtype, [&](auto t) -> int {
     using T = typename decltype(t)::type;
@@ -1097,10 +1123,13 @@ int vs_adjoint_backward(vs_adjoint_plan* P, double seed, double* grad_U0, double
   });
   if (rc) return rc;
   const int M = P->M;
-  std::vector<double> acc(4 + 2 * M);
+  std::vector<double> acc(4 + 2 * M), accw(P->n_accw);
   cudaError_t e = cudaMemcpyAsync(acc.data(), P->d_acc, sizeof(double) * acc.size(), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(accw.data(), P->d_acc_w, sizeof(double) * accw.size(), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return cuda_status(e, "vs_adjoint_backward result");
+  for (double v : accw) acc[1] += v;  // d/domega, block partials in a fixed order
   const vs_adjoint_cfg& c = P->cfg;
   const double domega = -3.0 * (c.D / c.Re) * P->omega * P->omega;
   if (grad_U0) *grad_U0 = seed * (acc[0] + acc[3] + acc[1] * domega);

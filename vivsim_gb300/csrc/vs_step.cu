@@ -1540,11 +1540,14 @@ static int chain_width(const double* x, const double* y, int M, int R) {
 // u at the touched nodes (vivsim/lbm3d/basic.py:90-106)
 template <class L, typename T>
 __global__ void k_static_node_u(const T* __restrict__ fin, int nx, int ny, int nz, const int* __restrict__ meta,
-                                const int32_t* __restrict__ node_cell, int U, T* __restrict__ nu) {
+                                const int32_t* __restrict__ node_cell, int U, T* __restrict__ nu,
+                                const int* __restrict__ Ud) {
+  // U: the node-array stride; Ud (moving bodies): the number of touched nodes this step
   const int ey = meta[META_WY], ez = meta[META_WZ];
   const int ox = meta[META_OX], oy = meta[META_OY], oz = meta[META_OZ];
   const int64_t n = (int64_t)nx * ny * nz;
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < U; k += gridDim.x * blockDim.x) {
+  const int nU = Ud ? *Ud : U;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nU; k += gridDim.x * blockDim.x) {
     const int cell = node_cell[k];
     const int wx = cell / (ey * ez), wy = (cell / ez) % ey, wz = cell % ez;
     const int64_t pn = ((int64_t)(ox + wx) * ny + (oy + wy)) * nz + (oz + wz);
@@ -1606,8 +1609,9 @@ template <typename T>
 __global__ void k_static_spread(const int32_t* __restrict__ seg, const int32_t* __restrict__ sids,
                                 const int32_t* __restrict__ node_cell, const T* __restrict__ W,
                                 const T* __restrict__ F, int U, int S, T scale, T* __restrict__ out, T* gw, int cells,
-                                int M, T* state, T* force_hist) {
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < U; k += gridDim.x * blockDim.x) {
+                                int M, T* state, T* force_hist, const int* __restrict__ Ud) {
+  const int nU = Ud ? *Ud : U;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nU; k += gridDim.x * blockDim.x) {
     const int lo = seg[k], hi = seg[k + 1];
     T a[3] = {T(0), T(0), T(0)};
     for (int i = lo; i < hi; ++i) {
@@ -1647,6 +1651,69 @@ __global__ void k_static_spread(const int32_t* __restrict__ seg, const int32_t* 
     state[9 + tid] = red[tid][0];
     if (force_hist) force_hist[tid] = red[tid][0];
   }
+}
+
+// moving 3-D body (examples/3d/oscillating_cylinder.py:228-283): markers X0 + d, window
+// origin floor(min X) - R + 1 (rounded as the markers are), weights and window-cell keys of
+// every (marker, stencil point) pair, from coordinates relative to the window
+// (ib3d/stencil.py:7-59).  The window must stay inside the body's box (else VS_ERR_RANGE).
+template <typename T>
+__global__ void k_mov3_stencil(const T* __restrict__ X0, const T* __restrict__ state, double lo0, double lo1,
+                               double lo2, int R, int kernel, int c0, int c1, int c2, int bx0, int bx1, int by0,
+                               int by1, int bz0, int bz1, int* meta, T* __restrict__ W, int32_t* __restrict__ keys,
+                               int M) {
+  const T d0 = state[6], d1 = state[7], d2 = state[8];
+  const int o0 = ifloor((T)lo0 + d0) - R + 1, o1 = ifloor((T)lo1 + d1) - R + 1, o2 = ifloor((T)lo2 + d2) - R + 1;
+  const bool inside = o0 >= bx0 && o0 + c0 <= bx1 && o1 >= by0 && o1 + c1 <= by1 && o2 >= bz0 && o2 + c2 <= bz1;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    meta[META_OX] = o0; meta[META_OY] = o1; meta[META_OZ] = o2;
+    meta[META_WX] = inside ? c0 : 0; meta[META_WY] = c1; meta[META_WZ] = c2;
+    if (!inside) meta[META_STATUS] = VS_ERR_RANGE;
+  }
+  const int w = 2 * R, s = w * w * w;
+  const int64_t total = (int64_t)M * s;
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < total; p += (int64_t)gridDim.x * blockDim.x) {
+    const int mk = (int)(p / s), k = (int)(p % s);
+    const int ox = k / (w * w) - R + 1, oy = (k / w) % w - R + 1, oz = k % w - R + 1;
+    const T x = (X0[3 * mk] + d0) - (T)o0, y = (X0[3 * mk + 1] + d1) - (T)o1, z = (X0[3 * mk + 2] + d2) - (T)o2;
+    const int sx = ifloor(x) + ox, sy = ifloor(y) + oy, sz = ifloor(z) + oz;
+    W[p] = (delta(kernel, (T)sx - x) * delta(kernel, (T)sy - y)) * delta(kernel, (T)sz - z);
+    const bool ok = inside && sx >= 0 && sx < c0 && sy >= 0 && sy < c1 && sz >= 0 && sz < c2;
+    keys[p] = ok ? (sx * c1 + sy) * c2 + sz : -1;  // out-of-window pairs are dropped (and flagged)
+    if (!ok && inside) meta[META_STATUS] = VS_ERR_RANGE;
+  }
+}
+
+// touched-node count of this step's CSR (uid is 0-based), and the end of the last segment
+__global__ void k_csr_count(const int32_t* __restrict__ uid, int64_t P, int* U, int32_t* seg) {
+  const int u = uid[P - 1] + 1;
+  *U = u;
+  seg[u] = (int32_t)P;
+}
+
+// added mass h += a A (vortex_induced_vibration.py:136) and the Newmark update (dyn.py:5-51)
+// of the free DOFs; h (without the added mass) comes from the spread kernel's reduction
+template <typename T>
+__global__ void k_body_newmark(T* state, int f0, int f1, int f2, T k1, T k2, T c1, T c2, T dt, T damp, T stiff,
+                               T den, T area, T* force_hist) {
+  const int c = threadIdx.x;
+  if (c >= 3) return;
+  const int fr = c == 0 ? f0 : (c == 1 ? f1 : f2);
+  const T ac = state[c], vc = state[3 + c], dc = state[6 + c];
+  const T hh = add_rn(state[9 + c], mul_rn(ac, area));
+  T an = ac, vn = vc, dn = dc;
+  if (fr) {
+    const T v1 = add_rn(vc, mul_rn(k1, ac));
+    const T v2 = add_rn(add_rn(dc, mul_rn(dt, vc)), mul_rn(k2, ac));
+    an = sub_rn(sub_rn(hh, mul_rn(damp, v1)), mul_rn(stiff, v2)) / den;
+    vn = add_rn(mul_rn(c1, an), v1);
+    dn = add_rn(mul_rn(c2, an), v2);
+  }
+  state[c] = an;
+  state[3 + c] = vn;
+  state[6 + c] = dn;
+  state[9 + c] = hh;
+  if (force_hist) force_hist[c] = hh;
 }
 
 __global__ void k_compact_csr(const int32_t* __restrict__ skeys, const int32_t* __restrict__ head,
@@ -1757,6 +1824,8 @@ struct vs_body_plan {
   double nm[9];  // k1, k2, c1, c2, dt, damping, stiffness, den, area
   int box[6];    // region the body's window never leaves (half-open x0,x1,y0,y1,z0,z1)
   double lo_t[2];  // 2-D: smallest marker x and y, rounded to the plan precision
+  double lo_t3;    // 3-D: smallest marker z, rounded
+  int* d_U;        // moving 3-D body: touched nodes of the current step (device)
   cudaStream_t side;
   cudaEvent_t ev_fork, ev_join;
   cudaStream_t side2;    // cluster form: the lazy face planes, beside the grid launch
@@ -1777,7 +1846,7 @@ static void free_lattice(vs_lattice_plan* p) {
 static void free_body(vs_body_plan* b) {
   if (!b) return;
   void* ptrs[] = {b->d_X0, b->d_ds, b->d_state, b->d_gw, b->d_meta, b->d_W, b->d_I, b->d_ws, b->d_node_cell,
-                  b->d_seg, b->d_nu, b->d_nv, b->d_mk};
+                  b->d_seg, b->d_nu, b->d_nv, b->d_mk, b->d_U};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   if (b->ev_fork) cudaEventDestroy(b->ev_fork);
@@ -1971,25 +2040,47 @@ static int enqueue_body(vs_body_plan* B, const vs_lattice_plan* LP, const void* 
     using T = typename decltype(t)::type;
     const int U = B->U, M = B->M, S = B->S;
     const int cells = B->cap[0] * B->cap[1] * B->cap[2];
+    if (B->cfg.moving) {
+      // markers follow the body; the window follows its stencil box; the (node, pair) CSR
+      // is rebuilt for this step
+      const int64_t P = (int64_t)M * S;
+      cudaError_t e = cudaMemsetAsync(B->d_gw, 0, sizeof(T) * 3 * cells, st);
+      if (e != cudaSuccess) return cuda_status(e, "vs_step body window");
+      k_mov3_stencil<T><<<grid_for(P, 256), 256, 0, st>>>(
+          (const T*)B->d_X0, (const T*)B->d_state, B->lo_t[0], B->lo_t[1], B->lo_t3, B->cfg.radius, B->cfg.kernel,
+          B->cap[0], B->cap[1], B->cap[2], B->box[0], B->box[1], B->box[2], B->box[3], B->box[4], B->box[5],
+          B->d_meta, (T*)B->d_W, B->d_I, M);
+      IbCsrView v{};
+      int rc = ib_build_csr(B->d_I, P, cells, B->d_ws, M, S, &v, st);
+      if (rc) return rc;
+      k_csr_count<<<1, 1, 0, st>>>(v.uid, P, B->d_U, B->d_seg);
+      k_compact_csr<<<grid_for(P, 256), 256, 0, st>>>(v.skeys, v.head, v.uid, P, B->d_node_cell, B->d_seg);
+    }
     T* Ua = (T*)B->d_mk;
     T* Fs = Ua + 3 * M;
     T* Ft = Fs + 3 * M;
     const T ds2 = (T)B->cfg.ds_scalar;
-    const unsigned gn = grid_for(U, 128), gm = grid_for((int64_t)M * 32, 128);
+    const unsigned gn = grid_for(B->cfg.moving ? (int64_t)M * S : U, 128), gm = grid_for((int64_t)M * 32, 128);
     k_static_node_u<L, T><<<gn, 128, 0, st>>>((const T*)fin, LP->cfg.nx, LP->cfg.ny, LP->cfg.nz, B->d_meta,
-                                               B->d_node_cell, U, (T*)B->d_nu);
+                                               B->d_node_cell, U, (T*)B->d_nu, B->d_U);
     k_static_marker<T><<<gm, 128, 0, st>>>(1, B->cfg.n_iter > 0, (const T*)B->d_W, B->pair_uid, M, S,
                                            (const T*)B->d_nu, U, (const T*)B->d_state, (const T*)B->d_ds, ds2, Ua, Fs,
                                            Ft);
     for (int it = 0; it + 1 < B->cfg.n_iter; ++it) {
       k_static_spread<T><<<gn, 128, 0, st>>>(B->d_seg, B->sids, B->d_node_cell, (const T*)B->d_W, Fs, U, S, T(0.5),
-                                             (T*)B->d_nv, nullptr, cells, M, nullptr, nullptr);
+                                             (T*)B->d_nv, nullptr, cells, M, nullptr, nullptr, B->d_U);
       k_static_marker<T><<<gm, 128, 0, st>>>(0, 1, (const T*)B->d_W, B->pair_uid, M, S, (const T*)B->d_nv, U,
                                              (const T*)B->d_state, (const T*)B->d_ds, ds2, Ua, Fs, Ft);
     }
     k_static_spread<T><<<gn, 256, 0, st>>>(B->d_seg, B->sids, B->d_node_cell, (const T*)B->d_W, Ft, U, S, T(1),
-                                           nullptr, (T*)B->d_gw, cells, M, (T*)B->d_state, (T*)force_hist);
-    VS_CHECK_LAUNCH("vs_step fixed-body kernels");
+                                           nullptr, (T*)B->d_gw, cells, M, (T*)B->d_state,
+                                           B->cfg.moving ? nullptr : (T*)force_hist, B->d_U);
+    if (B->cfg.moving) {  // added mass and Newmark on the free DOFs
+      k_body_newmark<T><<<1, 32, 0, st>>>((T*)B->d_state, B->cfg.free_dof[0], B->cfg.free_dof[1], B->cfg.free_dof[2],
+                                          (T)B->nm[0], (T)B->nm[1], (T)B->nm[2], (T)B->nm[3], (T)B->nm[4],
+                                          (T)B->nm[5], (T)B->nm[6], (T)B->nm[7], (T)B->nm[8], (T*)force_hist);
+    }
+    VS_CHECK_LAUNCH("vs_step 3-D body kernels");
     return VS_OK;
   });
 }
@@ -2406,7 +2497,6 @@ int vs_body_plan_create(const vs_body_cfg* cfg, const vs_lattice_plan* lattice, 
   VS_REQUIRE(lattice->cfg.forcing == VS_FORCE_EDM || lattice->cfg.forcing == VS_FORCE_GUO_BGK ||
                  lattice->cfg.forcing == VS_FORCE_GUO_MRT,
              "an immersed body needs a forcing scheme on the lattice (EDM or Guo)");
-  VS_REQUIRE(cfg->dim == 2 || !cfg->moving, "moving 3-D bodies are not supported by this build");
   vs_body_plan* b = new (std::nothrow) vs_body_plan();
   if (!b) {
     set_error("out of host memory");
@@ -2444,6 +2534,7 @@ int vs_body_plan_create(const vs_body_cfg* cfg, const vs_lattice_plan* lattice, 
     }
   for (int d = 0; d < cfg->dim; ++d) b->cap[d] = (int)(floor(hi[d]) - floor(lo[d])) + w + 2;
   for (int d = 0; d < 2; ++d) b->lo_t[d] = ts == 8 ? lo[d] : (double)(float)lo[d];
+  b->lo_t3 = cfg->dim == 3 ? (ts == 8 ? lo[2] : (double)(float)lo[2]) : 0.0;
   if (cfg->dim == 2) b->cap[2] = 1;
   {
     // region the window can reach: the initial stencil box, widened along free DOFs by the
@@ -2606,6 +2697,53 @@ int vs_body_plan_create(const vs_body_cfg* cfg, const vs_lattice_plan* lattice, 
         }
       }
     }
+  } else if (cfg->moving) {
+    // moving 3-D body: the window follows the stencil box (one node of slack per axis for
+    // the floor of a moving coordinate); CSR rebuilt every step inside the workspace
+    const int nn[3] = {lattice->cfg.nx, lattice->cfg.ny, lattice->cfg.nz};
+    for (int d = 0; d < 3; ++d) {
+      b->cap[d] = (int)(floor(hi[d]) - floor(lo[d])) + w + 1;
+      if (b->box[2 * d + 1] - b->box[2 * d] < b->cap[d] || b->box[2 * d] < 0 || b->box[2 * d + 1] > nn[d]) {
+        free_body(b);
+        set_error("moving body window does not fit the grid along axis %d", d);
+        return VS_ERR_RANGE;
+      }
+    }
+    const int64_t wcells = (int64_t)b->cap[0] * b->cap[1] * b->cap[2];
+    const int64_t P = (int64_t)M * b->S;
+    VS_REQUIRE(P < (1ll << 31) && wcells < (1ll << 31), "moving body too large");
+    b->U = (int)P;  // node arrays are sized for every pair touching a distinct node
+    e = cudaFree(b->d_gw);
+    b->d_gw = nullptr;
+    if (e != cudaSuccess) return fail(e);
+    if ((e = cudaMalloc(&b->d_gw, ts * 3 * wcells)) != cudaSuccess) return fail(e);
+    if ((e = cudaMemset(b->d_gw, 0, ts * 3 * wcells)) != cudaSuccess) return fail(e);
+    if ((e = cudaMalloc(&b->d_W, ts * P)) != cudaSuccess) return fail(e);
+    if ((e = cudaMalloc(&b->d_I, sizeof(int32_t) * P)) != cudaSuccess) return fail(e);
+    b->ws_bytes = vs_ib_workspace_bytes(M, b->S);
+    if ((e = cudaMalloc(&b->d_ws, b->ws_bytes)) != cudaSuccess) return fail(e);
+    {
+      // the CSR views are fixed offsets into the workspace: fill them once from a dry build
+      // of an all-dropped key set (every key -1)
+      if ((e = cudaMemset(b->d_I, 0xff, sizeof(int32_t) * P)) != cudaSuccess) return fail(e);
+      IbCsrView v{};
+      int rc = ib_build_csr(b->d_I, P, wcells, b->d_ws, M, b->S, &v, nullptr);
+      if (rc) {
+        free_body(b);
+        return rc;
+      }
+      unsigned st0 = 0;
+      vs_ib_status(&st0, 1);  // the dry build's dropped keys are not an error
+      b->sids = v.sids;
+      b->pair_uid = v.pair_uid;
+    }
+    if ((e = cudaMalloc(&b->d_node_cell, sizeof(int32_t) * P)) != cudaSuccess) return fail(e);
+    if ((e = cudaMalloc(&b->d_seg, sizeof(int32_t) * (P + 1))) != cudaSuccess) return fail(e);
+    if ((e = cudaMalloc((void**)&b->d_U, sizeof(int))) != cudaSuccess) return fail(e);
+    if ((e = cudaMalloc(&b->d_nu, ts * 3 * P)) != cudaSuccess) return fail(e);
+    if ((e = cudaMalloc(&b->d_nv, ts * 3 * P)) != cudaSuccess) return fail(e);
+    if ((e = cudaMalloc(&b->d_mk, ts * 9 * M)) != cudaSuccess) return fail(e);
+    if ((e = cudaDeviceSynchronize()) != cudaSuccess) return fail(e);
   } else {
     // fixed 3-D body: stencil once over a fixed window around the markers
     const int nn[3] = {lattice->cfg.nx, lattice->cfg.ny, lattice->cfg.nz};
