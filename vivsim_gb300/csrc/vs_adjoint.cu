@@ -110,6 +110,11 @@ struct GridArgs {
   T omega, U0, rho_out;
   double* acc;  // [0] d/dU0 (boundaries), [1] d/domega
   double* acc_w;  // per-block partial sums of d/domega (one slot per grid-adjoint block)
+  int slot0;      // first slot of this launch
+  int mode;       // 0: every node; 1: outside the body's window; 2: the window only
+  const T* wstate;  // body state of the step (displacement -> window origin)
+  double lo0, lo1;  // smallest marker x, y (plan precision)
+  int R, cap[2];    // stencil half-width; window extent
 };
 
 __device__ __forceinline__ int wrap(int a, int n) { return a < 0 ? a + n : (a >= n ? a - n : a); }
@@ -199,9 +204,29 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_adj_grid(GridArgs<T> A) {
   const int nx = A.nx, ny = A.ny;
   const int64_t n = (int64_t)nx * ny;
-  const int x = blockIdx.y, y = blockIdx.x * blockDim.x + threadIdx.x;
-  double dw = 0.0;
-  if (y < ny) {
+  // the body's stencil window of this step (from its displacement), which the body adjoint
+  // feeds: mode 1 does every node outside it, mode 2 the window only, mode 0 everything
+  int wx0 = 0, wy0 = 0;
+  if (A.mode) {
+    wx0 = ifloor((T)A.lo0 + A.wstate[6]) - A.R + 1;
+    wy0 = ifloor((T)A.lo1 + A.wstate[7]) - A.R + 1;
+  }
+  int x, y;
+  bool live;
+  if (A.mode == 2) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    live = k < A.cap[0] * A.cap[1];
+    x = wx0 + (live ? k / A.cap[1] : 0);
+    y = wy0 + (live ? k % A.cap[1] : 0);
+    live = live && x >= 0 && x < nx && y >= 0 && y < ny;
+  } else {
+    x = blockIdx.y;
+    y = blockIdx.x * blockDim.x + threadIdx.x;
+    live = y < ny;
+    if (A.mode == 1 && x >= wx0 && x < wx0 + A.cap[0] && y >= wy0 && y < wy0 + A.cap[1]) live = false;
+  }
+  T dw = T(0);
+  if (live) {
     const int64_t p = (int64_t)x * ny + y;
     T f[9], l2[9];
 #pragma unroll
@@ -212,48 +237,57 @@ __global__ void __launch_bounds__(256) k_adj_grid(GridArgs<T> A) {
     T r, u[2], fe[9];
     macro(L9{}, f, r, u);
     feq9<T, T>(r, u[0], u[1], fe);
-    const T g0 = A.g[p], g1 = A.g[n + p];
-    // lambda_u from the forcing term: d/du_a of w_i (3 (c_i - u).g + 9 (c_i.u)(c_i.g))
-    T lu0 = A.lu[p], lu1 = A.lu[n + p];
-    // leave the body fields zero for the next (earlier) step, which writes only its stencils
-    if (g0 != T(0) || g1 != T(0) || lu0 != T(0) || lu1 != T(0)) {
-      A.g[p] = T(0);
-      A.g[n + p] = T(0);
-      A.lu[p] = T(0);
-      A.lu[n + p] = T(0);
+    const T ir = T(1) / r;
+    T g0 = T(0), g1 = T(0), lu0 = T(0), lu1 = T(0);
+    if (A.mode != 1) {  // only the window carries body force and the interpolation adjoint
+      g0 = A.g[p];
+      g1 = A.g[n + p];
+      lu0 = A.lu[p];
+      lu1 = A.lu[n + p];
+      // leave the body fields zero for the next (earlier) step, which writes only its stencils
+      if (g0 != T(0) || g1 != T(0) || lu0 != T(0) || lu1 != T(0)) {
+        A.g[p] = T(0);
+        A.g[n + p] = T(0);
+        A.lu[p] = T(0);
+        A.lu[n + p] = T(0);
+      }
     }
     T lrho = T(0);
 #pragma unroll
     for (int i = 0; i < 9; ++i) {
       const T cx = (T)q9_cx(i), cy = (T)q9_cy(i), wi = q9_w<T>(i);
       const T cu = cx * u[0] + cy * u[1], cg = cx * g0 + cy * g1;
+      // forcing term: d/du_a of w_i (3 (c_i - u).g + 9 (c_i.u)(c_i.g))
       lu0 += l2[i] * wi * (T(-3) * g0 + T(9) * cg * cx);
       lu1 += l2[i] * wi * (T(-3) * g1 + T(9) * cg * cy);
       // collision: omega feq_i(rho, u)
       const T lf = A.omega * l2[i];
-      lrho += lf * fe[i] / r;
+      lrho += lf * fe[i] * ir;
       const T rw = r * wi;
       lu0 += lf * rw * ((T(3) * cx + T(9) * cu * cx) - T(3) * u[0]);
       lu1 += lf * rw * ((T(3) * cy + T(9) * cu * cy) - T(3) * u[1]);
-      dw += (double)(l2[i] * (fe[i] - f[i]));
+      dw += l2[i] * (fe[i] - f[i]);
     }
+    lu0 *= ir;
+    lu1 *= ir;
 #pragma unroll
     for (int j = 0; j < 9; ++j) {
       const T cx = (T)q9_cx(j), cy = (T)q9_cy(j);
-      A.lam_out[j * n + p] = (T(1) - A.omega) * l2[j] + lrho + (lu0 * (cx - u[0]) + lu1 * (cy - u[1])) / r;
+      A.lam_out[j * n + p] = (T(1) - A.omega) * l2[j] + lrho + (lu0 * (cx - u[0]) + lu1 * (cy - u[1]));
     }
   }
   {
     // per-block partial of d/domega in its own slot (no contention; summed at the end)
     __shared__ double red[8];
+    double v = (double)dw;
 #pragma unroll
-    for (int o = 16; o >= 1; o >>= 1) dw += __shfl_down_sync(0xffffffffu, dw, o);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = dw;
+    for (int o = 16; o >= 1; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
     __syncthreads();
     if (threadIdx.x == 0) {
       double sum = 0;
       for (int k = 0; k < (int)(blockDim.x >> 5); ++k) sum += red[k];
-      A.acc_w[blockIdx.y * gridDim.x + blockIdx.x] += sum;
+      A.acc_w[A.slot0 + blockIdx.y * gridDim.x + blockIdx.x] += sum;
     }
   }
 }
@@ -340,6 +374,18 @@ __device__ __forceinline__ void node_sum(int nx_, int ny_, const unsigned long l
   }
 }
 
+// sum of v over the S consecutive threads of one marker's stencil pairs, complete in the
+// group's first lane (S a power of two up to 32)
+template <typename T, int S>
+__device__ __forceinline__ T group_sum(T v) {
+  static_assert(S <= 32 && (S & (S - 1)) == 0, "stencil groups of a power of two up to 32");
+  const unsigned lane = threadIdx.x & 31, base = lane & ~(unsigned)(S - 1);
+  const unsigned gm = S == 32 ? 0xffffffffu : (((1u << S) - 1u) << base);
+#pragma unroll
+  for (int o = S / 2; o >= 1; o >>= 1) v += __shfl_down_sync(gm, v, o, S);
+  return v;
+}
+
 template <typename T, int R>
 __global__ void __launch_bounds__(kAdjBodyThreads) k_adj_body(BodyArgs<T> A) {
   constexpr int WD = 2 * R, S = WD * WD;
@@ -358,9 +404,11 @@ __global__ void __launch_bounds__(kAdjBodyThreads) k_adj_body(BodyArgs<T> A) {
   T* Fs = nmu + 2 * P;         // [NF][2M] force steps; in reverse their adjoints
   T* Ft = Fs + 2 * M * NF;     // [2M]
   T* U = Ft + 2 * M;           // [2M]
-  T* mu = U + 2 * M;           // [2M] adjoint of U_k
-  T* lFt = mu + 2 * M;         // [2M] adjoint of Ft
-  T* red = lFt + 2 * M;        // [8] a, v, d, h adjoints
+  T* mu = U + 2 * M;           // [2M] adjoint of U_k (read)
+  T* mu2 = mu + 2 * M;         // [2M] adjoint of U_k (written)
+  T* lFt = mu2 + 2 * M;        // [2M] adjoint of Ft
+  T* lFs = lFt + 2 * M;        // [NF][2M] adjoints of the force steps
+  T* red = lFs + 2 * M * NF;   // [8] a, v, d, h adjoints
   const int NW = (M + 63) / 64;
   unsigned long long* cm = (unsigned long long*)(((uintptr_t)(red + 8) + 7) & ~(uintptr_t)7);  // [P][NW]
   int* fxy = (int*)(cm + (size_t)P * NW);  // [2M] stencil corners
@@ -428,34 +476,41 @@ __global__ void __launch_bounds__(kAdjBodyThreads) k_adj_body(BodyArgs<T> A) {
     }
   }
   __syncthreads();
-  // forward MDF (ib/mdf.py:38-64), every force step kept
-  for (int q = tid; q < 2 * M; q += nt) {
-    const int m = q >> 1, c = q & 1;
-    T acc = T(0);
-    for (int s = 0; s < S; ++s) acc += W[m * S + s] * un[2 * (m * S + s) + c];
-    U[q] = acc;
-    const T fs = (v[c] - acc) * A.ds2;
-    Fs[q] = fs;
-    Ft[q] = NI > 0 ? fs : T(0);
+  // forward MDF (ib/mdf.py:38-64), every force step kept; one thread per pair, the
+  // interpolation sums reduced within each marker's group of S threads
+  for (int p = tid; p < P; p += nt) {
+    const int m = p / S, s = p - m * S;
+    const T a0 = group_sum<T, S>(W[p] * un[2 * p]), a1 = group_sum<T, S>(W[p] * un[2 * p + 1]);
+    if (s == 0) {
+      const T acc[2] = {a0, a1};
+#pragma unroll
+      for (int c = 0; c < 2; ++c) {
+        U[2 * m + c] = acc[c];
+        const T fs = (v[c] - acc[c]) * A.ds2;
+        Fs[2 * m + c] = fs;
+        Ft[2 * m + c] = NI > 0 ? fs : T(0);
+      }
+    }
   }
   __syncthreads();
   for (int k = 0; k + 1 < NI; ++k) {
     const T* F = Fs + 2 * M * k;
-    for (int p = tid; p < P; p += nt) {  // spread(F_k) at each pair's node
+    for (int p = tid; p < P; p += nt) {
       const int m = p / S, s = p - m * S, ix = s / WD, iy = s - ix * WD;
-      node_sum<T, WD>(fxy[2 * m] + ix, fxy[2 * m + 1] + iy, cm + (size_t)p * NW, NW, fxy, W, F, nmu[2 * p],
-                      nmu[2 * p + 1]);
-    }
-    __syncthreads();
-    for (int q = tid; q < 2 * M; q += nt) {
-      const int m = q >> 1, c = q & 1;
-      T acc = T(0);
-      for (int s = 0; s < S; ++s) acc += W[m * S + s] * (T(0.5) * nmu[2 * (m * S + s) + c]);
-      const T uq = U[q] + acc;
-      U[q] = uq;
-      const T fs = (v[c] - uq) * A.ds2;
-      Fs[2 * M * (k + 1) + q] = fs;
-      Ft[q] = Ft[q] + fs;
+      T n0, n1;  // spread(F_k) at the pair's node
+      node_sum<T, WD>(fxy[2 * m] + ix, fxy[2 * m + 1] + iy, cm + (size_t)p * NW, NW, fxy, W, F, n0, n1);
+      const T a0 = group_sum<T, S>(W[p] * (T(0.5) * n0)), a1 = group_sum<T, S>(W[p] * (T(0.5) * n1));
+      if (s == 0) {
+        const T acc[2] = {a0, a1};
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+          const T uq = U[2 * m + c] + acc[c];
+          U[2 * m + c] = uq;
+          const T fs = (v[c] - uq) * A.ds2;
+          Fs[2 * M * (k + 1) + 2 * m + c] = fs;
+          Ft[2 * m + c] = Ft[2 * m + c] + fs;
+        }
+      }
     }
     __syncthreads();
   }
@@ -518,43 +573,53 @@ __global__ void __launch_bounds__(kAdjBodyThreads) k_adj_body(BodyArgs<T> A) {
   }
   __syncthreads();
   // lambda_Ft = interp(lambda_g) - lambda_h; mu_NI-1 = 0
-  for (int q = tid; q < 2 * M; q += nt) {
-    const int m = q >> 1, c = q & 1;
-    T acc = T(0);
-    for (int s = 0; s < S; ++s) acc += W[m * S + s] * lg[2 * (m * S + s) + c];
-    lFt[q] = acc - red[6 + c];
-    mu[q] = T(0);
+  for (int p = tid; p < P; p += nt) {
+    const int m = p / S, s = p - m * S;
+    const T a0 = group_sum<T, S>(W[p] * lg[2 * p]), a1 = group_sum<T, S>(W[p] * lg[2 * p + 1]);
+    if (s == 0) {
+      lFt[2 * m] = a0 - red[6];
+      lFt[2 * m + 1] = a1 - red[7];
+      mu[2 * m] = T(0);
+      mu[2 * m + 1] = T(0);
+    }
   }
   __syncthreads();
-  // MDF in reverse: for k = NI-1 .. 0
+  // MDF in reverse: for k = NI-1 .. 0 (one pass per iteration, mu double-buffered)
   //   lambda_Fs_k = lambda_Ft + [k < NI-1] 0.5 interp(nodeval(mu_k+1))
   //   lambda_W   += [k < NI-1] 0.5 (mu_k+1,m . nodeval(Fs_k) + Fs_k,m . nodeval(mu_k+1))
   //   mu_k = mu_k+1 - 2 ds lambda_Fs_k
+  T* mr = mu;
+  T* mw = mu2;
   for (int k = NI - 1; k >= 0; --k) {
-    T* F = Fs + 2 * M * k;
-    if (k + 1 < NI) {
-      for (int p = tid; p < P; p += nt) {
-        const int m = p / S, s = p - m * S, ix = s / WD, iy = s - ix * WD;
+    const T* F = Fs + 2 * M * k;
+    for (int p = tid; p < P; p += nt) {
+      const int m = p / S, s = p - m * S, ix = s / WD, iy = s - ix * WD;
+      T a0 = T(0), a1 = T(0);
+      if (k + 1 < NI) {
         const int gx = fxy[2 * m] + ix, gy = fxy[2 * m + 1] + iy;
         T m0, m1, f0, f1;
-        node_sum<T, WD>(gx, gy, cm + (size_t)p * NW, NW, fxy, W, mu, m0, m1);
+        node_sum<T, WD>(gx, gy, cm + (size_t)p * NW, NW, fxy, W, mr, m0, m1);
         node_sum<T, WD>(gx, gy, cm + (size_t)p * NW, NW, fxy, W, F, f0, f1);
-        nmu[2 * p] = m0;
-        nmu[2 * p + 1] = m1;
-        lW[p] += T(0.5) * ((mu[2 * m] * f0 + mu[2 * m + 1] * f1) + (F[2 * m] * m0 + F[2 * m + 1] * m1));
+        lW[p] += T(0.5) * ((mr[2 * m] * f0 + mr[2 * m + 1] * f1) + (F[2 * m] * m0 + F[2 * m + 1] * m1));
+        a0 = W[p] * (T(0.5) * m0);
+        a1 = W[p] * (T(0.5) * m1);
       }
-      __syncthreads();
-    }
-    for (int q = tid; q < 2 * M; q += nt) {
-      const int m = q >> 1, c = q & 1;
-      T acc = T(0);
-      if (k + 1 < NI)
-        for (int s = 0; s < S; ++s) acc += W[m * S + s] * (T(0.5) * nmu[2 * (m * S + s) + c]);
-      const T lfs = lFt[q] + acc;
-      F[q] = lfs;  // the forward force step is no longer needed
-      mu[q] = mu[q] - A.ds2 * lfs;
+      a0 = group_sum<T, S>(a0);
+      a1 = group_sum<T, S>(a1);
+      if (s == 0) {
+        const T acc[2] = {a0, a1};
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+          const T lfs = lFt[2 * m + c] + acc[c];
+          lFs[2 * M * k + 2 * m + c] = lfs;
+          mw[2 * m + c] = mr[2 * m + c] - A.ds2 * lfs;
+        }
+      }
     }
     __syncthreads();
+    T* t = mr;
+    mr = mw;
+    mw = t;
   }
   // lambda_v: every force step targets the body velocity
   if (tid < 32) {  // warp 0, fixed tree
@@ -562,39 +627,33 @@ __global__ void __launch_bounds__(kAdjBodyThreads) k_adj_body(BodyArgs<T> A) {
     for (int c = 0; c < 2; ++c) {
       T acc = T(0);
       for (int k = 0; k < NI; ++k)
-        for (int m = tid; m < M; m += 32) acc += A.ds2 * Fs[2 * M * k + 2 * m + c];
+        for (int m = tid; m < M; m += 32) acc += A.ds2 * lFs[2 * M * k + 2 * m + c];
 #pragma unroll
       for (int o = 16; o >= 1; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
       if (tid == 0) red[2 + c] += acc;
     }
   }
-  // interp^T: lambda_u at the nodes = nodeval(mu_0); weight adjoints of U0 = interp(u)
-  // and of g = spread(Ft)
+  // interp^T: lambda_u at the nodes = nodeval(mu_0); weight adjoints of U0 = interp(u) and
+  // of g = spread(Ft); then the marker position adjoints (X = X0 + d), summed per group
   for (int p = tid; p < P; p += nt) {
     const int m = p / S, s = p - m * S, ix = s / WD, iy = s - ix * WD;
     const int gx = fxy[2 * m] + ix, gy = fxy[2 * m + 1] + iy;
     T n0, n1;
-    node_sum<T, WD>(gx, gy, cm + (size_t)p * NW, NW, fxy, W, mu, n0, n1);
+    node_sum<T, WD>(gx, gy, cm + (size_t)p * NW, NW, fxy, W, mr, n0, n1);
     if (gx >= 0 && gx < nx && gy >= 0 && gy < ny) {
       const int64_t q = (int64_t)gx * ny + gy;
       A.lu[q] = n0;
       A.lu[n + q] = n1;
     }
-    lW[p] += (mu[2 * m] * un[2 * p] + mu[2 * m + 1] * un[2 * p + 1]) +
-             (Ft[2 * m] * lg[2 * p] + Ft[2 * m + 1] * lg[2 * p + 1]);
-  }
-  __syncthreads();
-  // marker positions: X = X0 + d
-  for (int m = tid; m < M; m += nt) {
-    T gx_ = T(0), gy_ = T(0);
-    for (int s = 0; s < S; ++s) {
-      gx_ += lW[m * S + s] * dWx[m * S + s];
-      gy_ += lW[m * S + s] * dWy[m * S + s];
+    const T lw = lW[p] + (mr[2 * m] * un[2 * p] + mr[2 * m + 1] * un[2 * p + 1]) +
+                 (Ft[2 * m] * lg[2 * p] + Ft[2 * m + 1] * lg[2 * p + 1]);
+    const T gxm = group_sum<T, S>(lw * dWx[p]), gym = group_sum<T, S>(lw * dWy[p]);
+    if (s == 0) {
+      lFt[2 * m] = gxm;  // lambda_Ft is no longer needed: reuse it for the position adjoints
+      lFt[2 * m + 1] = gym;
+      atomicAdd(A.dX + m, (double)gxm);
+      atomicAdd(A.dX + M + m, (double)gym);
     }
-    lFt[2 * m] = gx_;
-    lFt[2 * m + 1] = gy_;
-    atomicAdd(A.dX + m, (double)gx_);
-    atomicAdd(A.dX + M + m, (double)gy_);
   }
   __syncthreads();
   if (tid < 32) {
@@ -616,7 +675,7 @@ __global__ void __launch_bounds__(kAdjBodyThreads) k_adj_body(BodyArgs<T> A) {
 template <typename T>
 static size_t adj_body_smem(int M, int R, int n_iter) {
   const size_t S = 4 * R * R, P = M * S, NF = n_iter > 0 ? n_iter : 1, NW = (M + 63) / 64;
-  return sizeof(T) * (4 * P + 6 * P + 2 * M * NF + 8 * (size_t)M + 8) + 8 + 8 * P * NW + sizeof(int) * 2 * M + 16;
+  return sizeof(T) * (4 * P + 6 * P + 4 * M * NF + 10 * (size_t)M + 8) + 8 + 8 * P * NW + sizeof(int) * 2 * M + 16;
 }
 
 }  // namespace adj
@@ -653,7 +712,9 @@ struct vs_adjoint_plan {
   void* d_hist = nullptr;          // n_steps x 3
   double* d_acc = nullptr;         // [0] dU0 (boundary), [1] domega, [2] dK, [3] dU0 (initial state), [4..] dX0, dY0
   double* d_acc_w = nullptr;       // per-block partial sums of d/domega (grid adjoint)
-  int n_accw = 0;
+  int n_accw = 0, n_accw_grid = 0; // all slots; slots of the outside-window launch
+  double lo[2] = {0, 0};           // smallest marker x, y (plan precision)
+  int wcap[2] = {0, 0};            // extent of the body's stencil window
   int have_ck = 0;
   size_t body_smem = 0;
   int chain_k = 0;  // see BodyArgs::chain_k
@@ -776,12 +837,25 @@ static int reverse_steps(vs_adjoint_plan* P, int b, int len, int* cur, cudaStrea
     switch (c.radius) {
       case 1: k_adj_body<T, 1><<<1, kAdjBodyThreads, P->body_smem, st>>>(B); break;
       case 2: k_adj_body<T, 2><<<1, kAdjBodyThreads, P->body_smem, st>>>(B); break;
-      default: k_adj_body<T, 3><<<1, kAdjBodyThreads, P->body_smem, st>>>(B); break;
+      default: k_adj_body<T, 2><<<1, kAdjBodyThreads, P->body_smem, st>>>(B); break;
     }
+    // window nodes only after the body adjoint: the rest runs beside it (after the boundary
+    // adjoint, which it also needs)
+    G.wstate = sst + 12 * j;
+    G.lo0 = P->lo[0];
+    G.lo1 = P->lo[1];
+    G.R = c.radius;
+    G.cap[0] = P->wcap[0];
+    G.cap[1] = P->wcap[1];
+    G.mode = 1;
+    G.slot0 = 0;
+    k_adj_grid<T><<<dim3(grid_for(c.ny, 256), c.nx), 256, 0, P->aux>>>(G);
     e = cudaEventRecord(P->ev_b, P->aux);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(st, P->ev_b, 0);
     if (e != cudaSuccess) return cuda_status(e, "vs_adjoint_backward join");
-    k_adj_grid<T><<<dim3(grid_for(c.ny, 256), c.nx), 256, 0, st>>>(G);
+    G.mode = 2;
+    G.slot0 = P->n_accw_grid;
+    k_adj_grid<T><<<grid_for((int64_t)P->wcap[0] * P->wcap[1], 256), 256, 0, st>>>(G);
     VS_CHECK_LAUNCH("vs_adjoint_backward kernels");
     *cur = 1 - *cur;
   }
@@ -905,7 +979,7 @@ int vs_adjoint_plan_create(const vs_adjoint_cfg* cfg, vs_adjoint_plan** out) {
   VS_REQUIRE(cfg->n_markers >= 3 && cfg->offsets_host, "vs_adjoint_plan_create: markers and offsets needed");
   VS_REQUIRE(cfg->n_steps >= 1 && cfg->checkpoint_every >= 1, "vs_adjoint_plan_create: steps / checkpoints");
   VS_REQUIRE(cfg->obj_start >= 0 && cfg->obj_start < cfg->n_steps, "vs_adjoint_plan_create: objective window");
-  VS_REQUIRE(cfg->radius >= 1 && cfg->radius <= 3, "vs_adjoint_plan_create: radius 1..3");
+  VS_REQUIRE(cfg->radius >= 1 && cfg->radius <= 2, "vs_adjoint_plan_create: radius 1 or 2");
   VS_REQUIRE(cfg->U0 > 0 && cfg->D > 0 && cfg->Re > 0, "vs_adjoint_plan_create: U0, D, Re must be positive");
   vs_adjoint_plan* P = new (std::nothrow) vs_adjoint_plan();
   if (!P) {
@@ -1028,7 +1102,23 @@ int vs_adjoint_plan_create(const vs_adjoint_cfg* cfg, vs_adjoint_plan** out) {
   alloc(&P->d_X0, ts * 2 * M);
   alloc(&P->d_hist, ts * 3 * cfg->n_steps);
   alloc((void**)&P->d_acc, sizeof(double) * (4 + 2 * M));
-  P->n_accw = (int)grid_for(cfg->ny, 256) * cfg->nx;
+  {
+    double lx = 1e300, ly = 1e300, hx = -1e300, hy = -1e300;
+    for (int m = 0; m < M; ++m) {
+      lx = X[m] < lx ? X[m] : lx;
+      ly = Y[m] < ly ? Y[m] : ly;
+      hx = X[m] > hx ? X[m] : hx;
+      hy = Y[m] > hy ? Y[m] : hy;
+    }
+    const bool f32 = cfg->dtype == VS_F32;
+    P->lo[0] = f32 ? (double)(float)lx : lx;
+    P->lo[1] = f32 ? (double)(float)ly : ly;
+    // floor(hi + d) - floor(lo + d) <= floor(hi) - floor(lo) + 1, plus the stencil width
+    P->wcap[0] = (int)(floor(hx) - floor(lx)) + 2 * cfg->radius + 1;
+    P->wcap[1] = (int)(floor(hy) - floor(ly)) + 2 * cfg->radius + 1;
+  }
+  P->n_accw_grid = (int)grid_for(cfg->ny, 256) * cfg->nx;
+  P->n_accw = P->n_accw_grid + (int)grid_for((int64_t)P->wcap[0] * P->wcap[1], 256);
   alloc((void**)&P->d_acc_w, sizeof(double) * P->n_accw);
   if (e != cudaSuccess) return fail(cuda_status(e, "vs_adjoint_plan_create"));
   rc = dispatch_t(cfg->dtype, [&](auto t) -> int {
@@ -1053,7 +1143,7 @@ int vs_adjoint_plan_create(const vs_adjoint_cfg* cfg, vs_adjoint_plan** out) {
     switch (cfg->radius) {
       case 1: e2 = cudaFuncSetAttribute(k_adj_body<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin); break;
       case 2: e2 = cudaFuncSetAttribute(k_adj_body<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin); break;
-      default: e2 = cudaFuncSetAttribute(k_adj_body<T, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin); break;
+      default: e2 = cudaFuncSetAttribute(k_adj_body<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin); break;
     }
     return cuda_status(e2, "vs_adjoint_plan_create attribute");
   });
