@@ -334,7 +334,7 @@ int vs_post_components(int q, int what);
 
 /* ================================================================== adjoint ===
  * Gradients of a 2-D cylinder VIV objective by a hand-written discrete adjoint of the
- * fused step: D2Q9 BGK, exact-difference forcing, MDF immersed boundary, a 1-DOF
+ * fused step: D2Q9 (BGK, KBC, regularised or MRT collision), exact-difference forcing, MDF immersed boundary, a 1-DOF
  * transverse spring (Newmark), equilibrium inflow ux = U0 at x = 0, pressure NEE
  * outflow at x = nx-1, periodic y (examples/2d/vortex_induced_vibration.py:96-148 with
  * BGK).  The reference obtains such gradients with jax.grad through its jitted loop; this
@@ -354,6 +354,9 @@ typedef struct vs_adjoint_cfg {
   int kernel, radius, n_iter;
   double mass, stiffness, damping, added_mass_area;
   int n_steps, checkpoint_every, obj_start;
+  int collision;         /* VS_COLLIDE_BGK (default 0), _KBC, _REG or _MRT              */
+  double mrt_op[81];     /* MRT: the 9 x 9 operator at this omega, and its derivative     */
+  double mrt_dop[81];    /*      with respect to omega (row-major)                        */
 } vs_adjoint_cfg;
 typedef struct vs_adjoint_plan vs_adjoint_plan;
 int vs_adjoint_plan_create(const vs_adjoint_cfg* cfg, vs_adjoint_plan** out);

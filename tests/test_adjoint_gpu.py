@@ -24,23 +24,26 @@ def A():
     return adjoint
 
 
-def _J(A, U0, K, off):
-    p = A.CylinderDrag(U0=U0, stiffness=K, offsets=off, **CASE)
+def _J(A, U0, K, off, collision="bgk"):
+    p = A.CylinderDrag(U0=U0, stiffness=K, offsets=off, collision=collision, **CASE)
     J = p.forward(keep_checkpoints=False)
     p.close()
     return J
 
 
-def test_adjoint_matches_finite_differences(A):
+@pytest.mark.parametrize("collision", ["bgk", "kbc", "mrt", "reg"])
+def test_adjoint_matches_finite_differences(A, collision):
+    """BGK has a hand-derived node transpose; KBC, MRT and regularised go through the
+    dual-number node Jacobian."""
     off = np.random.default_rng(2).normal(0.0, 0.1, CASE["n_markers"])
-    base = A.CylinderDrag(U0=0.05, offsets=off, **CASE)
+    base = A.CylinderDrag(U0=0.05, offsets=off, collision=collision, **CASE)
     K = base.stiffness
     J = base.forward()
     gU0, gK, goff = base.backward()
     assert np.isfinite(J) and J != 0.0
     h = 1e-4
-    fd_U0 = (_J(A, 0.05 * (1 + h), K, off) - _J(A, 0.05 * (1 - h), K, off)) / (2 * 0.05 * h)
-    fd_K = (_J(A, 0.05, K * (1 + h), off) - _J(A, 0.05, K * (1 - h), off)) / (2 * K * h)
+    fd_U0 = (_J(A, 0.05 * (1 + h), K, off, collision) - _J(A, 0.05 * (1 - h), K, off, collision)) / (2 * 0.05 * h)
+    fd_K = (_J(A, 0.05, K * (1 + h), off, collision) - _J(A, 0.05, K * (1 - h), off, collision)) / (2 * K * h)
     assert abs(gU0 - fd_U0) <= 1e-3 * abs(fd_U0), (gU0, fd_U0)
     assert abs(gK - fd_K) <= 1e-3 * abs(fd_K), (gK, fd_K)
     scale = np.max(np.abs(goff))
@@ -48,7 +51,7 @@ def test_adjoint_matches_finite_differences(A):
         op, om = off.copy(), off.copy()
         op[m] += 1e-4
         om[m] -= 1e-4
-        fd = (_J(A, 0.05, K, op) - _J(A, 0.05, K, om)) / 2e-4
+        fd = (_J(A, 0.05, K, op, collision) - _J(A, 0.05, K, om, collision)) / 2e-4
         assert abs(goff[m] - fd) <= 1e-3 * max(abs(fd), 1e-2 * scale), (m, goff[m], fd)
 
 

@@ -74,7 +74,8 @@ class vs_adjoint_cfg(C.Structure):
                 ("kernel", C.c_int), ("radius", C.c_int), ("n_iter", C.c_int),
                 ("mass", C.c_double), ("stiffness", C.c_double), ("damping", C.c_double),
                 ("added_mass_area", C.c_double),
-                ("n_steps", C.c_int), ("checkpoint_every", C.c_int), ("obj_start", C.c_int)]
+                ("n_steps", C.c_int), ("checkpoint_every", C.c_int), ("obj_start", C.c_int),
+                ("collision", C.c_int), ("mrt_op", C.c_double * 81), ("mrt_dop", C.c_double * 81)]
 
 
 _i, _d, _p, _l, _z = C.c_int, C.c_double, C.c_void_p, C.c_int64, C.c_size_t

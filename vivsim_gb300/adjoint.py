@@ -20,7 +20,8 @@ import numpy as np
 import torch
 
 from . import _lib as V
-from .solver import KERNELS
+from ._ops import _M9, mrt_collision_operator
+from .solver import COLLISIONS, KERNELS
 
 
 class CylinderDrag:
@@ -28,7 +29,8 @@ class CylinderDrag:
 
     def __init__(self, nx=512, ny=256, U0=0.05, D=20.0, Re=100.0, n_markers=64, offsets=None, center=None,
                  mass_ratio=10.0, U_r=5.0, stiffness=None, damping=0.0, n_steps=4000, checkpoint_every=100,
-                 obj_start=None, kernel="peskin4", radius=2, n_iter=3, rho_out=1.0, dtype=torch.float32):
+                 obj_start=None, kernel="peskin4", radius=2, n_iter=3, rho_out=1.0, dtype=torch.float32,
+                 collision="bgk"):
         self.M = int(n_markers)
         off = np.zeros(self.M) if offsets is None else np.asarray(offsets, dtype=np.float64).reshape(-1)
         if off.shape[0] != self.M:
@@ -52,6 +54,18 @@ class CylinderDrag:
         cfg.n_steps = int(n_steps)
         cfg.checkpoint_every = int(checkpoint_every)
         cfg.obj_start = int(n_steps // 2 if obj_start is None else obj_start)
+        cfg.collision = COLLISIONS[collision]
+        if collision == "mrt":
+            # operator at omega = 1 / (3 U0 D / Re + 0.5) and its derivative in omega
+            # (only the two shear rates of lbm/collision/mrt.py:44 depend on omega)
+            omega = 1.0 / (3.0 * U0 * D / Re + 0.5)
+            op = mrt_collision_operator(9, omega, torch.float64).numpy().reshape(-1)
+            Mi = np.linalg.inv(_M9.astype(np.float64))
+            dS = np.diag([0, 0, 0, 0, 0, 0, 0, 1.0, 1.0])
+            dop = (Mi @ dS @ _M9.astype(np.float64)).reshape(-1)
+            for i in range(81):
+                cfg.mrt_op[i] = float(op[i])
+                cfg.mrt_dop[i] = float(dop[i])
         self.cfg = cfg
         self.stiffness = float(stiffness)
         h = C.c_void_p()

@@ -22,6 +22,7 @@
 #include <cmath>
 #include <cstring>
 #include <new>
+#include <type_traits>
 #include <vector>
 
 #include "vs_boundary.cuh"
@@ -85,18 +86,79 @@ __device__ __forceinline__ void pnee_right(const S* w, const S* nb, T rho_w, S* 
   for (int i = 0; i < 9; ++i) out[i] = fw[i] + (nb[i] - fe[i]);
 }
 
-// post-collision populations of node (x, y) without body force (BGK)
+// The collision of the step on scalar type S (T, or Dual<T> for derivatives): BGK, KBC,
+// regularised (vs_common.cuh restatements of lbm/collision/*.py) or MRT with operator op
+// (its derivative with respect to omega in dop, for the dual part).
+template <typename S, typename T>
+__device__ __forceinline__ void collide_any(int kind, S* f, const S* fe, S omega, const T* op, const T* dop) {
+  if (kind == VS_COLLIDE_MRT) {
+    S d[9], out[9];
+#pragma unroll
+    for (int j = 0; j < 9; ++j) d[j] = fe[j] - f[j];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+      S acc = S(0);
+#pragma unroll
+      for (int j = 0; j < 9; ++j) {
+        S o;
+        if constexpr (std::is_same<S, T>::value) o = op[i * 9 + j];
+        else o = S(op[i * 9 + j], dop[i * 9 + j] * omega.d);  // omega.d seeds d/domega
+        acc = j == 0 ? o * d[j] : acc + o * d[j];
+      }
+      out[i] = f[i] + acc;
+    }
+#pragma unroll
+    for (int i = 0; i < 9; ++i) f[i] = out[i];
+    return;
+  }
+  CollideParams<S> P;
+  P.omega = omega;
+  P.one_m_omega = S(1) - omega;
+  P.inv_omega = S(1) / omega;
+  P.one_m_inv = S(1) - S(1) / omega;
+  P.mrt = nullptr;
+  if (kind == VS_COLLIDE_KBC) collide_kbc(L9{}, f, fe, P);
+  else if (kind == VS_COLLIDE_REG) collide_reg(L9{}, f, fe, P);
+  else collide_bgk<L9>(f, fe, P);
+}
+
+// post-collision populations of node (x, y) without body force
 template <typename T>
 __device__ __forceinline__ void post_collide(const T* __restrict__ f, int64_t n, int ny, int x, int y, T omega,
-                                             T* out) {
+                                             T* out, int kind, const T* op) {
   const int64_t p = (int64_t)x * ny + y;
-  T fl[9], r, u[2], fe[9];
+  T r, u[2], fe[9];
 #pragma unroll
-  for (int i = 0; i < 9; ++i) fl[i] = f[i * n + p];
-  macro(L9{}, fl, r, u);
+  for (int i = 0; i < 9; ++i) out[i] = f[i * n + p];
+  macro(L9{}, out, r, u);
   feq9<T, T>(r, u[0], u[1], fe);
+  collide_any<T, T>(kind, out, fe, omega, op, op);
+}
+
+// lambda_f and d/domega of one node for collision + exact-difference forcing, by forward-mode
+// dual numbers (10 passes: the 9 populations and omega): the transposed Jacobian of any
+// collision model of the reference.  g is the node's body force.
+template <typename T>
+__device__ __forceinline__ void node_adjoint_dual(const T* f, T g0, T g1, const T* l2, T omega, int kind, const T* op,
+                                                  const T* dop, T* lam_f, T& lomega) {
+  for (int k = 0; k < 10; ++k) {
+    Dual<T> fd[9], r, u[2], fe[9];
 #pragma unroll
-  for (int i = 0; i < 9; ++i) out[i] = (T(1) - omega) * fl[i] + omega * fe[i];
+    for (int i = 0; i < 9; ++i) fd[i] = Dual<T>(f[i], (T)(k == i));
+    macro(L9{}, fd, r, u);
+    feq9<Dual<T>, T>(r, u[0], u[1], fe);
+    const Dual<T> om(omega, (T)(k == 9));
+    collide_any<Dual<T>, T>(kind, fd, fe, om, op, dop);
+    const Dual<T> gd[2] = {Dual<T>(g0, T(0)), Dual<T>(g1, T(0))};
+    T sum = T(0);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+      const Dual<T> out = fd[i] + guo_i(L9{}, i, gd, u);
+      sum += l2[i] * out.d;
+    }
+    if (k < 9) lam_f[k] = sum;
+    else lomega = sum;
+  }
 }
 
 template <typename T>
@@ -115,6 +177,9 @@ struct GridArgs {
   const T* wstate;  // body state of the step (displacement -> window origin)
   double lo0, lo1;  // smallest marker x, y (plan precision)
   int R, cap[2];    // stencil half-width; window extent
+  int kind;         // collision model (VS_COLLIDE_*)
+  const T* op;      // MRT operator (device, 9 x 9) and its derivative with respect to omega
+  const T* dop;
 };
 
 __device__ __forceinline__ int wrap(int a, int n) { return a < 0 ? a + n : (a >= n ? a - n : a); }
@@ -154,9 +219,9 @@ __global__ void __launch_bounds__(kRows * 18) k_adj_bc(GridArgs<T> A) {
   if (live && k < 9) {
     // streamed population k at the wall (x = nx-1) and at its neighbour (x = nx-2)
     T src[9];
-    post_collide(A.f, n, ny, wrap(nx - 1 - q9_cx(k), nx), wrap(y - q9_cy(k), ny), A.omega, src);
+    post_collide(A.f, n, ny, wrap(nx - 1 - q9_cx(k), nx), wrap(y - q9_cy(k), ny), A.omega, src, A.kind, A.op);
     w[r][k] = src[k];
-    post_collide(A.f, n, ny, nx - 2 - q9_cx(k), wrap(y - q9_cy(k), ny), A.omega, src);
+    post_collide(A.f, n, ny, nx - 2 - q9_cx(k), wrap(y - q9_cy(k), ny), A.omega, src, A.kind, A.op);
     nb[r][k] = src[k];
     lo[r][k] = A.lam[k * n + (int64_t)(nx - 1) * ny + y];
   }
@@ -252,6 +317,18 @@ __global__ void __launch_bounds__(256) k_adj_grid(GridArgs<T> A) {
         A.lu[n + p] = T(0);
       }
     }
+    if (A.kind != VS_COLLIDE_BGK) {
+      // other collision models: transposed Jacobian by dual numbers, plus the immersed
+      // boundary's lambda_u through u = m / rho
+      T lf[9], lom;
+      node_adjoint_dual<T>(f, g0, g1, l2, A.omega, A.kind, A.op, A.dop, lf, lom);
+      dw = lom;
+#pragma unroll
+      for (int j = 0; j < 9; ++j) {
+        const T cx = (T)q9_cx(j), cy = (T)q9_cy(j);
+        A.lam_out[j * n + p] = lf[j] + (lu0 * (cx - u[0]) + lu1 * (cy - u[1])) * ir;
+      }
+    } else {
     T lrho = T(0);
 #pragma unroll
     for (int i = 0; i < 9; ++i) {
@@ -274,6 +351,7 @@ __global__ void __launch_bounds__(256) k_adj_grid(GridArgs<T> A) {
     for (int j = 0; j < 9; ++j) {
       const T cx = (T)q9_cx(j), cy = (T)q9_cy(j);
       A.lam_out[j * n + p] = (T(1) - A.omega) * l2[j] + lrho + (lu0 * (cx - u[0]) + lu1 * (cy - u[1]));
+    }
     }
   }
   {
@@ -714,6 +792,7 @@ struct vs_adjoint_plan {
   double* d_acc_w = nullptr;       // per-block partial sums of d/domega (grid adjoint)
   int n_accw = 0, n_accw_grid = 0; // all slots; slots of the outside-window launch
   double lo[2] = {0, 0};           // smallest marker x, y (plan precision)
+  void* d_op = nullptr;            // MRT operator and its omega derivative (9 x 9 each)
   int wcap[2] = {0, 0};            // extent of the body's stencil window
   int have_ck = 0;
   size_t body_smem = 0;
@@ -727,6 +806,7 @@ static void free_plan(vs_adjoint_plan* p) {
   if (p->body) vs_body_plan_destroy(p->body);
   if (p->lat) vs_lattice_plan_destroy(p->lat);
   if (p->d_acc_w) cudaFree(p->d_acc_w);
+  if (p->d_op) cudaFree(p->d_op);
   void* bufs[] = {p->d_f0,  p->d_fa,       p->d_fb,     p->d_ck,        p->d_ck_state, p->d_seg[0],
                   p->d_seg[1], p->d_seg_state[0], p->d_seg_state[1], p->d_lam[0], p->d_lam[1], p->d_g,
                   p->d_lu,  p->d_lstate,  p->d_X0,     p->d_hist,      p->d_acc,      p->d_seg_start};
@@ -803,6 +883,9 @@ static int reverse_steps(vs_adjoint_plan* P, int b, int len, int* cur, cudaStrea
     G.rho_out = (T)c.rho_out;
     G.acc = P->d_acc;
     G.acc_w = P->d_acc_w;
+    G.kind = c.collision;
+    G.op = (const T*)P->d_op;
+    G.dop = (const T*)P->d_op + 81;
     // the boundary adjoint touches the x = 0, nx-2, nx-1 columns only, the body adjoint
     // reads the stencils (kept clear of them): run them side by side
     cudaError_t e = cudaEventRecord(P->ev_f, st);
@@ -981,6 +1064,8 @@ int vs_adjoint_plan_create(const vs_adjoint_cfg* cfg, vs_adjoint_plan** out) {
   VS_REQUIRE(cfg->obj_start >= 0 && cfg->obj_start < cfg->n_steps, "vs_adjoint_plan_create: objective window");
   VS_REQUIRE(cfg->radius >= 1 && cfg->radius <= 2, "vs_adjoint_plan_create: radius 1 or 2");
   VS_REQUIRE(cfg->U0 > 0 && cfg->D > 0 && cfg->Re > 0, "vs_adjoint_plan_create: U0, D, Re must be positive");
+  VS_REQUIRE(cfg->collision >= VS_COLLIDE_BGK && cfg->collision <= VS_COLLIDE_REG,
+             "vs_adjoint_plan_create: bad collision %d", cfg->collision);
   vs_adjoint_plan* P = new (std::nothrow) vs_adjoint_plan();
   if (!P) {
     set_error("out of host memory");
@@ -1038,7 +1123,9 @@ int vs_adjoint_plan_create(const vs_adjoint_cfg* cfg, vs_adjoint_plan** out) {
   lc.nx = cfg->nx;
   lc.ny = cfg->ny;
   lc.nz = 1;
-  lc.collision = VS_COLLIDE_BGK;
+  lc.collision = cfg->collision;
+  if (cfg->collision == VS_COLLIDE_MRT)
+    for (int i = 0; i < 81; ++i) lc.mrt_op[i] = cfg->mrt_op[i];
   lc.omega = P->omega;
   lc.forcing = VS_FORCE_EDM;
   lc.n_bc = 2;
@@ -1102,6 +1189,7 @@ int vs_adjoint_plan_create(const vs_adjoint_cfg* cfg, vs_adjoint_plan** out) {
   alloc(&P->d_X0, ts * 2 * M);
   alloc(&P->d_hist, ts * 3 * cfg->n_steps);
   alloc((void**)&P->d_acc, sizeof(double) * (4 + 2 * M));
+  alloc(&P->d_op, ts * 162);
   {
     double lx = 1e300, ly = 1e300, hx = -1e300, hy = -1e300;
     for (int m = 0; m < M; ++m) {
@@ -1129,7 +1217,13 @@ int vs_adjoint_plan_create(const vs_adjoint_cfg* cfg, vs_adjoint_plan** out) {
       x0[m] = (T)X[m];
       x0[M + m] = (T)Y[m];
     }
+    std::vector<T> ops(162);
+    for (int i = 0; i < 81; ++i) {
+      ops[i] = (T)cfg->mrt_op[i];
+      ops[81 + i] = (T)cfg->mrt_dop[i];
+    }
     cudaError_t e2 = cudaMemcpy(P->d_f0, f0.data(), fbytes, cudaMemcpyHostToDevice);
+    if (e2 == cudaSuccess) e2 = cudaMemcpy(P->d_op, ops.data(), ts * 162, cudaMemcpyHostToDevice);
     if (e2 == cudaSuccess) e2 = cudaMemcpy(P->d_X0, x0.data(), ts * 2 * M, cudaMemcpyHostToDevice);
     if (e2 != cudaSuccess) return cuda_status(e2, "vs_adjoint_plan_create upload");
     P->body_smem = adj_body_smem<T>(M, cfg->radius, cfg->n_iter);
