@@ -46,7 +46,13 @@ enum {
   VS_WALL_GIVEN = 0,          /* rho_wall and u_wall given                          */
   VS_WALL_VELOCITY = 1,       /* u_wall given, rho_wall recovered (wrap_velocity)    */
   VS_WALL_PRESSURE = 2,       /* rho_wall given, u_wall recovered (wrap_pressure)    */
-  VS_WALL_FORCE_CORRECTED = 3 /* u_wall shifted by -g/(2 rho) (wrap_force_corrected) */
+  VS_WALL_FORCE_CORRECTED = 3, /* u_wall shifted by -g/(2 rho) (wrap_force_corrected) */
+  VS_WALL_CHARACTERISTIC = 4   /* fused step only: rho_wall and u_wall per face node from
+                                  boundary_characteristic (lbm/boundary/cbc.py:14-53,
+                                  lbm3d/boundary/cbc.py:16-51) of the step's input moments
+                                  at the wall and the next two planes; kind NEE, NEBB or EQ
+                                  then imposes them after streaming (a non-reflective
+                                  outflow) */
 };
 /* 1-D discrete delta kernels, vivsim/ib/kernels.py */
 enum { VS_KERNEL_PESKIN3 = 0, VS_KERNEL_PESKIN4 = 1, VS_KERNEL_COSINE4 = 2 };
@@ -331,6 +337,25 @@ int vs_post(int q, int dtype, int what, const void* u, const void* f, int nx, in
 int vs_post_pressure(int dtype, const void* rho, int64_t n, double cs2, void* out, void* stream);
 /* Components of a vs_post field (leading dimension of out). */
 int vs_post_components(int q, int what);
+
+/* ========================================================== grid refinement ===
+ * Transfers between D2Q9 blocks of neighbouring refinement levels (factor 2), called after
+ * streaming — vivsim/multigrid.py.  Both update the destination in place: only the three
+ * populations of the direction cross the interface line; the reference returns the
+ * updated array.  Shapes along the interface follow the reference's broadcasting (fine
+ * extent 2 x coarse extent, or a length-1 operand); anything else is VS_ERR_INVALID_ARG,
+ * where the reference raises its shape error.  init_grid, get_omega and coord_to_indices
+ * (multigrid.py:21-55, 131-170) are host arithmetic in vivsim_gb300.multigrid. */
+enum { VS_REFINE_LEFT = 0, VS_REFINE_RIGHT = 1, VS_REFINE_UP = 2, VS_REFINE_DOWN = 3 };
+/* fine_to_coarse(f_fine, f_coarse, dir) — multigrid.py:58-95: the coarse block's buffer line
+ * (last x line for left, first for right, first y line for up, last for down) gets the
+ * 2 x 2 average of the fine populations that move in dir */
+int vs_fine_to_coarse(int dtype, const void* f_fine, int nxf, int nyf, void* f_coarse, int nxc, int nyc, int dir,
+                      void* stream);
+/* coarse_to_fine(f_coarse, f_fine, dir) — multigrid.py:97-128: each coarse population of
+ * the interface line onto the even and the odd fine node it covers */
+int vs_coarse_to_fine(int dtype, const void* f_coarse, int nxc, int nyc, void* f_fine, int nxf, int nyf, int dir,
+                      void* stream);
 
 /* ================================================================== adjoint ===
  * Gradients of a 2-D cylinder VIV objective by a hand-written discrete adjoint of the

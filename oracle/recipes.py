@@ -43,9 +43,19 @@ def _collide(L, f, feq, kind, omega, mrt_op):
     raise ValueError(kind)
 
 
-def _apply_bcs(L, table, f_post, f, bcs):
+def _apply_bcs(L, table, f_post, f, bcs, moments=None):
+    """Face boundaries in order.  ``("cbc", loc, {"scheme": s})`` is a characteristic outflow:
+    the wall state from boundary_characteristic of the step's input moments (rho, u),
+    imposed by scheme s ("nee", "nebb" or "eq")."""
     for name, loc, kw in bcs:
-        if name == "bb":
+        if name == "cbc":
+            rho, u = moments
+            rn, un = L.boundary_characteristic(rho, u, loc)
+            vel = dict(ux_wall=un[0], uy_wall=un[1])
+            if un.shape[0] == 3:
+                vel["uz_wall"] = un[2]
+            f = table[kw["scheme"]](f, loc, rho_wall=rn, **vel)
+        elif name == "bb":
             f = L.boundary_bounce_back(f_post, f, loc, **kw)
         elif name == "spec":
             f = L.boundary_specular_reflection(f_post, f, loc, **kw)
@@ -68,6 +78,7 @@ def cavity_step(f, omega, u_lid):
 def lbm_step_2d(f, collision, omega=None, mrt_op=None, bcs=(), g=None, forcing="edm"):
     """Plain D2Q9 step with an optional body-force field (examples/2d/poiseuille_channel.py:82-143)."""
     rho, u = L2.get_macroscopic(f)
+    moments = (rho, u)  # a characteristic wall reads get_macroscopic's u, before any correction
     if g is not None and forcing in ("guo_bgk", "guo_mrt"):
         u = u + L2.get_velocity_correction(g, rho)
     feq = L2.get_equilibrium(rho, u)
@@ -81,7 +92,7 @@ def lbm_step_2d(f, collision, omega=None, mrt_op=None, bcs=(), g=None, forcing="
             f = L2.forcing_guo_mrt(f, g, u, L2.get_mrt_forcing_operator(omega, f.dtype))
     f_post = f
     f = L2.streaming(f)
-    return _apply_bcs(L2, _BC2, f_post, f, bcs)
+    return _apply_bcs(L2, _BC2, f_post, f, bcs, moments)
 
 
 class Body2D:
@@ -125,7 +136,7 @@ def ib_lbm_step_2d(f, body, collision, omega=None, mrt_op=None, bcs=()):
     f = L2.forcing_edm(f, g, u)
     f_post = f
     f = L2.streaming(f)
-    return _apply_bcs(L2, _BC2, f_post, f, bcs), h
+    return _apply_bcs(L2, _BC2, f_post, f, bcs, (rho, u)), h
 
 
 def lbm_step_3d(f, collision, omega=None, mrt_op=None, bcs=()):
@@ -134,7 +145,7 @@ def lbm_step_3d(f, collision, omega=None, mrt_op=None, bcs=()):
     f = _collide(L3, f, L3.get_equilibrium(rho, u), collision, omega, mrt_op)
     f_post = f
     f = L3.streaming(f)
-    return _apply_bcs(L3, _BC3, f_post, f, bcs)
+    return _apply_bcs(L3, _BC3, f_post, f, bcs, (rho, u))
 
 
 def ib_lbm_step_3d(f, W, I, marker_u, ds, collision, omega=None, mrt_op=None, bcs=(), n_iter=3):
@@ -151,7 +162,7 @@ def ib_lbm_step_3d(f, W, I, marker_u, ds, collision, omega=None, mrt_op=None, bc
     h = mh[0].copy()
     for i in range(1, mh.shape[0]):
         h = h + mh[i]
-    return _apply_bcs(L3, _BC3, f_post, f, bcs), h
+    return _apply_bcs(L3, _BC3, f_post, f, bcs, (rho, u)), h
 
 
 def fibonacci_sphere(n, radius, center):
@@ -162,3 +173,26 @@ def fibonacci_sphere(n, radius, center):
     return np.stack([center[0] + radius * np.cos(theta) * np.sin(phi),
                      center[1] + radius * np.sin(theta) * np.sin(phi),
                      center[2] + radius * np.cos(phi)], axis=1)
+
+
+def refined_channel_cycle(fc, ff, omega_c, omega_f, u0):
+    """One coarse step of a two-level channel built from vivsim/multigrid.py's transfers.
+
+    The coarse block (level 0, one buffer column on its right) has the equilibrium inflow
+    ux = u0 on its left; the fine block (level 1) continues it to the right and ends in a
+    pressure-NEE outflow; y is periodic in both.  The reference ships the transfers but no
+    driver that uses them, so the order is this recipe's: the coarse block steps
+    (collide, stream, inflow); the fine block takes two steps, each followed by
+    coarse_to_fine(.., 'right') from the new coarse state and the outflow; then
+    fine_to_coarse(.., 'left') refills the coarse buffer column.
+    """
+    from . import multigrid as mg
+    rho, u = L2.get_macroscopic(fc)
+    fc = L2.streaming(L2.collision_bgk(fc, L2.get_equilibrium(rho, u), omega_c))
+    fc = L2.boundary_equilibrium(fc, "left", ux_wall=u0)
+    for _ in range(2):
+        rho, u = L2.get_macroscopic(ff)
+        ff = L2.streaming(L2.collision_bgk(ff, L2.get_equilibrium(rho, u), omega_f))
+        ff = mg.coarse_to_fine(fc, ff, "right")
+        ff = L2.boundary_pressure_nee(ff, "right")
+    return mg.fine_to_coarse(ff, fc, "left"), ff

@@ -249,6 +249,8 @@ def generate(mode, jax, jnp, lbm, lbm3d, ib, ib3d, dyn):
     recipes_2d(put, jnp, lbm, ib, dyn, dt, rng)
     recipes_3d(put, jnp, lbm3d, ib3d, dt, rng)
     post_golden(put, jnp, dt)
+    refine_golden(put, jnp, lbm, dt)
+    cbc_golden(put, jnp, lbm, lbm3d, dt)
     return G
 
 
@@ -271,6 +273,109 @@ def post_golden(put, jnp, dt):
             put(f"{tag}.{name}", getattr(post, name)(jnp.asarray(u)))
     put("p.rho", rho)
     put("p.pressure", post.pressure(jnp.asarray(rho)))
+
+
+REFINE_SHAPES = {  # (fine, coarse) populations shapes per direction, plus a broadcast case
+    "left": ((9, 5, 12), (9, 7, 6)), "right": ((9, 4, 10), (9, 6, 5)),
+    "up": ((9, 12, 5), (9, 6, 7)), "down": ((9, 10, 3), (9, 5, 4)),
+}
+
+
+def refine_golden(put, jnp, lbm, dt):
+    """vivsim/multigrid.py: the two transfers in every direction, get_omega over levels, and
+    a two-level channel run of the transfers (its own seed, so the other vectors do not move).
+    The channel's order of operations restates oracle/recipes.py:refined_channel_cycle: the
+    reference ships the transfers without a driver."""
+    from vivsim import multigrid as mg
+    rng = np.random.default_rng(4242)
+    for d, (sf, sc) in REFINE_SHAPES.items():
+        ff = rng.uniform(0.0, 0.2, sf).astype(dt)
+        fc = rng.uniform(0.0, 0.2, sc).astype(dt)
+        put(f"mg.{d}.ff", ff)
+        put(f"mg.{d}.fc", fc)
+        put(f"mg.{d}.f2c", mg.fine_to_coarse(jnp.asarray(ff), jnp.asarray(fc), d))
+        put(f"mg.{d}.c2f", mg.coarse_to_fine(jnp.asarray(fc), jnp.asarray(ff), d))
+    # a coarse line of length 1 broadcasts onto every fine node
+    ff = rng.uniform(0.0, 0.2, (9, 3, 7)).astype(dt)
+    fc = rng.uniform(0.0, 0.2, (9, 4, 1)).astype(dt)
+    put("mg.bc.ff", ff)
+    put("mg.bc.fc", fc)
+    put("mg.bc.c2f", mg.coarse_to_fine(jnp.asarray(fc), jnp.asarray(ff), "right"))
+    put("mg.omega", np.array([mg.get_omega(nu, lv) for nu in (0.004, 0.02, 0.1) for lv in (-2, -1, 0, 1, 2, 3)]))
+    put("mg.init", np.array([mg.init_grid(w, h, lv, bx, by)[0].shape[1:] for w, h, lv, bx, by in
+                             ((16, 8, 0, 1, 0), (16, 8, 1, 0, 0), (16, 8, -1, 0, 2), (10, 6, 2, 1, 1))]))
+    # two-level channel: coarse 16 x 16 (+1 buffer column), fine 8 x 16 at level 1
+    nu, u0, H = 0.02, 0.05, 16
+    om_c, om_f = mg.get_omega(nu, 0), mg.get_omega(nu, 1)
+    uc = np.zeros((2, 17, H), dt)
+    uc[0] = u0
+    uc[1] = rng.normal(0.0, 1e-3, (17, H))
+    uf = np.zeros((2, 16, 2 * H), dt)
+    uf[0] = u0
+    uf[1] = rng.normal(0.0, 1e-3, (16, 2 * H))
+    fc = lbm.get_equilibrium(jnp.ones((17, H), dtype=dt), jnp.asarray(uc))
+    ff = lbm.get_equilibrium(jnp.ones((16, 2 * H), dtype=dt), jnp.asarray(uf))
+    put("rc.fc0", fc)
+    put("rc.ff0", ff)
+    put("rc.omega", np.array([om_c, om_f, u0]))
+    for s in range(6):
+        rho, u = lbm.get_macroscopic(fc)
+        fc = lbm.streaming(lbm.collision_bgk(fc, lbm.get_equilibrium(rho, u), om_c))
+        fc = lbm.boundary_equilibrium(fc, "left", ux_wall=u0)
+        for _ in range(2):
+            rho, u = lbm.get_macroscopic(ff)
+            ff = lbm.streaming(lbm.collision_bgk(ff, lbm.get_equilibrium(rho, u), om_f))
+            ff = mg.coarse_to_fine(fc, ff, "right")
+            ff = lbm.boundary_pressure_nee(ff, "right")
+        fc = mg.fine_to_coarse(ff, fc, "left")
+        if s in (0, 5):
+            put(f"rc.fc{s + 1}", fc)
+            put(f"rc.ff{s + 1}", ff)
+
+
+def cbc_golden(put, jnp, lbm, lbm3d, dt):
+    """Channels whose outflow takes its wall state from boundary_characteristic
+    (lbm/boundary/cbc.py:14-53, lbm3d/boundary/cbc.py:16-51) of the step's input moments and
+    imposes it with NEE / equilibrium / NEBB (its own seed, so the other vectors do not
+    move).  The reference uses the condition in no example; this recipe takes the moments
+    the step already has (get_macroscopic before colliding)."""
+    rng = np.random.default_rng(9090)
+    nu, u0 = 0.02, 0.05
+    om = lbm.get_omega(nu)
+    nx, ny = 24, 16
+    rho0 = (1 + 0.02 * rng.normal(0.0, 1.0, (nx, ny))).astype(dt)
+    u = np.zeros((2, nx, ny), dt)
+    u[0] = u0 + 0.01 * rng.normal(0.0, 1.0, (nx, ny))
+    u[1] = 0.01 * rng.normal(0.0, 1.0, (nx, ny))
+    f0 = lbm.get_equilibrium(jnp.asarray(rho0), jnp.asarray(u))
+    put("cbc2.f0", f0)
+    put("cbc2.omega", np.array([om, u0]))
+    for scheme in ("nee", "eq", "nebb"):
+        wall = {"nee": lbm.boundary_nee, "eq": lbm.boundary_equilibrium, "nebb": lbm.boundary_nebb}[scheme]
+        f = f0
+        for step in range(1, 9):
+            rho, uu = lbm.get_macroscopic(f)
+            f = lbm.streaming(lbm.collision_kbc(f, lbm.get_equilibrium(rho, uu), om))
+            f = lbm.boundary_equilibrium(f, "left", ux_wall=u0)
+            rn, un = lbm.boundary_characteristic(rho, uu, "right")
+            f = wall(f, "right", rho_wall=rn, ux_wall=un[0], uy_wall=un[1])
+            if step in (1, 8):
+                put(f"cbc2.{scheme}.f{step}", f)
+    nx, ny, nz = 12, 8, 8
+    rho0 = (1 + 0.02 * rng.normal(0.0, 1.0, (nx, ny, nz))).astype(dt)
+    u = np.zeros((3, nx, ny, nz), dt)
+    u[0] = u0 + 0.01 * rng.normal(0.0, 1.0, (nx, ny, nz))
+    u[1:] = 0.01 * rng.normal(0.0, 1.0, (2, nx, ny, nz))
+    f = lbm3d.get_equilibrium(jnp.asarray(rho0), jnp.asarray(u))
+    put("cbc3.f0", f)
+    for step in range(1, 5):
+        rho, uu = lbm3d.get_macroscopic(f)
+        f = lbm3d.streaming(lbm3d.collision_bgk(f, lbm3d.get_equilibrium(rho, uu), om))
+        f = lbm3d.boundary_equilibrium(f, "left", ux_wall=u0)
+        rn, un = lbm3d.boundary_characteristic(rho, uu, "right")
+        f = lbm3d.boundary_nee(f, "right", rho_wall=rn, ux_wall=un[0], uy_wall=un[1], uz_wall=un[2])
+        if step in (1, 4):
+            put(f"cbc3.f{step}", f)
 
 
 def recipes_2d(put, jnp, lbm, ib, dyn, dt, rng):

@@ -293,3 +293,57 @@ def test_post_oracle(mode):
             err = rel_err(np.asarray(getattr(post, name)(u)), G[f"{tag}.{name}"])
             assert err <= TOL[mode], f"{tag}.{name}: {err:.3e}"
     assert rel_err(post.pressure(G["p.rho"]), G["p.pressure"]) <= TOL[mode]
+
+
+REFINE_DIRS = ("left", "right", "up", "down")
+
+
+def test_multigrid_oracle(mode):
+    """Transfers are copies and one 4-term average: bit-exact against the reference."""
+    from oracle import multigrid as mg
+    G = golden(mode)
+    for d in REFINE_DIRS:
+        ff, fc = G[f"mg.{d}.ff"], G[f"mg.{d}.fc"]
+        assert np.array_equal(mg.fine_to_coarse(ff, fc, d), G[f"mg.{d}.f2c"]), d
+        assert np.array_equal(mg.coarse_to_fine(fc, ff, d), G[f"mg.{d}.c2f"]), d
+    assert np.array_equal(mg.coarse_to_fine(G["mg.bc.fc"], G["mg.bc.ff"], "right"), G["mg.bc.c2f"])
+    om = [mg.get_omega(nu, lv) for nu in (0.004, 0.02, 0.1) for lv in (-2, -1, 0, 1, 2, 3)]
+    assert np.array_equal(np.array(om), G["mg.omega"])
+    shapes = [mg.init_grid(w, h, lv, bx, by)[0].shape[1:] for w, h, lv, bx, by in
+              ((16, 8, 0, 1, 0), (16, 8, 1, 0, 0), (16, 8, -1, 0, 2), (10, 6, 2, 1, 1))]
+    assert np.array_equal(np.array(shapes), G["mg.init"])
+    assert mg.coord_to_indices(10.5, 7.25, 2, 3, 2) == (34, 17)
+
+
+def test_recipe_refined_channel(mode):
+    G = golden(mode)
+    fc, ff = G["rc.fc0"], G["rc.ff0"]
+    om_c, om_f, u0 = G["rc.omega"]
+    for s in range(6):
+        fc, ff = recipes.refined_channel_cycle(fc, ff, float(om_c), float(om_f), float(u0))
+        if s in (0, 5):
+            check(mode, fc, f"rc.fc{s + 1}", TOL_RECIPE[mode])
+            check(mode, ff, f"rc.ff{s + 1}", TOL_RECIPE[mode])
+
+
+@pytest.mark.parametrize("scheme", ["nee", "eq", "nebb"])
+def test_recipe_characteristic_outflow_2d(mode, scheme):
+    G = golden(mode)
+    om, u0 = (float(x) for x in G["cbc2.omega"])
+    f = G["cbc2.f0"]
+    bcs = [("eq", "left", dict(ux_wall=u0)), ("cbc", "right", dict(scheme=scheme))]
+    for step in range(1, 9):
+        f = recipes.lbm_step_2d(f, "kbc", om, bcs=bcs)
+        if step in (1, 8):
+            check(mode, f, f"cbc2.{scheme}.f{step}", TOL_RECIPE[mode])
+
+
+def test_recipe_characteristic_outflow_3d(mode):
+    G = golden(mode)
+    om, u0 = (float(x) for x in G["cbc2.omega"])
+    f = G["cbc3.f0"]
+    bcs = [("eq", "left", dict(ux_wall=u0)), ("cbc", "right", dict(scheme="nee"))]
+    for step in range(1, 5):
+        f = recipes.lbm_step_3d(f, "bgk", om, bcs=bcs)
+        if step in (1, 4):
+            check(mode, f, f"cbc3.f{step}", TOL_RECIPE[mode])

@@ -452,3 +452,79 @@ def test_moving_sphere_3d_matches_oracle(S, dt):
     assert rel_err(N(sim.f), f) <= tol
     assert rel_err(st["d"], d) <= (1e-4 if dt == "f32" else 1e-9)
     step.check()
+
+
+@pytest.mark.parametrize("scheme", ["nee", "eq", "nebb"])
+def test_characteristic_outflow_golden(S, mode, scheme):
+    """Outflow wall state from boundary_characteristic of the step's input moments, imposed
+    by NEE / equilibrium / NEBB, against the reference's functions chained the same way."""
+    G = golden(mode)
+    dt = torch.float64 if mode == "f64" else torch.float32
+    om, u0 = (float(x) for x in G["cbc2.omega"])
+    kind = {"nee": "nee", "eq": "equilibrium", "nebb": "nebb"}[scheme]
+    bcs = [S.boundary("equilibrium", "left", ux_wall=u0), S.boundary(kind, "right", mode="characteristic")]
+    for graph in (False, True):
+        step = S.LatticeStep(9, (24, 16), "kbc", om, dtype=dt, boundaries=bcs)
+        s = torch.cuda.Stream()
+        with torch.cuda.stream(s):
+            sim = S.Simulation(step, T(G["cbc2.f0"]))
+            sim.run(1, graph=graph)
+            f1 = N(sim.f)
+            sim.run(7, graph=graph)
+            torch.cuda.synchronize()
+        assert rel_err(f1, G[f"cbc2.{scheme}.f1"]) <= tol(mode, 1), graph
+        assert rel_err(N(sim.f), G[f"cbc2.{scheme}.f8"]) <= tol(mode, 8), graph
+
+
+def test_characteristic_outflow_golden_3d(S, mode):
+    G = golden(mode)
+    dt = torch.float64 if mode == "f64" else torch.float32
+    om, u0 = (float(x) for x in G["cbc2.omega"])
+    step = S.LatticeStep(19, (12, 8, 8), "bgk", om, dtype=dt,
+                         boundaries=[S.boundary("equilibrium", "left", ux_wall=u0),
+                                     S.boundary("nee", "right", mode="characteristic")])
+    sim = S.Simulation(step, T(G["cbc3.f0"]))
+    sim.run(1)
+    assert rel_err(N(sim.f), G["cbc3.f1"]) <= tol(mode, 1)
+    sim.run(3)
+    assert rel_err(N(sim.f), G["cbc3.f4"]) <= tol(mode, 4)
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_viv_characteristic_outflow_matches_oracle(S, graph):
+    """The 64 x 48 VIV case with a characteristic NEE outflow instead of the pressure NEE:
+    the moving body's kernels and the outflow's moments kernel share the step."""
+    nx, ny, D, U0, M = 64, 48, 12.0, 0.05, 38
+    om = L2.get_omega(U0 * D / 60.0)
+    th = np.linspace(0, 2 * np.pi, M, endpoint=False)
+    X0 = (20.0 + 0.5 * D * np.cos(th)).astype(np.float32)
+    Y0 = (24.0 + 0.5 * D * np.sin(th)).astype(np.float32)
+    rng = np.random.default_rng(5)
+    u = np.zeros((2, nx, ny), np.float32)
+    u[0] = U0
+    u[1] = 1e-4 * rng.standard_normal((nx, ny))
+    f0 = L2.get_equilibrium(np.ones((nx, ny), np.float32), u)
+    area = math.pi * (D / 2) ** 2
+    mass = 10 * area
+    K = (2 * math.pi * U0 / (5 * D)) ** 2 * mass * 1.1
+    ds = math.pi * D / M
+    bcs = [("eq", "left", dict(ux_wall=U0)), ("cbc", "right", dict(scheme="nee"))]
+    body_o = recipes.Body2D(X0, Y0, ds, mass, K, 0.0, area, free=(False, True), n_iter=3,
+                            v=np.array([0, 1e-3], np.float32))
+    step = S.LatticeStep(9, (nx, ny), "kbc", om, forcing="edm",
+                         boundaries=[S.boundary("equilibrium", "left", ux_wall=U0),
+                                     S.boundary("nee", "right", mode="characteristic")])
+    body = S.RigidBody(step, np.stack([X0, Y0], 1), ds, moving=True, free_dof=(False, True), mass=mass,
+                       stiffness=K, added_mass_area=area, v0=(0, 1e-3, 0))
+    f = f0
+    for _ in range(20):
+        f, h = recipes.ib_lbm_step_2d(f, body_o, "kbc", om, None, bcs)
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        sim = S.Simulation(step, T(f0), body)
+        sim.run(20, graph=graph)
+        torch.cuda.synchronize()
+    assert rel_err(N(sim.f), f) <= 1e-5
+    st = body.state()
+    assert rel_err(st["d"][:2], body_o.d) <= 1e-4
+    assert rel_err(st["h"][:2], h) <= 3e-4

@@ -26,6 +26,7 @@ UNITS = {
     "vs_step.cu": [],
     "vs_adjoint.cu": [],
     "vs_post.cu": [],
+    "vs_refine.cu": [],
 }
 
 

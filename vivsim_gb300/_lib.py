@@ -12,16 +12,18 @@ import torch
 from . import _build
 
 VS_OK = 0
+VS_ERR_INVALID_ARG = 1
 VS_F32, VS_F64 = 0, 1
 VS_COLLIDE_BGK, VS_COLLIDE_KBC, VS_COLLIDE_MRT, VS_COLLIDE_REG = 0, 1, 2, 3
 VS_FORCE_NONE, VS_FORCE_EDM, VS_FORCE_GUO_BGK, VS_FORCE_GUO_MRT = 0, 1, 2, 3
 VS_LEFT, VS_RIGHT, VS_BOTTOM, VS_TOP, VS_BACK, VS_FRONT = range(6)
 VS_BC_NEE, VS_BC_NEBB, VS_BC_EQ, VS_BC_BB, VS_BC_SPECULAR = range(5)
-VS_WALL_GIVEN, VS_WALL_VELOCITY, VS_WALL_PRESSURE, VS_WALL_FORCE_CORRECTED = range(4)
+VS_WALL_GIVEN, VS_WALL_VELOCITY, VS_WALL_PRESSURE, VS_WALL_FORCE_CORRECTED, VS_WALL_CHARACTERISTIC = range(5)
 VS_KERNEL_PESKIN3, VS_KERNEL_PESKIN4, VS_KERNEL_COSINE4 = range(3)
 VS_MAX_BC = 8
 VS_GRID_AUTO, VS_GRID_PLAIN, VS_GRID_TMA = 0, 1, 2
 
+REFINE_DIRS = {"left": 0, "right": 1, "up": 2, "down": 3}
 LOCS = {"left": VS_LEFT, "right": VS_RIGHT, "bottom": VS_BOTTOM, "top": VS_TOP, "back": VS_BACK,
         "front": VS_FRONT}
 
@@ -134,6 +136,8 @@ _SIGS = {
     "vs_adjoint_forward": (_i, [_p, _i, C.POINTER(_d), _p]),
     "vs_adjoint_backward": (_i, [_p, _d, C.POINTER(_d), C.POINTER(_d), C.POINTER(_d), _p]),
     "vs_lattice_status": (_i, [_p, _i, _p]),
+    "vs_fine_to_coarse": (_i, [_i, _p, _i, _i, _p, _i, _i, _i, _p]),
+    "vs_coarse_to_fine": (_i, [_i, _p, _i, _i, _p, _i, _i, _i, _p]),
 }
 
 _LIB = None

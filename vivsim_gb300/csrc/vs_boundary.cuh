@@ -252,6 +252,29 @@ __device__ __forceinline__ void bc_node(const WallArgs<T>& A, int64_t j, const T
   }
 }
 
+// boundary_characteristic at one face node (lbm/boundary/cbc.py:14-53, lbm3d/boundary/cbc.py:
+// 16-51) from the density r and normal velocity u of the wall (1) and the next two planes
+// (2, 3); sg is the inward normal sign.  Every product and sum is rounded on its own, in
+// the reference's order, so per-operator and fused callers agree to the bit.
+template <typename T>
+__device__ __forceinline__ void cbc_values(int sg, T cs, T r1, T r2, T r3, T u1, T u2, T u3, T& rho_next,
+                                           T& un_next) {
+  const T dc = (T)(-0.5 * sg);
+  const T drho = mul_rn(dc, add_rn(sub_rn(mul_rn(T(3), r1), mul_rn(T(4), r2)), r3));
+  const T dun = mul_rn(dc, add_rn(sub_rn(mul_rn(T(3), u1), mul_rn(T(4), u2)), u3));
+  const T sgcs = mul_rn((T)sg, cs);
+  const T cout = sub_rn(dun, mul_rn(sgcs / r1, drho));
+  const T lout = mul_rn(sub_rn(u1, sgcs), cout);
+  rho_next = sub_rn(r1, mul_rn(mul_rn(T(0.5), r1) / cs, lout));
+  un_next = sub_rn(u1, mul_rn(T(0.5), lout));
+}
+
+// the reference's sound speed of each lattice: 1 / jnp.sqrt(3) (2-D), jnp.sqrt(1 / 3) (3-D)
+template <typename T>
+__host__ __device__ inline T cbc_cs(int dim) {
+  return dim == 2 ? (T)1 / sqrt((T)3) : sqrt((T)(1.0 / 3.0));
+}
+
 template <class L>
 __host__ __device__ constexpr bool bc_needs_neighbor(int kind, int mode) {
   return kind == VS_BC_NEE || mode == VS_WALL_PRESSURE;

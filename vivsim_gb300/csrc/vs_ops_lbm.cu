@@ -169,19 +169,13 @@ __global__ void k_characteristic(int dim, int loc, const T* __restrict__ rho, co
   const int64_t n = (int64_t)nx * ny * nz;
   const int64_t nf = face_size(loc, nn);
   const int a = loc_axis(loc), sg = loc_sign(loc);
-  const T cs = dim == 2 ? (T)1 / sqrt((T)3) : sqrt((T)(1.0 / 3.0));
+  const T cs = cbc_cs<T>(dim);
   for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < nf; j += (int64_t)gridDim.x * blockDim.x) {
     const int64_t p0 = face_node(loc, nn, j, 0), p1 = face_node(loc, nn, j, 1), p2 = face_node(loc, nn, j, 2);
-    const T r1 = rho[p0], r2 = rho[p1], r3 = rho[p2];
-    const T u1 = u[a * n + p0], u2 = u[a * n + p1], u3 = u[a * n + p2];
-    const T dc = (T)(-0.5 * sg);
-    const T drho = dc * ((T(3) * r1 - T(4) * r2) + r3);
-    const T dun = dc * ((T(3) * u1 - T(4) * u2) + u3);
-    const T sgcs = (T)sg * cs;
-    const T cout = dun - (sgcs / r1) * drho;
-    const T lout = (u1 - sgcs) * cout;
-    rho_next[j] = r1 - ((T(0.5) * r1) / cs) * lout;
-    for (int d = 0; d < dim; ++d) u_next[d * nf + j] = d == a ? u1 - T(0.5) * lout : u[d * n + p0];
+    T rn, un;
+    cbc_values<T>(sg, cs, rho[p0], rho[p1], rho[p2], u[a * n + p0], u[a * n + p1], u[a * n + p2], rn, un);
+    rho_next[j] = rn;
+    for (int d = 0; d < dim; ++d) u_next[d * nf + j] = d == a ? un : u[d * n + p0];
   }
 }
 

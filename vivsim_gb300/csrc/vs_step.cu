@@ -1772,6 +1772,7 @@ struct vs_lattice_plan {
   int dim;
   int64_t n;
   void* pre_buf[VS_MAX_BC];  // bounce-back face buffers
+  void* cbc_buf[VS_MAX_BC];  // characteristic walls: rho_next, u_next (1 + dim face arrays)
   int bc_group[VS_MAX_BC];   // group id of each boundary op
   int n_groups;
   int lazy_ok;               // all boundaries in one launch group and none needs pre-stream data
@@ -1838,6 +1839,8 @@ static void free_lattice(vs_lattice_plan* p) {
   if (!p) return;
   for (int k = 0; k < VS_MAX_BC; ++k)
     if (p->pre_buf[k]) cudaFree(p->pre_buf[k]);
+  for (int k = 0; k < VS_MAX_BC; ++k)
+    if (p->cbc_buf[k]) cudaFree(p->cbc_buf[k]);
   if (p->graph) cudaGraphExecDestroy(p->graph);
   if (p->d_status) cudaFree(p->d_status);
   delete p;
@@ -1867,6 +1870,18 @@ static WallArgs<T> wall_args_from_bc(const vs_bc& bc, const vs_lattice_plan* L, 
   A.n[1] = L->cfg.ny;
   A.n[2] = L->cfg.nz;
   double rho = bc.rho, u3[3] = {bc.ux, bc.uy, bc.uz};
+  if (bc.mode == VS_WALL_CHARACTERISTIC) {  // wall data per node, written by k_cbc_face this step
+    const int64_t nf = face_size(bc.loc, A.n);
+    const T* buf = (const T*)L->cbc_buf[k];
+    A.mode = VS_WALL_GIVEN;
+    A.rho_arr = buf;
+    for (int d = 0; d < L->dim; ++d) A.u_arr[d] = buf + (1 + d) * nf;
+    const double zero[3] = {0.0, 0.0, 0.0};
+    wall_args_scalars(A, 1.0, zero, L->dim);
+    A.un_scalar = 0;
+    A.all_scalar = 0;
+    return A;
+  }
   if (bc.mode == VS_WALL_FORCE_CORRECTED) {
     const double g3[3] = {bc.gx, bc.gy, bc.gz};
     for (int d = 0; d < 3; ++d) u3[d] = u3[d] - (g3[d] * 0.5) / rho;
@@ -1878,6 +1893,61 @@ static WallArgs<T> wall_args_from_bc(const vs_bc& bc, const vs_lattice_plan* L, 
   A.pre_stride = face_size(bc.loc, A.n);
   A.pre_face = 1;
   return A;
+}
+
+// Characteristic walls: rho_next and u_next of every face node from the step's INPUT
+// populations (the moments a composed step takes with get_macroscopic before colliding) at
+// the wall and the next two planes, into the plan's face buffer; the face epilogue then
+// imposes them with the boundary's scheme.  A masked node whose obstacle bounce-back is
+// still pending (applied on load) is swapped first, as the grid kernel does.
+template <class L, typename T>
+__global__ void k_cbc_face(const T* __restrict__ f, int nx, int ny, int nz, int loc, const uint8_t* mask,
+                           int mask_load, T* __restrict__ buf) {
+  const int nn[3] = {nx, ny, nz};
+  const int64_t n = (int64_t)nx * ny * nz;
+  const int64_t nf = face_size(loc, nn);
+  const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (j >= nf) return;
+  const int a = loc_axis(loc), sg = loc_sign(loc);
+  T r[3], un[3], u0[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const int64_t p = face_node(loc, nn, j, k);
+    const bool swap = mask_load && mask && mask[p];
+    T fl[L::Q], rr, uu[3] = {T(0), T(0), T(0)};
+#pragma unroll
+    for (int i = 0; i < L::Q; ++i) fl[i] = f[(int64_t)(swap ? L::opp(i) : i) * n + p];
+    macro(L{}, fl, rr, uu);
+    r[k] = rr;
+    un[k] = uu[a];
+    if (k == 0)
+#pragma unroll
+      for (int d = 0; d < 3; ++d) u0[d] = uu[d];
+  }
+  T rn, vn;
+  cbc_values<T>(sg, cbc_cs<T>(L::D), r[0], r[1], r[2], un[0], un[1], un[2], rn, vn);
+  buf[j] = rn;
+#pragma unroll
+  for (int d = 0; d < L::D; ++d) buf[(1 + d) * nf + j] = d == a ? vn : u0[d];
+}
+
+static int enqueue_cbc(const vs_lattice_plan* LP, const void* fin, cudaStream_t st) {
+  const vs_lattice_cfg& c = LP->cfg;
+  for (int k = 0; k < c.n_bc; ++k) {
+    if (c.bc[k].mode != VS_WALL_CHARACTERISTIC) continue;
+    const int nn[3] = {c.nx, c.ny, c.nz};
+    const int64_t nf = face_size(c.bc[k].loc, nn);
+    int rc = dispatch(c.q, c.dtype, [&](auto l, auto t) -> int {
+      using LL = decltype(l);
+      using T = typename decltype(t)::type;
+      k_cbc_face<LL, T><<<grid_for(nf, 128), 128, 0, st>>>((const T*)fin, c.nx, c.ny, c.nz, c.bc[k].loc,
+                                                           c.obstacle_mask, LP->bb_load, (T*)LP->cbc_buf[k]);
+      VS_CHECK_LAUNCH("vs_step characteristic wall");
+      return VS_OK;
+    });
+    if (rc) return rc;
+  }
+  return VS_OK;
 }
 
 static int enqueue_bcs(const vs_lattice_plan* L, void* f, cudaStream_t st) {
@@ -2320,6 +2390,8 @@ static int enqueue_step(const vs_lattice_plan* LP, vs_body_plan* B, const void* 
                         bool bb_out = true) {
   int rc;
   const_cast<vs_lattice_plan*>(LP)->bb_load = bb_in ? 1 : 0;  // read by make_step_params below
+  rc = enqueue_cbc(LP, fin, st);
+  if (rc) return rc;
   if (B && B->cluster) {
     cudaError_t e = cudaEventRecord(B->ev_fork, st);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(B->side, B->ev_fork, 0);
@@ -2409,7 +2481,9 @@ int vs_lattice_plan_create(const vs_lattice_cfg* cfg, vs_lattice_plan** out) {
     const vs_bc& b = cfg->bc[k];
     VS_REQUIRE(b.loc >= 0 && b.loc < 2 * dim, "boundary %d: loc %d invalid", k, b.loc);
     VS_REQUIRE(b.kind >= VS_BC_NEE && b.kind <= VS_BC_SPECULAR, "boundary %d: bad kind", k);
-    VS_REQUIRE(b.mode >= VS_WALL_GIVEN && b.mode <= VS_WALL_FORCE_CORRECTED, "boundary %d: bad mode", k);
+    VS_REQUIRE(b.mode >= VS_WALL_GIVEN && b.mode <= VS_WALL_CHARACTERISTIC, "boundary %d: bad mode", k);
+    VS_REQUIRE(b.mode != VS_WALL_CHARACTERISTIC || b.kind == VS_BC_NEE || b.kind == VS_BC_NEBB || b.kind == VS_BC_EQ,
+               "boundary %d: a characteristic wall is imposed by NEE, NEBB or equilibrium", k);
     VS_REQUIRE(!((b.kind == VS_BC_BB || b.kind == VS_BC_SPECULAR) && b.mode != VS_WALL_GIVEN),
                "boundary %d: bounce-back takes no wall mode", k);
   }
@@ -2425,6 +2499,13 @@ int vs_lattice_plan_create(const vs_lattice_cfg* cfg, vs_lattice_plan** out) {
   const int nn[3] = {cfg->nx, cfg->ny, nz};
   for (int k = 0; k < cfg->n_bc; ++k) {
     const vs_bc& b = cfg->bc[k];
+    if (b.mode == VS_WALL_CHARACTERISTIC) {
+      cudaError_t e = cudaMalloc(&p->cbc_buf[k], dsize(cfg->dtype) * (1 + dim) * face_size(b.loc, nn));
+      if (e != cudaSuccess) {
+        free_lattice(p);
+        return cuda_status(e, "vs_lattice_plan_create");
+      }
+    }
     if (b.kind == VS_BC_BB || b.kind == VS_BC_SPECULAR) {
       cudaError_t e = cudaMalloc(&p->pre_buf[k], dsize(cfg->dtype) * cfg->q * face_size(b.loc, nn));
       if (e != cudaSuccess) {
@@ -2463,7 +2544,9 @@ int vs_lattice_plan_create(const vs_lattice_cfg* cfg, vs_lattice_plan** out) {
   }
   p->lazy_ok = p->n_groups == 1;
   for (int k = 0; k < cfg->n_bc; ++k)
-    if (cfg->bc[k].kind == VS_BC_BB || cfg->bc[k].kind == VS_BC_SPECULAR) p->lazy_ok = 0;
+    if (cfg->bc[k].kind == VS_BC_BB || cfg->bc[k].kind == VS_BC_SPECULAR ||
+        cfg->bc[k].mode == VS_WALL_CHARACTERISTIC)
+      p->lazy_ok = 0;
   *out = p;
   return VS_OK;
 }
@@ -3175,6 +3258,11 @@ int vs_batch_plan_create(vs_lattice_plan* const* lattices, vs_body_plan* const* 
       set_error("vs_batch_plan_create: case %d has an obstacle mask (not supported in a batch)", k);
       return fail(VS_ERR_UNSUPPORTED);
     }
+    for (int b = 0; b < Lk->cfg.n_bc; ++b)
+      if (Lk->cfg.bc[b].mode == VS_WALL_CHARACTERISTIC) {
+        set_error("vs_batch_plan_create: case %d has a characteristic wall (not supported in a batch)", k);
+        return fail(VS_ERR_UNSUPPORTED);
+      }
     if (k == 0) {
       bp->q = Lk->cfg.q;
       bp->dtype = Lk->cfg.dtype;

@@ -21,7 +21,7 @@ FORCINGS = {"none": V.VS_FORCE_NONE, "edm": V.VS_FORCE_EDM, "guo_bgk": V.VS_FORC
 BC_KINDS = {"nee": V.VS_BC_NEE, "nebb": V.VS_BC_NEBB, "equilibrium": V.VS_BC_EQ, "eq": V.VS_BC_EQ,
             "bounce_back": V.VS_BC_BB, "specular_reflection": V.VS_BC_SPECULAR}
 WALL_MODES = {"given": V.VS_WALL_GIVEN, "velocity": V.VS_WALL_VELOCITY, "pressure": V.VS_WALL_PRESSURE,
-              "force_corrected": V.VS_WALL_FORCE_CORRECTED}
+              "force_corrected": V.VS_WALL_FORCE_CORRECTED, "characteristic": V.VS_WALL_CHARACTERISTIC}
 KERNELS = {"peskin3": V.VS_KERNEL_PESKIN3, "peskin4": V.VS_KERNEL_PESKIN4, "cosine4": V.VS_KERNEL_COSINE4}
 
 
@@ -31,7 +31,10 @@ def boundary(kind, loc, mode="given", rho_wall=1.0, ux_wall=0.0, uy_wall=0.0, uz
 
     ``kind`` names the reference scheme (boundary_nee / _nebb / _equilibrium /
     _bounce_back / _specular_reflection) and ``mode`` its wrapper (velocity / pressure /
-    force_corrected, lbm/boundary/_helpers.py:175-239).
+    force_corrected, lbm/boundary/_helpers.py:175-239).  ``mode="characteristic"`` takes
+    the wall density and velocity of every face node from boundary_characteristic
+    (lbm/boundary/cbc.py:14-53) of the step's input moments: a non-reflective outflow,
+    imposed by the nee, nebb or equilibrium scheme.
     """
     return dict(kind=kind, loc=loc, mode=mode, rho=rho_wall, ux=ux_wall, uy=uy_wall, uz=uz_wall, gx=gx_wall,
                 gy=gy_wall, gz=gz_wall)
@@ -284,3 +287,102 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+class Refined:
+    """Blocks of several refinement levels (vivsim/multigrid.py) advanced together.
+
+    ``blocks`` are Simulations, one per block, each with its own LatticeStep (omega from
+    ``multigrid.get_omega(nu, level)``, the block's own face boundaries); ``levels`` their
+    refinement levels; ``links`` (coarse, fine, side) pairs of block indices whose levels
+    differ by one, ``side`` being where the fine block lies relative to the coarse one
+    ('left', 'right', 'up', 'down').  The coarse block carries the buffer line on that side.
+
+    One cycle advances the coarsest level by one step, and level L by 2**(L - L_min) steps,
+    recursively: the blocks of a level step (collide, stream, their boundaries); the
+    coarse_to_fine transfer into each of them from its coarser neighbour's new state;
+    then the next finer level runs two cycles and fine_to_coarse refills this level's
+    buffer lines.  For one coarse and one fine block this is oracle/recipes.py's
+    refined_channel_cycle.  With ``graph=True`` two cycles (which bring every ping-pong
+    buffer back to where it started) are captured once into a CUDA graph and replayed.
+    """
+
+    _F2C = {"right": "left", "left": "right", "up": "down", "down": "up"}
+
+    def __init__(self, blocks, levels, links):
+        from . import multigrid as _mg
+        self._mg = _mg
+        self.blocks = list(blocks)
+        self.levels = [int(x) for x in levels]
+        if len(self.levels) != len(self.blocks) or not self.blocks:
+            raise ValueError("one level per block, at least one block")
+        for b in self.blocks:
+            if b.step.q != 9 or b.body is not None:
+                raise ValueError("refined blocks are D2Q9 lattices without bodies (vivsim/multigrid.py)")
+        self.links = []
+        for c, f, side in links:
+            if side not in self._F2C:
+                raise ValueError("side must be one of 'left', 'right', 'up', 'down'")
+            if self.levels[f] != self.levels[c] + 1:
+                raise ValueError("a link joins a block to a block exactly one level finer")
+            self.links.append((int(c), int(f), side))
+        self.lmin, self.lmax = min(self.levels), max(self.levels)
+        self._graph = None
+        self._graph_parity = None
+
+    def f(self, i):
+        return self.blocks[i].f
+
+    def _step(self, i):
+        b = self.blocks[i]
+        src, dst = (b._a, b._b) if b._cur_is_a else (b._b, b._a)
+        V.call("vs_step", b.step.handle, None, V.ptr(src), V.ptr(dst), None, V.stream())
+        b._cur_is_a = not b._cur_is_a
+
+    def _cycle(self, level):
+        for i, lv in enumerate(self.levels):
+            if lv == level:
+                self._step(i)
+        for c, f, side in self.links:
+            if self.levels[f] == level:
+                self._mg.transfer_("coarse_to_fine", self.f(c), self.f(f), side)
+        if level < self.lmax:
+            self._cycle(level + 1)
+            self._cycle(level + 1)
+            for c, f, side in self.links:
+                if self.levels[c] == level:
+                    self._mg.transfer_("fine_to_coarse", self.f(f), self.f(c), self._F2C[side])
+
+    def _parity(self):
+        return tuple(b._cur_is_a for b in self.blocks)
+
+    def run(self, n_cycles, graph=False):
+        """Advance n_cycles steps of the coarsest level."""
+        n = int(n_cycles)
+        if not graph:
+            for _ in range(n):
+                self._cycle(self.lmin)
+            return
+        while n > 0:
+            if self._graph is None and n >= 3:
+                self._cycle(self.lmin)  # first launches (lazy attributes) outside the capture
+                n -= 1
+                g = torch.cuda.CUDAGraph()
+                s = torch.cuda.Stream()
+                s.wait_stream(torch.cuda.current_stream())
+                with torch.cuda.stream(s):
+                    saved = self._parity()
+                    g.capture_begin()
+                    self._cycle(self.lmin)
+                    self._cycle(self.lmin)
+                    g.capture_end()
+                    for b, p in zip(self.blocks, saved):  # capture launched nothing
+                        b._cur_is_a = p
+                torch.cuda.current_stream().wait_stream(s)
+                self._graph, self._graph_parity = g, saved
+            if self._graph is not None and n >= 2 and self._parity() == self._graph_parity:
+                self._graph.replay()
+                n -= 2
+            else:
+                self._cycle(self.lmin)
+                n -= 1
