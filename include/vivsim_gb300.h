@@ -230,7 +230,11 @@ int vs_lattice_plan_destroy(vs_lattice_plan* plan);
 int vs_lattice_status(const vs_lattice_plan* plan, int reset, void* stream);
 
 /* Immersed body advanced by the IB step (dyn.py + ib/mdf.py).  Markers follow a rigid
- * 2-DOF translation d (get_markers_coords_2dof); DOFs with free[k] = 0 stay at zero. */
+ * translation d (get_markers_coords_2dof); DOFs with free[k] = 0 stay at zero.  In 2-D,
+ * free_dof[2] = 1 adds a rotation by the angle d[2] about (center_x, center_y): markers
+ * from get_markers_coords_3dof, MDF target velocities from get_markers_velocity_3dof, the
+ * torque from get_torque_to_obj (dyn.py:84-154), h[2] = torque + a[2] * added_inertia and
+ * Newmark with (inertia, rot_stiffness, rot_damping). */
 typedef struct vs_body_cfg {
   int dim;        /* 2 or 3, must match the lattice                                    */
   int dtype;
@@ -244,10 +248,12 @@ typedef struct vs_body_cfg {
   int radius;            /* stencil half-width (2 for the 4-point kernels)             */
   int n_iter;            /* MDF iterations                                             */
   int moving;            /* 0: stencil built once (fixed body), 1: rebuilt every step  */
-  int free_dof[3];       /* Newmark-integrated translational DOFs                      */
+  int free_dof[3];       /* Newmark-integrated DOFs: x, y, z (3-D) or x, y, angle (2-D)  */
   double mass, stiffness, damping, added_mass_area; /* h += a * area, vortex_induced_vibration.py:136 */
   double d0[3], v0[3], a0[3];                       /* initial body state                 */
   int window_margin;     /* extra nodes around the marker stencils reserved for motion */
+  double center_x, center_y;                 /* 2-D rotation: initial centre of the body  */
+  double inertia, rot_stiffness, rot_damping, added_inertia;
 } vs_body_cfg;
 
 typedef struct vs_body_plan vs_body_plan;

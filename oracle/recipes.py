@@ -96,18 +96,28 @@ def lbm_step_2d(f, collision, omega=None, mrt_op=None, bcs=(), g=None, forcing="
 
 
 class Body2D:
-    """Rigid 2-DOF body carried between steps: markers relative to a displacement d."""
+    """Rigid body carried between steps: markers relative to a displacement d.
+
+    ``free`` has two entries (x, y translation) or three; a free third DOF is the rotation
+    angle about ``center`` (dyn.get_markers_coords_3dof), integrated with ``inertia``,
+    ``rot_k``, ``rot_c`` and the added inertia ``rot_added``.
+    """
 
     def __init__(self, X0, Y0, ds, mass, stiffness, damping, area, free=(False, True),
-                 kernel="peskin4", radius=2, n_iter=3, d=None, v=None, a=None):
+                 kernel="peskin4", radius=2, n_iter=3, d=None, v=None, a=None, center=None, inertia=0.0,
+                 rot_k=0.0, rot_c=0.0, rot_added=0.0):
         self.X0, self.Y0 = np.asarray(X0), np.asarray(Y0)
         self.ds, self.mass, self.k, self.c, self.area = ds, mass, stiffness, damping, area
         self.free = tuple(bool(x) for x in free)
+        self.rot = len(self.free) > 2 and self.free[2]
+        self.center = center
+        self.inertia, self.rot_k, self.rot_c, self.rot_added = inertia, rot_k, rot_c, rot_added
         self.kernel, self.radius, self.n_iter = kernel, radius, n_iter
         dt = self.X0.dtype
-        self.d = np.zeros(2, dt) if d is None else np.asarray(d, dt)
-        self.v = np.zeros(2, dt) if v is None else np.asarray(v, dt)
-        self.a = np.zeros(2, dt) if a is None else np.asarray(a, dt)
+        nd = 3 if self.rot else 2
+        self.d = np.zeros(nd, dt) if d is None else np.asarray(d, dt)
+        self.v = np.zeros(nd, dt) if v is None else np.asarray(v, dt)
+        self.a = np.zeros(nd, dt) if a is None else np.asarray(a, dt)
 
 
 def ib_lbm_step_2d(f, body, collision, omega=None, mrt_op=None, bcs=()):
@@ -121,17 +131,26 @@ def ib_lbm_step_2d(f, body, collision, omega=None, mrt_op=None, bcs=()):
     rho, u = L2.get_macroscopic(f)
     feq = L2.get_equilibrium(rho, u)
     f = _collide(L2, f, feq, collision, omega, mrt_op)
-    mx, my = dyn.get_markers_coords_2dof(body.X0, body.Y0, body.d)
-    W, I = ib.get_ib_stencil(mx, my, ny, ib.KERNELS[body.kernel], body.radius)
     M = body.X0.shape[0]
-    mv = np.repeat(body.v[None, :], M, axis=0)
+    if body.rot:  # markers turn with d[2] about the initial centre (dyn.py:84-120)
+        cx, cy = body.center
+        mx, my = dyn.get_markers_coords_3dof(body.X0, body.Y0, cx, cy, body.d)
+        mv = dyn.get_markers_velocity_3dof(mx, my, cx, cy, body.d, body.v)
+    else:
+        mx, my = dyn.get_markers_coords_2dof(body.X0, body.Y0, body.d)
+        mv = np.repeat(body.v[None, :], M, axis=0)
+    W, I = ib.get_ib_stencil(mx, my, ny, ib.KERNELS[body.kernel], body.radius)
     g, mh = ib.multi_direct_forcing(u, W, I, mv, body.ds, body.n_iter)
     h = dyn.get_force_to_obj(mh)
-    h = h + body.a * body.area
+    h = h + body.a[:2] * body.area
+    if body.rot:  # torque (dyn.py:139-154) plus added inertia
+        tq = dyn.get_torque_to_obj(mx, my, cx, cy, body.d, mh)
+        h = np.concatenate([h, np.asarray([tq + body.a[2] * body.rot_added], h.dtype)])
     a, v, d = body.a.copy(), body.v.copy(), body.d.copy()
-    for k in range(2):
+    for k in range(len(body.d)):
         if body.free[k]:
-            a[k], v[k], d[k] = dyn.newmark(body.a[k], body.v[k], body.d[k], h[k], body.mass, body.k, body.c)
+            m, kk, c = (body.mass, body.k, body.c) if k < 2 else (body.inertia, body.rot_k, body.rot_c)
+            a[k], v[k], d[k] = dyn.newmark(body.a[k], body.v[k], body.d[k], h[k], m, kk, c)
     body.a, body.v, body.d = a, v, d
     f = L2.forcing_edm(f, g, u)
     f_post = f

@@ -528,3 +528,72 @@ def test_viv_characteristic_outflow_matches_oracle(S, graph):
     st = body.state()
     assert rel_err(st["d"][:2], body_o.d) <= 1e-4
     assert rel_err(st["h"][:2], h) <= 3e-4
+
+
+def _rotating_ellipse(S, npdt, steps, graph=False):
+    """Ellipse (semi-axes 8 and 4) free to move in y and to turn against a torsional spring,
+    KBC, equilibrium inflow, pressure-NEE outflow; fused run and oracle run."""
+    tdt = torch.float32 if npdt == np.float32 else torch.float64
+    nx, ny, U0, M = 64, 48, 0.05, 40
+    om = L2.get_omega(U0 * 16.0 / 60.0)
+    th = np.linspace(0, 2 * np.pi, M, endpoint=False)
+    X0 = (24.0 + 8.0 * np.cos(th)).astype(npdt)
+    Y0 = (24.0 + 4.0 * np.sin(th)).astype(npdt)
+    rng = np.random.default_rng(8)
+    u = np.zeros((2, nx, ny), npdt)
+    u[0] = U0
+    u[1] = 1e-4 * rng.standard_normal((nx, ny))
+    f0 = L2.get_equilibrium(np.ones((nx, ny), npdt), u).astype(npdt)
+    area = math.pi * 8 * 4
+    mass = 10 * area
+    inertia = mass * (64 + 16) / 4
+    K = (2 * math.pi * U0 / 80) ** 2 * mass
+    Kr = (2 * math.pi * U0 / 60) ** 2 * inertia
+    ds = 1.2
+    bcs = [("eq", "left", dict(ux_wall=U0)), ("pnee", "right", dict(rho_wall=1.0))]
+    body_o = recipes.Body2D(X0, Y0, ds, mass, K, 0.0, area, free=(False, True, True), n_iter=3,
+                            v=np.array([0, 1e-3, 2e-3], npdt), center=(24.0, 24.0), inertia=inertia, rot_k=Kr,
+                            rot_c=0.0, rot_added=0.5 * inertia)
+    f = f0
+    hist_o = []
+    for _ in range(steps):
+        f, h = recipes.ib_lbm_step_2d(f, body_o, "kbc", om, None, bcs)
+        hist_o.append(h)
+    step = S.LatticeStep(9, (nx, ny), "kbc", om, dtype=tdt, forcing="edm",
+                         boundaries=[S.boundary("equilibrium", "left", ux_wall=U0),
+                                     S.boundary("nee", "right", mode="pressure", rho_wall=1.0)])
+    body = S.RigidBody(step, np.stack([X0, Y0], 1), ds, moving=True, free_dof=(False, True, True), mass=mass,
+                       stiffness=K, added_mass_area=area, v0=(0, 1e-3, 2e-3), center=(24.0, 24.0),
+                       inertia=inertia, rot_stiffness=Kr, added_inertia=0.5 * inertia)
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        sim = S.Simulation(step, T(f0), body)
+        hist = sim.run(steps, graph=graph, force_history=True)
+        torch.cuda.synchronize()
+    return (N(sim.f), body.state(), N(hist)), (f, body_o, np.array(hist_o))
+
+
+@pytest.mark.parametrize("dt", ["f32", "f64"])
+def test_rotating_body_matches_oracle(S, dt, monkeypatch):
+    """A body with a free rotation (get_markers_coords_3dof / get_markers_velocity_3dof /
+    get_torque_to_obj) in the fused step against the oracle, in each body-kernel form; the
+    three forms give identical bits."""
+    npdt = np.float32 if dt == "f32" else np.float64
+    tf, tst, th = (1e-5, 1e-4, 1e-3) if dt == "f32" else (1e-11, 1e-10, 1e-9)
+    runs = {}
+    for form, env in (("cluster", None), ("single", "VIVSIM_GB300_BODY_SINGLE"), ("general", "VIVSIM_GB300_BODY_CSR")):
+        if env:
+            monkeypatch.setenv(env, "1")
+        (fg, st, hist), (fo, body_o, hist_o) = _rotating_ellipse(S, npdt, 20)
+        if env:
+            monkeypatch.delenv(env)
+        assert rel_err(fg, fo) <= tf, form
+        assert rel_err(st["d"], body_o.d) <= tst, form
+        assert abs(st["d"][2]) > 1e-3, "the body must have turned"
+        assert rel_err(hist, hist_o) <= th, form
+        runs[form] = (fg, hist)
+    for form in ("single", "general"):
+        assert np.array_equal(runs["cluster"][0], runs[form][0]), form
+        assert np.array_equal(runs["cluster"][1], runs[form][1]), form
+    (fgr, _, _), _ = _rotating_ellipse(S, npdt, 20, graph=True)
+    assert np.array_equal(runs["cluster"][0], fgr)

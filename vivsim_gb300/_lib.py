@@ -65,7 +65,10 @@ class vs_body_cfg(C.Structure):
                 ("mass", C.c_double), ("stiffness", C.c_double), ("damping", C.c_double),
                 ("added_mass_area", C.c_double),
                 ("d0", C.c_double * 3), ("v0", C.c_double * 3), ("a0", C.c_double * 3),
-                ("window_margin", C.c_int)]
+                ("window_margin", C.c_int),
+                ("center_x", C.c_double), ("center_y", C.c_double),
+                ("inertia", C.c_double), ("rot_stiffness", C.c_double), ("rot_damping", C.c_double),
+                ("added_inertia", C.c_double)]
 
 
 class vs_adjoint_cfg(C.Structure):

@@ -456,9 +456,112 @@ struct BodyParams {
   T* force_hist;
   int free_dof[3];
   T k1, k2, c1, c2, dt, damp, stiff, den, area;
+  int rot;                                   // free rotation about (cx, cy): DOF 2 is the angle
+  T cx, cy;                                  // initial centre of the body
+  T rot_damp, rot_stiff, rot_den, rot_added;  // rotational Newmark constants, added inertia
 };
 
 constexpr int kBodyThreads = 512;
+
+// Rigid 2-D body kinematics (vivsim/dyn.py:68-120): the markers translate with d
+// (get_markers_coords_2dof) or, with the rotation free, also turn by d[2] about the initial
+// centre (get_markers_coords_3dof) and move with get_markers_velocity_3dof.  Products and
+// sums are rounded one at a time in the reference's order.
+template <typename T>
+struct Kin2 {
+  T d0, d1, v0, v1, v2, cs, sn, cx, cy;
+  int rot;
+  __device__ __forceinline__ Kin2(const BodyParams<T>& B, const T* d, const T* v)
+      : d0(d[0]), d1(d[1]), v0(v[0]), v1(v[1]), v2(v[2]), cs(T(1)), sn(T(0)), cx(B.cx), cy(B.cy), rot(B.rot) {
+    if (rot) {
+      cs = cos(d[2]);
+      sn = sin(d[2]);
+    }
+  }
+  // marker position
+  __device__ __forceinline__ void xy(const BodyParams<T>& B, int m, T& x, T& y) const {
+    if (!rot) {
+      x = B.X0[m] + d0;
+      y = B.Y0[m] + d1;
+      return;
+    }
+    const T xr = sub_rn(B.X0[m], cx), yr = sub_rn(B.Y0[m], cy);
+    x = sub_rn(add_rn(add_rn(cx, d0), mul_rn(xr, cs)), mul_rn(yr, sn));
+    y = add_rn(add_rn(add_rn(cy, d1), mul_rn(xr, sn)), mul_rn(yr, cs));
+  }
+  // MDF target velocity of a marker at (x, y), component c
+  __device__ __forceinline__ T target(T x, T y, int c) const {
+    if (!rot) return c == 0 ? v0 : v1;
+    if (c == 0) return sub_rn(v0, mul_rn(v2, sub_rn(sub_rn(y, cy), d1)));
+    return add_rn(v1, mul_rn(v2, sub_rn(sub_rn(x, cx), d0)));
+  }
+  __device__ __forceinline__ T target(const BodyParams<T>& B, int m, int c) const {
+    if (!rot) return c == 0 ? v0 : v1;
+    T x, y;
+    xy(B, m, x, y);
+    return target(x, y, c);
+  }
+};
+
+// Warp 0 ends the body step: the force h = sum_m(-F_total) in a fixed tree (dyn.py:126-136);
+// with the rotation free, the torque sum_m(x_rel h_y - y_rel h_x) (dyn.py:139-154); added
+// mass h += a A (vortex_induced_vibration.py:136) and added inertia; Newmark per free DOF
+// (dyn.py:5-51).  Ft holds every marker's total MDF force.
+template <typename T>
+__device__ __forceinline__ void body2d_finish(const BodyParams<T>& B, const Kin2<T>& K, const T* Ft, int M,
+                                              const T* a, const T* v, const T* d) {
+  const int tid = threadIdx.x;
+  T h[3];
+#pragma unroll
+  for (int c = 0; c < 2; ++c) {
+    T acc = T(0);
+    for (int m = tid; m < M; m += 32) acc = m == tid ? -Ft[2 * m + c] : acc + (-Ft[2 * m + c]);
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) acc = acc + __shfl_down_sync(0xffffffffu, acc, o);
+    h[c] = acc;
+  }
+  h[2] = T(0);
+  if (K.rot) {
+    const T ox = add_rn(K.cx, K.d0), oy = add_rn(K.cy, K.d1);
+    T acc = T(0);
+    for (int m = tid; m < M; m += 32) {
+      T x, y;
+      K.xy(B, m, x, y);
+      const T t = sub_rn(mul_rn(sub_rn(x, ox), -Ft[2 * m + 1]), mul_rn(sub_rn(y, oy), -Ft[2 * m]));
+      acc = m == tid ? t : acc + t;
+    }
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) acc = acc + __shfl_down_sync(0xffffffffu, acc, o);
+    h[2] = acc;
+  }
+#pragma unroll
+  for (int c = 0; c < 3; ++c) h[c] = __shfl_sync(0xffffffffu, h[c], 0);
+  if (tid < 3) {
+    const int c = tid;
+    if (c == 2 && !K.rot) {
+      B.state[9 + 2] = T(0);
+      if (B.force_hist) B.force_hist[2] = T(0);
+      return;
+    }
+    const T ac = a[c], vc = v[c], dc = d[c];
+    const T hh = add_rn(h[c], mul_rn(ac, c < 2 ? B.area : B.rot_added));
+    T an = ac, vn = vc, dn = dc;
+    if (B.free_dof[c]) {
+      const T damp = c < 2 ? B.damp : B.rot_damp, stiff = c < 2 ? B.stiff : B.rot_stiff;
+      const T den = c < 2 ? B.den : B.rot_den;
+      const T v1 = add_rn(vc, mul_rn(B.k1, ac));
+      const T v2 = add_rn(add_rn(dc, mul_rn(B.dt, vc)), mul_rn(B.k2, ac));
+      an = sub_rn(sub_rn(hh, mul_rn(damp, v1)), mul_rn(stiff, v2)) / den;
+      vn = add_rn(mul_rn(B.c1, an), v1);
+      dn = add_rn(mul_rn(B.c2, an), v2);
+    }
+    B.state[c] = an;
+    B.state[3 + c] = vn;
+    B.state[6 + c] = dn;
+    B.state[9 + c] = hh;
+    if (B.force_hist) B.force_hist[c] = hh;
+  }
+}
 
 // Block scan over the window cells: cnt[k] pairs per cell -> CSR.  Writes, per cell,
 // the scatter cursor (first sorted position, into cnt[]) and the touched-node slot (or -1,
@@ -588,13 +691,14 @@ __global__ void __launch_bounds__(kBodyThreads) k_body2d(const __grid_constant__
   }
 
   // one round trip: state, last corner, marker coordinates
-  T a[2], v[2], d[2];
+  T a[3], v[3], d[3];
 #pragma unroll
-  for (int c = 0; c < 2; ++c) {
+  for (int c = 0; c < 3; ++c) {
     a[c] = B.state[c];
     v[c] = B.state[3 + c];
     d[c] = B.state[6 + c];
   }
+  const Kin2<T> kin(B, d, v);
   const int ox = B.meta[META_PX] - 1, oy = B.meta[META_PY] - 1;  // region corner
   const int ya = oy >= 0 ? oy - oy % AL : 0;                     // 16-byte aligned row start
   const int64_t n = (int64_t)B.nx * B.ny;
@@ -624,7 +728,9 @@ __global__ void __launch_bounds__(kBodyThreads) k_body2d(const __grid_constant__
   // values per axis, one thread per (marker, axis, offset)
   for (int t = tid; t < M * 2 * WD; t += nt) {
     const int m = t / (2 * WD), r = t - m * (2 * WD), ax = r / WD, o = r - ax * WD;
-    const T xm = (ax == 0 ? B.X0[m] : B.Y0[m]) + d[ax];
+    T px, py;
+    kin.xy(B, m, px, py);
+    const T xm = ax == 0 ? px : py;
     const int fx = ifloor(xm);
     (ax == 0 ? wx : wy)[m * WD + o] = delta(B.kernel, (T)(fx + o - R + 1) - xm);
     if (o == 0) {
@@ -710,7 +816,7 @@ __global__ void __launch_bounds__(kBodyThreads) k_body2d(const __grid_constant__
     if ((t & (LN - 1)) == 0) {
       U[q] = acc;
       const T d2 = B.ds_arr ? B.ds_arr[m] * T(2) : B.ds2_scalar;
-      const T fs = mul_rn(v[c] - acc, d2);
+      const T fs = mul_rn(kin.target(B, m, c) - acc, d2);
       Fs[q] = fs;
       Ft[q] = B.n_iter > 0 ? fs : T(0);
     }
@@ -741,7 +847,7 @@ __global__ void __launch_bounds__(kBodyThreads) k_body2d(const __grid_constant__
         const T uq = U[q] + acc;
         U[q] = uq;
         const T d2 = B.ds_arr ? B.ds_arr[m] * T(2) : B.ds2_scalar;
-        const T fs = mul_rn(v[c] - uq, d2);
+        const T fs = mul_rn(kin.target(B, m, c) - uq, d2);
         Fs[q] = fs;
         Ft[q] = Ft[q] + fs;
       }
@@ -776,40 +882,7 @@ __global__ void __launch_bounds__(kBodyThreads) k_body2d(const __grid_constant__
   }
   // total force h = sum_m(-F_total) (dyn.py:126-136) by warp 0 in a fixed tree, added
   // mass h += a A (vortex_induced_vibration.py:136), Newmark update (dyn.py:5-51)
-  if (tid < 32) {
-    T h[2];
-#pragma unroll
-    for (int c = 0; c < 2; ++c) {
-      T acc = T(0);
-      for (int m = tid; m < M; m += 32) acc = m == tid ? -Ft[2 * m + c] : acc + (-Ft[2 * m + c]);
-#pragma unroll
-      for (int o = 16; o >= 1; o >>= 1) acc = acc + __shfl_down_sync(0xffffffffu, acc, o);
-      h[c] = acc;
-    }
-    const T h0 = __shfl_sync(0xffffffffu, h[0], 0), h1 = __shfl_sync(0xffffffffu, h[1], 0);
-    if (tid < 2) {
-      const int c = tid;
-      const T ac = c == 0 ? a[0] : a[1], vc = c == 0 ? v[0] : v[1], dc = c == 0 ? d[0] : d[1];
-      const T hh = add_rn(c == 0 ? h0 : h1, mul_rn(ac, B.area));
-      T an = ac, vn = vc, dn = dc;
-      if (B.free_dof[c]) {
-        const T v1 = add_rn(vc, mul_rn(B.k1, ac));
-        const T v2 = add_rn(add_rn(dc, mul_rn(B.dt, vc)), mul_rn(B.k2, ac));
-        an = sub_rn(sub_rn(hh, mul_rn(B.damp, v1)), mul_rn(B.stiff, v2)) / B.den;
-        vn = add_rn(mul_rn(B.c1, an), v1);
-        dn = add_rn(mul_rn(B.c2, an), v2);
-      }
-      B.state[c] = an;
-      B.state[3 + c] = vn;
-      B.state[6 + c] = dn;
-      B.state[9 + c] = hh;
-      if (B.force_hist) B.force_hist[c] = hh;
-    }
-    if (tid == 2) {
-      B.state[9 + 2] = T(0);
-      if (B.force_hist) B.force_hist[2] = T(0);
-    }
-  }
+  if (tid < 32) body2d_finish<T>(B, kin, Ft, M, a, v, d);
 }
 
 // shared memory of k_body2d for M markers, radius R, region EX x EY, staged rows of RL
@@ -931,13 +1004,14 @@ __device__ __forceinline__ void body2d_chain(const BodyParams<T>& B) {
     }
   }
 
-  T a[2], v[2], d[2];
+  T a[3], v[3], d[3];
 #pragma unroll
-  for (int c = 0; c < 2; ++c) {
+  for (int c = 0; c < 3; ++c) {
     a[c] = B.state[c];
     v[c] = B.state[3 + c];
     d[c] = B.state[6 + c];
   }
+  const Kin2<T> kin(B, d, v);
   const int ox = B.meta[META_PX] - 1, oy = B.meta[META_PY] - 1;  // predicted region corner
   const int ya = oy >= 0 ? oy - oy % AL : 0;
   const int64_t n = (int64_t)B.nx * B.ny;
@@ -964,7 +1038,8 @@ __device__ __forceinline__ void body2d_chain(const BodyParams<T>& B) {
   // (ib/stencil.py:7-51), one thread per (marker, lane), PER stencil points each
   for (int t = tid; t < M * LN; t += nt) {
     const int m = t / LN, sub = t - m * LN;
-    const T xm = B.X0[m] + d[0], ym = B.Y0[m] + d[1];
+    T xm, ym;
+    kin.xy(B, m, xm, ym);
     const int fx = ifloor(xm), fy = ifloor(ym);
     if (sub == 0) {
       fxy[2 * m] = fx - R + 1;
@@ -1046,7 +1121,7 @@ __device__ __forceinline__ void body2d_chain(const BodyParams<T>& B) {
 #pragma unroll
       for (int c = 0; c < 2; ++c) {
         U[2 * m + c] = acc[c];
-        const T fs = mul_rn(v[c] - acc[c], d2);
+        const T fs = mul_rn(kin.target(B, m, c) - acc[c], d2);
         Fa[2 * m + c] = fs;
         Ft[2 * m + c] = B.n_iter > 0 ? fs : T(0);
       }
@@ -1082,7 +1157,7 @@ __device__ __forceinline__ void body2d_chain(const BodyParams<T>& B) {
         for (int c = 0; c < 2; ++c) {
           const T uq = U[2 * m + c] + acc[c];
           U[2 * m + c] = uq;
-          const T fs = mul_rn(v[c] - uq, d2);
+          const T fs = mul_rn(kin.target(B, m, c) - uq, d2);
           Fnext[2 * m + c] = fs;
           Ft[2 * m + c] = Ft[2 * m + c] + fs;
         }
@@ -1120,40 +1195,7 @@ __device__ __forceinline__ void body2d_chain(const BodyParams<T>& B) {
   }
   // total force h = sum_m(-F_total) (dyn.py:126-136) in a fixed tree by warp 0, added mass
   // h += a A (vortex_induced_vibration.py:136), Newmark update (dyn.py:5-51)
-  if (tid < 32) {
-    T h[2];
-#pragma unroll
-    for (int c = 0; c < 2; ++c) {
-      T acc = T(0);
-      for (int m = tid; m < M; m += 32) acc = m == tid ? -Ft[2 * m + c] : acc + (-Ft[2 * m + c]);
-#pragma unroll
-      for (int o = 16; o >= 1; o >>= 1) acc = acc + __shfl_down_sync(0xffffffffu, acc, o);
-      h[c] = acc;
-    }
-    const T h0 = __shfl_sync(0xffffffffu, h[0], 0), h1 = __shfl_sync(0xffffffffu, h[1], 0);
-    if (tid < 2) {
-      const int c = tid;
-      const T ac = c == 0 ? a[0] : a[1], vc = c == 0 ? v[0] : v[1], dc = c == 0 ? d[0] : d[1];
-      const T hh = add_rn(c == 0 ? h0 : h1, mul_rn(ac, B.area));
-      T an = ac, vn = vc, dn = dc;
-      if (B.free_dof[c]) {
-        const T v1 = add_rn(vc, mul_rn(B.k1, ac));
-        const T v2 = add_rn(add_rn(dc, mul_rn(B.dt, vc)), mul_rn(B.k2, ac));
-        an = sub_rn(sub_rn(hh, mul_rn(B.damp, v1)), mul_rn(B.stiff, v2)) / B.den;
-        vn = add_rn(mul_rn(B.c1, an), v1);
-        dn = add_rn(mul_rn(B.c2, an), v2);
-      }
-      B.state[c] = an;
-      B.state[3 + c] = vn;
-      B.state[6 + c] = dn;
-      B.state[9 + c] = hh;
-      if (B.force_hist) B.force_hist[c] = hh;
-    }
-    if (tid == 2) {
-      B.state[9 + 2] = T(0);
-      if (B.force_hist) B.force_hist[2] = T(0);
-    }
-  }
+  if (tid < 32) body2d_finish<T>(B, kin, Ft, M, a, v, d);
 }
 
 template <typename T, int R>
@@ -1208,13 +1250,14 @@ __global__ void __launch_bounds__(kClusterThreads) k_body2d_cluster(const __grid
   // arrive now, wait just before the first remote store
   asm volatile("barrier.cluster.arrive.relaxed.aligned;\n" ::: "memory");
 
-  T a[2], v[2], d[2];
+  T a[3], v[3], d[3];
 #pragma unroll
-  for (int c = 0; c < 2; ++c) {
+  for (int c = 0; c < 3; ++c) {
     a[c] = B.state[c];
     v[c] = B.state[3 + c];
     d[c] = B.state[6 + c];
   }
+  const Kin2<T> kin(B, d, v);
   const int slot = B.pred_slot;
   const int ox = B.meta[slot ? META_PX2 : META_PX] - 1, oy = B.meta[slot ? META_PY2 : META_PY] - 1;
   const bool region_ok = ox >= B.box[0] && oy >= B.box[2] && ox + EX <= B.box[1] && oy + EY <= B.box[3];
@@ -1241,8 +1284,10 @@ __global__ void __launch_bounds__(kClusterThreads) k_body2d_cluster(const __grid
   T fl[9];
   if (has_pair) {
     const int ix = s / WD, iy = s - ix * WD;
-    nxp = ifloor(B.X0[m] + d[0]) - R + 1 + ix;
-    nyp = ifloor(B.Y0[m] + d[1]) - R + 1 + iy;
+    T px, py;
+    kin.xy(B, m, px, py);
+    nxp = ifloor(px) - R + 1 + ix;
+    nyp = ifloor(py) - R + 1 + iy;
     const int cx = nxp - ox, cy = nyp - oy;
     in_region = cx >= 0 && cx < EX && cy >= 0 && cy < EY;
     if (in_region) {
@@ -1253,8 +1298,7 @@ __global__ void __launch_bounds__(kClusterThreads) k_body2d_cluster(const __grid
   }
   // all marker positions in one round trip (the own pair's above is the same load)
   for (int mm = tid; mm < M; mm += nt) {
-    xs[mm] = B.X0[mm] + d[0];
-    xs[M + mm] = B.Y0[mm] + d[1];
+    kin.xy(B, mm, xs[mm], xs[M + mm]);
   }
   if (tid == 0) {
     flags[0] = 0;
@@ -1376,7 +1420,7 @@ __global__ void __launch_bounds__(kClusterThreads) k_body2d_cluster(const __grid
 #pragma unroll
       for (int c = 0; c < 2; ++c) {
         U[2 * m + c] = acc[c];
-        fs[c] = mul_rn(v[c] - acc[c], d2);
+        fs[c] = mul_rn(kin.target(B, m, c) - acc[c], d2);
         Ft[2 * m + c] = B.n_iter > 0 ? fs[c] : T(0);
       }
     }
@@ -1399,7 +1443,7 @@ __global__ void __launch_bounds__(kClusterThreads) k_body2d_cluster(const __grid
         for (int c = 0; c < 2; ++c) {
           const T uq = U[2 * m + c] + acc[c];
           U[2 * m + c] = uq;
-          fs[c] = mul_rn(v[c] - uq, d2);
+          fs[c] = mul_rn(kin.target(B, m, c) - uq, d2);
           ft[c] = Ft[2 * m + c] + fs[c];
           Ft[2 * m + c] = ft[c];
         }
@@ -1431,38 +1475,9 @@ __global__ void __launch_bounds__(kClusterThreads) k_body2d_cluster(const __grid
   // the body force of every CTA (and the window descriptor) are in place
   cluster.sync();
   if (ok && rank == 0 && tid < 32) {
-    // h = sum_m(-F_total) in warp 0's fixed tree, added mass, Newmark (as the chain form)
-    T h[2];
-#pragma unroll
-    for (int c = 0; c < 2; ++c) {
-      T acc = T(0);
-      for (int mm = tid; mm < M; mm += 32) acc = mm == tid ? -Ft[2 * mm + c] : acc + (-Ft[2 * mm + c]);
-#pragma unroll
-      for (int o = 16; o >= 1; o >>= 1) acc = acc + __shfl_down_sync(0xffffffffu, acc, o);
-      h[c] = acc;
-    }
-    const T h0 = __shfl_sync(0xffffffffu, h[0], 0), h1 = __shfl_sync(0xffffffffu, h[1], 0);
-    if (tid < 2) {
-      const int c = tid;
-      const T ac = c == 0 ? a[0] : a[1], vc = c == 0 ? v[0] : v[1], dc = c == 0 ? d[0] : d[1];
-      const T hh = add_rn(c == 0 ? h0 : h1, mul_rn(ac, B.area));
-      T an = ac, vn = vc, dn = dc;
-      if (B.free_dof[c]) {
-        const T v1 = add_rn(vc, mul_rn(B.k1, ac));
-        const T v2 = add_rn(add_rn(dc, mul_rn(B.dt, vc)), mul_rn(B.k2, ac));
-        an = sub_rn(sub_rn(hh, mul_rn(B.damp, v1)), mul_rn(B.stiff, v2)) / B.den;
-        vn = add_rn(mul_rn(B.c1, an), v1);
-        dn = add_rn(mul_rn(B.c2, an), v2);
-      }
-      B.state[c] = an;
-      B.state[3 + c] = vn;
-      B.state[6 + c] = dn;
-      B.state[9 + c] = hh;
-      if (B.force_hist) B.force_hist[c] = hh;
-    }
+    // h = sum_m(-F_total) (and the torque) in warp 0's fixed tree, added mass, Newmark
+    body2d_finish<T>(B, kin, Ft, M, a, v, d);
     if (tid == 2) {
-      B.state[9 + 2] = T(0);
-      if (B.force_hist) B.force_hist[2] = T(0);
       B.meta[slot ? META_PX : META_PX2] = flags[1];  // the next step reads the other slot
       B.meta[slot ? META_PY : META_PY2] = flags[2];
     }
@@ -1519,13 +1534,16 @@ static bool getenv_flag(const char* name) {
 
 // Chain width of a rigid 2-D marker set (coordinates in the plan precision): the largest
 // cyclic index distance between two markers whose stencils can share a node under some
-// translation, i.e. |dx| < 2R and |dy| < 2R (with a small margin for rounding).
-static int chain_width(const double* x, const double* y, int M, int R) {
-  const double lim = 2.0 * R + 1e-3;
+// translation, i.e. |dx| < 2R and |dy| < 2R (with a small margin for rounding).  A body that
+// also turns can bring any pair closer than 2R sqrt(2) to that test's 45-degree corner, so
+// there the distance decides.
+static int chain_width(const double* x, const double* y, int M, int R, int rot) {
+  const double lim = 2.0 * R + 1e-3, lim_r = 2.0 * R * sqrt(2.0) + 1e-3;
   int K = 0;
   for (int i = 0; i < M; ++i)
     for (int j = i + 1; j < M; ++j) {
-      if (fabs(x[i] - x[j]) < lim && fabs(y[i] - y[j]) < lim) {
+      const double dx = x[i] - x[j], dy = y[i] - y[j];
+      if (rot ? hypot(dx, dy) < lim_r : (fabs(dx) < lim && fabs(dy) < lim)) {
         const int dd = j - i, cyc = dd < M - dd ? dd : M - dd;
         K = cyc > K ? cyc : K;
       }
@@ -1746,11 +1764,27 @@ __global__ void k_mask_bb(T* f, const uint8_t* __restrict__ mask, int64_t n) {
 // body state from a device copy; a 2-D body's window prediction restarts from the new
 // displacement (floor of the smallest marker coordinate, as vs_body_set_state does)
 template <typename T>
-__global__ void k_set_state(T* state, const T* src, int* meta, double lo0, double lo1, int R) {
+__global__ void k_set_state(T* state, const T* src, int* meta, double lo0, double lo1, int R,
+                            const __grid_constant__ BodyParams<T> B) {
   const int i = threadIdx.x;
   if (i < 12) state[i] = src[i];
   if (meta && i < 2) {
-    const int c = (int)floor((i == 0 ? (T)lo0 : (T)lo1) + src[6 + i]) - R + 1;
+    int c;
+    if (B.rot) {  // smallest stencil corner of the turned markers, as the body kernel finds it
+      T d[3], v[3] = {T(0), T(0), T(0)};
+      for (int k = 0; k < 3; ++k) d[k] = src[6 + k];
+      const Kin2<T> kin(B, d, v);
+      int lo = INT_MAX;
+      for (int m = 0; m < B.M; ++m) {
+        T x, y;
+        kin.xy(B, m, x, y);
+        const int f = ifloor(i == 0 ? x : y);
+        lo = f < lo ? f : lo;
+      }
+      c = lo - R + 1;
+    } else {
+      c = (int)floor((i == 0 ? (T)lo0 : (T)lo1) + src[6 + i]) - R + 1;
+    }
     meta[META_PX + i] = c;
     meta[META_PX2 + i] = c;
   }
@@ -1822,7 +1856,8 @@ struct vs_body_plan {
   CUtensorMap maps[2]; // tensor maps of the last two population buffers seen
   const void* map_ptr[2];
   int map_next;
-  double nm[9];  // k1, k2, c1, c2, dt, damping, stiffness, den, area
+  double nm[13];  // k1, k2, c1, c2, dt, damping, stiffness, den, area; rotation: damping, stiffness, den, added inertia
+  int rot;        // 2-D body with a free rotation (DOF 2 is the angle about the initial centre)
   int box[6];    // region the body's window never leaves (half-open x0,x1,y0,y1,z0,z1)
   double lo_t[2];  // 2-D: smallest marker x and y, rounded to the plan precision
   double lo_t3;    // 3-D: smallest marker z, rounded
@@ -1834,6 +1869,19 @@ struct vs_body_plan {
 };
 
 static size_t dsize(int dtype) { return dtype == VS_F64 ? 8 : 4; }
+
+// the marker geometry k_set_state needs (turning 2-D bodies)
+template <typename T>
+static BodyParams<T> kin_params(const vs_body_plan* b) {
+  BodyParams<T> P{};
+  P.X0 = (const T*)b->d_X0;
+  P.Y0 = (const T*)b->d_X0 + b->M;
+  P.M = b->M;
+  P.rot = b->rot;
+  P.cx = (T)b->cfg.center_x;
+  P.cy = (T)b->cfg.center_y;
+  return P;
+}
 
 static void free_lattice(vs_lattice_plan* p) {
   if (!p) return;
@@ -2087,6 +2135,10 @@ static BodyParams<T> body_params2d(vs_body_plan* B, const vs_lattice_plan* LP, c
   for (int c = 0; c < 3; ++c) P.free_dof[c] = B->cfg.free_dof[c];
   P.k1 = (T)B->nm[0]; P.k2 = (T)B->nm[1]; P.c1 = (T)B->nm[2]; P.c2 = (T)B->nm[3]; P.dt = (T)B->nm[4];
   P.damp = (T)B->nm[5]; P.stiff = (T)B->nm[6]; P.den = (T)B->nm[7]; P.area = (T)B->nm[8];
+  P.rot = B->rot;
+  P.cx = (T)B->cfg.center_x;
+  P.cy = (T)B->cfg.center_y;
+  P.rot_damp = (T)B->nm[9]; P.rot_stiff = (T)B->nm[10]; P.rot_den = (T)B->nm[11]; P.rot_added = (T)B->nm[12];
   P.chain_k = B->chain_k;
   return P;
 }
@@ -2577,6 +2629,8 @@ int vs_body_plan_create(const vs_body_cfg* cfg, const vs_lattice_plan* lattice, 
   VS_REQUIRE(cfg->radius >= 1 && cfg->radius <= 3, "stencil radius must be 1..3");
   VS_REQUIRE(cfg->kernel >= VS_KERNEL_PESKIN3 && cfg->kernel <= VS_KERNEL_COSINE4, "bad kernel");
   VS_REQUIRE(cfg->n_iter >= 0 && cfg->n_iter <= 64, "n_iter must be 0..64");
+  VS_REQUIRE(!(cfg->dim == 2 && cfg->free_dof[2]) || (cfg->moving && cfg->inertia > 0),
+             "a free rotation needs a moving body with a positive moment of inertia");
   VS_REQUIRE(lattice->cfg.forcing == VS_FORCE_EDM || lattice->cfg.forcing == VS_FORCE_GUO_BGK ||
                  lattice->cfg.forcing == VS_FORCE_GUO_MRT,
              "an immersed body needs a forcing scheme on the lattice (EDM or Guo)");
@@ -2615,6 +2669,17 @@ int vs_body_plan_create(const vs_body_cfg* cfg, const vs_lattice_plan* lattice, 
       if (cfg->dim == 2) put(d * M + m, v);
       else put(m * 3 + d, v);
     }
+  b->rot = cfg->dim == 2 && cfg->free_dof[2] ? 1 : 0;
+  double rmax = 0.0;
+  if (b->rot) {
+    // a turning body sweeps the disc about its centre: window and box cover every angle
+    for (int m = 0; m < M; ++m) {
+      const double r = hypot(cfg->x0_host[m] - cfg->center_x, cfg->y0_host[m] - cfg->center_y);
+      rmax = r > rmax ? r : rmax;
+    }
+    lo[0] = cfg->center_x - rmax; hi[0] = cfg->center_x + rmax;
+    lo[1] = cfg->center_y - rmax; hi[1] = cfg->center_y + rmax;
+  }
   for (int d = 0; d < cfg->dim; ++d) b->cap[d] = (int)(floor(hi[d]) - floor(lo[d])) + w + 2;
   for (int d = 0; d < 2; ++d) b->lo_t[d] = ts == 8 ? lo[d] : (double)(float)lo[d];
   b->lo_t3 = cfg->dim == 3 ? (ts == 8 ? lo[2] : (double)(float)lo[2]) : 0.0;
@@ -2698,6 +2763,10 @@ int vs_body_plan_create(const vs_body_cfg* cfg, const vs_lattice_plan* lattice, 
   b->nm[6] = cfg->stiffness;
   b->nm[7] = cfg->mass + b->nm[2] * cfg->damping + b->nm[3] * cfg->stiffness;
   b->nm[8] = cfg->added_mass_area;
+  b->nm[9] = cfg->rot_damping;
+  b->nm[10] = cfg->rot_stiffness;
+  b->nm[11] = cfg->inertia + b->nm[2] * cfg->rot_damping + b->nm[3] * cfg->rot_stiffness;
+  b->nm[12] = cfg->added_inertia;
   if (cfg->dim == 2) {
     const int EX = b->cap[0] + 2, EY = b->cap[1] + 2;
     if ((int64_t)M * b->S >= 65536 || (int64_t)EX * EY >= 65536) {
@@ -2718,7 +2787,7 @@ int vs_body_plan_create(const vs_body_cfg* cfg, const vs_lattice_plan* lattice, 
         xr[m] = ts == 8 ? cfg->x0_host[m] : (double)(float)cfg->x0_host[m];
         yr[m] = ts == 8 ? cfg->y0_host[m] : (double)(float)cfg->y0_host[m];
       }
-      b->chain_k = chain_width(xr.data(), yr.data(), M, cfg->radius);
+      b->chain_k = chain_width(xr.data(), yr.data(), M, cfg->radius, b->rot);
       b->chain = (M <= 32 || 2 * b->chain_k + 1 <= 31) && !getenv_flag("VIVSIM_GB300_BODY_CSR");
     }
     auto smem_of = [&](int rl) {
@@ -2745,6 +2814,15 @@ int vs_body_plan_create(const vs_body_cfg* cfg, const vs_lattice_plan* lattice, 
       meta0[META_PX2] = meta0[META_PX];
       meta0[META_PY2] = meta0[META_PY];
       if ((e = cudaMemcpy(b->d_meta, meta0, sizeof(meta0), cudaMemcpyHostToDevice)) != cudaSuccess) return fail(e);
+      if (b->rot) {  // a turning body: the corner of its markers at the initial angle
+        if (ts == 8)
+          k_set_state<double><<<1, 32>>>((double*)b->d_state, (const double*)b->d_state, b->d_meta, 0.0, 0.0,
+                                         cfg->radius, kin_params<double>(b));
+        else
+          k_set_state<float><<<1, 32>>>((float*)b->d_state, (const float*)b->d_state, b->d_meta, 0.0, 0.0,
+                                        cfg->radius, kin_params<float>(b));
+        if ((e = cudaGetLastError()) != cudaSuccess || (e = cudaDeviceSynchronize()) != cudaSuccess) return fail(e);
+      }
     }
     // the limit is a property of the kernel function, shared by every plan: raise it to the
     // device maximum once rather than to this plan's size (a smaller later plan would
@@ -2918,7 +2996,17 @@ int vs_body_set_state(vs_body_plan* plan, const double* state_host, void* stream
   cudaStream_t st = as_stream(stream);
   cudaError_t e = cudaMemcpyAsync(plan->d_state, buf, ts * 12, cudaMemcpyHostToDevice, st);
   int corner[2];
-  if (plan->dim == 2 && plan->d_meta) {
+  if (plan->rot && plan->d_meta && e == cudaSuccess) {
+    // a turning body: the corner of its turned markers, found on the device
+    const int rc = dispatch_t(plan->cfg.dtype, [&](auto t) -> int {
+      using T = typename decltype(t)::type;
+      k_set_state<T><<<1, 32, 0, st>>>((T*)plan->d_state, (const T*)plan->d_state, plan->d_meta, 0.0, 0.0,
+                                        plan->cfg.radius, kin_params<T>(plan));
+      VS_CHECK_LAUNCH("vs_body_set_state");
+      return VS_OK;
+    });
+    if (rc) return rc;
+  } else if (plan->dim == 2 && plan->d_meta) {
     // the 2-D body kernel predicts its window from the last stencil corner: restart that
     // prediction from the new displacement (floor of the smallest marker coordinate)
     for (int d = 0; d < 2; ++d) {
@@ -2940,7 +3028,7 @@ int vs_body_set_state_device(vs_body_plan* plan, const void* state, void* stream
     using T = typename decltype(t)::type;
     k_set_state<T><<<1, 32, 0, as_stream(stream)>>>((T*)plan->d_state, (const T*)state,
                                                     plan->dim == 2 ? plan->d_meta : nullptr, plan->lo_t[0],
-                                                    plan->lo_t[1], plan->cfg.radius);
+                                                    plan->lo_t[1], plan->cfg.radius, kin_params<T>(plan));
     VS_CHECK_LAUNCH("vs_body_set_state_device");
     return VS_OK;
   });

@@ -124,11 +124,18 @@ class LatticeStep:
 
 
 class RigidBody:
-    """Immersed rigid body: markers, IB stencil, MDF and a Newmark spring-mass update."""
+    """Immersed rigid body: markers, IB stencil, MDF and a Newmark spring-mass update.
+
+    ``free_dof`` names the Newmark-integrated DOFs: x, y, z in 3-D; x, y and the rotation
+    angle about ``center`` in 2-D (get_markers_coords_3dof / get_markers_velocity_3dof /
+    get_torque_to_obj, vivsim/dyn.py:84-154), the latter with ``inertia``,
+    ``rot_stiffness``, ``rot_damping`` and h[2] = torque + a[2] * ``added_inertia``.
+    """
 
     def __init__(self, step, markers, ds, kernel="peskin4", radius=2, n_iter=3, moving=False,
                  free_dof=(False, False, False), mass=1.0, stiffness=0.0, damping=0.0, added_mass_area=0.0,
-                 d0=(0, 0, 0), v0=(0, 0, 0), a0=(0, 0, 0)):
+                 d0=(0, 0, 0), v0=(0, 0, 0), a0=(0, 0, 0), center=None, inertia=0.0, rot_stiffness=0.0,
+                 rot_damping=0.0, added_inertia=0.0):
         X = np.asarray(markers.cpu() if isinstance(markers, torch.Tensor) else markers, dtype=np.float64)
         if X.ndim != 2 or X.shape[1] != step.dim:
             raise ValueError(f"markers must have shape (n_markers, {step.dim})")
@@ -157,6 +164,11 @@ class RigidBody:
             cfg.free_dof[i] = 1 if (i < len(free_dof) and free_dof[i]) else 0
         cfg.mass, cfg.stiffness, cfg.damping = float(mass), float(stiffness), float(damping)
         cfg.added_mass_area = float(added_mass_area)
+        if center is None:
+            center = (float(np.mean(X[:, 0])), float(np.mean(X[:, 1])))
+        cfg.center_x, cfg.center_y = float(center[0]), float(center[1])
+        cfg.inertia, cfg.rot_stiffness = float(inertia), float(rot_stiffness)
+        cfg.rot_damping, cfg.added_inertia = float(rot_damping), float(added_inertia)
         for name, val in (("d0", d0), ("v0", v0), ("a0", a0)):
             arr = getattr(cfg, name)
             for i in range(3):
