@@ -248,13 +248,12 @@ def test_body_chain_form_equals_general_form(S, monkeypatch):
     for env in ("VIVSIM_GB300_BODY_SINGLE", "VIVSIM_GB300_BODY_CSR"):
         monkeypatch.setenv(env, "1")
         fb, sb, hb = _viv_small(S, X, 30)
+        monkeypatch.delenv(env)
         assert np.array_equal(fa, fb), env
         assert np.array_equal(ha, hb), env
         for k in ("a", "v", "d", "h"):
             assert np.array_equal(sa[k], sb[k]), (env, k)
     # and through graph replay
-    monkeypatch.delenv("VIVSIM_GB300_BODY_SINGLE")
-    monkeypatch.delenv("VIVSIM_GB300_BODY_CSR")
     with torch.cuda.stream(torch.cuda.Stream()):
         fg, sg, hg = _viv_small(S, X, 30, graph=True)
         torch.cuda.synchronize()

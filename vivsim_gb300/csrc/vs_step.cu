@@ -257,9 +257,50 @@ __global__ void __launch_bounds__(256) k_step(const __grid_constant__ StepParams
   step_block<L, T, COLL, WALLS>(P, blockIdx.x, blockIdx.y);
 }
 
+// The main launch of a batch walks each case's nodes in memory order: chunk j of a
+// case is nodes [j * blockDim.x, (j + 1) * blockDim.x) of its flattened grid, so a block is
+// full whatever the case's row length (rows of 64 nodes would leave 3/4 of a 256-thread
+// block idle) and a warp still reads 32 consecutive addresses.
+template <class L, typename T, int COLL, bool WALLS>
+__device__ __forceinline__ void step_flat(const StepParams<L, T>& P, int chunk) {
+  const int p = chunk * (int)blockDim.x + (int)threadIdx.x;
+  if (p >= P.n) return;
+  int x, y, z;
+  if constexpr (L::D == 2) {
+    x = p / P.ny;
+    y = p - x * P.ny;
+    z = 0;
+  } else {
+    const int syz = P.ny * P.nz;
+    x = p / syz;
+    const int r = p - x * syz;
+    y = r / P.nz;
+    z = r - y * P.nz;
+  }
+  if (P.skip_box && x >= P.box[0] && x < P.box[1] && y >= P.box[2] && y < P.box[3] && z >= P.box[4] &&
+      z < P.box[5])
+    return;
+  if (P.dyn_meta) {
+    const int bx = P.dyn_meta[P.dyn_slot ? META_PX2 : META_PX] - 1, by = P.dyn_meta[P.dyn_slot ? META_PY2 : META_PY] - 1;
+    if (x >= bx && x < bx + P.dyn_ext[0] && y >= by && y < by + P.dyn_ext[1]) return;
+  }
+  if (P.skip_walls && (x == 0 || x == P.nx - 1)) return;
+  T f[L::Q];
+#pragma unroll
+  for (int i = 0; i < L::Q; ++i) f[i] = __ldg(P.fin + (size_t)i * P.n + p);
+  step_node<L, T, COLL, WALLS>(P, x, y, z, p, f);
+}
+
+template <class L, typename T, int COLL>
+__global__ void __launch_bounds__(256) k_step_batch_flat(const StepParams<L, T>* __restrict__ Ps,
+                                                         const int2* __restrict__ blk) {
+  const int2 cb = blk[blockIdx.x];
+  step_flat<L, T, COLL, false>(Ps[cb.x], cb.y);
+}
+
 // Grid kernel over many independent lattices in one launch: block b works on lattice
 // blk[b].x, as block blk[b].y of that lattice's own launch geometry (chunks x rows,
-// row-major), with that lattice's parameters.
+// row-major), with that lattice's parameters (the batch's region launch).
 template <class L, typename T, int COLL, bool WALLS>
 __global__ void __launch_bounds__(256) k_step_batch(const StepParams<L, T>* __restrict__ Ps,
                                                     const int2* __restrict__ blk) {
@@ -3218,8 +3259,10 @@ static int batch_build(vs_batch_plan* bp, void* const* fa, void* const* fb) {
         if (grid_setup<L, T>(bp->L[k], Bk, fin, fout, Bk ? 1 : 0, lazy_in, bp->tb, P, g, tb)) {
           const int idx = (int)main[p][first].size();
           main[p][first].push_back(P);
-          if (p == 0 && first == 1)
-            for (int j = 0; j < (int)(g.x * g.y); ++j) bm.push_back(make_int2(idx, j));
+          if (p == 0 && first == 1) {  // flat chunks of the case's nodes (k_step_batch_flat)
+            const int nch = (int)((bp->L[k]->n + bp->tb - 1) / bp->tb);
+            for (int j = 0; j < nch; ++j) bm.push_back(make_int2(idx, j));
+          }
         }
         if (!chain_body) continue;
         if (grid_setup<L, T>(bp->L[k], Bk, fin, fout, 2, lazy_in, bp->tb, P, g, tb)) {
@@ -3278,7 +3321,7 @@ static int batch_step_t(vs_batch_plan* bp, int s, int n_steps, void* const* fa, 
     }
   }
   if (bp->n_blk_main > 0)
-    k_step_batch<L, T, COLL, false><<<bp->n_blk_main, bp->tb, 0, st>>>(
+    k_step_batch_flat<L, T, COLL><<<bp->n_blk_main, bp->tb, 0, st>>>(
         (const StepParams<L, T>*)bp->d_main[p][first], bp->d_blk_main);
   if (fork) {
     e = cudaEventRecord(bp->ev_join, bp->side);
