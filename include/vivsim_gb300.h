@@ -219,15 +219,21 @@ typedef struct vs_lattice_cfg {
   const uint8_t* obstacle_mask; /* device, one byte per node or NULL: obstacle_bounce_back after
                                     the face boundaries (lbm/boundary/bb.py:98-110); the plan
                                     keeps the pointer, the caller keeps the memory alive */
+  int watchdog_every;      /* > 0: vs_run / vs_run_graph scan the populations for NaN/Inf after
+                              every watchdog_every-th step and after the last one; a hit sets
+                              the plan's status word to VS_ERR_NONFINITE (vs_lattice_status) */
 } vs_lattice_cfg;
 
 typedef struct vs_lattice_plan vs_lattice_plan;
 int vs_lattice_plan_create(const vs_lattice_cfg* cfg, vs_lattice_plan** out);
 int vs_lattice_plan_destroy(vs_lattice_plan* plan);
-/* Device status of the plan's grid kernels: VS_OK, or VS_ERR_TIMEOUT when a bounded wait
- * for a bulk copy gave up (that launch left its nodes unwritten).  Synchronises the stream;
- * reset != 0 clears the word. */
+/* Device status of the plan's grid kernels: VS_OK, VS_ERR_TIMEOUT when a bounded wait
+ * for a bulk copy gave up (that launch left its nodes unwritten), or VS_ERR_NONFINITE when
+ * the watchdog found a NaN/Inf population.  Synchronises the stream; reset != 0 clears it. */
 int vs_lattice_status(const vs_lattice_plan* plan, int reset, void* stream);
+/* NaN/Inf scan of n values: sets *status_dev (a device int) to VS_ERR_NONFINITE when one is
+ * not finite and leaves it unchanged otherwise.  Asynchronous. */
+int vs_check_finite(int dtype, const void* f, int64_t n, int* status_dev, void* stream);
 
 /* Immersed body advanced by the IB step (dyn.py + ib/mdf.py).  Markers follow a rigid
  * translation d (get_markers_coords_2dof); DOFs with free[k] = 0 stay at zero.  In 2-D,

@@ -596,3 +596,66 @@ def test_rotating_body_matches_oracle(S, dt, monkeypatch):
         assert np.array_equal(runs["cluster"][1], runs[form][1]), form
     (fgr, _, _), _ = _rotating_ellipse(S, npdt, 20, graph=True)
     assert np.array_equal(runs["cluster"][0], fgr)
+
+
+def test_watchdog_reports_nonfinite_populations(S):
+    """A NaN planted in the input populations (a host-side fault) reaches the plan's status
+    word through the watchdog scan; a clean run reports nothing."""
+    from vivsim_gb300 import _lib as V
+    nx, ny = 64, 48
+    u = np.zeros((2, nx, ny), np.float32)
+    u[0] = 0.05
+    f0 = L2.get_equilibrium(np.ones((nx, ny), np.float32), u)
+    bad = f0.copy()
+    bad[3, 10, 20] = np.nan
+    for graph in (False, True):
+        step = S.LatticeStep(9, (nx, ny), "bgk", 1.5, watchdog_every=5,
+                             boundaries=[S.boundary("equilibrium", "left", ux_wall=0.05)])
+        s = torch.cuda.Stream()
+        with torch.cuda.stream(s):
+            S.Simulation(step, T(f0)).run(12, graph=graph)
+            step.check()  # clean
+            S.Simulation(step, T(bad)).run(12, graph=graph)
+            with pytest.raises(V.VivsimError) as err:
+                step.check()
+            assert err.value.status == V.VS_ERR_NONFINITE
+            step.check()  # the status word was reset
+    t = torch.ones(1000, device="cuda", dtype=torch.float64)
+    assert S.check_finite(t)
+    t[777] = float("inf")
+    assert not S.check_finite(t)
+
+
+def test_checkpoint_resume_is_bit_exact(S, tmp_path):
+    """save() after 12 steps, load() into a fresh plan, 18 more steps: the same bits as 30
+    uninterrupted steps (moving body, cluster form, lazy faces)."""
+    th = np.linspace(0, 2 * np.pi, 40, endpoint=False)
+    X = np.stack([30 + 6 * np.cos(th), 32 + 6 * np.sin(th)], 1)
+    fa, sa, _ = _viv_small(S, X, 30)
+    nx, ny = 96, 64
+    rng = np.random.default_rng(3)
+    u = np.zeros((2, nx, ny), np.float32)
+    u[0] = 0.05
+    u[1] = 1e-3 * rng.standard_normal((nx, ny))
+    f0 = T(L2.get_equilibrium(np.ones((nx, ny), np.float32), u))
+
+    def make():
+        step = S.LatticeStep(9, (nx, ny), "kbc", 1.8, forcing="edm",
+                             boundaries=[S.boundary("equilibrium", "left", ux_wall=0.05),
+                                         S.boundary("nee", "right", mode="pressure")])
+        body = S.RigidBody(step, X, 0.94, moving=True, free_dof=(False, True), mass=500.0, stiffness=0.05,
+                           added_mass_area=113.0, v0=(0, 2e-3, 0))
+        return step, body
+
+    step, body = make()
+    sim = S.Simulation(step, f0, body)
+    sim.run(12)
+    sim.save(tmp_path / "ck.npz")
+    step2, body2 = make()
+    sim2 = S.Simulation(step2, torch.zeros_like(f0), body2)
+    sim2.load(tmp_path / "ck.npz")
+    sim2.run(18)
+    assert np.array_equal(N(sim2.f), fa)
+    st = body2.state()
+    for k in ("a", "v", "d"):
+        assert np.array_equal(st[k], sa[k]), k

@@ -13,6 +13,7 @@ from . import _build
 
 VS_OK = 0
 VS_ERR_INVALID_ARG = 1
+VS_ERR_NONFINITE = 6
 VS_F32, VS_F64 = 0, 1
 VS_COLLIDE_BGK, VS_COLLIDE_KBC, VS_COLLIDE_MRT, VS_COLLIDE_REG = 0, 1, 2, 3
 VS_FORCE_NONE, VS_FORCE_EDM, VS_FORCE_GUO_BGK, VS_FORCE_GUO_MRT = 0, 1, 2, 3
@@ -53,7 +54,7 @@ class vs_lattice_cfg(C.Structure):
                 ("collision", C.c_int), ("omega", C.c_double), ("mrt_op", C.c_double * 361),
                 ("forcing", C.c_int), ("g_uniform", C.c_double * 3), ("mrt_fop", C.c_double * 361),
                 ("n_bc", C.c_int), ("bc", vs_bc * VS_MAX_BC), ("variant", C.c_int),
-                ("obstacle_mask", C.c_void_p)]
+                ("obstacle_mask", C.c_void_p), ("watchdog_every", C.c_int)]
 
 
 class vs_body_cfg(C.Structure):
@@ -139,6 +140,7 @@ _SIGS = {
     "vs_adjoint_forward": (_i, [_p, _i, C.POINTER(_d), _p]),
     "vs_adjoint_backward": (_i, [_p, _d, C.POINTER(_d), C.POINTER(_d), C.POINTER(_d), _p]),
     "vs_lattice_status": (_i, [_p, _i, _p]),
+    "vs_check_finite": (_i, [_i, _p, _l, _p, _p]),
     "vs_fine_to_coarse": (_i, [_i, _p, _i, _i, _p, _i, _i, _i, _p]),
     "vs_coarse_to_fine": (_i, [_i, _p, _i, _i, _p, _i, _i, _i, _p]),
 }

@@ -584,8 +584,12 @@ __device__ __forceinline__ void body2d_finish(const BodyParams<T>& B, const Kin2
       if (B.force_hist) B.force_hist[2] = T(0);
       return;
     }
-    const T ac = a[c], vc = v[c], dc = d[c];
-    const T hh = add_rn(h[c], mul_rn(ac, c < 2 ? B.area : B.rot_added));
+    // selects, not indexing by the thread: the state stays in registers
+    const T ac = c == 0 ? a[0] : (c == 1 ? a[1] : a[2]);
+    const T vc = c == 0 ? v[0] : (c == 1 ? v[1] : v[2]);
+    const T dc = c == 0 ? d[0] : (c == 1 ? d[1] : d[2]);
+    const T hc = c == 0 ? h[0] : (c == 1 ? h[1] : h[2]);
+    const T hh = add_rn(hc, mul_rn(ac, c < 2 ? B.area : B.rot_added));
     T an = ac, vn = vc, dn = dc;
     if (B.free_dof[c]) {
       const T damp = c < 2 ? B.damp : B.rot_damp, stiff = c < 2 ? B.stiff : B.rot_stiff;
@@ -1831,6 +1835,15 @@ __global__ void k_set_state(T* state, const T* src, int* meta, double lo0, doubl
   }
 }
 
+// NaN/Inf watchdog: any non-finite value sets the status word (first error kept)
+template <typename T>
+__global__ void k_check_finite(const T* __restrict__ f, int64_t n, int* status) {
+  bool bad = false;
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x)
+    bad |= !isfinite(f[p]);
+  if (__syncthreads_or(bad) && threadIdx.x == 0) atomicCAS(status, 0, VS_ERR_NONFINITE);
+}
+
 template <typename T>
 __global__ void k_fill(T* p, T v, int64_t n) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
@@ -2652,8 +2665,22 @@ int vs_lattice_status(const vs_lattice_plan* plan, int reset, void* stream) {
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e == cudaSuccess && reset && v) e = cudaMemset(plan->d_status, 0, sizeof(int));
   if (e != cudaSuccess) return cuda_status(e, "vs_lattice_status");
-  if (v) set_error("a grid kernel gave up waiting for its bulk copies (device status %d)", v);
+  if (v == VS_ERR_NONFINITE) set_error("the watchdog found a NaN or Inf population");
+  else if (v) set_error("a grid kernel gave up waiting for its bulk copies (device status %d)", v);
   return v;
+}
+
+int vs_check_finite(int dtype, const void* f, int64_t n, int* status_dev, void* stream) {
+  VS_REQUIRE(f && status_dev && n >= 0, "vs_check_finite: bad arguments");
+  if (n == 0) return VS_OK;
+  return dispatch_t(dtype, [&](auto t) -> int {
+    using T = typename decltype(t)::type;
+    const int64_t blocks = (n + 255) / 256;
+    k_check_finite<T><<<(unsigned)(blocks < 4096 ? blocks : 4096), 256, 0, as_stream(stream)>>>((const T*)f, n,
+                                                                                                status_dev);
+    VS_CHECK_LAUNCH("vs_check_finite");
+    return VS_OK;
+  });
 }
 
 int vs_lattice_plan_destroy(vs_lattice_plan* plan) {
@@ -3124,6 +3151,11 @@ int vs_run(const vs_lattice_plan* lattice, vs_body_plan* body, void* f_a, void* 
     int rc = enqueue_step(lattice, body, src, dst, hist, as_stream(stream), lazy && s > 0, !lazy || s == n_steps - 1,
                           s > 0, s == n_steps - 1);
     if (rc) return rc;
+    const int K = lattice->cfg.watchdog_every;
+    if (K > 0 && ((s + 1) % K == 0 || s == n_steps - 1)) {
+      rc = vs_check_finite(lattice->cfg.dtype, dst, lattice->n * lattice->cfg.q, lattice->d_status, stream);
+      if (rc) return rc;
+    }
   }
   return VS_OK;
 }

@@ -40,6 +40,15 @@ def boundary(kind, loc, mode="given", rho_wall=1.0, ux_wall=0.0, uy_wall=0.0, uz
                 gy=gy_wall, gz=gz_wall)
 
 
+def check_finite(f):
+    """True when every value of the CUDA tensor f is finite (one scan kernel; synchronises)."""
+    V.require_cuda(f)
+    f = V.cont(f)
+    status = torch.zeros(1, dtype=torch.int32, device=f.device)
+    V.call("vs_check_finite", V.dtype_code(f), V.ptr(f), f.numel(), V.ptr(status), V.stream())
+    return int(status.item()) == 0
+
+
 def _tdtype(dtype):
     return torch.float64 if dtype in (torch.float64, "float64", np.float64) else torch.float32
 
@@ -48,7 +57,7 @@ class LatticeStep:
     """Plan of the fused collide-force-stream-boundary step on one grid."""
 
     def __init__(self, q, shape, collision="bgk", omega=1.0, dtype=torch.float32, mrt_op=None, forcing="none",
-                 g=None, boundaries=(), variant="auto", obstacle_mask=None):
+                 g=None, boundaries=(), variant="auto", obstacle_mask=None, watchdog_every=0):
         if q not in (9, 19):
             raise ValueError("q must be 9 (D2Q9) or 19 (D3Q19)")
         self.q = q
@@ -98,6 +107,7 @@ class LatticeStep:
             V.require_cuda(m)
             self._mask = m.to(torch.uint8).contiguous()
             cfg.obstacle_mask = V.ptr(self._mask)
+        cfg.watchdog_every = int(watchdog_every)  # NaN/Inf scan every K steps of a run (check() reports it)
         self.cfg = cfg
         handle = C.c_void_p()
         V.call("vs_lattice_plan_create", C.byref(cfg), C.byref(handle))
@@ -108,7 +118,8 @@ class LatticeStep:
         return int(np.prod(self.shape))
 
     def check(self, reset=True):
-        """Raise if a grid kernel of this plan reported a device-side error (synchronises)."""
+        """Raise if a grid kernel of this plan reported a device-side error, or the watchdog
+        found a NaN/Inf population (synchronises)."""
         V.call("vs_lattice_status", self.handle, 1 if reset else 0, V.stream())
 
     def close(self):
@@ -218,6 +229,26 @@ class Simulation:
     def f(self):
         """Current populations (reference convention: after streaming and boundaries)."""
         return self._a if self._cur_is_a else self._b
+
+    def save(self, path):
+        """Checkpoint to an .npz file: the populations and the body state (a, v, d)."""
+        data = {"f": self.f.detach().cpu().numpy()}
+        if self.body is not None:
+            st = self.body.state()
+            data.update(a=st["a"], v=st["v"], d=st["d"])
+        np.savez(path, **data)
+
+    def load(self, path):
+        """Resume from a checkpoint written by save(): the run continues bit for bit."""
+        z = np.load(path)
+        f = torch.from_numpy(z["f"])
+        if tuple(f.shape) != tuple(self.f.shape):
+            raise ValueError(f"checkpoint populations have shape {tuple(f.shape)}, expected {tuple(self.f.shape)}")
+        self.f.copy_(f.to(device=self.f.device, dtype=self.f.dtype))
+        if self.body is not None:
+            if "d" not in z:
+                raise ValueError("checkpoint holds no body state")
+            self.body.set_state(a=z["a"], v=z["v"], d=z["d"])
 
     def run(self, n_steps, graph=False, force_history=False):
         """Advance n_steps; returns the (n_steps, 3) body-force history when asked."""
