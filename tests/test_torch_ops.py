@@ -24,6 +24,9 @@ def test_registered_with_fake_shapes():
         assert torch.ops.vivsim.interpolate(u, W, I).shape == (5, 2)
         g, h = torch.ops.vivsim.multi_direct_forcing(u, W, I, torch.empty(5, 2), 1.0, 3)
         assert g.shape == u.shape and h.shape == (5, 2)
+        fc = torch.empty(9, 9, 4)
+        assert torch.ops.vivsim.fine_to_coarse(f, fc, "left").shape == fc.shape
+        assert torch.ops.vivsim.coarse_to_fine(fc, f, "right").shape == f.shape
 
 
 @pytest.mark.gpu
@@ -38,3 +41,6 @@ def test_values_match_the_shims(mode):
     assert rel_err(torch.ops.vivsim.collision_kbc(f, feq, 1.7).cpu().numpy(),
                    lbm.collision_kbc(f, feq, 1.7).cpu().numpy()) == 0.0
     assert rel_err(torch.ops.vivsim.streaming(f).cpu().numpy(), G["d2.streaming"]) <= 1e-12
+    ff, fc = (torch.from_numpy(np.ascontiguousarray(G[k])).cuda() for k in ("mg.left.ff", "mg.left.fc"))
+    assert np.array_equal(torch.ops.vivsim.fine_to_coarse(ff, fc, "left").cpu().numpy(), G["mg.left.f2c"])
+    assert np.array_equal(torch.ops.vivsim.coarse_to_fine(fc, ff, "left").cpu().numpy(), G["mg.left.c2f"])

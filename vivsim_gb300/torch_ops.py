@@ -13,6 +13,7 @@ import torch
 from . import ib as _ib
 from . import lbm as _lbm
 from . import lbm3d as _lbm3d
+from . import multigrid as _mg
 
 
 def _lat(f):
@@ -109,3 +110,25 @@ def multi_direct_forcing(grid_u: torch.Tensor, stencil_weights: torch.Tensor, st
 @multi_direct_forcing.register_fake
 def _(grid_u, stencil_weights, stencil_indices, marker_u_target, marker_ds, n_iter):
     return torch.empty_like(grid_u), marker_u_target.new_empty(marker_u_target.shape)
+
+
+@torch.library.custom_op("vivsim::fine_to_coarse", mutates_args=())
+def fine_to_coarse(f_fine: torch.Tensor, f_coarse: torch.Tensor, dir: str) -> torch.Tensor:
+    out = _mg.fine_to_coarse(f_fine, f_coarse, dir)
+    return out.clone() if out.data_ptr() == f_coarse.data_ptr() else out  # an operator returns no alias
+
+
+@fine_to_coarse.register_fake
+def _(f_fine, f_coarse, dir):
+    return torch.empty_like(f_coarse)
+
+
+@torch.library.custom_op("vivsim::coarse_to_fine", mutates_args=())
+def coarse_to_fine(f_coarse: torch.Tensor, f_fine: torch.Tensor, dir: str) -> torch.Tensor:
+    out = _mg.coarse_to_fine(f_coarse, f_fine, dir)
+    return out.clone() if out.data_ptr() == f_fine.data_ptr() else out
+
+
+@coarse_to_fine.register_fake
+def _(f_coarse, f_fine, dir):
+    return torch.empty_like(f_fine)
