@@ -73,3 +73,30 @@ def test_batch_rejects_mixed_collisions(S):
     b = configs.build_solver(configs.periodic2d(n=64, collision="bgk"))[2]
     with pytest.raises(RuntimeError, match="differs"):
         S.Batch([a, b])
+
+
+def test_batch_and_single_runs_interleave(S):
+    """Odd-length batch runs, single-case runs of the same simulations in between (the body
+    kernels hand the window prediction over in alternating slots), then the batch again."""
+    cases = _cases()
+    stream = torch.cuda.Stream()
+    with torch.cuda.stream(stream):
+        ref = _build(S, cases)
+        for sim in ref:
+            sim.run(35)
+        bat = _build(S, cases)
+        batch = S.Batch(bat, threads_per_block=128, steps_per_graph=4)
+        batch.run(9)
+        batch.run(13)
+        for sim in bat:
+            sim.run(5)
+        batch.run(1)
+        batch.run(7)
+        torch.cuda.synchronize()
+    for k, ((fa, sa), (fb, sb)) in enumerate(zip(_state(ref), _state(bat))):
+        assert np.array_equal(fa, fb), f"case {k}: populations differ"
+        if sa is not None:
+            for key in ("a", "v", "d", "h"):
+                assert np.array_equal(sa[key], sb[key]), f"case {k}: body {key} differs"
+    for sim in ref + bat:
+        sim.step.check()

@@ -3509,6 +3509,17 @@ int vs_batch_run(vs_batch_plan* plan, void* const* f_a, void* const* f_b, int n_
     VS_REQUIRE(f_a[k] && f_b[k] && f_a[k] != f_b[k], "vs_batch_run: case %d needs two distinct buffers", k);
   if (n_steps == 0) return VS_OK;
   cudaStream_t st = as_stream(stream);
+  // The batched chain form reads its window prediction from slot 0 (and writes both slots):
+  // after a single-case run of the cluster form the current prediction may sit in slot 1
+  for (int k : plan->chain_bodies) {
+    vs_body_plan* Bk = plan->B[k];
+    if (Bk->parity) {
+      cudaError_t e = cudaMemcpyAsync(Bk->d_meta + META_PX, Bk->d_meta + META_PX2, 2 * sizeof(int),
+                                      cudaMemcpyDeviceToDevice, st);
+      if (e != cudaSuccess) return cuda_status(e, "vs_batch_run prediction slot");
+      Bk->parity = 0;
+    }
+  }
   bool same = plan->built_tb == plan->tb && (int)plan->fa.size() == plan->n;
   for (int k = 0; same && k < plan->n; ++k) same = plan->fa[k] == f_a[k] && plan->fb[k] == f_b[k];
   if (!same) {

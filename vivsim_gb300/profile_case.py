@@ -3,9 +3,13 @@
     python -m vivsim_gb300.profile_case --case periodic2d --n 4096 --steps 3
     python -m vivsim_gb300.profile_case --case sphere3d --steps 3
     python -m vivsim_gb300.profile_case --case viv2d --steps 20 --graph
+    python -m vivsim_gb300.profile_case --batch 64 --steps 8
+    python -m vivsim_gb300.profile_case --adjoint --steps 400
 
 Each step launches the body kernel (cases with a body), the grid kernel ``k_step`` and
-the face kernel(s); ``--grid-only`` launches only ``k_step``.  Prints the mean step time.
+the face kernel(s); ``--grid-only`` launches only ``k_step``.  ``--batch N`` runs the
+N-case VIV sweep as one batch (seed 3, as bench.py), ``--adjoint`` the differentiable
+cylinder's forward and reverse sweep over ``--steps`` steps.  Prints the mean step time.
 """
 
 import argparse
@@ -26,7 +30,13 @@ def main():
     ap.add_argument("--graph", action="store_true")
     ap.add_argument("--grid-only", action="store_true")
     ap.add_argument("--variant", choices=["auto", "plain", "tma"], default="auto")
+    ap.add_argument("--batch", type=int, default=0, help="run the N-case VIV sweep as one batch")
+    ap.add_argument("--adjoint", action="store_true", help="forward + reverse sweep of the adjoint cylinder")
     a = ap.parse_args()
+    if a.batch:
+        return batch(a.batch, a.steps)
+    if a.adjoint:
+        return adjoint(a.steps)
     kw = {}
     if a.n is not None and a.case in ("periodic2d", "cavity"):
         kw["n"] = a.n
@@ -54,6 +64,43 @@ def main():
     ms = e0.elapsed_time(e1) / a.steps
     n = math.prod(case["shape"])
     print(f"{case['name']}: {ms * 1e3:.1f} us/step, {n / ms / 1e3:.1f} MLUPS")
+
+
+def _timed(fn):
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1)
+
+
+def batch(n_cases, steps):
+    from . import solver
+    cases = configs.viv_sweep(n_cases, 3)
+    nodes = sum(math.prod(c["shape"]) for c in cases)
+    stream = torch.cuda.Stream()
+    with torch.cuda.stream(stream):
+        b = solver.Batch([configs.build_solver(c)[2] for c in cases], threads_per_block=64, steps_per_graph=0)
+        b.run(2)
+        torch.cuda.synchronize()
+        ms = _timed(lambda: b.run(steps)) / steps
+    print(f"batch of {n_cases} VIV cases ({nodes} nodes): {ms * 1e3:.1f} us/step, {nodes / ms / 1e3:.1f} MLUPS")
+
+
+def adjoint(steps):
+    import numpy as np
+    from . import adjoint as A
+    off = np.random.default_rng(2).normal(0.0, 0.1, 64)
+    stream = torch.cuda.Stream()
+    with torch.cuda.stream(stream):
+        plan = A.CylinderDrag(nx=512, ny=256, D=20.0, Re=100.0, n_markers=64, offsets=off, n_steps=steps,
+                              checkpoint_every=100, obj_start=steps // 2)
+        plan.forward()
+        ms_f = _timed(plan.forward)
+        ms_b = _timed(plan.backward)
+        plan.close()
+    print(f"adjoint cylinder, {steps} steps: forward {ms_f:.2f} ms, reverse sweep {ms_b:.2f} ms")
 
 
 if __name__ == "__main__":

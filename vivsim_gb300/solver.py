@@ -345,8 +345,7 @@ class Refined:
     recursively: the blocks of a level step (collide, stream, their boundaries); the
     coarse_to_fine transfer into each of them from its coarser neighbour's new state;
     then the next finer level runs two cycles and fine_to_coarse refills this level's
-    buffer lines.  For one coarse and one fine block this is oracle/recipes.py's
-    refined_channel_cycle.  With ``graph=True`` two cycles (which bring every ping-pong
+    buffer lines.  With ``graph=True`` two cycles (which bring every ping-pong
     buffer back to where it started) are captured once into a CUDA graph and replayed.
     """
 
