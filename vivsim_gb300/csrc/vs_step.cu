@@ -291,8 +291,10 @@ __device__ __forceinline__ void step_flat(const StepParams<L, T>& P, int chunk) 
   step_node<L, T, COLL, WALLS>(P, x, y, z, p, f);
 }
 
+// (6 blocks of 256 threads per SM by registers: at the default 48 registers the loads in
+// flight were too few, 5 % slower on the 64-case sweep; 8 blocks spill)
 template <class L, typename T, int COLL>
-__global__ void __launch_bounds__(256) k_step_batch_flat(const StepParams<L, T>* __restrict__ Ps,
+__global__ void __launch_bounds__(256, 6) k_step_batch_flat(const StepParams<L, T>* __restrict__ Ps,
                                                          const int2* __restrict__ blk) {
   const int2 cb = blk[blockIdx.x];
   step_flat<L, T, COLL, false>(Ps[cb.x], cb.y);
@@ -1307,20 +1309,10 @@ __global__ void __launch_bounds__(kClusterThreads) k_body2d_cluster(const __grid
   const int ox = B.meta[slot ? META_PX2 : META_PX] - 1, oy = B.meta[slot ? META_PY2 : META_PY] - 1;
   const bool region_ok = ox >= B.box[0] && oy >= B.box[2] && ox + EX <= B.box[1] && oy + EY <= B.box[3];
   const int64_t n = (int64_t)SP.nx * SP.ny;
-  // Prefetch: the populations of this thread's first window node (read at the end) and
-  // of its own pair's node are both known now and f_in does not change during the step.
+  // The populations of the thread's own pair's node (needed first) and of its first window
+  // node (needed at the end) are both known now and f_in does not change during the step;
+  // the pair's loads are issued first.
   const int kw = rank * nt + tid;
-  int wx = 0, wy = 0, wp = -1;
-  T fw[9];
-  if (kw < NB) {
-    wx = ox + kw / EY;
-    wy = oy + kw % EY;
-    if (wx >= 0 && wx < SP.nx && wy >= 0 && wy < SP.ny && !(SP.skip_walls && (wx == 0 || wx == SP.nx - 1))) {
-      wp = wx * SP.ny + wy;
-#pragma unroll
-      for (int i = 0; i < 9; ++i) fw[i] = __ldg(SP.fin + (size_t)i * n + wp);
-    }
-  }
   const int own = m1 - m0;
   const int lp = tid, m = m0 + lp / S, s = lp - (lp / S) * S;
   const bool has_pair = lp < own * S;
@@ -1339,6 +1331,18 @@ __global__ void __launch_bounds__(kClusterThreads) k_body2d_cluster(const __grid
       const int64_t pn = (int64_t)nxp * SP.ny + nyp;
 #pragma unroll
       for (int i = 0; i < 9; ++i) fl[i] = __ldg(B.fin + i * n + pn);
+    }
+  }
+  // prefetch of the window node, behind the pair's loads
+  int wx = 0, wy = 0, wp = -1;
+  T fw[9];
+  if (kw < NB) {
+    wx = ox + kw / EY;
+    wy = oy + kw % EY;
+    if (wx >= 0 && wx < SP.nx && wy >= 0 && wy < SP.ny && !(SP.skip_walls && (wx == 0 || wx == SP.nx - 1))) {
+      wp = wx * SP.ny + wy;
+#pragma unroll
+      for (int i = 0; i < 9; ++i) fw[i] = __ldg(SP.fin + (size_t)i * n + wp);
     }
   }
   // all marker positions in one round trip (the own pair's above is the same load)
