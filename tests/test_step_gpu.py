@@ -659,3 +659,14 @@ def test_checkpoint_resume_is_bit_exact(S, tmp_path):
     st = body2.state()
     for k in ("a", "v", "d"):
         assert np.array_equal(st[k], sa[k]), k
+
+
+def test_bounded_wait_reports_timeout(S):
+    """A bounded device wait on a barrier that nothing completes gives up and reports
+    VS_ERR_TIMEOUT; the context stays usable for the next launches."""
+    from vivsim_gb300 import _lib as V
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    V.call("vs_selftest_bounded_wait", 4096, V.ptr(status), V.stream())
+    assert int(status.item()) == V.VS_ERR_TIMEOUT
+    t = torch.ones(64, device="cuda")
+    assert S.check_finite(t)

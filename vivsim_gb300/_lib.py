@@ -13,6 +13,7 @@ from . import _build
 
 VS_OK = 0
 VS_ERR_INVALID_ARG = 1
+VS_ERR_TIMEOUT = 5
 VS_ERR_NONFINITE = 6
 VS_F32, VS_F64 = 0, 1
 VS_COLLIDE_BGK, VS_COLLIDE_KBC, VS_COLLIDE_MRT, VS_COLLIDE_REG = 0, 1, 2, 3
@@ -141,6 +142,7 @@ _SIGS = {
     "vs_adjoint_backward": (_i, [_p, _d, C.POINTER(_d), C.POINTER(_d), C.POINTER(_d), _p]),
     "vs_lattice_status": (_i, [_p, _i, _p]),
     "vs_check_finite": (_i, [_i, _p, _l, _p, _p]),
+    "vs_selftest_bounded_wait": (_i, [_i, _p, _p]),
     "vs_fine_to_coarse": (_i, [_i, _p, _i, _i, _p, _i, _i, _i, _p]),
     "vs_coarse_to_fine": (_i, [_i, _p, _i, _i, _p, _i, _i, _i, _p]),
 }

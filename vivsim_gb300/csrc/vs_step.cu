@@ -362,6 +362,19 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, int li
 constexpr int kTmaStages = 4;
 constexpr int kTmaWaitLimit = 1 << 22;  // try_wait suspends in hardware between polls
 
+// Self-test of the bounded waits: an mbarrier expects 16 bytes that no copy delivers (no
+// copy is in flight), the wait gives up after `limit` polls and the kernel reports
+// VS_ERR_TIMEOUT, as the grid and body kernels do when their staged copies never land.
+__global__ void k_selftest_wait(int* status, int limit) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    tma::mbar_init(&bar, 1);
+    tma::fence_init();
+    tma::mbar_expect_tx(&bar, 16);
+    *status = tma::mbar_wait(&bar, 0, limit) ? VS_OK : VS_ERR_TIMEOUT;
+  }
+}
+
 template <class L, typename T, int COLL, int TB>
 __global__ void __launch_bounds__(TB) k_step_tma(const __grid_constant__ StepParams<L, T> P, int tiles,
                                                  int tiles_per_row, int* status) {
@@ -2672,6 +2685,13 @@ int vs_lattice_status(const vs_lattice_plan* plan, int reset, void* stream) {
   if (v == VS_ERR_NONFINITE) set_error("the watchdog found a NaN or Inf population");
   else if (v) set_error("a grid kernel gave up waiting for its bulk copies (device status %d)", v);
   return v;
+}
+
+int vs_selftest_bounded_wait(int limit, int* status_dev, void* stream) {
+  VS_REQUIRE(status_dev && limit > 0 && limit <= (1 << 20), "vs_selftest_bounded_wait: bad arguments");
+  k_selftest_wait<<<1, 32, 0, as_stream(stream)>>>(status_dev, limit);
+  VS_CHECK_LAUNCH("vs_selftest_bounded_wait");
+  return VS_OK;
 }
 
 int vs_check_finite(int dtype, const void* f, int64_t n, int* status_dev, void* stream) {
