@@ -44,3 +44,26 @@ def test_links_must_join_neighbouring_levels():
         S.Refined(blocks, [0, 2], [(0, 1, "right")])
     with pytest.raises(ValueError):
         S.Refined(blocks, [0, 1], [(0, 1, "north")])
+
+
+def test_subcycling_counts_for_random_layouts():
+    """Level L takes 2**(L - L_min) steps per cycle; each link's coarse_to_fine runs once per
+    fine step and its fine_to_coarse once per coarse step."""
+    import random
+    rnd = random.Random(5)
+    for _ in range(30):
+        n_levels = rnd.randint(1, 4)
+        levels = sorted(rnd.randint(0, n_levels - 1) for _ in range(rnd.randint(1, 6)))
+        levels = [lv - levels[0] for lv in levels]
+        links = []
+        for f, lf in enumerate(levels):
+            coarse = [c for c, lc in enumerate(levels) if lc == lf - 1]
+            if coarse:
+                links.append((rnd.choice(coarse), f, rnd.choice(["left", "right", "up", "down"])))
+        R, log = _layout(levels, links)
+        R.run(2)
+        for i, lv in enumerate(levels):
+            assert sum(1 for e in log if e == ("step", i)) == 2 * 2 ** lv
+        for c, f, side in links:
+            assert sum(1 for e in log if e[0] == "coarse_to_fine" and e[1:3] == (c, f)) == 2 * 2 ** levels[f]
+            assert sum(1 for e in log if e[0] == "fine_to_coarse" and e[1:3] == (f, c)) == 2 * 2 ** levels[c]
