@@ -41,31 +41,32 @@ enum {
 // ------------------------------------------------------------------ grid kernel
 template <class L, typename T>
 struct StepParams {
+  // the fields every launch reads come first (a launch fetches only the lines it touches)
   const T* fin;
   T* fout;
   int nx, ny, nz, n;
   int chunks;                    // blocks along the contiguous axis (3-D)
   int gx;                        // blocks per launch row (the launch's grid.x)
   int nreg;                      // 0: the whole grid; else the union of reg[0..nreg)
-  int reg[3][6];                 // regions x0, x1, y0, y1, z0, z1 (half-open)
-  int rowstart[4];               // first launch row (x plane) of each region
   int skip_box;                  // nodes inside box[] are left to another launch
-  int box[6];
   int skip_walls;                // the x = 0 and x = nx-1 planes are left to another launch
-  const uint8_t* mask;           // obstacle cells (one byte per node) or null
   int mask_load;                 // apply the previous step's obstacle bounce-back on load
-  const int* dyn_meta;           // non-null: the skipped box is the body's predicted window,
-  int dyn_slot, dyn_ext[2];      //   read from this prediction slot, extent dyn_ext
-  CollideParams<T> cp;
+  int dyn_slot, dyn_ext[2];      // predicted window: slot and extent (with dyn_meta)
   int forcing;
   int has_g0;
+  int n_lazy;                    // face boundaries of the previous step applied on load
+  int n_pre;                     // faces whose pre-stream populations are kept (bounce-back)
+  const uint8_t* mask;           // obstacle cells (one byte per node) or null
+  const int* dyn_meta;           // non-null: the skipped box is the body's predicted window
+  CollideParams<T> cp;
   T g0[3];
   T guo_scale;                   // 1 - omega / 2 (Guo-BGK)
   const T* gw;                   // IB force window (D, wx, wy, wz) or null
   const int* meta;               // window descriptor (device)
-  int n_lazy;                    // face boundaries of the previous step applied on load
+  int box[6];
+  int reg[3][6];                 // regions x0, x1, y0, y1, z0, z1 (half-open)
+  int rowstart[4];               // first launch row (x plane) of each region
   WallArgs<T> lazy[2];
-  int n_pre;                     // faces whose pre-stream populations are kept (bounce-back)
   int pre_loc[VS_MAX_BC];
   T* pre_buf[VS_MAX_BC];
   T op[L::Q * L::Q];             // MRT collision operator
@@ -493,28 +494,28 @@ __global__ void k_bc(const __grid_constant__ BcGroup<T> G, T* f) {
 template <typename T>
 struct BodyParams {
   const T* fin;
-  int nx, ny;
   const T* X0;
   const T* Y0;
   const T* ds_arr;
-  T ds2_scalar;  // 2 * ds as the reference forms it: (T)ds * 2
-  int M, kernel, n_iter;
-  int chain_k;       // chain kernel: markers share stencil nodes only within +-chain_k (cyclic)
-  int pred_slot;     // cluster kernel: prediction slot to read (the other one is written)
-  int cap_x, cap_y;  // window region: (cap_x + 2) x (cap_y + 2) cells from the predicted corner
-  int row_len;       // staged row length (multiple of 16 bytes), the TMA box's inner extent
-  int bulk;          // stage the region with one tensor-map TMA copy
-  CUtensorMap map;   // f as a (ny, nx, 9) tensor, box (row_len, cap_x + 2, 9)
-  int box[4];  // the window must stay inside x0..x1, y0..y1 (half-open)
   T* state;  // a[3], v[3], d[3], h[3]
   T* gw;
   int* meta;
   T* force_hist;
+  int nx, ny;
+  int M, kernel, n_iter;
+  int chain_k;       // chain kernel: markers share stencil nodes only within +-chain_k (cyclic)
+  int pred_slot;     // prediction slot to read (the cluster form writes the other one)
+  int cap_x, cap_y;  // window region: (cap_x + 2) x (cap_y + 2) cells from the predicted corner
+  int row_len;       // staged row length (multiple of 16 bytes), the TMA box's inner extent
+  int bulk;          // stage the region with one tensor-map TMA copy
+  int box[4];        // the window must stay inside x0..x1, y0..y1 (half-open)
   int free_dof[3];
+  int rot;           // free rotation about (cx, cy): DOF 2 is the angle
+  T ds2_scalar;      // 2 * ds as the reference forms it: (T)ds * 2
   T k1, k2, c1, c2, dt, damp, stiff, den, area;
-  int rot;                                   // free rotation about (cx, cy): DOF 2 is the angle
-  T cx, cy;                                  // initial centre of the body
+  T cx, cy;                                   // initial centre of the body
   T rot_damp, rot_stiff, rot_den, rot_added;  // rotational Newmark constants, added inertia
+  CUtensorMap map;   // f as a (ny, nx, 9) tensor, box (row_len, cap_x + 2, 9)
 };
 
 constexpr int kBodyThreads = 512;
