@@ -55,3 +55,31 @@ def test_invalid_arguments_return_status_without_gpu(lib):
     assert b"distinct" in lib.vs_last_error() or b"q must" in lib.vs_last_error()
     rc = lib.vs_collision(9, 5, 0, C.c_void_p(8), C.c_void_p(8), 1.0, C.c_void_p(8), 4, None)
     assert rc == 1 and b"dtype" in lib.vs_last_error()
+
+
+def test_refinement_and_watchdog_validation_without_gpu(lib):
+    """Shape and argument checks of the refinement transfers, the watchdog scan and the
+    self-test run before any CUDA call (the pointers below are never dereferenced)."""
+    import ctypes as C
+    p = C.c_void_p(64)
+    # fine extent 12 along the interface onto a coarse extent of 5: the reference's shape error
+    assert lib.vs_fine_to_coarse(0, p, 5, 12, p, 7, 5, 0, None) == 1
+    assert b"does not match" in lib.vs_last_error()
+    assert lib.vs_coarse_to_fine(0, p, 7, 4, p, 5, 12, 0, None) == 1
+    assert b"does not match" in lib.vs_last_error()
+    assert lib.vs_fine_to_coarse(0, p, 1, 12, p, 7, 6, 0, None) == 1  # one fine node across
+    assert lib.vs_fine_to_coarse(0, p, 5, 12, p, 7, 6, 7, None) == 1  # no such direction
+    assert b"dir must be" in lib.vs_last_error()
+    assert lib.vs_check_finite(0, None, 10, p, None) == 1
+    assert lib.vs_selftest_bounded_wait(0, p, None) == 1
+    assert lib.vs_selftest_bounded_wait(1 << 21, p, None) == 1
+
+
+def test_plan_validation_without_gpu(lib):
+    """A lattice plan is validated before it allocates: bad wall combinations raise."""
+    from vivsim_gb300 import _lib as V
+    from vivsim_gb300 import solver as S
+    with pytest.raises(V.VivsimError, match="no wall mode"):
+        S.LatticeStep(9, (16, 16), "bgk", 1.0, boundaries=[S.boundary("bounce_back", "right", mode="characteristic")])
+    with pytest.raises(V.VivsimError, match="too small"):
+        S.LatticeStep(9, (3, 16), "bgk", 1.0)
