@@ -79,7 +79,7 @@ def test_plan_validation_without_gpu(lib):
     """A lattice plan is validated before it allocates: bad wall combinations raise."""
     from vivsim_gb300 import _lib as V
     from vivsim_gb300 import solver as S
-    with pytest.raises(V.VivsimError, match="no wall mode"):
+    with pytest.raises(V.VivsimError, match="characteristic wall is imposed by NEE"):
         S.LatticeStep(9, (16, 16), "bgk", 1.0, boundaries=[S.boundary("bounce_back", "right", mode="characteristic")])
     with pytest.raises(V.VivsimError, match="too small"):
         S.LatticeStep(9, (3, 16), "bgk", 1.0)
