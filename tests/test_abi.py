@@ -83,3 +83,15 @@ def test_plan_validation_without_gpu(lib):
         S.LatticeStep(9, (16, 16), "bgk", 1.0, boundaries=[S.boundary("bounce_back", "right", mode="characteristic")])
     with pytest.raises(V.VivsimError, match="too small"):
         S.LatticeStep(9, (3, 16), "bgk", 1.0)
+
+
+def test_jax_adapter_needs_jax():
+    """The XLA FFI adapter imports without JAX and refuses to run without it."""
+    from vivsim_gb300 import jax_ffi
+    try:
+        import jax  # noqa: F401
+        pytest.skip("JAX is installed here")
+    except ImportError:
+        pass
+    with pytest.raises(ImportError):
+        jax_ffi.collision_kbc(None, None, 1.7)
