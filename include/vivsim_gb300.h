@@ -232,11 +232,12 @@ int vs_lattice_plan_destroy(vs_lattice_plan* plan);
  * the watchdog found a NaN/Inf population.  Synchronises the stream; reset != 0 clears it. */
 int vs_lattice_status(const vs_lattice_plan* plan, int reset, void* stream);
 /* NaN/Inf scan of n values: sets *status_dev (a device int) to VS_ERR_NONFINITE when one is
- * not finite and leaves it unchanged otherwise.  Asynchronous. */
+ * not finite and leaves it unchanged otherwise.  Asynchronous.  The reference has no
+ * counterpart (a JAX run would carry the NaN on); this is the fused run's watchdog. */
 int vs_check_finite(int dtype, const void* f, int64_t n, int* status_dev, void* stream);
-/* Failure-detection self-test: one bounded mbarrier wait on bytes that never arrive
- * (limit polls, at most 2^20); *status_dev receives VS_ERR_TIMEOUT and the context stays
- * usable.  Asynchronous. */
+/* Failure-detection self-test (no counterpart in the reference): one bounded mbarrier wait
+ * on bytes that never arrive (limit polls, at most 2^20); *status_dev receives
+ * VS_ERR_TIMEOUT and the context stays usable.  Asynchronous. */
 int vs_selftest_bounded_wait(int limit, int* status_dev, void* stream);
 
 /* Immersed body advanced by the IB step (dyn.py + ib/mdf.py).  Markers follow a rigid
