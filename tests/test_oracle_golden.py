@@ -347,3 +347,38 @@ def test_recipe_characteristic_outflow_3d(mode):
         f = recipes.lbm_step_3d(f, "bgk", om, bcs=bcs)
         if step in (1, 4):
             check(mode, f, f"cbc3.f{step}", TOL_RECIPE[mode])
+
+
+def test_oracle_known_answers():
+    """The oracle on two of the reference's known-answer examples (CPU, a few seconds):
+    the Taylor-Green vortex decay (examples/2d/taylor_green_vortex.py, 64^2, 4000 steps)
+    and Couette flow (examples/2d/couette_flow.py, 16^2, 12000 steps) against their
+    analytic fields."""
+    n, u0, nu = 64, 0.02, 0.02
+    k = 2 * math.pi / n
+    x = np.arange(n, dtype=np.float32)[:, None]
+    y = np.arange(n, dtype=np.float32)[None, :]
+
+    def tgv(t):
+        dec = np.exp(-nu * 2 * k * k * t)
+        return np.stack([u0 * np.sin(k * x) * np.cos(k * y) * dec,
+                         -u0 * np.cos(k * x) * np.sin(k * y) * dec]).astype(np.float32)
+    om = L2.get_omega(nu)
+    f = L2.get_equilibrium(np.ones((n, n), np.float32), tgv(0.0))
+    for _ in range(4000):
+        r, u = L2.get_macroscopic(f)
+        f = L2.streaming(L2.collision_bgk(f, L2.get_equilibrium(r, u), om))
+    _, u = L2.get_macroscopic(f)
+    ut = tgv(4000.0)
+    assert np.linalg.norm(u - ut) / np.linalg.norm(ut) < 3e-3
+    n, u0, nu = 16, 0.08, 0.10
+    om = L2.get_omega(nu)
+    f = L2.get_equilibrium(np.ones((n, n), np.float32), np.zeros((2, n, n), np.float32))
+    for _ in range(12000):
+        r, u = L2.get_macroscopic(f)
+        f = L2.streaming(L2.collision_bgk(f, L2.get_equilibrium(r, u), om))
+        f = L2.boundary_nee(f, "bottom")
+        f = L2.boundary_nee(f, "top", ux_wall=u0)
+    _, u = L2.get_macroscopic(f)
+    ut = np.broadcast_to(u0 * np.arange(n, dtype=np.float32) / (n - 1), (n, n))
+    assert np.linalg.norm(u[0] - ut) / np.linalg.norm(ut) < 1e-4
