@@ -464,9 +464,22 @@ def oracle_stepper(case):
     return one
 
 
+def cpu_stepper(case):
+    """(step closure, threads, description): the oracle's step over all host cores
+    (oracle/threaded.py, bit-equal to the serial restatement), or the serial one where
+    the threaded step does not apply (3-D bodies)."""
+    from oracle.threaded import ThreadedStep
+    try:
+        t = ThreadedStep(case)
+    except NotImplementedError:
+        return oracle_stepper(case), 1, "NumPy restatement of the reference, single thread"
+    return t, t.threads, f"NumPy restatement of the reference, node stages split over {t.threads} threads"
+
+
 def cpu_baseline(case, budget_s):
-    """Oracle (NumPy, one core) on a bounded sample of the same workload: full grid, few steps."""
-    one = oracle_stepper(case)
+    """The oracle on the host's cores on a bounded sample of the same workload: full grid,
+    few steps."""
+    one, cores, what = cpu_stepper(case)
     n = int(math.prod(case["shape"]))
     t0 = time.perf_counter()
     one()  # first step (allocation warm-up) is timed too, it is a full step
@@ -475,8 +488,8 @@ def cpu_baseline(case, budget_s):
         one()
         steps += 1
     secs = time.perf_counter() - t0
-    return {"value": round(n * steps / secs / 1e6, 3), "unit": "MLUPS", "cores": 1, "kind": "port",
-            "sample": f"{steps} time steps of {case['name']} on the full grid (NumPy oracle, single thread)"}
+    return {"value": round(n * steps / secs / 1e6, 3), "unit": "MLUPS", "cores": cores, "kind": "port",
+            "sample": f"{steps} time steps of {case['name']} on the full grid ({what})"}
 
 
 def reference_arm(args, world, rank):
@@ -484,7 +497,7 @@ def reference_arm(args, world, rank):
         return
     from vivsim_gb300 import configs
     case = configs.CASES[args.workload]()
-    one = oracle_stepper(case)
+    one, cores, what = cpu_stepper(case)
     n = int(math.prod(case["shape"]))
     for _ in range(args.warmup):
         one()
@@ -499,9 +512,9 @@ def reference_arm(args, world, rank):
         "ms_per_step": round(secs / args.steps * 1e3, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded numpy draws of the named configuration)",
         "config": {"workload": case["name"], "time_steps_per_bench_step": 1, "nodes": n},
-        "cpu_baseline": {"value": round(v, 3), "unit": "MLUPS", "cores": 1, "kind": "port",
+        "cpu_baseline": {"value": round(v, 3), "unit": "MLUPS", "cores": cores, "kind": "port",
                          "sample": f"{args.steps} timed time steps of {case['name']} on the full grid "
-                                   "(NumPy restatement of the reference; JAX is not installed)"},
+                                   f"({what}; JAX is not installed)"},
         "e2e": {"value": round(v, 3), "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)

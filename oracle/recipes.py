@@ -131,6 +131,17 @@ def ib_lbm_step_2d(f, body, collision, omega=None, mrt_op=None, bcs=()):
     rho, u = L2.get_macroscopic(f)
     feq = L2.get_equilibrium(rho, u)
     f = _collide(L2, f, feq, collision, omega, mrt_op)
+    g, h = body_forces_2d(u, body, ny)
+    f = L2.forcing_edm(f, g, u)
+    f_post = f
+    f = L2.streaming(f)
+    return _apply_bcs(L2, _BC2, f_post, f, bcs, (rho, u)), h
+
+
+def body_forces_2d(u, body, ny):
+    """The immersed-boundary part of ib_lbm_step_2d (examples/2d/vortex_induced_vibration.py:
+    108-141): marker kinematics, stencil, MDF, body force (and torque) and the Newmark
+    update of ``body``.  Returns the grid force g and the body force h."""
     M = body.X0.shape[0]
     if body.rot:  # markers turn with d[2] about the initial centre (dyn.py:84-120)
         cx, cy = body.center
@@ -152,10 +163,7 @@ def ib_lbm_step_2d(f, body, collision, omega=None, mrt_op=None, bcs=()):
             m, kk, c = (body.mass, body.k, body.c) if k < 2 else (body.inertia, body.rot_k, body.rot_c)
             a[k], v[k], d[k] = dyn.newmark(body.a[k], body.v[k], body.d[k], h[k], m, kk, c)
     body.a, body.v, body.d = a, v, d
-    f = L2.forcing_edm(f, g, u)
-    f_post = f
-    f = L2.streaming(f)
-    return _apply_bcs(L2, _BC2, f_post, f, bcs, (rho, u)), h
+    return g, h
 
 
 def lbm_step_3d(f, collision, omega=None, mrt_op=None, bcs=()):

@@ -382,3 +382,45 @@ def test_oracle_known_answers():
     _, u = L2.get_macroscopic(f)
     ut = np.broadcast_to(u0 * np.arange(n, dtype=np.float32) / (n - 1), (n, n))
     assert np.linalg.norm(u[0] - ut) / np.linalg.norm(ut) < 1e-4
+
+
+def test_threaded_cpu_step_equals_the_serial_recipes():
+    """The CPU baseline's thread-parallel step (oracle/threaded.py) gives the serial
+    recipes' bits: VIV with a moving body, the cavity, and a D3Q19 channel."""
+    from oracle.threaded import ThreadedStep
+    from vivsim_gb300 import configs
+    viv = configs.viv2d(nx=96, ny=64, D=12.0, center=(30.0, 32.0), n_markers=38, seed=5)
+    b = viv["body"]
+    X = b["markers"].astype(np.float32)
+    body = recipes.Body2D(X[:, 0], X[:, 1], b["ds"], b["mass"], b["stiffness"], b["damping"], b["added_mass_area"],
+                          free=b["free_dof"][:2], kernel=b["kernel"], n_iter=b["n_iter"])
+    t = ThreadedStep(viv, threads=4)
+    f = viv["f0"].copy()
+    for _ in range(3):
+        t()
+        f, _ = recipes.ib_lbm_step_2d(f, body, viv["collision"], viv["omega"], None, t.bcs)
+    assert np.array_equal(t.f, f)
+    assert np.array_equal(t.body.d, body.d) and np.array_equal(t.body.v, body.v)
+    t.close()
+    cav = configs.cavity(n=32)
+    t = ThreadedStep(cav, threads=3)
+    f = cav["f0"].copy()
+    for _ in range(3):
+        t()
+        f = recipes.lbm_step_2d(f, cav["collision"], cav["omega"], None, t.bcs)
+    assert np.array_equal(t.f, f)
+    t.close()
+    n = (12, 8, 6)
+    rng = np.random.default_rng(3)
+    u = (0.02 * rng.standard_normal((3,) + n)).astype(np.float32)
+    f0 = L3.get_equilibrium(np.ones(n, np.float32), u)
+    ch = dict(q=19, collision="reg", omega=1.7, body=None, f0=f0,
+              boundaries=[("equilibrium", "left", "given", dict(ux_wall=0.03)),
+                          ("nee", "right", "pressure", dict(rho_wall=1.0))])
+    t = ThreadedStep(ch, threads=4)
+    f = f0.copy()
+    for _ in range(3):
+        t()
+        f = recipes.lbm_step_3d(f, "reg", 1.7, None, t.bcs)
+    assert np.array_equal(t.f, f)
+    t.close()
