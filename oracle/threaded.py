@@ -85,14 +85,18 @@ class ThreadedStep:
         self.op = L2.get_mrt_collision_operator(self.om, np.float32) if (self.coll == "mrt" and self.q == 9) else None
         self.f = case["f0"].copy()
         self.body = None
+        self.body3 = None
         b = case["body"]
-        if b is not None:
-            if self.q != 9:
-                raise NotImplementedError("threaded CPU step: 2-D bodies only")
+        if b is not None and self.q == 9:
             X = b["markers"].astype(np.float32)
             self.body = recipes.Body2D(X[:, 0], X[:, 1], b["ds"], b["mass"], b["stiffness"], b["damping"],
                                        b["added_mass_area"], free=b["free_dof"][:2], kernel=b["kernel"],
                                        n_iter=b["n_iter"])
+        elif b is not None:  # a fixed 3-D body: static stencil (recipes.ib_lbm_step_3d)
+            from . import ib as OIB
+            X = b["markers"].astype(np.float32)
+            W, I = OIB.get_ib_stencil_3d(X, case["shape"])
+            self.body3 = (W, I, np.zeros((X.shape[0], 3), np.float32), b["ds"], b["n_iter"])
         self.threads = threads or host_threads()
         nx = self.f.shape[1]
         k = min(self.threads * 2, nx)
@@ -122,12 +126,17 @@ class ThreadedStep:
             fp[:, lo:hi] = recipes._collide(L, f[:, lo:hi], L.get_equilibrium(r, uu), self.coll, self.om, self.op)
 
         self._map(collide, self.slabs)
+        g = None
         if self.body is not None:
             g, _ = recipes.body_forces_2d(u, self.body, grid[1])
-
+        elif self.body3 is not None:
+            from . import ib as OIB
+            W, I, mu, ds, n_iter = self.body3
+            g, _ = OIB.multi_direct_forcing(u, W, I, mu, ds, n_iter)
+        if g is not None:
             def force(sl):
                 lo, hi = sl
-                fp[:, lo:hi] = L2.forcing_edm(fp[:, lo:hi], g[:, lo:hi], u[:, lo:hi])
+                fp[:, lo:hi] = L.forcing_edm(fp[:, lo:hi], g[:, lo:hi], u[:, lo:hi])
 
             self._map(force, self.slabs)
         out = np.empty_like(fp)

@@ -424,3 +424,15 @@ def test_threaded_cpu_step_equals_the_serial_recipes():
         f = recipes.lbm_step_3d(f, "reg", 1.7, None, t.bcs)
     assert np.array_equal(t.f, f)
     t.close()
+    sph = configs.sphere3d(nx=32, ny=24, nz=24, D=8.0, center=(12.0, 12.0, 12.0), n_markers=200)
+    t = ThreadedStep(sph, threads=4)
+    b = sph["body"]
+    X = b["markers"].astype(np.float32)
+    W, I = ib.get_ib_stencil_3d(X, sph["shape"])
+    f = sph["f0"].copy()
+    for _ in range(2):
+        t()
+        f, _ = recipes.ib_lbm_step_3d(f, W, I, np.zeros((X.shape[0], 3), np.float32), b["ds"], sph["collision"],
+                                      sph["omega"], None, t.bcs, b["n_iter"])
+    assert np.array_equal(t.f, f)
+    t.close()
