@@ -95,3 +95,23 @@ def test_jax_adapter_needs_jax():
         pass
     with pytest.raises(ImportError):
         jax_ffi.collision_kbc(None, None, 1.7)
+
+
+def test_plain_c_host(tmp_path):
+    """A C99 program includes the header, links the library and runs its argument checks
+    (tests/c_host/abi_check.c; no GPU needed)."""
+    import shutil
+    import subprocess
+    from vivsim_gb300 import _build
+    cc = shutil.which("gcc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    lib = _build.lib_path()
+    if not os.path.exists(lib):
+        _build.build()
+    exe = str(tmp_path / "abi_check")
+    subprocess.run([cc, "-std=c99", "-Wall", os.path.join(ROOT, "tests", "c_host", "abi_check.c"), "-o", exe,
+                    "-I", os.path.join(ROOT, "include"), "-L", os.path.dirname(lib), "-lvivsim_gb300",
+                    "-Wl,-rpath," + os.path.dirname(lib)], check=True)
+    r = subprocess.run([exe], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
