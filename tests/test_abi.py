@@ -115,3 +115,16 @@ def test_plain_c_host(tmp_path):
                     "-Wl,-rpath," + os.path.dirname(lib)], check=True)
     r = subprocess.run([exe], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
+
+
+def test_solver_rejects_unknown_names():
+    """Unknown schemes, wall modes, faces, collisions and forcings raise ValueError (as the
+    reference raises on an unknown face) before anything is allocated."""
+    from vivsim_gb300 import solver as S
+    for bad in (S.boundary("neex", "left"), S.boundary("nee", "leftish"), S.boundary("nee", "left", mode="fast")):
+        with pytest.raises(ValueError):
+            S.LatticeStep(9, (16, 16), "bgk", 1.0, boundaries=[bad])
+    with pytest.raises(ValueError):
+        S.LatticeStep(9, (16, 16), "lbgk", 1.0)
+    with pytest.raises(ValueError):
+        S.LatticeStep(9, (16, 16), "bgk", 1.0, forcing="shan_chen")

@@ -66,6 +66,10 @@ class LatticeStep:
         if len(self.shape) != self.dim:
             raise ValueError(f"shape must have {self.dim} entries")
         self.dtype = _tdtype(dtype)
+        if collision not in COLLISIONS:
+            raise ValueError(f"collision must be one of {', '.join(repr(x) for x in COLLISIONS)}")
+        if forcing not in FORCINGS:
+            raise ValueError(f"forcing must be one of {', '.join(repr(x) for x in FORCINGS)}")
         self.collision = collision
         self.omega = float(omega)
         cfg = V.vs_lattice_cfg()
@@ -93,6 +97,9 @@ class LatticeStep:
         cfg.n_bc = len(boundaries)
         for k, b in enumerate(boundaries):
             s = cfg.bc[k]
+            for key, table in (("kind", BC_KINDS), ("mode", WALL_MODES), ("loc", V.LOCS)):
+                if b[key] not in table:
+                    raise ValueError(f"boundary {k}: {key} must be one of {', '.join(repr(x) for x in table)}")
             s.kind = BC_KINDS[b["kind"]]
             s.mode = WALL_MODES[b["mode"]]
             s.loc = V.LOCS[b["loc"]]
