@@ -17,7 +17,11 @@ from oracle import dyn, ib
 from oracle import lbm2d as L2
 from oracle import lbm3d as L3
 from oracle import recipes
+from oracle.lattice import Q9_C as Q9_C_
 from oracle.lattice import Q9_FACES, Q19_FACES
+from oracle.lattice import Q9_OPP as Q9_OPP_
+from oracle.lattice import Q19_C as Q19_C_
+from oracle.lattice import Q19_OPP as Q19_OPP_
 
 TOL = {"f32": 2e-6, "f64": 1e-12}
 TOL_RECIPE = {"f32": 2e-5, "f64": 1e-11}
@@ -436,3 +440,34 @@ def test_threaded_cpu_step_equals_the_serial_recipes():
                                       sph["omega"], None, t.bcs, b["n_iter"])
     assert np.array_equal(t.f, f)
     t.close()
+
+
+@pytest.mark.parametrize("coll", ["bgk", "kbc", "reg", "mrt"])
+def test_oracle_collisions_conserve_mass_and_momentum(coll):
+    """Every collision of the oracle keeps each node's density and momentum (float64 data).
+    The lattice weights are float32 values, as in the reference under x64, so the
+    equilibrium's moments match rho and rho u only to about 1e-8."""
+    rng = np.random.default_rng(6)
+    for L, q, shape in ((L2, 9, (6, 5)), (L3, 19, (4, 3, 5))):
+        d = len(shape)
+        rho = 1 + 0.05 * rng.standard_normal(shape)
+        u = 0.05 * rng.standard_normal((d,) + shape)
+        feq = L.get_equilibrium(rho, u)
+        f = feq + 0.01 * rng.standard_normal((q,) + shape) * feq
+        op = L.get_mrt_collision_operator(1.7, np.float64) if coll == "mrt" else None
+        fo = recipes._collide(L, f, L.get_equilibrium(*L.get_macroscopic(f)), coll, 1.7, op)
+        r0, u0 = L.get_macroscopic(f)
+        r1, u1 = L.get_macroscopic(fo)
+        assert np.max(np.abs(r1 - r0)) < 1e-7, (coll, q)
+        assert np.max(np.abs(r1 * u1 - r0 * u0)) < 1e-7, (coll, q)
+
+
+def test_oracle_streaming_is_a_permutation():
+    """Streaming moves every population to its neighbour and back again."""
+    rng = np.random.default_rng(8)
+    for L, C, opp, shape in ((L2, Q9_C_, Q9_OPP_, (7, 5)), (L3, Q19_C_, Q19_OPP_, (4, 5, 3))):
+        f = rng.random((len(opp),) + shape)
+        g = L.streaming(f)
+        back = L.streaming(g[list(opp)])[list(opp)]
+        assert np.array_equal(back, f)
+        assert np.allclose(g.sum(axis=tuple(range(1, g.ndim))), f.sum(axis=tuple(range(1, f.ndim))))
