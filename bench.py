@@ -255,22 +255,25 @@ def adjoint_over_forward(torch, steps):
     plan.forward(keep_checkpoints=True)
     plan.backward()  # captures the graphs (untimed)
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    J = plan.forward(keep_checkpoints=False)
-    t_fwd = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    plan.forward(keep_checkpoints=True)
-    t_fck = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    gU0, gK, goff = plan.backward()
-    t_bwd = time.perf_counter() - t0
+
+    def timed(fn):  # CUDA events on the stream the plan launches on (each call ends with a sync)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        out = fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return out, e0.elapsed_time(e1) / 1e3
+
+    J, t_fwd = timed(lambda: plan.forward(keep_checkpoints=False))
+    _, t_fck = timed(lambda: plan.forward(keep_checkpoints=True))
+    (gU0, gK, goff), t_bwd = timed(plan.backward)
     plan.close()
     return {"workload": f"diff_cylinder_d2q9_bgk_512x256_m64_{steps}steps_ckpt100", "objective": J,
             "forward_s": round(t_fwd, 4), "forward_with_checkpoints_s": round(t_fck, 4),
             "reverse_s": round(t_bwd, 4), "adjoint_over_forward": round(t_bwd / t_fwd, 3),
             "gradient_over_forward": round((t_fck + t_bwd) / t_fwd, 3),
             "grad_U0": gU0, "grad_stiffness": gK, "grad_offsets_norm": float(np.linalg.norm(goff)),
-            "timing": "host wall clock around synchronising calls (each call ends with a stream sync)"}
+            "timing": "CUDA events on the launching stream around each call (each call ends with a stream sync)"}
 
 
 def job_seconds(torch, dist, secs, device):
@@ -389,10 +392,10 @@ def gb300_arm(args, world, rank, local):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic (seeded numpy draws of the named configuration)",
-        "config": {"workload": case["name"], "time_steps_per_bench_step": args.chunk, "nodes": n,
-                   "l2": "flushed (512 MiB write) before every bench step; the two population buffers "
-                         f"({2 * n * BYTES_PER_UPDATE[case['q']] // 2 / 1e6:.1f} MB) stay L2-resident within one",
-                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+        "config": arm_config(case, world),
+        "time_steps_per_bench_step": args.chunk,
+        "l2": "flushed (512 MiB write) before every bench step; the two population buffers "
+              f"({2 * n * BYTES_PER_UPDATE[case['q']] // 2 / 1e6:.1f} MB) stay L2-resident within one",
         "roofline": rl,
         "roofline_hbm_bound": extras,
         "batched_vs_sequential": extras_batch,
@@ -408,6 +411,12 @@ def gb300_arm(args, world, rank, local):
     print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
+
+
+def arm_config(case, world):
+    """The workload as both arms name it (the same dict on the GPU arm and the reference arm)."""
+    return {"workload": case["name"], "nodes": int(math.prod(case["shape"])),
+            "parallelism": f"replicas x{world}" if world > 1 else "single GPU"}
 
 
 def step_groups(case):
@@ -492,29 +501,125 @@ def cpu_baseline(case, budget_s):
             "sample": f"{steps} time steps of {case['name']} on the full grid ({what})"}
 
 
+REF_DIR = os.path.join(HERE, "baseline", "_ref")
+
+
+def reference_probe():
+    """Can the reference itself run here?  vivsim is installed without its dependencies
+    under baseline/_ref; its JAX path needs JAX.  Returns (True, detail) or (False, why)."""
+    if not os.path.isdir(os.path.join(REF_DIR, "vivsim")):
+        return False, "the reference is not installed under baseline/_ref"
+    try:
+        import jax  # noqa: F401
+    except Exception as e:  # ImportError, or a broken install
+        return False, f"vivsim is installed under baseline/_ref but import jax failed ({type(e).__name__}: {e})"
+    return True, f"jax {jax.__version__}"
+
+
+def reference_jax_stepper(case, chunk):
+    """The reference's own time step for `case`: vivsim's functions (from baseline/_ref)
+    composed as its examples compose them (examples/2d/lid_driven_cavity.py:55-63,
+    examples/2d/vortex_induced_vibration.py:96-148 with a full-grid stencil,
+    examples/3d/flow_past_sphere.py:139-180 with a static stencil), jitted over a
+    lax.scan of `chunk` steps on the host CPU in float32.  Returns (run, threads, what):
+    run() advances `chunk` steps and blocks until they are done."""
+    os.environ.setdefault("JAX_PLATFORMS", "cpu")
+    if REF_DIR not in sys.path:
+        sys.path.insert(0, REF_DIR)
+    import jax
+    import jax.numpy as jnp
+    from vivsim import dyn, ib, ib3d, lbm, lbm3d
+
+    q, coll, om = case["q"], case["collision"], case["omega"]
+    L = lbm if q == 9 else lbm3d
+    names = {("nee", "given"): "boundary_nee", ("nebb", "given"): "boundary_nebb",
+             ("equilibrium", "given"): "boundary_equilibrium", ("nee", "pressure"): "boundary_pressure_nee",
+             ("nee", "velocity"): "boundary_velocity_nee", ("nebb", "force_corrected"): "boundary_force_corrected_nebb"}
+    bcs = [(getattr(L, names[(k, m)]), loc, kw) for (k, loc, m, kw) in case["boundaries"]]
+    if coll == "mrt":
+        mrt_op = L.get_mrt_collision_operator(om)
+        collide = lambda f, feq: L.collision_mrt(f, feq, mrt_op)  # noqa: E731
+    else:
+        fn = {"bgk": L.collision_bgk, "kbc": L.collision_kbc, "reg": L.collision_reg}[coll]
+        collide = lambda f, feq: fn(f, feq, om)  # noqa: E731
+    b = case["body"]
+    kern = {"peskin3": ib.kernel_peskin_3pt, "peskin4": ib.kernel_peskin_4pt, "cosine4": ib.kernel_cosine_4pt}
+    if b is not None and q == 19:
+        X = jnp.asarray(b["markers"], jnp.float32)
+        W3, I3 = ib3d.get_ib_stencil(X, tuple(case["shape"]), kernel=kern[b["kernel"]], stencil_radius=b["radius"])
+        mu0 = jnp.zeros((X.shape[0], 3), jnp.float32)
+    if b is not None and q == 9:
+        X0 = jnp.asarray(b["markers"][:, 0], jnp.float32)
+        Y0 = jnp.asarray(b["markers"][:, 1], jnp.float32)
+        ny = case["shape"][1]
+        free = b["free_dof"][:2]
+
+    def step(carry, _):
+        f, a, v, d = carry
+        rho, u = L.get_macroscopic(f)
+        f = collide(f, L.get_equilibrium(rho, u))
+        if b is not None and q == 9:
+            mx, my = dyn.get_markers_coords_2dof(X0, Y0, d)
+            W, I = ib.get_ib_stencil(mx, my, ny, kernel=kern[b["kernel"]], stencil_radius=b["radius"])
+            mv = jnp.repeat(v[None, :], X0.shape[0], axis=0)
+            g, mh = ib.multi_direct_forcing(u, W, I, mv, b["ds"], n_iter=b["n_iter"])
+            h = dyn.get_force_to_obj(mh) + a * b["added_mass_area"]
+            an, vn, dn = dyn.newmark(a, v, d, h, b["mass"], b["stiffness"], b["damping"])
+            keep = jnp.asarray([0.0 if fr else 1.0 for fr in free], jnp.float32)
+            a, v, d = (keep * a + (1 - keep) * an, keep * v + (1 - keep) * vn, keep * d + (1 - keep) * dn)
+            f = L.forcing_edm(f, g, u)
+        elif b is not None:
+            g, _mh = ib.multi_direct_forcing(u, W3, I3, mu0, b["ds"], n_iter=b["n_iter"])
+            f = L.forcing_edm(f, g, u)
+        f = L.streaming(f)
+        for fn, loc, kw in bcs:
+            f = fn(f, loc=loc, **kw)
+        return (f, a, v, d), None
+
+    run_chunk = jax.jit(lambda carry: jax.lax.scan(step, carry, None, length=chunk)[0])
+    z = jnp.zeros(2, jnp.float32)
+    state = {"c": (jnp.asarray(case["f0"]), z, z, z)}
+
+    def run():
+        state["c"] = jax.block_until_ready(run_chunk(state["c"]))
+
+    threads = os.cpu_count() or 1
+    return run, threads, f"the reference's own JAX path (jit + lax.scan of {chunk} steps, XLA CPU)"
+
+
 def reference_arm(args, world, rank):
     if rank != 0:
         return
     from vivsim_gb300 import configs
     case = configs.CASES[args.workload]()
-    one, cores, what = cpu_stepper(case)
     n = int(math.prod(case["shape"]))
+    ok, probe = reference_probe()
+    if ok:  # the reference's own JAX CPU path: a bench step is one scanned chunk of steps
+        chunk = 10
+        one, cores, what = reference_jax_stepper(case, chunk)
+        kind = "reference"
+    else:  # the oracle's restatement of the reference over the host cores
+        chunk = 1
+        one, cores, what = cpu_stepper(case)
+        kind = "port"
     for _ in range(args.warmup):
         one()
     t0 = time.perf_counter()
     for _ in range(args.steps):
         one()
     secs = time.perf_counter() - t0
-    v = n * args.steps / secs / 1e6
+    v = n * chunk * args.steps / secs / 1e6
     line = {
         "impl": "reference", "metric": "MLUPS (fused IB-LBM step; HBM roofline per fused step)", "value": round(v, 3),
         "unit": "MLUPS", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(secs / args.steps * 1e3, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded numpy draws of the named configuration)",
-        "config": {"workload": case["name"], "time_steps_per_bench_step": 1, "nodes": n},
-        "cpu_baseline": {"value": round(v, 3), "unit": "MLUPS", "cores": cores, "kind": "port",
-                         "sample": f"{args.steps} timed time steps of {case['name']} on the full grid "
-                                   f"({what}; JAX is not installed)"},
+        "config": arm_config(case, world),
+        "time_steps_per_bench_step": chunk,
+        "reference_probe": probe,
+        "cpu_baseline": {"value": round(v, 3), "unit": "MLUPS", "cores": cores, "kind": kind,
+                         "sample": f"{args.steps * chunk} timed time steps of {case['name']} on the full grid "
+                                   f"({what})"},
         "e2e": {"value": round(v, 3), "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)

@@ -32,7 +32,11 @@ enum {
   VS_ERR_UNSUPPORTED = 3, /* valid request this build does not implement           */
   VS_ERR_RANGE = 4,       /* a stencil index / window fell outside its grid        */
   VS_ERR_TIMEOUT = 5,     /* a bounded device-side wait gave up                    */
-  VS_ERR_NONFINITE = 6    /* the NaN/Inf watchdog saw a non-finite population      */
+  VS_ERR_NONFINITE = 6,   /* the NaN/Inf watchdog saw a non-finite population      */
+  VS_ERR_TIMEOUT_INFLIGHT = 7 /* a wait gave up and a bulk copy it waited for had not
+                               * landed by the end of a second bounded wait: the copy may
+                               * write shared memory after its block left, so device state
+                               * is not to be trusted (start a new context)              */
 };
 enum { VS_F32 = 0, VS_F64 = 1 };
 enum { VS_COLLIDE_BGK = 0, VS_COLLIDE_KBC = 1, VS_COLLIDE_MRT = 2, VS_COLLIDE_REG = 3 };
@@ -146,12 +150,15 @@ int vs_ib_mdf(int dtype, const void* grid_u, int c, int64_t n_grid, const void* 
               const void* u_target, const void* ds, double ds_scalar, int n_iter, void* grid_force,
               void* marker_force, void* workspace, size_t workspace_bytes, void* stream);
 
-/* spread() like vs_ib_spread, for callers that may not allocate device memory while they
- * run (an open CUDA graph capture, a host runtime that owns all device memory and passes
- * no workspace).  No counterpart in the reference: vivsim's spread is a JAX scatter-add
- * whose scratch XLA provides.  Scratch is a fixed 4 MiB device array of the library, one
- * per device, looked up by the first call on each device (make that call before any
- * stream capture); nothing is allocated.  Limit: m * s <= 65536 marker-stencil pairs
+/* spread() like vs_ib_spread, for callers that cannot allocate device memory while they
+ * run: a host runtime that owns every device allocation and hands its custom calls no
+ * scratch (an XLA FFI handler registered without a workspace, an engine with its own
+ * pool), or a real-time loop that may not enter the allocator.  No counterpart in the
+ * reference: vivsim's spread is a JAX scatter-add whose scratch XLA provides.  Scratch is
+ * a fixed 4 MiB device array of the library, one per device, held until the process
+ * exits; the first call on each device looks its address up (make that call before any
+ * stream capture), and so does the first call after the device's context was replaced
+ * (cudaDeviceReset); nothing is allocated.  Limit: m * s <= 65536 marker-stencil pairs
  * (4096 markers of a 4x4 stencil), else VS_ERR_INVALID_ARG.  All calls on a device share
  * the scratch, so calls that may overlap on the device (different streams, several host
  * threads) race: issue them in order on one stream.  Results equal vs_ib_spread's. */
@@ -228,8 +235,10 @@ typedef struct vs_lattice_plan vs_lattice_plan;
 int vs_lattice_plan_create(const vs_lattice_cfg* cfg, vs_lattice_plan** out);
 int vs_lattice_plan_destroy(vs_lattice_plan* plan);
 /* Device status of the plan's grid kernels: VS_OK, VS_ERR_TIMEOUT when a bounded wait
- * for a bulk copy gave up (that launch left its nodes unwritten), or VS_ERR_NONFINITE when
- * the watchdog found a NaN/Inf population.  Synchronises the stream; reset != 0 clears it. */
+ * for a bulk copy gave up (that launch left its nodes unwritten; the late copies landed
+ * before the block left), VS_ERR_TIMEOUT_INFLIGHT when a late copy had still not landed
+ * after a second bounded wait, or VS_ERR_NONFINITE when the watchdog found a NaN/Inf
+ * population.  Synchronises the stream; reset != 0 clears it. */
 int vs_lattice_status(const vs_lattice_plan* plan, int reset, void* stream);
 /* NaN/Inf scan of n values: sets *status_dev (a device int) to VS_ERR_NONFINITE when one is
  * not finite and leaves it unchanged otherwise.  Asynchronous.  The reference has no
@@ -265,6 +274,10 @@ typedef struct vs_body_cfg {
   int window_margin;     /* extra nodes around the marker stencils reserved for motion */
   double center_x, center_y;                 /* 2-D rotation: initial centre of the body  */
   double inertia, rot_stiffness, rot_damping, added_inertia;
+  int fsi_iter;          /* 2-D moving body: fluid-structure sub-iterations per step (0 or 1:
+                          * one pass).  Each pass places the markers with the latest state,
+                          * redoes stencil, MDF and force, and restarts Newmark from the
+                          * step's saved state (examples/2d/vortex_induced_vibration.py:114-139) */
 } vs_body_cfg;
 
 typedef struct vs_body_plan vs_body_plan;

@@ -100,12 +100,14 @@ class Body2D:
 
     ``free`` has two entries (x, y translation) or three; a free third DOF is the rotation
     angle about ``center`` (dyn.get_markers_coords_3dof), integrated with ``inertia``,
-    ``rot_k``, ``rot_c`` and the added inertia ``rot_added``.
+    ``rot_k``, ``rot_c`` and the added inertia ``rot_added``.  ``fsi_iter`` is the number of
+    fluid-structure sub-iterations per step (examples/2d/vortex_induced_vibration.py:114-139).
     """
 
     def __init__(self, X0, Y0, ds, mass, stiffness, damping, area, free=(False, True),
                  kernel="peskin4", radius=2, n_iter=3, d=None, v=None, a=None, center=None, inertia=0.0,
-                 rot_k=0.0, rot_c=0.0, rot_added=0.0):
+                 rot_k=0.0, rot_c=0.0, rot_added=0.0, fsi_iter=1):
+        self.fsi_iter = int(fsi_iter)
         self.X0, self.Y0 = np.asarray(X0), np.asarray(Y0)
         self.ds, self.mass, self.k, self.c, self.area = ds, mass, stiffness, damping, area
         self.free = tuple(bool(x) for x in free)
@@ -141,27 +143,32 @@ def ib_lbm_step_2d(f, body, collision, omega=None, mrt_op=None, bcs=()):
 def body_forces_2d(u, body, ny):
     """The immersed-boundary part of ib_lbm_step_2d (examples/2d/vortex_induced_vibration.py:
     108-141): marker kinematics, stencil, MDF, body force (and torque) and the Newmark
-    update of ``body``.  Returns the grid force g and the body force h."""
+    update of ``body``, repeated ``body.fsi_iter`` times: each pass places the markers with
+    the latest state and restarts Newmark from the step's saved one (:111-139).  Returns the
+    last pass's grid force g and body force h."""
     M = body.X0.shape[0]
-    if body.rot:  # markers turn with d[2] about the initial centre (dyn.py:84-120)
-        cx, cy = body.center
-        mx, my = dyn.get_markers_coords_3dof(body.X0, body.Y0, cx, cy, body.d)
-        mv = dyn.get_markers_velocity_3dof(mx, my, cx, cy, body.d, body.v)
-    else:
-        mx, my = dyn.get_markers_coords_2dof(body.X0, body.Y0, body.d)
-        mv = np.repeat(body.v[None, :], M, axis=0)
-    W, I = ib.get_ib_stencil(mx, my, ny, ib.KERNELS[body.kernel], body.radius)
-    g, mh = ib.multi_direct_forcing(u, W, I, mv, body.ds, body.n_iter)
-    h = dyn.get_force_to_obj(mh)
-    h = h + body.a[:2] * body.area
-    if body.rot:  # torque (dyn.py:139-154) plus added inertia
-        tq = dyn.get_torque_to_obj(mx, my, cx, cy, body.d, mh)
-        h = np.concatenate([h, np.asarray([tq + body.a[2] * body.rot_added], h.dtype)])
-    a, v, d = body.a.copy(), body.v.copy(), body.d.copy()
-    for k in range(len(body.d)):
-        if body.free[k]:
-            m, kk, c = (body.mass, body.k, body.c) if k < 2 else (body.inertia, body.rot_k, body.rot_c)
-            a[k], v[k], d[k] = dyn.newmark(body.a[k], body.v[k], body.d[k], h[k], m, kk, c)
+    a_old, v_old, d_old = body.a, body.v, body.d
+    a, v, d = a_old, v_old, d_old
+    for _ in range(body.fsi_iter):
+        if body.rot:  # markers turn with d[2] about the initial centre (dyn.py:84-120)
+            cx, cy = body.center
+            mx, my = dyn.get_markers_coords_3dof(body.X0, body.Y0, cx, cy, d)
+            mv = dyn.get_markers_velocity_3dof(mx, my, cx, cy, d, v)
+        else:
+            mx, my = dyn.get_markers_coords_2dof(body.X0, body.Y0, d)
+            mv = np.repeat(v[None, :], M, axis=0)
+        W, I = ib.get_ib_stencil(mx, my, ny, ib.KERNELS[body.kernel], body.radius)
+        g, mh = ib.multi_direct_forcing(u, W, I, mv, body.ds, body.n_iter)
+        h = dyn.get_force_to_obj(mh)
+        h = h + a[:2] * body.area
+        if body.rot:  # torque (dyn.py:139-154) plus added inertia
+            tq = dyn.get_torque_to_obj(mx, my, cx, cy, d, mh)
+            h = np.concatenate([h, np.asarray([tq + a[2] * body.rot_added], h.dtype)])
+        a, v, d = a_old.copy(), v_old.copy(), d_old.copy()
+        for k in range(len(body.d)):
+            if body.free[k]:
+                m, kk, c = (body.mass, body.k, body.c) if k < 2 else (body.inertia, body.rot_k, body.rot_c)
+                a[k], v[k], d[k] = dyn.newmark(a_old[k], v_old[k], d_old[k], h[k], m, kk, c)
     body.a, body.v, body.d = a, v, d
     return g, h
 

@@ -71,9 +71,13 @@ def host_threads():
 
 
 class ThreadedStep:
-    """One time step of a benchmark case (the dict of vivsim_gb300.configs) per call."""
+    """One time step of a benchmark case (the dict of vivsim_gb300.configs) per call.
 
-    def __init__(self, case, threads=None):
+    ``dtype`` (float32 by default, as the benchmark) sets the precision of the populations,
+    the markers and the MRT operator; float64 gives the double-precision oracle of the
+    same case from the same (float32) initial populations."""
+
+    def __init__(self, case, threads=None, dtype=np.float32):
         self.q = case["q"]
         self.L = L2 if self.q == 9 else L3
         self.C = Q9_C if self.q == 9 else Q19_C
@@ -82,21 +86,22 @@ class ThreadedStep:
                  ("nee", "pressure"): "pnee", ("nee", "velocity"): "vnee", ("nebb", "force_corrected"): "fcnebb"}
         self.bcs = [(names[(k, m)], loc, kw) for (k, loc, m, kw) in case["boundaries"]]
         self.coll, self.om = case["collision"], case["omega"]
-        self.op = L2.get_mrt_collision_operator(self.om, np.float32) if (self.coll == "mrt" and self.q == 9) else None
-        self.f = case["f0"].copy()
+        dt = np.dtype(dtype)
+        self.op = L2.get_mrt_collision_operator(self.om, dt) if (self.coll == "mrt" and self.q == 9) else None
+        self.f = case["f0"].astype(dt)
         self.body = None
         self.body3 = None
         b = case["body"]
         if b is not None and self.q == 9:
-            X = b["markers"].astype(np.float32)
+            X = b["markers"].astype(dt)
             self.body = recipes.Body2D(X[:, 0], X[:, 1], b["ds"], b["mass"], b["stiffness"], b["damping"],
                                        b["added_mass_area"], free=b["free_dof"][:2], kernel=b["kernel"],
                                        n_iter=b["n_iter"])
         elif b is not None:  # a fixed 3-D body: static stencil (recipes.ib_lbm_step_3d)
             from . import ib as OIB
-            X = b["markers"].astype(np.float32)
+            X = b["markers"].astype(dt)
             W, I = OIB.get_ib_stencil_3d(X, case["shape"])
-            self.body3 = (W, I, np.zeros((X.shape[0], 3), np.float32), b["ds"], b["n_iter"])
+            self.body3 = (W, I, np.zeros((X.shape[0], 3), dt), b["ds"], b["n_iter"])
         self.threads = threads or host_threads()
         nx = self.f.shape[1]
         k = min(self.threads * 2, nx)
@@ -112,6 +117,7 @@ class ThreadedStep:
             pass
 
     def __call__(self):
+        """Advance self.f (and the body) by one step; self.h is the step's body force."""
         L, f = self.L, self.f
         grid = f.shape[1:]
         rho = np.empty(grid, f.dtype)
@@ -127,12 +133,17 @@ class ThreadedStep:
 
         self._map(collide, self.slabs)
         g = None
+        self.h = None
         if self.body is not None:
-            g, _ = recipes.body_forces_2d(u, self.body, grid[1])
+            g, self.h = recipes.body_forces_2d(u, self.body, grid[1])
         elif self.body3 is not None:
             from . import ib as OIB
             W, I, mu, ds, n_iter = self.body3
-            g, _ = OIB.multi_direct_forcing(u, W, I, mu, ds, n_iter)
+            g, mh = OIB.multi_direct_forcing(u, W, I, mu, ds, n_iter)
+            h = mh[0].copy()  # total force, summed in marker order as recipes.ib_lbm_step_3d does
+            for i in range(1, mh.shape[0]):
+                h = h + mh[i]
+            self.h = h
         if g is not None:
             def force(sl):
                 lo, hi = sl

@@ -454,6 +454,37 @@ def recipes_2d(put, jnp, lbm, ib, dyn, dt, rng):
                 put(f"viv.{coll}.h{step}", h)
                 put(f"viv.{coll}.body{step}", jnp.stack([a, v, d]))
 
+    # Fluid-structure sub-iterations, examples/2d/vortex_induced_vibration.py:111-139 with
+    # FSI_ITER = 2: each pass places the markers with the latest (a, v, d) and restarts the
+    # 2-DOF Newmark update from the step's saved state.  Full-grid stencil, KBC, equilibrium
+    # inflow, pressure-NEE outflow, both translations free.
+    u = jnp.zeros((2, nx, ny))
+    u = u.at[0].set(U0)
+    u = u.at[1].set(jnp.asarray(pert))
+    f = lbm.get_equilibrium(jnp.ones((nx, ny)), u)
+    d = jnp.zeros(2); v = jnp.zeros(2).at[1].set(1e-2 * U0); a = jnp.zeros(2)
+    for step in range(1, 7):
+        rho, u = lbm.get_macroscopic(f)
+        feq = lbm.get_equilibrium(rho, u)
+        f = lbm.collision_kbc(f, feq, om)
+        a_old, v_old, d_old = a, v, d
+        for _ in range(2):
+            mxx, myy = dyn.get_markers_coords_2dof(X0, Y0, d)
+            W, I = ib.get_ib_stencil(mxx, myy, ny, kernel=ib.kernel_peskin_4pt, stencil_radius=2)
+            mv = jnp.repeat(v[None, :], M, axis=0)
+            g, mh = ib.multi_direct_forcing(u, W, I, mv, ds, n_iter=3)
+            h = dyn.get_force_to_obj(mh)
+            h += a * area
+            a, v, d = dyn.newmark_2dof(a_old, v_old, d_old, h, mass, K, 0.0)
+        f = lbm.forcing_edm(f, g, u)
+        f = lbm.streaming(f)
+        f = lbm.boundary_equilibrium(f, loc="left", ux_wall=U0)
+        f = lbm.boundary_pressure_nee(f, loc="right", rho_wall=1.0)
+        if step in (1, 6):
+            put(f"vivfsi.f{step}", f)
+            put(f"vivfsi.h{step}", h)
+            put(f"vivfsi.body{step}", jnp.stack([a, v, d]))
+
     # Windowed IB region as in examples/2d/vortex_induced_vibration.py:104-146 (2-DOF,
     # force-corrected NEBB inflow, equilibrium outflow, dynamic window).
     nx, ny, D, U0 = 40, 28, 8.0, 0.05

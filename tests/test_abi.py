@@ -128,3 +128,7 @@ def test_solver_rejects_unknown_names():
         S.LatticeStep(9, (16, 16), "lbgk", 1.0)
     with pytest.raises(ValueError):
         S.LatticeStep(9, (16, 16), "bgk", 1.0, forcing="shan_chen")
+    with pytest.raises(ValueError):
+        S.LatticeStep(9, (16, 16), "bgk", 1.0, variant="fastest")
+    with pytest.raises(ValueError):  # a boundary without its face
+        S.LatticeStep(9, (16, 16), "bgk", 1.0, boundaries=[dict(kind="nee", mode="given")])

@@ -1,0 +1,156 @@
+"""The fused float32 step against the float32 oracle at the benchmark configurations' own sizes.
+
+Configurations (vivsim_gb300/configs.py, seeded synthetic inputs):
+
+* cavity: D2Q9 BGK 256 x 256, NEE walls, lid ux = 0.1, all 1000 steps
+  (examples/2d/lid_driven_cavity.py:55-73);
+* VIV: D2Q9 KBC and MRT 1024 x 512, cylinder D = 40 with 126 markers, Peskin 4-point, MDF 3,
+  transverse spring, equilibrium inflow, pressure-NEE outflow, 50 steps
+  (examples/2d/vortex_induced_vibration.py:96-157);
+* sphere: D3Q19 regularised and BGK 256 x 128 x 128, 1810 markers, MDF 3, 2 steps
+  (examples/3d/flow_past_sphere.py:139-180).
+
+The oracle is the NumPy restatement of the reference run over the host's cores
+(oracle/threaded.py, bit-equal to the serial recipes).  Errors are norm-relative,
+max|a - b| / max|b|, per field.
+
+* Per step: the fused step started from the oracle's own state at step n (populations and,
+  for the moving cylinder, the body state) against the oracle's step n + 1: at most 1e-6 on
+  f, rho and u.  The body force of that step: at most 1e-5 (a sum of 126 marker forces of
+  both signs: cancellation lifts the ulp-level differences of a tree-ordered sum).
+* Whole run: the fused run against the float32 oracle's run of the same length: at most 1e-4 on
+  rho and u after the cavity's 1000 steps; 1e-5 on f after 50 VIV steps and after the
+  two sphere steps.  The kernel's distance from the float64 oracle is checked against the
+  float32 oracle's own distance from it (the float32 rounding that any float32 run carries).
+"""
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import rel_err
+from oracle import lbm2d as L2
+from oracle import lbm3d as L3
+from oracle.threaded import ThreadedStep
+
+pytestmark = pytest.mark.gpu
+
+PER_STEP = 1e-6
+BODY_FORCE = 1e-5
+
+
+@pytest.fixture(scope="module")
+def cfg():
+    import vivsim_gb300
+    vivsim_gb300.build()
+    from vivsim_gb300 import configs
+    return configs
+
+
+def moments(f):
+    L = L2 if f.shape[0] == 9 else L3
+    return L.get_macroscopic(f)
+
+
+def field_errors(a, b):
+    """(f, rho, u) errors of populations a against b, moments taken in float64."""
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    ra, ua = moments(a)
+    rb, ub = moments(b)
+    return rel_err(a, b), rel_err(ra, rb), rel_err(ua, ub)
+
+
+def load_state(sim, body, ts):
+    """Put the oracle's populations (and body state) into the fused solver."""
+    sim.f.copy_(torch.from_numpy(np.ascontiguousarray(ts.f)))
+    if body is not None and ts.body is not None:
+        ob = ts.body
+        pad = lambda x: [float(v) for v in x] + [0.0] * (3 - len(x))  # noqa: E731
+        body.set_state(a=pad(ob.a), v=pad(ob.v), d=pad(ob.d))
+
+
+def per_step_check(cfg, case, n_steps, check_at):
+    """Advance the oracle n_steps; at each step in check_at, one fused step from the same
+    state.  Returns the worst (f, rho, u, force) errors and the oracle at the end."""
+    _, body, sim = cfg.build_solver(case)
+    ts = ThreadedStep(case)
+    worst = np.zeros(4)
+    for n in range(n_steps):
+        if n in check_at:
+            load_state(sim, body, ts)
+            hist = sim.run(1, force_history=body is not None)
+            ts()
+            errs = list(field_errors(sim.f.cpu().numpy(), ts.f))
+            if hist is not None and ts.h is not None:
+                d = len(ts.h)
+                errs.append(rel_err(hist[0, :d].cpu().numpy(), ts.h))
+            else:
+                errs.append(0.0)
+            worst = np.maximum(worst, errs)
+        else:
+            ts()
+    return worst, ts
+
+
+def free_run(cfg, case, n_steps, chunk=100):
+    _, body, sim = cfg.build_solver(case)
+    done = 0
+    stream = torch.cuda.Stream()  # graph capture needs a non-default stream
+    with torch.cuda.stream(stream):
+        while done < n_steps:
+            k = min(chunk, n_steps - done)
+            sim.run(k, graph=k > 2)
+            done += k
+    torch.cuda.synchronize()
+    return sim.f.cpu().numpy(), (body.state() if body is not None else None)
+
+
+def test_cavity_256_full_run(cfg):
+    """Config 1: every step of the 1000-step run checked at 5 points, and the whole run."""
+    case = cfg.cavity()
+    worst, ts = per_step_check(cfg, case, 1000, {0, 1, 10, 100, 500, 999})
+    print(f"\ncavity per step: f {worst[0]:.2e} rho {worst[1]:.2e} u {worst[2]:.2e}")
+    assert worst[0] <= PER_STEP and worst[1] <= PER_STEP and worst[2] <= PER_STEP, worst
+    fk, _ = free_run(cfg, case, 1000)
+    ef, er, eu = field_errors(fk, ts.f)
+    assert er <= 1e-4 and eu <= 1e-4, (ef, er, eu)
+    # float32 drift from the float64 oracle: the kernel's against the oracle's own
+    t64 = ThreadedStep(case, dtype=np.float64)
+    for _ in range(1000):
+        t64()
+    _, kr, ku = field_errors(fk, t64.f)
+    _, orr, ou = field_errors(ts.f, t64.f)
+    print(f"cavity 1000 steps: kernel-oracle32 rho {er:.2e} u {eu:.2e}; vs oracle64: kernel rho {kr:.2e} u {ku:.2e},"
+          f" oracle32 rho {orr:.2e} u {ou:.2e}")
+    assert kr <= 2.0 * orr + 1e-7 and ku <= 2.0 * ou + 1e-7, dict(kernel=(kr, ku), oracle=(orr, ou))
+
+
+@pytest.mark.parametrize("collision", ["kbc", "mrt"])
+def test_viv_1024x512_per_step(cfg, collision):
+    """Config 2 (KBC and its MRT variant): 50 steps, per-step checks incl. the body force."""
+    case = cfg.viv2d(collision=collision)
+    worst, ts = per_step_check(cfg, case, 50, {0, 1, 10, 25, 49})
+    print(f"\nviv {collision} per step: f {worst[0]:.2e} rho {worst[1]:.2e} u {worst[2]:.2e} force {worst[3]:.2e}")
+    assert worst[0] <= PER_STEP and worst[1] <= PER_STEP and worst[2] <= PER_STEP, worst
+    assert worst[3] <= BODY_FORCE, worst
+    fk, st = free_run(cfg, case, 50)
+    ef, er, eu = field_errors(fk, ts.f)
+    print(f"viv {collision} 50 steps: f {ef:.2e} rho {er:.2e} u {eu:.2e} d_y {st['d'][1]:.6e} / {ts.body.d[1]:.6e}")
+    assert ef <= 1e-5 and er <= 1e-5 and eu <= 1e-5, (ef, er, eu)
+    d_oracle = float(ts.body.d[1])
+    assert abs(st["d"][1] - d_oracle) <= 1e-5 * max(abs(d_oracle), 1e-12) + 1e-12, (st["d"][1], d_oracle)
+
+
+@pytest.mark.parametrize("collision", ["reg", "bgk"])
+def test_sphere_256x128x128_per_step(cfg, collision):
+    """Config 3 (regularised and its BGK variant): two steps, both checked."""
+    case = cfg.sphere3d(collision=collision)
+    worst, ts = per_step_check(cfg, case, 2, {0, 1})
+    print(f"\nsphere {collision} per step: f {worst[0]:.2e} rho {worst[1]:.2e} u {worst[2]:.2e} force {worst[3]:.2e}")
+    assert worst[0] <= PER_STEP and worst[1] <= PER_STEP and worst[2] <= PER_STEP, worst
+    assert worst[3] <= BODY_FORCE, worst
+    fk, _ = free_run(cfg, case, 2)
+    ef, er, eu = field_errors(fk, ts.f)
+    print(f"sphere {collision} 2 steps: f {ef:.2e} rho {er:.2e} u {eu:.2e}")
+    assert ef <= 1e-5 and er <= 1e-5 and eu <= 1e-5, (ef, er, eu)

@@ -259,6 +259,30 @@ def test_recipe_viv(mode, coll):
     check(mode, f, f"viv.{coll}.f6", TOL_RECIPE[mode])
 
 
+def test_recipe_viv_fsi_subiterations(mode):
+    """FSI_ITER = 2 (examples/2d/vortex_induced_vibration.py:111-139), both translations free."""
+    G = golden(mode)
+    dt = G["viv.X0"].dtype
+    nx, ny, U0, D, M = 40, 24, 0.05, 8.0, 24
+    om = L2.get_omega(U0 * D / 20.0)
+    u = np.zeros((2, nx, ny), dt)
+    u[0] = U0
+    u[1] = G["viv.pert"]
+    f = L2.get_equilibrium(np.ones((nx, ny), dt), u)
+    area = math.pi * (D / 2) ** 2
+    mass = area * 10.0
+    K = (2 * math.pi * U0 / (5.0 * D)) ** 2 * mass * (1 + 1 / 10.0)
+    body = recipes.Body2D(G["viv.X0"], G["viv.Y0"], math.pi * D / M, mass, K, 0.0, area, free=(True, True),
+                          n_iter=3, v=np.array([0.0, 1e-2 * U0], dt), fsi_iter=2)
+    bcs = [("eq", "left", dict(ux_wall=U0)), ("pnee", "right", dict(rho_wall=1.0))]
+    for step in range(1, 7):
+        f, h = recipes.ib_lbm_step_2d(f, body, "kbc", om, None, bcs)
+        if step in (1, 6):
+            check(mode, f, f"vivfsi.f{step}", TOL_RECIPE[mode])
+            check(mode, h, f"vivfsi.h{step}", 1e-4 if mode == "f32" else 1e-10)
+            check(mode, np.stack([body.a, body.v, body.d]), f"vivfsi.body{step}", 1e-4 if mode == "f32" else 1e-10)
+
+
 @pytest.mark.parametrize("coll", ["reg", "bgk", "kbc"])
 def test_recipe_sphere(mode, coll):
     G = golden(mode)

@@ -237,6 +237,43 @@ def _viv_small(S, X, steps, graph=False):
     return N(sim.f), body.state(), N(hist)
 
 
+@pytest.mark.parametrize("form", ["single", "general"])
+def test_viv_fsi_subiterations_golden(S, mode, form, monkeypatch):
+    """FSI_ITER = 2 (examples/2d/vortex_induced_vibration.py:111-139) against the reference's
+    golden trajectory, in the chain and the general form of the body kernel (sub-iterations
+    run without the cluster form)."""
+    monkeypatch.setenv("VIVSIM_GB300_BODY_SINGLE" if form == "single" else "VIVSIM_GB300_BODY_CSR", "1")
+    G = golden(mode)
+    dt = torch.float64 if mode == "f64" else torch.float32
+    nx, ny, U0, D, M = 40, 24, 0.05, 8.0, 24
+    om = L2.get_omega(U0 * D / 20.0)
+    u = np.zeros((2, nx, ny), G["viv.X0"].dtype)
+    u[0] = U0
+    u[1] = G["viv.pert"]
+    f0 = L2.get_equilibrium(np.ones((nx, ny), u.dtype), u)
+    step = S.LatticeStep(9, (nx, ny), "kbc", om, dtype=dt, forcing="edm",
+                         boundaries=[S.boundary("equilibrium", "left", ux_wall=U0),
+                                     S.boundary("nee", "right", mode="pressure", rho_wall=1.0)])
+    area = math.pi * (D / 2) ** 2
+    mass = area * 10.0
+    K = (2 * math.pi * U0 / (5.0 * D)) ** 2 * mass * (1 + 1 / 10.0)
+    X = np.stack([G["viv.X0"], G["viv.Y0"]], axis=1)
+    body = S.RigidBody(step, X, math.pi * D / M, n_iter=3, moving=True, free_dof=(True, True), mass=mass,
+                       stiffness=K, added_mass_area=area, v0=(0.0, 1e-2 * U0, 0.0), fsi_iter=2)
+    sim = S.Simulation(step, T(f0), body)
+    btol = 1e-4 if mode == "f32" else 1e-10
+    h1 = sim.run(1, force_history=True)
+    st = body.state()
+    assert rel_err(N(sim.f), G["vivfsi.f1"]) <= tol(mode, 1)
+    assert rel_err(N(h1)[0, :2], G["vivfsi.h1"]) <= btol
+    assert rel_err(np.stack([st["a"][:2], st["v"][:2], st["d"][:2]]), G["vivfsi.body1"]) <= btol
+    sim.run(5)
+    st = body.state()
+    assert rel_err(N(sim.f), G["vivfsi.f6"]) <= tol(mode, 6)
+    assert rel_err(st["h"][:2], G["vivfsi.h6"]) <= btol
+    assert rel_err(np.stack([st["a"][:2], st["v"][:2], st["d"][:2]]), G["vivfsi.body6"]) <= btol
+
+
 def test_body_chain_form_equals_general_form(S, monkeypatch):
     """The body kernel's cluster form, its single-CTA chain form (neighbour search by marker
     index) and the general form (shared-memory sort) sum every node in the same order:

@@ -15,6 +15,7 @@ VS_OK = 0
 VS_ERR_INVALID_ARG = 1
 VS_ERR_TIMEOUT = 5
 VS_ERR_NONFINITE = 6
+VS_ERR_TIMEOUT_INFLIGHT = 7
 VS_F32, VS_F64 = 0, 1
 VS_COLLIDE_BGK, VS_COLLIDE_KBC, VS_COLLIDE_MRT, VS_COLLIDE_REG = 0, 1, 2, 3
 VS_FORCE_NONE, VS_FORCE_EDM, VS_FORCE_GUO_BGK, VS_FORCE_GUO_MRT = 0, 1, 2, 3
@@ -70,7 +71,7 @@ class vs_body_cfg(C.Structure):
                 ("window_margin", C.c_int),
                 ("center_x", C.c_double), ("center_y", C.c_double),
                 ("inertia", C.c_double), ("rot_stiffness", C.c_double), ("rot_damping", C.c_double),
-                ("added_inertia", C.c_double)]
+                ("added_inertia", C.c_double), ("fsi_iter", C.c_int)]
 
 
 class vs_adjoint_cfg(C.Structure):

@@ -5,6 +5,8 @@
 // radix-sorted stably, so the contributions to a node are summed in increasing
 // (marker, stencil point) order — the order of the reference's scatter-add — by one
 // thread per node, with no floating-point atomics.
+#include <cuda.h>
+
 #include <cub/device/device_radix_sort.cuh>
 #include <cub/device/device_scan.cuh>
 
@@ -211,21 +213,27 @@ static size_t ws_bytes(int m, int s) {
   return b;
 }
 
-static IbWorkspace carve(void* base, int m, int s) {
+// Lays the workspace out from base.  with_tail = false lays out only what a spread uses
+// (the pair arrays and the CUB storage) and forms no pointer beyond them.
+static IbWorkspace carve(void* base, int m, int s, bool with_tail = true) {
   const int64_t P = (int64_t)m * s;
   IbWorkspace w{};
   char* p = (char*)base;
   int32_t** arrs[7] = {&w.keys, &w.ids, &w.skeys, &w.sids, &w.head, &w.uid, &w.pair_uid};
+  size_t off = 0;
   for (auto a : arrs) {
-    *a = (int32_t*)p;
-    p += align256(sizeof(int32_t) * P);
+    *a = (int32_t*)(p + off);
+    off += align256(sizeof(int32_t) * P);
   }
   w.cub_bytes = align256(cub_sort_bytes(P));
-  w.cub_tmp = p;
-  p += w.cub_bytes;
-  w.tail = p;
-  p += mdf_float_bytes(m, s);
-  w.total = (size_t)(p - (char*)base);
+  w.cub_tmp = p + off;
+  off += w.cub_bytes;
+  w.tail = nullptr;
+  if (with_tail) {
+    w.tail = p + off;
+    off += mdf_float_bytes(m, s);
+  }
+  w.total = off;
   return w;
 }
 
@@ -626,12 +634,12 @@ int vs_torque_to_obj(int dtype, const void* x, const void* y, int m, double xc, 
 }  // extern "C"
 
 // ------------------------------------------------------------------ spread without allocation
-// vs_ib_spread_noalloc serves callers that must not allocate device memory while they run:
-// a host loop that holds a CUDA graph capture open (an allocation would end or invalidate
-// the capture), a foreign runtime that owns every device allocation and hands out no
-// scratch (an XLA custom call registered without a workspace), or a latency-critical loop
-// that cannot afford a pool miss.  Its scratch is one file-scope device array, set up once
-// per device and shared by every call on that device.
+// vs_ib_spread_noalloc serves callers that cannot allocate device memory while they run:
+// a foreign runtime that owns every device allocation and hands out no scratch (an XLA
+// custom call registered without a workspace), or a latency-critical loop that cannot
+// afford a trip into the allocator.  Its scratch is one file-scope device array, set up
+// once per device (and again after the device's context is replaced) and shared by every
+// call on that device.
 namespace vs {
 namespace {
 
@@ -643,17 +651,48 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratch
 
 std::mutex g_noalloc_mu;
 void* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+unsigned long long g_noalloc_ctx[kNoAllocMaxDevices] = {};  // context id the address belongs to
 
-// Address of this device's copy of g_noalloc_scratch.  The first call on a device looks it
-// up (loading this module on that device if it is not loaded yet) and caches it.
+typedef CUresult (*PfnCtxGetCurrent)(CUcontext*);
+typedef CUresult (*PfnCtxGetId)(CUcontext, unsigned long long*);
+
+// Unique id of the calling thread's current context (never reused within a process), or 0
+// when the driver offers none.  A device reset ends the primary context; the next one
+// gets a new id, so an address cached under the old id is looked up again.
+unsigned long long current_context_id() {
+  static PfnCtxGetCurrent get_current = nullptr;
+  static PfnCtxGetId get_id = nullptr;
+  static bool looked_up = false;
+  if (!looked_up) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = (PfnCtxGetCurrent)p;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = (PfnCtxGetId)p;
+    looked_up = true;
+  }
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (get_current && get_id && get_current(&ctx) == CUDA_SUCCESS && ctx && get_id(ctx, &id) == CUDA_SUCCESS)
+    return id;
+  return 0;
+}
+
+// Address of this device's copy of g_noalloc_scratch.  The first call on a device (and the
+// first call after the device's context was replaced, e.g. by cudaDeviceReset) looks it up,
+// loading this module on that device if it is not loaded yet, and caches it.
 int noalloc_scratch(void** out) {
   int dev = -1;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return cuda_status(e, "vs_ib_spread_noalloc: cudaGetDevice");
   VS_REQUIRE(dev >= 0 && dev < kNoAllocMaxDevices, "vs_ib_spread_noalloc: device %d beyond %d", dev,
              kNoAllocMaxDevices);
+  const unsigned long long ctx = current_context_id();
   std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if (!g_noalloc_ptr[dev]) {
+  if (!g_noalloc_ptr[dev] || g_noalloc_ctx[dev] != ctx) {
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess) return cuda_status(e, "vs_ib_spread_noalloc: cudaGetSymbolAddress");
@@ -662,13 +701,14 @@ int noalloc_scratch(void** out) {
       return VS_ERR_CUDA;
     }
     g_noalloc_ptr[dev] = p;
+    g_noalloc_ctx[dev] = ctx;
   }
   *out = g_noalloc_ptr[dev];
   return VS_OK;
 }
 
 // Scratch the spread itself touches: the seven pair arrays and the CUB sort/scan storage
-// (the MDF tail that carve() also lays out is never dereferenced by a spread).
+// (carve(.., false) lays out exactly these).
 size_t spread_scratch_bytes(int m, int s) {
   const int64_t P = (int64_t)m * s;
   return 7 * align256(sizeof(int32_t) * P) + align256(cub_sort_bytes(P));
@@ -702,7 +742,7 @@ int vs_ib_spread_noalloc(int dtype, const void* marker_values, const void* grid_
     using T = typename decltype(t)::type;
     cudaStream_t st = as_stream(stream);
     const int64_t P = (int64_t)m * s;
-    IbWorkspace w = carve(scratch, m, s);
+    IbWorkspace w = carve(scratch, m, s, false);
     if (grid_out != grid_in) {
       k_copy<T><<<grid_for((int64_t)c * n_grid, 256), 256, 0, st>>>((const T*)grid_in, (T*)grid_out,
                                                                     (int64_t)c * n_grid);

@@ -40,6 +40,7 @@ const char* vs_status_string(int status) {
     case VS_ERR_RANGE: return "index out of range";
     case VS_ERR_TIMEOUT: return "device wait timed out";
     case VS_ERR_NONFINITE: return "non-finite populations";
+    case VS_ERR_TIMEOUT_INFLIGHT: return "device wait timed out with a bulk copy still in flight";
     default: return "unknown status";
   }
 }

@@ -361,7 +361,17 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, int li
 }  // namespace tma
 
 constexpr int kTmaStages = 4;
-constexpr int kTmaWaitLimit = 1 << 22;  // try_wait suspends in hardware between polls
+constexpr int kTmaWaitLimit = 1 << 22;   // try_wait suspends in hardware between polls
+constexpr int kTmaDrainLimit = 1 << 24;  // second wait, for copies already issued, after a timeout
+
+// A block whose wait gave up must not leave while a bulk copy it issued may still write
+// its shared memory.  No copy is issued after a failed wait, so only copies already
+// counted by the barrier can be outstanding: wait for them once more (bounded).  Returns
+// the status to record: VS_ERR_TIMEOUT when they landed, VS_ERR_TIMEOUT_INFLIGHT when
+// one still had not (it may land after the block has left).
+__device__ __forceinline__ int tma_drain(uint64_t* bar, unsigned parity) {
+  return tma::mbar_wait(bar, parity, kTmaDrainLimit) ? VS_ERR_TIMEOUT : VS_ERR_TIMEOUT_INFLIGHT;
+}
 
 // Self-test of the bounded waits: an mbarrier expects 16 bytes that no copy delivers (no
 // copy is in flight), the wait gives up after `limit` polls and the kernel reports
@@ -418,11 +428,17 @@ __global__ void __launch_bounds__(TB) k_step_tma(const __grid_constant__ StepPar
     const unsigned parity = (unsigned)((k / kTmaStages) & 1);
     const bool ok = tma::mbar_wait(&full[stage], parity, kTmaWaitLimit);
     if (__syncthreads_or(!ok)) {
-      // some copy never completed: report, give the outstanding ones a bounded chance, leave
-      if (tid == 0) atomicExch(status, VS_ERR_TIMEOUT);
-      for (int j = 1; j < kTmaStages; ++j) {
-        const int tj = t + j * gridDim.x;
-        if (tj < tiles) tma::mbar_wait(&full[(k + j) % kTmaStages], (unsigned)(((k + j) / kTmaStages) & 1), 1 << 16);
+      // some copy never completed: no stage is refilled past this point; drain the stages
+      // already issued (this one and the next kTmaStages - 1 tiles), report, leave
+      if (tid == 0) {
+        int st = VS_ERR_TIMEOUT;
+        for (int j = 0; j < kTmaStages; ++j) {
+          const int tj = t + j * gridDim.x;
+          if (tj < tiles && tma_drain(&full[(k + j) % kTmaStages], (unsigned)(((k + j) / kTmaStages) & 1)) !=
+                                VS_ERR_TIMEOUT)
+            st = VS_ERR_TIMEOUT_INFLIGHT;
+        }
+        atomicMax(status, st);
       }
       return;
     }
@@ -498,6 +514,8 @@ struct BodyParams {
   const T* Y0;
   const T* ds_arr;
   T* state;  // a[3], v[3], d[3], h[3]
+  T* base;   // fluid-structure sub-iterations: the step's saved a[3], v[3], d[3] (else null)
+  int fsi_first;  // with base: this pass saves the state it starts from into base
   T* gw;
   int* meta;
   T* force_hist;
@@ -563,7 +581,10 @@ struct Kin2 {
 // Warp 0 ends the body step: the force h = sum_m(-F_total) in a fixed tree (dyn.py:126-136);
 // with the rotation free, the torque sum_m(x_rel h_y - y_rel h_x) (dyn.py:139-154); added
 // mass h += a A (vortex_induced_vibration.py:136) and added inertia; Newmark per free DOF
-// (dyn.py:5-51).  Ft holds every marker's total MDF force.
+// (dyn.py:5-51).  Ft holds every marker's total MDF force; a, v, d the state this pass
+// started from.  With fluid-structure sub-iterations (B.base) the added mass uses that
+// latest a while Newmark restarts from the step's saved state, as the reference's
+// `for _ in range(FSI_ITER)` loop does (examples/2d/vortex_induced_vibration.py:114-139).
 template <typename T>
 __device__ __forceinline__ void body2d_finish(const BodyParams<T>& B, const Kin2<T>& K, const T* Ft, int M,
                                               const T* a, const T* v, const T* d) {
@@ -606,12 +627,24 @@ __device__ __forceinline__ void body2d_finish(const BodyParams<T>& B, const Kin2
     const T dc = c == 0 ? d[0] : (c == 1 ? d[1] : d[2]);
     const T hc = c == 0 ? h[0] : (c == 1 ? h[1] : h[2]);
     const T hh = add_rn(hc, mul_rn(ac, c < 2 ? B.area : B.rot_added));
-    T an = ac, vn = vc, dn = dc;
+    T ab = ac, vb = vc, db = dc;  // Newmark's starting state
+    if (B.base) {
+      if (B.fsi_first) {
+        B.base[c] = ac;
+        B.base[3 + c] = vc;
+        B.base[6 + c] = dc;
+      } else {
+        ab = B.base[c];
+        vb = B.base[3 + c];
+        db = B.base[6 + c];
+      }
+    }
+    T an = ab, vn = vb, dn = db;
     if (B.free_dof[c]) {
       const T damp = c < 2 ? B.damp : B.rot_damp, stiff = c < 2 ? B.stiff : B.rot_stiff;
       const T den = c < 2 ? B.den : B.rot_den;
-      const T v1 = add_rn(vc, mul_rn(B.k1, ac));
-      const T v2 = add_rn(add_rn(dc, mul_rn(B.dt, vc)), mul_rn(B.k2, ac));
+      const T v1 = add_rn(vb, mul_rn(B.k1, ab));
+      const T v2 = add_rn(add_rn(db, mul_rn(B.dt, vb)), mul_rn(B.k2, ab));
       an = sub_rn(sub_rn(hh, mul_rn(damp, v1)), mul_rn(stiff, v2)) / den;
       vn = add_rn(mul_rn(B.c1, an), v1);
       dn = add_rn(mul_rn(B.c2, an), v2);
@@ -818,10 +851,10 @@ __global__ void __launch_bounds__(kBodyThreads) k_body2d(const __grid_constant__
   __syncthreads();
   if (misc[4] || !region_ok) {
     // the body moved a node or more in one step, or its region left the box
-    if (bulk && tid == 0) tma::mbar_wait(bar, 0, kTmaWaitLimit);  // let the staged copies land
-    __syncthreads();
+    // let the staged copy land before the block leaves (bounded; reported if it does not)
     if (tid == 0) {
-      B.meta[META_STATUS] = VS_ERR_RANGE;
+      const bool landed = !bulk || tma::mbar_wait(bar, 0, kTmaWaitLimit) || tma_drain(bar, 0) == VS_ERR_TIMEOUT;
+      B.meta[META_STATUS] = landed ? VS_ERR_RANGE : VS_ERR_TIMEOUT_INFLIGHT;
       B.meta[META_WX] = 0; B.meta[META_WY] = 0; B.meta[META_WZ] = 0;
     }
     return;
@@ -837,7 +870,7 @@ __global__ void __launch_bounds__(kBodyThreads) k_body2d(const __grid_constant__
   if (bulk) staged = tma::mbar_wait(bar, 0, kTmaWaitLimit);
   if (__syncthreads_or(!staged)) {
     if (tid == 0) {
-      B.meta[META_STATUS] = VS_ERR_TIMEOUT;
+      B.meta[META_STATUS] = tma_drain(bar, 0);  // the copy is waited for once more before the block leaves
       B.meta[META_WX] = 0; B.meta[META_WY] = 0; B.meta[META_WZ] = 0;
     }
     return;
@@ -1121,10 +1154,10 @@ __device__ __forceinline__ void body2d_chain(const BodyParams<T>& B) {
   __syncthreads();
   if (misc[4] || !region_ok) {
     // the body moved a node or more in one step, or its region left the box
-    if (bulk && tid == 0) tma::mbar_wait(bar, 0, kTmaWaitLimit);
-    __syncthreads();
+    // let the staged copy land before the block leaves (bounded; reported if it does not)
     if (tid == 0) {
-      B.meta[META_STATUS] = VS_ERR_RANGE;
+      const bool landed = !bulk || tma::mbar_wait(bar, 0, kTmaWaitLimit) || tma_drain(bar, 0) == VS_ERR_TIMEOUT;
+      B.meta[META_STATUS] = landed ? VS_ERR_RANGE : VS_ERR_TIMEOUT_INFLIGHT;
       B.meta[META_WX] = 0; B.meta[META_WY] = 0; B.meta[META_WZ] = 0;
     }
     return;
@@ -1133,7 +1166,7 @@ __device__ __forceinline__ void body2d_chain(const BodyParams<T>& B) {
   if (bulk) staged = tma::mbar_wait(bar, 0, kTmaWaitLimit);
   if (__syncthreads_or(!staged)) {
     if (tid == 0) {
-      B.meta[META_STATUS] = VS_ERR_TIMEOUT;
+      B.meta[META_STATUS] = tma_drain(bar, 0);  // the copy is waited for once more before the block leaves
       B.meta[META_WX] = 0; B.meta[META_WY] = 0; B.meta[META_WZ] = 0;
     }
     return;
@@ -1903,6 +1936,8 @@ struct vs_body_plan {
   void* d_X0;     // (M) x, (M) y [, (M) z]  or (M,3) coords for 3-D
   void* d_ds;     // (M) or null
   void* d_state;  // 12 values
+  void* d_base;   // fluid-structure sub-iterations: the step's saved state (9 values) or null
+  int fsi;        // fluid-structure passes per step (>= 1)
   void* d_gw;     // window force (C, cells)
   int* d_meta;
   // 3-D fixed body: stencil and its compacted CSR (built once)
@@ -1968,8 +2003,8 @@ static void free_lattice(vs_lattice_plan* p) {
 
 static void free_body(vs_body_plan* b) {
   if (!b) return;
-  void* ptrs[] = {b->d_X0, b->d_ds, b->d_state, b->d_gw, b->d_meta, b->d_W, b->d_I, b->d_ws, b->d_node_cell,
-                  b->d_seg, b->d_nu, b->d_nv, b->d_mk, b->d_U};
+  void* ptrs[] = {b->d_X0, b->d_ds, b->d_state, b->d_base, b->d_gw, b->d_meta, b->d_W, b->d_I, b->d_ws,
+                  b->d_node_cell, b->d_seg, b->d_nu, b->d_nv, b->d_mk, b->d_U};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   if (b->ev_fork) cudaEventDestroy(b->ev_fork);
@@ -2201,6 +2236,8 @@ static BodyParams<T> body_params2d(vs_body_plan* B, const vs_lattice_plan* LP, c
   }
   for (int q = 0; q < 4; ++q) P.box[q] = B->box[q];
   P.state = (T*)B->d_state;
+  P.base = B->fsi > 1 ? (T*)B->d_base : nullptr;
+  P.fsi_first = 1;
   P.gw = (T*)B->d_gw;
   P.meta = B->d_meta;
   P.force_hist = (T*)force_hist;
@@ -2221,10 +2258,15 @@ static int enqueue_body(vs_body_plan* B, const vs_lattice_plan* LP, const void* 
   if (B->dim == 2) {
     return dispatch_t(dtype, [&](auto t) -> int {
       using T = typename decltype(t)::type;
-      const BodyParams<T> P = body_params2d<T>(B, LP, fin, force_hist, true);
-      if (B->chain) body2d_chain_launch<T>(B->cfg.radius, B->smem, st, P);
-      else body2d_launch<T>(B->cfg.radius, B->smem, st, P);
-      VS_CHECK_LAUNCH("vs_step body kernel");
+      BodyParams<T> P = body_params2d<T>(B, LP, fin, force_hist, true);
+      // one pass per fluid-structure sub-iteration; the last one leaves the force window,
+      // the body force and the state of the step
+      for (int it = 0; it < B->fsi; ++it) {
+        P.fsi_first = it == 0;
+        if (B->chain) body2d_chain_launch<T>(B->cfg.radius, B->smem, st, P);
+        else body2d_launch<T>(B->cfg.radius, B->smem, st, P);
+        VS_CHECK_LAUNCH("vs_step body kernel");
+      }
       return VS_OK;
     });
   }
@@ -2538,17 +2580,31 @@ static int enqueue_step(const vs_lattice_plan* LP, vs_body_plan* B, const void* 
     if (e != cudaSuccess) return cuda_status(e, "vs_step join");
     B->parity ^= 1;
   } else if (B) {
+    // side stream: body kernels, then the box's nodes (they need the new force window);
+    // third stream: the lazy face planes; main stream: every other node.  The three
+    // launches read f_in only and write disjoint words of f_out, so they run side by side
+    // and the step takes max(grid, body + box, planes).
     cudaError_t e = cudaEventRecord(B->ev_fork, st);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(B->side, B->ev_fork, 0);
     if (e != cudaSuccess) return cuda_status(e, "vs_step fork");
     rc = enqueue_body(B, LP, fin, force_hist, B->side);
     if (rc) return rc;
+    rc = enqueue_grid(LP, B, fin, fout, B->side, 2, false);
+    if (rc) return rc;
+    if (lazy_in) {
+      e = cudaStreamWaitEvent(B->side2, B->ev_fork, 0);
+      if (e != cudaSuccess) return cuda_status(e, "vs_step fork");
+      rc = enqueue_grid(LP, B, fin, fout, B->side2, 3, true);
+      if (rc) return rc;
+      e = cudaEventRecord(B->ev_join2, B->side2);
+      if (e != cudaSuccess) return cuda_status(e, "vs_step join");
+    }
     rc = enqueue_grid(LP, B, fin, fout, st, 1, lazy_in);
     if (rc) return rc;
     e = cudaEventRecord(B->ev_join, B->side);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(st, B->ev_join, 0);
+    if (e == cudaSuccess && lazy_in) e = cudaStreamWaitEvent(st, B->ev_join2, 0);
     if (e != cudaSuccess) return cuda_status(e, "vs_step join");
-    rc = enqueue_grid(LP, B, fin, fout, st, 2, lazy_in);
   } else {
     rc = enqueue_grid(LP, B, fin, fout, st, 0, lazy_in);
   }
@@ -2684,6 +2740,8 @@ int vs_lattice_status(const vs_lattice_plan* plan, int reset, void* stream) {
   if (e == cudaSuccess && reset && v) e = cudaMemset(plan->d_status, 0, sizeof(int));
   if (e != cudaSuccess) return cuda_status(e, "vs_lattice_status");
   if (v == VS_ERR_NONFINITE) set_error("the watchdog found a NaN or Inf population");
+  else if (v == VS_ERR_TIMEOUT_INFLIGHT)
+    set_error("a grid kernel gave up waiting for its bulk copies and one had still not landed when it left");
   else if (v) set_error("a grid kernel gave up waiting for its bulk copies (device status %d)", v);
   return v;
 }
@@ -2727,6 +2785,9 @@ int vs_body_plan_create(const vs_body_cfg* cfg, const vs_lattice_plan* lattice, 
   VS_REQUIRE(lattice->cfg.forcing == VS_FORCE_EDM || lattice->cfg.forcing == VS_FORCE_GUO_BGK ||
                  lattice->cfg.forcing == VS_FORCE_GUO_MRT,
              "an immersed body needs a forcing scheme on the lattice (EDM or Guo)");
+  VS_REQUIRE(cfg->fsi_iter >= 0 && cfg->fsi_iter <= 64, "fsi_iter must be 0..64");
+  VS_REQUIRE(cfg->fsi_iter <= 1 || (cfg->dim == 2 && cfg->moving),
+             "fluid-structure sub-iterations need a moving 2-D body");
   vs_body_plan* b = new (std::nothrow) vs_body_plan();
   if (!b) {
     set_error("out of host memory");
@@ -2823,6 +2884,8 @@ int vs_body_plan_create(const vs_body_cfg* cfg, const vs_lattice_plan* lattice, 
     if ((e = cudaMemcpy(b->d_ds, hd.data(), ts * M, cudaMemcpyHostToDevice)) != cudaSuccess) return fail(e);
   }
   if ((e = cudaMalloc(&b->d_state, ts * 12)) != cudaSuccess) return fail(e);
+  b->fsi = cfg->fsi_iter > 1 ? cfg->fsi_iter : 1;
+  if (b->fsi > 1 && (e = cudaMalloc(&b->d_base, ts * 9)) != cudaSuccess) return fail(e);
   {
     double st[12] = {0};
     for (int c = 0; c < 3; ++c) {
@@ -2928,7 +2991,7 @@ int vs_body_plan_create(const vs_body_cfg* cfg, const vs_lattice_plan* lattice, 
     // cluster form: one pair per thread over up to 8 CTAs, each holding a contiguous share
     // of the markers (ceil(M / CL) markers' pairs per CTA)
     b->cluster = 0;
-    if (b->chain && !getenv_flag("VIVSIM_GB300_BODY_SINGLE")) {
+    if (b->chain && b->fsi == 1 && !getenv_flag("VIVSIM_GB300_BODY_SINGLE")) {
       int cl_ok = 0;
       cudaDeviceGetAttribute(&cl_ok, cudaDevAttrClusterLaunch, dev);
       int c = 1;
@@ -3145,7 +3208,10 @@ int vs_body_get_state(const vs_body_plan* plan, double* state_host, void* stream
   if (e != cudaSuccess) return cuda_status(e, "vs_body_get_state");
   for (int i = 0; i < 12; ++i) state_host[i] = ts == 8 ? ((double*)buf)[i] : (double)((float*)buf)[i];
   if (meta[META_STATUS] != 0) {
-    set_error("immersed body left its window or the grid (stencil out of range)");
+    if (meta[META_STATUS] == VS_ERR_RANGE) set_error("immersed body left its window or the grid (stencil out of range)");
+    else if (meta[META_STATUS] == VS_ERR_TIMEOUT_INFLIGHT)
+      set_error("a body kernel gave up waiting for its bulk copy, which had still not landed when it left");
+    else set_error("a body kernel gave up waiting for its bulk copy (device status %d)", meta[META_STATUS]);
     return meta[META_STATUS];
   }
   return VS_OK;
@@ -3461,7 +3527,8 @@ int vs_batch_plan_create(vs_lattice_plan* const* lattices, vs_body_plan* const* 
     }
     bp->L.push_back(Lk);
     bp->B.push_back(Bk);
-    const bool batched_body = Bk && Bk->dim == 2 && Bk->chain;
+    // one pass per step in the batched body launch; bodies with sub-iterations run their own
+    const bool batched_body = Bk && Bk->dim == 2 && Bk->chain && Bk->fsi == 1;
     bp->lazy.push_back(batched_body && lazy_boundaries(Lk, Bk) ? 1 : 0);
     if (batched_body) {
       if (bp->chain_bodies.empty()) bp->radius = Bk->cfg.radius;

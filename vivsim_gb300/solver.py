@@ -98,14 +98,17 @@ class LatticeStep:
         for k, b in enumerate(boundaries):
             s = cfg.bc[k]
             for key, table in (("kind", BC_KINDS), ("mode", WALL_MODES), ("loc", V.LOCS)):
-                if b[key] not in table:
+                if b.get(key) not in table:
                     raise ValueError(f"boundary {k}: {key} must be one of {', '.join(repr(x) for x in table)}")
             s.kind = BC_KINDS[b["kind"]]
             s.mode = WALL_MODES[b["mode"]]
             s.loc = V.LOCS[b["loc"]]
             for name in ("rho", "ux", "uy", "uz", "gx", "gy", "gz"):
-                setattr(s, name, float(b[name]))
-        cfg.variant = {"auto": V.VS_GRID_AUTO, "plain": V.VS_GRID_PLAIN, "tma": V.VS_GRID_TMA}[variant]
+                setattr(s, name, float(b.get(name, 1.0 if name == "rho" else 0.0)))
+        variants = {"auto": V.VS_GRID_AUTO, "plain": V.VS_GRID_PLAIN, "tma": V.VS_GRID_TMA}
+        if variant not in variants:
+            raise ValueError(f"variant must be one of {', '.join(repr(x) for x in variants)}")
+        cfg.variant = variants[variant]
         self._mask = None
         if obstacle_mask is not None:  # obstacle_bounce_back after the face boundaries, every step
             m = obstacle_mask if isinstance(obstacle_mask, torch.Tensor) else torch.as_tensor(obstacle_mask)
@@ -148,12 +151,15 @@ class RigidBody:
     angle about ``center`` in 2-D (get_markers_coords_3dof / get_markers_velocity_3dof /
     get_torque_to_obj, vivsim/dyn.py:84-154), the latter with ``inertia``,
     ``rot_stiffness``, ``rot_damping`` and h[2] = torque + a[2] * ``added_inertia``.
+    ``fsi_iter`` (moving 2-D bodies) repeats markers, stencil, MDF, force and Newmark that
+    many times per step, each pass from the latest state with Newmark restarting from the
+    step's saved one: the FSI_ITER loop of examples/2d/vortex_induced_vibration.py:111-139.
     """
 
     def __init__(self, step, markers, ds, kernel="peskin4", radius=2, n_iter=3, moving=False,
                  free_dof=(False, False, False), mass=1.0, stiffness=0.0, damping=0.0, added_mass_area=0.0,
                  d0=(0, 0, 0), v0=(0, 0, 0), a0=(0, 0, 0), center=None, inertia=0.0, rot_stiffness=0.0,
-                 rot_damping=0.0, added_inertia=0.0):
+                 rot_damping=0.0, added_inertia=0.0, fsi_iter=1):
         X = np.asarray(markers.cpu() if isinstance(markers, torch.Tensor) else markers, dtype=np.float64)
         if X.ndim != 2 or X.shape[1] != step.dim:
             raise ValueError(f"markers must have shape (n_markers, {step.dim})")
@@ -187,6 +193,7 @@ class RigidBody:
         cfg.center_x, cfg.center_y = float(center[0]), float(center[1])
         cfg.inertia, cfg.rot_stiffness = float(inertia), float(rot_stiffness)
         cfg.rot_damping, cfg.added_inertia = float(rot_damping), float(added_inertia)
+        cfg.fsi_iter = int(fsi_iter)
         for name, val in (("d0", d0), ("v0", v0), ("a0", a0)):
             arr = getattr(cfg, name)
             for i in range(3):
