@@ -173,11 +173,13 @@ def time_chunks(torch, run, K, W, flush):
 
 
 def grid_kernel_time(torch, step, body, sim, launches, flush):
-    """Average duration of the grid kernel alone (vs_step_grid_only), L2 flushed once."""
+    """Average duration of the grid kernel alone (vs_step_grid_only), L2 flushed once.  The
+    kernel is timed over the whole grid without the body: the bulk launch of a step, which
+    in a step leaves only the body's small box to another launch."""
     from vivsim_gb300 import _lib as V
     a = sim.f
     b = torch.empty_like(a)
-    bh = body.handle if body is not None else None
+    bh = None
     flush()
     V.call("vs_step_grid_only", step.handle, bh, V.ptr(a), V.ptr(b), V.stream())
     torch.cuda.synchronize()
@@ -198,7 +200,7 @@ def roofline(torch, case, step, body, sim, flush, peak, peak_kind, launches):
     n = int(math.prod(case["shape"]))
     bytes_per_launch = BYTES_PER_UPDATE[case["q"]] * n
     achieved = bytes_per_launch / t / 1e9
-    return {"kernel": "k_step (grid: collide + force + push-stream)", "workload": case["name"], "bound": "hbm",
+    return {"kernel": "k_step_fast (grid: collide + push-stream, bulk launch)", "workload": case["name"], "bound": "hbm",
             "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
             "peak_source": f"{peak_kind} hbm_gbs", "bytes_per_launch": bytes_per_launch,
             "traffic": traffic_from_profiles(case["name"]), "kernel_us": round(t * 1e6, 3),

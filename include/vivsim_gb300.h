@@ -423,6 +423,71 @@ int vs_adjoint_forward(vs_adjoint_plan* plan, int keep_checkpoints, double* J_ou
 int vs_adjoint_backward(vs_adjoint_plan* plan, double seed, double* grad_U0, double* grad_K, double* grad_offsets,
                         void* stream);
 
+/* ==================================================== vector-Jacobian products ===
+ * Reverse-mode building blocks of the per-operator functions, so that a caller can
+ * differentiate an update step it composes itself (the reference differentiates its
+ * jitted loop with jax.grad; a composed torch step differentiates through these).
+ * Each takes the forward inputs it needs and the cotangent g_out of the result and writes
+ * the cotangents of the inputs.  Node-local Jacobians are exact: forward-mode dual numbers
+ * through the same formulas as the forward kernels.  *_node outputs hold one value per
+ * node (or face node) whose sum is the cotangent of a scalar parameter: reduce them with
+ * vs_sum_ordered, which sums in a fixed order (deterministic).  Asynchronous. */
+/* streaming (lbm/basic.py:60-85, lbm3d/basic.py:52-87): g_in_i(x) = g_out_i(x + c_i) */
+int vs_streaming_vjp(int q, int dtype, const void* g_out, void* g_in, int nx, int ny, int nz, void* stream);
+/* get_macroscopic (lbm/basic.py:88-111, lbm3d/basic.py:90-106): g_f from g_rho (n,) and
+ * g_u (d, n); either may be NULL (zero) */
+int vs_macroscopic_vjp(int q, int dtype, const void* f, const void* g_rho, const void* g_u, void* g_f, int64_t n,
+                       void* stream);
+/* get_equilibrium (lbm/basic.py:114-135, lbm3d/basic.py:109-130): g_rho, g_u from g_feq */
+int vs_equilibrium_vjp(int q, int dtype, const void* rho, const void* u, const void* g_feq, void* g_rho, void* g_u,
+                       int64_t n, void* stream);
+/* collision_bgk / _kbc / _reg (lbm/basic.py:138-156, lbm/collision/kbc.py:10-60,
+ * reg.py:4-49; lbm3d/basic.py:133-146, lbm3d/collision/kbc.py:8-42, reg.py:44-62):
+ * g_f, g_feq, and per node the share of g_omega (g_omega_node may be NULL) */
+int vs_collision_vjp(int q, int dtype, int kind, const void* f, const void* feq, double omega, const void* g_out,
+                     void* g_f, void* g_feq, void* g_omega_node, int64_t n, void* stream);
+/* collision_mrt (lbm/collision/mrt.py:66-88, lbm3d/collision/mrt.py:83-98): g_f, g_feq and,
+ * when g_op != NULL, the cotangent of the q x q operator (device doubles, row-major) */
+int vs_collision_mrt_vjp(int q, int dtype, const void* f, const void* feq, const double* op_host, const void* g_out,
+                         void* g_f, void* g_feq, double* g_op, int64_t n, void* stream);
+/* forcing_edm / forcing_guo_bgk (lbm/forcing/edm.py:4-31, guo.py:38-59; 3-D edm.py:6-26,
+ * guo.py:41-55): g_f (may be NULL), g_g, g_u and per node g_out . guo, whose sum times
+ * -1/2 is the Guo-BGK cotangent of omega (g_scale_node may be NULL) */
+int vs_forcing_vjp(int q, int dtype, int kind, const void* g, const void* u, double omega, const void* g_out,
+                   void* g_f, void* g_g, void* g_u, void* g_scale_node, int64_t n, void* stream);
+/* forcing_guo_mrt (lbm/forcing/guo.py:62-107, lbm3d/forcing/guo.py:58-87): g_f, g_g, g_u
+ * and, when g_op != NULL (needs guo_scratch of q x n values), the operator's cotangent */
+int vs_forcing_guo_mrt_vjp(int q, int dtype, const void* g, const void* u, const double* op_host, const void* g_out,
+                           void* g_f, void* g_g, void* g_u, void* guo_scratch, double* g_op, int64_t n, void* stream);
+/* boundary_nee / _nebb / _equilibrium / _bounce_back / _specular_reflection and their
+ * velocity / pressure forms (the sources cited at vs_boundary), scalar wall values:
+ * g_in (and g_before_stream for bounce-back) from g_out; g_wall_node (4 per face node,
+ * may be NULL): shares of the cotangents of rho_wall, ux_wall, uy_wall, uz_wall.  A
+ * force-corrected wall is the given wall with the corrected velocity. */
+int vs_boundary_vjp(int q, int dtype, int kind, int mode, int loc, const void* f_in, const void* f_before_stream,
+                    const void* g_out, void* g_in, void* g_before_stream, void* g_wall_node, int nx, int ny, int nz,
+                    double rho_wall, double ux_wall, double uy_wall, double uz_wall, void* stream);
+/* out[m, s] = sum_c A[m, c] grid[c, I[m, s]]: the stencil weights' cotangent of
+ * interpolate (A = g_U, grid = the interpolated field) and of spread (A = the spread
+ * values, grid = g_out) (ib/stencil.py:54-110).  The field cotangents are the other
+ * operation: interpolate^T = spread, spread^T = interpolate. */
+int vs_ib_pair_dot(int dtype, const void* A, const void* grid, int c, int64_t n_grid, const int32_t* I, int m, int s,
+                   void* out, void* stream);
+/* get_ib_stencil (ib/stencil.py:7-51, ib3d/stencil.py:7-59): marker-coordinate
+ * cotangents from g_W (m, s); z and g_z NULL in 2-D */
+int vs_ib_stencil_vjp(int kernel, int radius, int dtype, int dim, const void* x, const void* y, const void* z,
+                      const void* g_W, void* g_x, void* g_y, void* g_z, int m, void* stream);
+/* newmark (dyn.py:5-51): g_a, g_v, g_d, g_h (ndof each) from the next state's cotangents
+ * (any may be NULL = zero); scalar branch: g_mkc[3] = cotangents of m, k, c; matrix
+ * branch: g_mats = g_M, g_K, g_C (3 ndof x ndof, row-major) */
+int vs_newmark_vjp(int dtype, int ndof, const void* a, const void* v, const void* d, const void* h, double m, double k,
+                   double c, const void* m_mat, const void* k_mat, const void* c_mat, double dt, double gamma,
+                   double beta, const void* g_a_next, const void* g_v_next, const void* g_d_next, void* g_a,
+                   void* g_v, void* g_d, void* g_h, void* g_mkc, void* g_mats, void* stream);
+/* Deterministic sum of n values x[0], x[stride], ... into *out (a device double);
+ * scratch: 256 device doubles.  No counterpart in the reference (XLA reduces there). */
+int vs_sum_ordered(int dtype, const void* x, int64_t n, int64_t stride, double* scratch, double* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

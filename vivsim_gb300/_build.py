@@ -27,6 +27,7 @@ UNITS = {
     "vs_adjoint.cu": [],
     "vs_post.cu": [],
     "vs_refine.cu": [],
+    "vs_grad.cu": [],
 }
 
 

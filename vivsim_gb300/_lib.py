@@ -141,6 +141,19 @@ _SIGS = {
     "vs_adjoint_plan_destroy": (_i, [_p]),
     "vs_adjoint_forward": (_i, [_p, _i, C.POINTER(_d), _p]),
     "vs_adjoint_backward": (_i, [_p, _d, C.POINTER(_d), C.POINTER(_d), C.POINTER(_d), _p]),
+    "vs_streaming_vjp": (_i, [_i, _i, _p, _p, _i, _i, _i, _p]),
+    "vs_macroscopic_vjp": (_i, [_i, _i, _p, _p, _p, _p, _l, _p]),
+    "vs_equilibrium_vjp": (_i, [_i, _i, _p, _p, _p, _p, _p, _l, _p]),
+    "vs_collision_vjp": (_i, [_i, _i, _i, _p, _p, _d, _p, _p, _p, _p, _l, _p]),
+    "vs_collision_mrt_vjp": (_i, [_i, _i, _p, _p, C.POINTER(_d), _p, _p, _p, _p, _l, _p]),
+    "vs_forcing_vjp": (_i, [_i, _i, _i, _p, _p, _d, _p, _p, _p, _p, _p, _l, _p]),
+    "vs_forcing_guo_mrt_vjp": (_i, [_i, _i, _p, _p, C.POINTER(_d), _p, _p, _p, _p, _p, _p, _l, _p]),
+    "vs_boundary_vjp": (_i, [_i, _i, _i, _i, _i, _p, _p, _p, _p, _p, _p, _i, _i, _i, _d, _d, _d, _d, _p]),
+    "vs_ib_pair_dot": (_i, [_i, _p, _p, _i, _l, _p, _i, _i, _p, _p]),
+    "vs_ib_stencil_vjp": (_i, [_i, _i, _i, _i, _p, _p, _p, _p, _p, _p, _p, _i, _p]),
+    "vs_newmark_vjp": (_i, [_i, _i, _p, _p, _p, _p, _d, _d, _d, _p, _p, _p, _d, _d, _d, _p, _p, _p, _p, _p, _p, _p,
+                           _p, _p, _p]),
+    "vs_sum_ordered": (_i, [_i, _p, _l, _l, _p, _p, _p]),
     "vs_lattice_status": (_i, [_p, _i, _p]),
     "vs_check_finite": (_i, [_i, _p, _l, _p, _p]),
     "vs_selftest_bounded_wait": (_i, [_i, _p, _p]),

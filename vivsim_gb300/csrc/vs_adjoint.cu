@@ -27,35 +27,14 @@
 
 #include "vs_boundary.cuh"
 #include "vs_dispatch.cuh"
+#include "vs_dual.cuh"
 #include "vs_ib.cuh"
 
 namespace vs {
 namespace adj {
 
-// ------------------------------------------------------------------ dual numbers
-template <typename T>
-struct Dual {
-  T v, d;
-  __device__ Dual() : v(0), d(0) {}
-  __device__ Dual(T a, T b) : v(a), d(b) {}
-  template <typename U>
-  __device__ Dual(U a) : v((T)a), d(0) {}
-};
-template <typename T>
-__device__ __forceinline__ Dual<T> operator+(Dual<T> a, Dual<T> b) { return Dual<T>(a.v + b.v, a.d + b.d); }
-template <typename T>
-__device__ __forceinline__ Dual<T> operator-(Dual<T> a, Dual<T> b) { return Dual<T>(a.v - b.v, a.d - b.d); }
-template <typename T>
-__device__ __forceinline__ Dual<T> operator-(Dual<T> a) { return Dual<T>(-a.v, -a.d); }
-template <typename T>
-__device__ __forceinline__ Dual<T> operator*(Dual<T> a, Dual<T> b) {
-  return Dual<T>(a.v * b.v, a.d * b.v + a.v * b.d);
-}
-template <typename T>
-__device__ __forceinline__ Dual<T> operator/(Dual<T> a, Dual<T> b) {
-  const T q = a.v / b.v;
-  return Dual<T>(q, (a.d - q * b.d) / b.v);
-}
+// dual numbers: vs_dual.cuh
+using vs::Dual;
 
 // feq_i(rho, u) in the reference's form (lbm/basic.py:114-135), generic scalar S
 template <typename S, typename T>
@@ -407,29 +386,6 @@ struct BodyArgs {
 };
 
 constexpr int kAdjBodyThreads = 1024;
-
-// derivative of the delta kernels (ib/kernels.py), d phi / d r
-template <typename T>
-__device__ __forceinline__ T ddelta(int kernel, T r) {
-  const T a = fabs(r), sg = r < T(0) ? T(-1) : T(1);
-  if (kernel == VS_KERNEL_PESKIN4) {
-    if (a >= T(2)) return T(0);
-    if (a < T(1)) {
-      const T q = sqrt((T(1) + T(4) * a) - T(4) * (a * a));
-      return sg * T(0.125) * (T(-2) + (T(2) - T(4) * a) / q);
-    }
-    const T q = sqrt((T(-7) + T(12) * a) - T(4) * (a * a));
-    return sg * T(0.125) * (T(-2) - (T(6) - T(4) * a) / q);
-  }
-  if (kernel == VS_KERNEL_PESKIN3) {
-    if (a >= T(1.5)) return T(0);
-    if (a < T(0.5)) return sg * (-(T(3) * a) / sqrt(T(1) - T(3) * (a * a))) / T(3);
-    return sg * (T(-3) - (T(3) - T(3) * a) / sqrt((T(-2) + T(6) * a) - T(3) * (a * a))) / T(6);
-  }
-  if (a >= T(2)) return T(0);
-  const T k = (T)3.14159265358979323846 * T(0.5);
-  return sg * T(-0.25) * k * sin(k * a);
-}
 
 // Node sum over the pairs that reach the node (nx_, ny_) of a pair: sum_p W_p F[m_p] (both
 // components), the contributing markers given by the pair's bit mask (NW 64-bit words,

@@ -97,12 +97,10 @@ __host__ __device__ inline int64_t face_node(int loc, const int* n, int64_t j, i
 }
 
 // f0 + f_t0 + f_t1 + 2 (f_o0 + f_o1 + f_o2) (lbm/boundary/_helpers.py:124-135)
-// (Products and sums of the face formulas are rounded one by one (mul_rn / add_rn), so
-// the fused step's faces agree with the per-operator kernels to the bit.)
 template <typename T>
 __device__ __forceinline__ T rho_numerator(L9, int loc, const T* w) {
-  return add_rn(add_rn(add_rn(w[0], w[f9_tan(loc, 0)]), w[f9_tan(loc, 1)]),
-                mul_rn(T(2), add_rn(add_rn(w[f9_out(loc, 0)], w[f9_out(loc, 1)]), w[f9_out(loc, 2)])));
+  return ((w[0] + w[f9_tan(loc, 0)]) + w[f9_tan(loc, 1)]) +
+         T(2) * ((w[f9_out(loc, 0)] + w[f9_out(loc, 1)]) + w[f9_out(loc, 2)]);
 }
 // sum f_zero + 2 sum f_out (lbm3d/boundary/_helpers.py:37-44)
 template <typename T>
@@ -116,7 +114,7 @@ __device__ __forceinline__ T rho_numerator(L19, int loc, const T* w) {
     if (c == 0) { z = fz ? w[i] : z + w[i]; fz = false; }
     else if (c == -sg) { o = fo ? w[i] : o + w[i]; fo = false; }
   }
-  return add_rn(z, mul_rn(T(2), o));
+  return z + T(2) * o;
 }
 
 // Tangential wall velocity copied from the neighbour for a pressure boundary.
@@ -156,11 +154,11 @@ __device__ __forceinline__ void bc_node(const WallArgs<T>& A, int64_t j, const T
   bool un_scalar = A.un_scalar && !(A.u_arr[0] || A.u_arr[1] || A.u_arr[2]);
   bool all_scalar = un_scalar && A.all_scalar && !A.rho_arr;
   if (A.mode == VS_WALL_VELOCITY) {
-    const T omu = un_scalar ? A.one_m_un : sub_rn(T(1), (sg > 0 ? u[a] : -u[a]));
+    const T omu = un_scalar ? A.one_m_un : T(1) - (sg > 0 ? u[a] : -u[a]);
     rho = rho_numerator(L{}, A.loc, w) / omu;
     all_scalar = false;
   } else if (A.mode == VS_WALL_PRESSURE) {
-    const T nvs = sub_rn(T(1), rho_numerator(L{}, A.loc, w) / rho);
+    const T nvs = T(1) - rho_numerator(L{}, A.loc, w) / rho;
     u[a] = sg > 0 ? nvs : -nvs;
     pressure_tangential(L{}, A.loc, nb, u);
     un_scalar = false;
@@ -178,7 +176,7 @@ __device__ __forceinline__ void bc_node(const WallArgs<T>& A, int64_t j, const T
       macro(L{}, nb, rn, un);
       const T usqn = usq_of(L{}, un);
 #pragma unroll
-      for (int i = 0; i < Q; ++i) out[i] = add_rn(feq_i(L{}, i, rho, u, usq), sub_rn(nb[i], feq_i(L{}, i, rn, un, usqn)));
+      for (int i = 0; i < Q; ++i) out[i] = feq_i(L{}, i, rho, u, usq) + (nb[i] - feq_i(L{}, i, rn, un, usqn));
     }
     return;
   }
@@ -186,30 +184,28 @@ __device__ __forceinline__ void bc_node(const WallArgs<T>& A, int64_t j, const T
     const T un = sg > 0 ? u[a] : -u[a];
     const T ut = sg > 0 ? u[1 - a] : -u[1 - a];
     if (A.kind == VS_BC_NEBB) {  // lbm/boundary/nebb.py:46-58
-      const T shear = mul_rn(mul_rn(T(0.5), sub_rn(w[f9_tan(A.loc, 0)], w[f9_tan(A.loc, 1)])), (T)sg);
+      const T shear = (T(0.5) * (w[f9_tan(A.loc, 0)] - w[f9_tan(A.loc, 1)])) * (T)sg;
       T nt, tt, n23;
       if (all_scalar) {
         nt = A.t16; tt = A.t05; n23 = A.t23;
       } else if (un_scalar) {
-        nt = mul_rn(A.c16un, rho); tt = mul_rn(A.c05ut, rho); n23 = mul_rn(A.c23un, rho);
+        nt = A.c16un * rho; tt = A.c05ut * rho; n23 = A.c23un * rho;
       } else {
-        nt = mul_rn(mul_rn((T)(1.0 / 6.0), un), rho);
-        tt = mul_rn(mul_rn(T(0.5), ut), rho);
-        n23 = mul_rn(mul_rn((T)(2.0 / 3.0), un), rho);
+        nt = ((T)(1.0 / 6.0) * un) * rho; tt = (T(0.5) * ut) * rho; n23 = ((T)(2.0 / 3.0) * un) * rho;
       }
-      out[f9_in(A.loc, 0)] = add_rn(w[f9_out(A.loc, 0)], n23);
-      out[f9_in(A.loc, 1)] = add_rn(add_rn(sub_rn(w[f9_out(A.loc, 1)], shear), nt), tt);
-      out[f9_in(A.loc, 2)] = sub_rn(add_rn(add_rn(w[f9_out(A.loc, 2)], shear), nt), tt);
+      out[f9_in(A.loc, 0)] = w[f9_out(A.loc, 0)] + n23;
+      out[f9_in(A.loc, 1)] = ((w[f9_out(A.loc, 1)] - shear) + nt) + tt;
+      out[f9_in(A.loc, 2)] = ((w[f9_out(A.loc, 2)] + shear) + nt) - tt;
     } else {  // bounce-back / specular, lbm/boundary/bb.py:15-95
       T v0, v1, v2;
       if (un_scalar) {
-        v0 = add_rn(pre[f9_out(A.loc, 0)], A.c23un);
-        v1 = add_rn(pre[f9_out(A.loc, 1)], A.b16p);
-        v2 = add_rn(pre[f9_out(A.loc, 2)], A.b16m);
+        v0 = pre[f9_out(A.loc, 0)] + A.c23un;
+        v1 = pre[f9_out(A.loc, 1)] + A.b16p;
+        v2 = pre[f9_out(A.loc, 2)] + A.b16m;
       } else {
-        v0 = add_rn(pre[f9_out(A.loc, 0)], mul_rn((T)(2.0 / 3.0), un));
-        v1 = add_rn(pre[f9_out(A.loc, 1)], mul_rn((T)(1.0 / 6.0), add_rn(un, ut)));
-        v2 = add_rn(pre[f9_out(A.loc, 2)], mul_rn((T)(1.0 / 6.0), sub_rn(un, ut)));
+        v0 = pre[f9_out(A.loc, 0)] + (T)(2.0 / 3.0) * un;
+        v1 = pre[f9_out(A.loc, 1)] + (T)(1.0 / 6.0) * (un + ut);
+        v2 = pre[f9_out(A.loc, 2)] + (T)(1.0 / 6.0) * (un - ut);
       }
       out[f9_in(A.loc, 0)] = v0;
       if (A.kind == VS_BC_BB) {
@@ -225,7 +221,7 @@ __device__ __forceinline__ void bc_node(const WallArgs<T>& A, int64_t j, const T
       for (int i = 0; i < 19; ++i) {
         if (q19_c(i, a) != sg) continue;
         const int o = q19_opp(i);
-        out[i] = sub_rn(add_rn(w[o], feq_i(L{}, i, rho, u, usq)), feq_i(L{}, o, rho, u, usq));
+        out[i] = (w[o] + feq_i(L{}, i, rho, u, usq)) - feq_i(L{}, o, rho, u, usq);
       }
     } else {  // lbm3d/boundary/bb.py:20-53; in/out paired in listed (increasing) order
       T rp = pre[0];
@@ -249,8 +245,8 @@ __device__ __forceinline__ void bc_node(const WallArgs<T>& A, int64_t j, const T
           cu = first ? t : cu + t;
           first = false;
         }
-        const T corr = mul_rn(mul_rn(mul_rn(T(2), q19_w<T>(i)), rp), cu) / (T)(1.0 / 3.0);
-        out[i] = add_rn(pre[outs[k++]], corr);
+        const T corr = (((T(2) * q19_w<T>(i)) * rp) * cu) / (T)(1.0 / 3.0);
+        out[i] = pre[outs[k++]] + corr;
       }
     }
   }

@@ -147,20 +147,16 @@ __device__ __forceinline__ void macro(L19, const T* f, T& rho, T* u) {
 
 // ------------------------------------------------------------------ equilibria
 // D2Q9: feq_i = rho w_i (1 + 3 cu + 4.5 cu^2 - 1.5 u^2), vivsim/lbm/basic.py:114-135.
-// (Every product and sum of feq_i, usq_of and guo_i is rounded on its own: the face
-// boundaries and the forcing of the fused step then round exactly as the per-operator
-// kernels, which are built without multiply-add contraction.)
 template <typename T>
 __device__ __forceinline__ T feq_i(L9, int i, T rho, const T* u, T usq) {
   const int cx = q9_cx(i), cy = q9_cy(i);
   const T a = cx == 0 ? T(0) : (cx > 0 ? u[0] : -u[0]);
   const T b = cy == 0 ? T(0) : (cy > 0 ? u[1] : -u[1]);
-  const T uc = add_rn(a, b);
-  return mul_rn(mul_rn(rho, q9_w<T>(i)),
-                sub_rn(add_rn(add_rn(T(1), mul_rn(T(3), uc)), mul_rn(T(4.5), mul_rn(uc, uc))), mul_rn(T(1.5), usq)));
+  const T uc = a + b;
+  return (rho * q9_w<T>(i)) * (((T(1) + T(3) * uc) + T(4.5) * (uc * uc)) - T(1.5) * usq);
 }
 template <typename T>
-__device__ __forceinline__ T usq_of(L9, const T* u) { return add_rn(mul_rn(u[0], u[0]), mul_rn(u[1], u[1])); }
+__device__ __forceinline__ T usq_of(L9, const T* u) { return u[0] * u[0] + u[1] * u[1]; }
 
 // D3Q19: feq = rho w (1 + cu/cs2 + (cu)^2/(2 cs2^2) - u^2/(2 cs2)), vivsim/lbm3d/basic.py:109-130.
 // cs2 = 1/3 enters as a (weakly typed) constant of the working precision, exactly as
@@ -179,13 +175,10 @@ __device__ __forceinline__ T feq_i(L19, int i, T rho, const T* u, T usq) {
   }
   const T cs2 = (T)(1.0 / 3.0);
   const T cs4 = (T)((1.0 / 3.0) * (1.0 / 3.0));
-  return mul_rn(mul_rn(rho, q19_w<T>(i)), sub_rn(add_rn(add_rn(T(1), uc / cs2), mul_rn(T(0.5), mul_rn(uc, uc)) / cs4),
-                                                 mul_rn(T(0.5), usq) / cs2));
+  return (rho * q19_w<T>(i)) * (((T(1) + uc / cs2) + (T(0.5) * (uc * uc)) / cs4) - (T(0.5) * usq) / cs2);
 }
 template <typename T>
-__device__ __forceinline__ T usq_of(L19, const T* u) {
-  return add_rn(add_rn(mul_rn(u[0], u[0]), mul_rn(u[1], u[1])), mul_rn(u[2], u[2]));
-}
+__device__ __forceinline__ T usq_of(L19, const T* u) { return (u[0] * u[0] + u[1] * u[1]) + u[2] * u[2]; }
 
 template <class L, typename T>
 __device__ __forceinline__ void equilibrium(T rho, const T* u, T* feq) {
@@ -387,9 +380,9 @@ __device__ __forceinline__ void collide(int kind, T* f, const T* feq, const Coll
 template <typename T>
 __device__ __forceinline__ T guo_i(L9, int i, const T* g, const T* u) {
   const T cx = (T)q9_cx(i), cy = (T)q9_cy(i);
-  const T uc = add_rn(mul_rn(u[0], cx), mul_rn(u[1], cy));
-  return mul_rn(q9_w<T>(i), add_rn(mul_rn(g[0], add_rn(mul_rn(T(3), sub_rn(cx, u[0])), mul_rn(T(9), mul_rn(uc, cx)))),
-                                   mul_rn(g[1], add_rn(mul_rn(T(3), sub_rn(cy, u[1])), mul_rn(T(9), mul_rn(uc, cy))))));
+  const T uc = u[0] * cx + u[1] * cy;
+  return q9_w<T>(i) * (g[0] * (T(3) * (cx - u[0]) + T(9) * (uc * cx)) +
+                       g[1] * (T(3) * (cy - u[1]) + T(9) * (uc * cy)));
 }
 // D3Q19: w_i [3 (c.g - g.u) + 9 (c.g)(c.u)], vivsim/lbm3d/forcing/guo.py:13-38.
 template <typename T>
@@ -406,8 +399,8 @@ __device__ __forceinline__ T guo_i(L19, int i, const T* g, const T* u) {
     cg = first ? tg : cg + tg;
     first = false;
   }
-  const T gu = add_rn(add_rn(mul_rn(g[0], u[0]), mul_rn(g[1], u[1])), mul_rn(g[2], u[2]));
-  return mul_rn(q19_w<T>(i), add_rn(mul_rn(T(3), sub_rn(cg, gu)), mul_rn(mul_rn(T(9), cg), cu)));
+  const T gu = (g[0] * u[0] + g[1] * u[1]) + g[2] * u[2];
+  return q19_w<T>(i) * (T(3) * (cg - gu) + (T(9) * cg) * cu);
 }
 
 }  // namespace vs

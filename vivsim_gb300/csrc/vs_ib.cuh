@@ -42,6 +42,29 @@ __device__ __forceinline__ T delta(int kernel, T r) {
   return kernel == VS_KERNEL_PESKIN3 ? delta_peskin3(r) : (kernel == VS_KERNEL_PESKIN4 ? delta_peskin4(r) : delta_cosine4(r));
 }
 
+// derivative of the delta kernels (ib/kernels.py), d phi / d r
+template <typename T>
+__device__ __forceinline__ T ddelta(int kernel, T r) {
+  const T a = fabs(r), sg = r < T(0) ? T(-1) : T(1);
+  if (kernel == VS_KERNEL_PESKIN4) {
+    if (a >= T(2)) return T(0);
+    if (a < T(1)) {
+      const T q = sqrt((T(1) + T(4) * a) - T(4) * (a * a));
+      return sg * T(0.125) * (T(-2) + (T(2) - T(4) * a) / q);
+    }
+    const T q = sqrt((T(-7) + T(12) * a) - T(4) * (a * a));
+    return sg * T(0.125) * (T(-2) - (T(6) - T(4) * a) / q);
+  }
+  if (kernel == VS_KERNEL_PESKIN3) {
+    if (a >= T(1.5)) return T(0);
+    if (a < T(0.5)) return sg * (-(T(3) * a) / sqrt(T(1) - T(3) * (a * a))) / T(3);
+    return sg * (T(-3) - (T(3) - T(3) * a) / sqrt((T(-2) + T(6) * a) - T(3) * (a * a))) / T(6);
+  }
+  if (a >= T(2)) return T(0);
+  const T k = (T)3.14159265358979323846 * T(0.5);
+  return sg * T(-0.25) * k * sin(k * a);
+}
+
 // floor() to int32 as in jnp.floor(x).astype(jnp.int32)
 template <typename T>
 __device__ __forceinline__ int ifloor(T x) { return (int)floor(x); }

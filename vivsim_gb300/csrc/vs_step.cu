@@ -19,277 +19,46 @@
 #include <cmath>
 #include <cstdlib>
 #include <new>
+#include <type_traits>
 #include <vector>
 
 #include "vs_boundary.cuh"
 #include "vs_dispatch.cuh"
 #include "vs_fast.cuh"
+#include "vs_grid.cuh"
 #include "vs_ib.cuh"
 
 namespace vs {
 
-// device window descriptor (int[8]): origin, extent, sticky status
-// META_PX/PY: lower corner of the body's last stencil bounding box (2-D moving bodies
-// predict their next window from it)
-// META_PX2/PY2: a second prediction slot; the cluster-form body reads one slot while the
-// concurrent grid kernel reads the same slot for the box it skips, and writes the other
-enum {
-  META_OX = 0, META_OY, META_OZ, META_WX, META_WY, META_WZ, META_STATUS, META_PX, META_PY, META_PX2, META_PY2,
-  META_N = 12
-};
-
-// ------------------------------------------------------------------ grid kernel
-template <class L, typename T>
-struct StepParams {
-  // the fields every launch reads come first (a launch fetches only the lines it touches)
-  const T* fin;
-  T* fout;
-  int nx, ny, nz, n;
-  int chunks;                    // blocks along the contiguous axis (3-D)
-  int gx;                        // blocks per launch row (the launch's grid.x)
-  int nreg;                      // 0: the whole grid; else the union of reg[0..nreg)
-  int skip_box;                  // nodes inside box[] are left to another launch
-  int skip_walls;                // the x = 0 and x = nx-1 planes are left to another launch
-  int mask_load;                 // apply the previous step's obstacle bounce-back on load
-  int dyn_slot, dyn_ext[2];      // predicted window: slot and extent (with dyn_meta)
-  int forcing;
-  int has_g0;
-  int n_lazy;                    // face boundaries of the previous step applied on load
-  int n_pre;                     // faces whose pre-stream populations are kept (bounce-back)
-  const uint8_t* mask;           // obstacle cells (one byte per node) or null
-  const int* dyn_meta;           // non-null: the skipped box is the body's predicted window
-  CollideParams<T> cp;
-  T g0[3];
-  T guo_scale;                   // 1 - omega / 2 (Guo-BGK)
-  const T* gw;                   // IB force window (D, wx, wy, wz) or null
-  const int* meta;               // window descriptor (device)
-  int box[6];
-  int reg[3][6];                 // regions x0, x1, y0, y1, z0, z1 (half-open)
-  int rowstart[4];               // first launch row (x plane) of each region
-  WallArgs<T> lazy[2];
-  int pre_loc[VS_MAX_BC];
-  T* pre_buf[VS_MAX_BC];
-  T op[L::Q * L::Q];             // MRT collision operator
-  T fop[L::Q * L::Q];            // MRT forcing operator
-};
-
-// Per-node work of the grid kernels: (lazy face boundaries,) moments, equilibrium,
-// collision, forcing, push streaming.  f holds the node's loaded populations.
-template <class L, typename T, int COLL, bool WALLS>
-__device__ __forceinline__ void step_node(const StepParams<L, T>& P, int x, int y, int z, int p, T* f) {
-  constexpr int Q = L::Q;
-  const int syz = P.ny * P.nz;
-
-  // the previous step's face boundaries, applied to the wall nodes as they are loaded
-  // (all of them on the x faces, so they touch disjoint nodes and commute)
-  if constexpr (WALLS) for (int k = 0; k < P.n_lazy; ++k) {
-    const WallArgs<T>& A = P.lazy[k];
-    const int a = loc_axis(A.loc), sg = loc_sign(A.loc);
-    const int coord = a == 0 ? x : (a == 1 ? y : z);
-    const int nn[3] = {P.nx, P.ny, P.nz};
-    if (coord != (sg > 0 ? 0 : nn[a] - 1)) continue;
-    T nb[Q], out[Q];
-    if (bc_needs_neighbor<L>(A.kind, A.mode)) {
-      const int stride = a == 0 ? syz : (a == 1 ? P.nz : 1);
-      const int pn = p + sg * stride;
-#pragma unroll
-      for (int i = 0; i < Q; ++i) nb[i] = __ldg(P.fin + (size_t)i * P.n + pn);
-    }
-    bc_node<L, T>(A, 0, f, nb, nullptr, out);
-#pragma unroll
-    for (int i = 0; i < Q; ++i) f[i] = out[i];
-  }
-  // the previous step's obstacle bounce-back (lbm/boundary/bb.py:98-110), which follows its
-  // face boundaries: an obstacle cell's populations swap with their opposites
-  if (P.mask_load && P.mask[p]) {
-#pragma unroll
-    for (int i = 0; i < Q; ++i) {
-      const int o = L::opp(i);
-      if (o > i) {
-        const T t = f[i];
-        f[i] = f[o];
-        f[o] = t;
-      }
-    }
-  }
-
-  T rho, u[3] = {T(0), T(0), T(0)};
-  fast::macro<L>(f, rho, u);
-
-  T g[3] = {T(0), T(0), T(0)};
-  bool has_g = P.has_g0;
-  if (has_g) {
-#pragma unroll
-    for (int d = 0; d < L::D; ++d) g[d] = P.g0[d];
-  }
-  if (P.gw) {
-    const int wx = x - P.meta[META_OX], wy = y - P.meta[META_OY], wz = z - P.meta[META_OZ];
-    const int ex = P.meta[META_WX], ey = P.meta[META_WY], ez = P.meta[META_WZ];
-    if (wx >= 0 && wx < ex && wy >= 0 && wy < ey && wz >= 0 && wz < ez) {
-      const int cells = ex * ey * ez;
-      const int c = (wx * ey + wy) * ez + wz;
-#pragma unroll
-      for (int d = 0; d < L::D; ++d) g[d] = has_g ? g[d] + P.gw[d * cells + c] : P.gw[d * cells + c];
-      has_g = true;
-    }
-  }
-
-  // Guo forcing uses the half-force corrected velocity in the equilibrium
-  // (examples/2d/poiseuille_channel.py:103-105); EDM uses the plain one.
-  T ue[3] = {u[0], u[1], u[2]};
-  const bool guo = has_g && (P.forcing == VS_FORCE_GUO_BGK || P.forcing == VS_FORCE_GUO_MRT);
-  if (guo) {
-#pragma unroll
-    for (int d = 0; d < L::D; ++d) ue[d] = u[d] + (g[d] * T(0.5)) / rho;
-  }
-  T feq[Q];
-  fast::equilibrium<L>(rho, ue, feq);
-  fast::collide<L, COLL>(f, feq, P.cp, P.op);
-
-  if (has_g && P.forcing != VS_FORCE_NONE) {
-    if (P.forcing == VS_FORCE_EDM) {
-#pragma unroll
-      for (int i = 0; i < Q; ++i) f[i] = f[i] + guo_i(L{}, i, g, u);
-    } else if (P.forcing == VS_FORCE_GUO_BGK) {
-#pragma unroll
-      for (int i = 0; i < Q; ++i) f[i] = f[i] + guo_i(L{}, i, g, ue) * P.guo_scale;
-    } else {
-      T gl[Q];
-#pragma unroll
-      for (int i = 0; i < Q; ++i) gl[i] = guo_i(L{}, i, g, ue);
-#pragma unroll
-      for (int i = 0; i < Q; ++i) {
-        T acc = P.fop[i * Q] * gl[0];
-#pragma unroll
-        for (int j = 1; j < Q; ++j) acc = acc + P.fop[i * Q + j] * gl[j];
-        f[i] = f[i] + acc;
-      }
-    }
-  }
-
-  // keep the pre-stream populations of bounce-back faces (lbm/boundary/bb.py needs them)
-  for (int k = 0; k < P.n_pre; ++k) {
-    const int loc = P.pre_loc[k];
-    const int a = loc_axis(loc);
-    const int coord = a == 0 ? x : (a == 1 ? y : z);
-    const int nn[3] = {P.nx, P.ny, P.nz};
-    if (coord != (loc_sign(loc) > 0 ? 0 : nn[a] - 1)) continue;
-    const int b0 = a == 0 ? 1 : 0, b1 = a == 2 ? 1 : 2;
-    const int cc[3] = {x, y, z};
-    const int64_t nf = face_size(loc, nn);
-    const int64_t j = (int64_t)cc[b0] * nn[b1] + cc[b1];
-#pragma unroll
-    for (int i = 0; i < Q; ++i) P.pre_buf[k][i * nf + j] = f[i];
-  }
-
-  // push streaming with periodic wrap on every axis (lbm/basic.py:60-85):
-  // destination = p + per-axis offsets, each offset wrapping at the domain edge
-  const int dxp = x == P.nx - 1 ? -(P.nx - 1) * syz : syz;
-  const int dxm = x == 0 ? (P.nx - 1) * syz : -syz;
-  const int dyp = y == P.ny - 1 ? -(P.ny - 1) * P.nz : P.nz;
-  const int dym = y == 0 ? (P.ny - 1) * P.nz : -P.nz;
-  const int dzp = z == P.nz - 1 ? -(P.nz - 1) : 1;
-  const int dzm = z == 0 ? P.nz - 1 : -1;
-#pragma unroll
-  for (int i = 0; i < Q; ++i) {
-    const int cx = L::c(i, 0), cy = L::c(i, 1), cz = L::c(i, 2);
-    const int d = (cx > 0 ? dxp : (cx < 0 ? dxm : 0)) + (cy > 0 ? dyp : (cy < 0 ? dym : 0)) +
-                  (cz > 0 ? dzp : (cz < 0 ? dzm : 0));
-    P.fout[(size_t)i * P.n + (p + d)] = f[i];
-  }
-}
-
-// One thread per node.  blockIdx.y = x; blockIdx.x = (y, chunk of the contiguous axis)
-// in 3-D or the chunk of y in 2-D; threads run along the contiguous axis, so every load
-// and store of a warp covers 32 consecutive addresses.  Wrap-around offsets of the push
-// are per-block uniform except along the contiguous axis.
-// With nreg > 0 the launch rows walk a list of regions instead of the whole grid.
-// One block of the grid kernel: block (bx, by) of the launch geometry set up by
-// enqueue_grid (bx: chunk along the contiguous axis [x (y, chunk) in 3-D], by: row).
-template <class L, typename T, int COLL, bool WALLS>
-__device__ __forceinline__ void step_block(const StepParams<L, T>& P, int bx, int by) {
-  constexpr int Q = L::Q;
-  int x, y, z;
-  if (P.nreg == 0) {
-    x = by;
-    if constexpr (L::D == 2) {
-      y = bx * blockDim.x + threadIdx.x;
-      if (y >= P.ny) return;
-      z = 0;
-    } else {
-      y = bx / P.chunks;
-      z = (bx - y * P.chunks) * blockDim.x + threadIdx.x;
-      if (z >= P.nz) return;
-    }
-  } else {
-    const int r = by;
-    const int g = (r >= P.rowstart[1]) + (r >= P.rowstart[2]);
-    const int* R = P.reg[g];
-    x = R[0] + (r - P.rowstart[g]);
-    if constexpr (L::D == 2) {
-      y = R[2] + bx * blockDim.x + threadIdx.x;
-      if (y >= R[3]) return;
-      z = 0;
-    } else {
-      const int cy = bx / P.chunks;
-      y = R[2] + cy;
-      z = R[4] + (bx - cy * P.chunks) * blockDim.x + threadIdx.x;
-      if (y >= R[3] || z >= R[5]) return;
-    }
-  }
-  if (P.skip_box && x >= P.box[0] && x < P.box[1] && y >= P.box[2] && y < P.box[3] && z >= P.box[4] &&
-      z < P.box[5])
-    return;
-  if (P.dyn_meta) {
-    const int bx = P.dyn_meta[P.dyn_slot ? META_PX2 : META_PX] - 1, by = P.dyn_meta[P.dyn_slot ? META_PY2 : META_PY] - 1;
-    if (x >= bx && x < bx + P.dyn_ext[0] && y >= by && y < by + P.dyn_ext[1]) return;
-  }
-  if (P.skip_walls && (x == 0 || x == P.nx - 1)) return;
-
-  const int p = (x * P.ny + y) * P.nz + z;
-  T f[Q];
-#pragma unroll
-  for (int i = 0; i < Q; ++i) f[i] = __ldg(P.fin + (size_t)i * P.n + p);
-  step_node<L, T, COLL, WALLS>(P, x, y, z, p, f);
-}
-
 template <class L, typename T, int COLL, bool WALLS>
 __global__ void __launch_bounds__(256) k_step(const __grid_constant__ StepParams<L, T> P) {
-  step_block<L, T, COLL, WALLS>(P, blockIdx.x, blockIdx.y);
+  step_block<L, T, COLL, WALLS ? (kFeatGeneral | kFeatWalls) : kFeatGeneral>(P, blockIdx.x, blockIdx.y);
 }
 
-// The main launch of a batch walks each case's nodes in memory order: chunk j of a
-// case is nodes [j * blockDim.x, (j + 1) * blockDim.x) of its flattened grid, so a block is
-// full whatever the case's row length (rows of 64 nodes would leave 3/4 of a 256-thread
-// block idle) and a warp still reads 32 consecutive addresses.
-template <class L, typename T, int COLL, bool WALLS>
-__device__ __forceinline__ void step_flat(const StepParams<L, T>& P, int chunk) {
-  const int p = chunk * (int)blockDim.x + (int)threadIdx.x;
-  if (p >= P.n) return;
-  int x, y, z;
-  if constexpr (L::D == 2) {
-    x = p / P.ny;
-    y = p - x * P.ny;
-    z = 0;
-  } else {
-    const int syz = P.ny * P.nz;
-    x = p / syz;
-    const int r = p - x * syz;
-    y = r / P.nz;
-    z = r - y * P.nz;
-  }
-  if (P.skip_box && x >= P.box[0] && x < P.box[1] && y >= P.box[2] && y < P.box[3] && z >= P.box[4] &&
-      z < P.box[5])
-    return;
-  if (P.dyn_meta) {
-    const int bx = P.dyn_meta[P.dyn_slot ? META_PX2 : META_PX] - 1, by = P.dyn_meta[P.dyn_slot ? META_PY2 : META_PY] - 1;
-    if (x >= bx && x < bx + P.dyn_ext[0] && y >= by && y < by + P.dyn_ext[1]) return;
-  }
-  if (P.skip_walls && (x == 0 || x == P.nx - 1)) return;
-  T f[L::Q];
-#pragma unroll
-  for (int i = 0; i < L::Q; ++i) f[i] = __ldg(P.fin + (size_t)i * P.n + p);
-  step_node<L, T, COLL, WALLS>(P, x, y, z, p, f);
+// The grid launches that read no per-node feature beyond (FEAT = kFeatSkip) the tests for
+// nodes another launch updates: the bulk of every HBM-bound step.  Compiled without the
+// force window, the load-time boundaries, the obstacle mask and the pre-stream copies, they
+// need fewer registers, and the launch shape below holds more loads in flight per SM.
+// FastShape: threads per block, resident blocks per SM (a register cap) and nodes per
+// thread (D2Q9: two nodes blockDim apart along y), chosen by timing the 8192^2 D2Q9 and
+// 256 x 128 x 128 / 512 x 256 x 256 D3Q19 grids on GB300.
+// Measured (fraction of the measured copy bandwidth at 72 / 152 B per node): D2Q9 KBC two
+// nodes x 128 threads, 8 blocks 0.90; D2Q9 BGK and MRT 256 threads, 8 blocks 0.99 and 0.93;
+// D3Q19 BGK and REG 128 threads, 10 blocks 0.96 and 0.95; D3Q19 KBC 64 threads, 16 blocks
+// 0.80 (the general kernel: 0.69-0.83).
+template <class L, int COLL>
+struct FastShape {
+  static constexpr bool heavy3 = L::Q == 19 && (COLL == VS_COLLIDE_KBC || COLL == VS_COLLIDE_MRT);
+  static constexpr int NPT = (L::Q == 9 && COLL == VS_COLLIDE_KBC) ? 2 : 1;
+  static constexpr int TB = L::Q == 9 ? (NPT == 2 ? 128 : 256) : (heavy3 ? 64 : 128);
+  static constexpr int MINB = L::Q == 9 ? 8 : (heavy3 ? 16 : 10);
+};
+
+template <class L, typename T, int COLL, int FEAT>
+__global__ void __launch_bounds__(FastShape<L, COLL>::TB, FastShape<L, COLL>::MINB)
+    k_step_fast(const __grid_constant__ StepParams<L, T> P) {
+  if constexpr (FastShape<L, COLL>::NPT == 2) step_block2<T, COLL, FEAT>(P, blockIdx.x, blockIdx.y);
+  else step_block<L, T, COLL, FEAT>(P, blockIdx.x, blockIdx.y);
 }
 
 // (6 blocks of 256 threads per SM by registers: at the default 48 registers the loads in
@@ -298,7 +67,7 @@ template <class L, typename T, int COLL>
 __global__ void __launch_bounds__(256, 6) k_step_batch_flat(const StepParams<L, T>* __restrict__ Ps,
                                                          const int2* __restrict__ blk) {
   const int2 cb = blk[blockIdx.x];
-  step_flat<L, T, COLL, false>(Ps[cb.x], cb.y);
+  step_flat<L, T, COLL, kFeatGeneral>(Ps[cb.x], cb.y);
 }
 
 // Grid kernel over many independent lattices in one launch: block b works on lattice
@@ -310,7 +79,7 @@ __global__ void __launch_bounds__(256) k_step_batch(const StepParams<L, T>* __re
   const int2 cb = blk[blockIdx.x];
   const StepParams<L, T>& P = Ps[cb.x];  // read through L1 (staging it in shared memory cost registers)
   const int by = cb.y / P.gx;
-  step_block<L, T, COLL, WALLS>(P, cb.y - by * P.gx, by);
+  step_block<L, T, COLL, WALLS ? (kFeatGeneral | kFeatWalls) : kFeatGeneral>(P, cb.y - by * P.gx, by);
 }
 
 
@@ -468,7 +237,7 @@ __global__ void __launch_bounds__(TB) k_step_tma(const __grid_constant__ StepPar
         z < P.box[5])
       continue;
     if (P.skip_walls && (x == 0 || x == P.nx - 1)) continue;
-    step_node<L, T, COLL, false>(P, x, y, z, p, f);
+    step_node<L, T, COLL, kFeatGeneral>(P, x, y, z, p, f);
   }
 }
 
@@ -1580,7 +1349,7 @@ __global__ void __launch_bounds__(kClusterThreads) k_body2d_cluster(const __grid
   }
   // the nodes of the predicted window, which the concurrent grid launch skips (the same
   // slot gives it the same window); lazy face planes are another launch's
-  if (wp >= 0) step_node<L9, T, COLL, false>(SP, wx, wy, 0, wp, fw);
+  if (wp >= 0) step_node<L9, T, COLL, kFeatGeneral>(SP, wx, wy, 0, wp, fw);
   for (int k = kw + CL * nt; k < NB; k += CL * nt) {
     const int x = ox + k / EY, y = oy + k % EY;
     if (x < 0 || x >= SP.nx || y < 0 || y >= SP.ny || (SP.skip_walls && (x == 0 || x == SP.nx - 1))) continue;
@@ -1588,7 +1357,7 @@ __global__ void __launch_bounds__(kClusterThreads) k_body2d_cluster(const __grid
     T f[9];
 #pragma unroll
     for (int i = 0; i < 9; ++i) f[i] = __ldg(SP.fin + (size_t)i * SP.n + p);
-    step_node<L9, T, COLL, false>(SP, x, y, 0, p, f);
+    step_node<L9, T, COLL, kFeatGeneral>(SP, x, y, 0, p, f);
   }
 }
 
@@ -2431,6 +2200,21 @@ static bool grid_setup(const vs_lattice_plan* LP, const vs_body_plan* B, const v
   return true;
 }
 
+// Launch geometry of k_step_fast: NPT nodes per thread along the contiguous axis, whole grid.
+// (false: the contiguous extent is shorter than one block's nodes; the general kernel runs)
+template <class L, int COLL>
+static bool launch_fast(StepParams<L, float> P, bool skip, cudaStream_t st) {
+  using S = FastShape<L, COLL>;
+  const int ext = L::D == 2 ? P.ny : P.nz;
+  if (ext < S::TB * S::NPT) return false;
+  P.chunks = (ext + S::TB * S::NPT - 1) / (S::TB * S::NPT);
+  const dim3 grid(L::D == 2 ? P.chunks : P.chunks * P.ny, P.nx);
+  P.gx = (int)grid.x;
+  if (skip) k_step_fast<L, float, COLL, kFeatSkip><<<grid, S::TB, 0, st>>>(P);
+  else k_step_fast<L, float, COLL, 0><<<grid, S::TB, 0, st>>>(P);
+  return true;
+}
+
 static int enqueue_grid(const vs_lattice_plan* LP, const vs_body_plan* B, const void* fin, void* fout,
                         cudaStream_t st, int mode = 0, bool lazy_walls = false, int slot = 0) {
   const vs_lattice_cfg& c = LP->cfg;
@@ -2455,6 +2239,25 @@ static int enqueue_grid(const vs_lattice_plan* LP, const vs_body_plan* B, const 
       if (trc) return trc;
       VS_CHECK_LAUNCH("vs_step grid kernel (TMA)");
       return VS_OK;
+    }
+    if constexpr (std::is_same<T, float>::value) {
+      // the bulk launches of a step: specialised kernel when no per-node feature is needed
+      const bool bulk = (mode == 0 || mode == 1 || mode == 4) && !walls && P.nreg == 0 && !P.gw && !P.has_g0 &&
+                        !P.mask_load && P.n_pre == 0;
+      if (bulk) {
+        const bool skip = P.skip_box || P.dyn_meta || P.skip_walls;
+        bool done;
+        switch (c.collision) {
+          case VS_COLLIDE_BGK: done = launch_fast<L, VS_COLLIDE_BGK>(P, skip, st); break;
+          case VS_COLLIDE_KBC: done = launch_fast<L, VS_COLLIDE_KBC>(P, skip, st); break;
+          case VS_COLLIDE_REG: done = launch_fast<L, VS_COLLIDE_REG>(P, skip, st); break;
+          default: done = launch_fast<L, VS_COLLIDE_MRT>(P, skip, st); break;
+        }
+        if (done) {
+          VS_CHECK_LAUNCH("vs_step grid kernel");
+          return VS_OK;
+        }
+      }
     }
 #define VS_LAUNCH_STEP(K)                                                              \
   (walls ? k_step<L, T, K, true><<<grid, tb, 0, st>>>(P) : k_step<L, T, K, false><<<grid, tb, 0, st>>>(P))

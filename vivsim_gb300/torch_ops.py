@@ -132,3 +132,81 @@ def coarse_to_fine(f_coarse: torch.Tensor, f_fine: torch.Tensor, dir: str) -> to
 @coarse_to_fine.register_fake
 def _(f_coarse, f_fine, dir):
     return torch.empty_like(f_fine)
+
+
+# ------------------------------------------------------------------ backward passes
+# Reverse-mode rules for the operators above, from the hand-written vector-Jacobian
+# kernels (csrc/vs_grad.cu, through vivsim_gb300.autodiff).  Scalar float arguments
+# (omega, marker_ds given as a float) are constants here; vivsim_gb300.autodiff takes them
+# as tensors when their gradient is wanted.
+
+from . import _lib as _V  # noqa: E402
+from . import autodiff as _ad  # noqa: E402
+
+
+def _save_inputs(ctx, inputs, output):
+    ctx.save_for_backward(*[x for x in inputs if isinstance(x, torch.Tensor)])
+    ctx.scalars = [x for x in inputs if not isinstance(x, torch.Tensor)]
+
+
+streaming.register_autograd(lambda ctx, g: _ad._Streaming.backward(ctx, g), setup_context=_save_inputs)
+get_macroscopic.register_autograd(lambda ctx, g_rho, g_u: _ad._Macroscopic.backward(ctx, g_rho, g_u),
+                                  setup_context=_save_inputs)
+get_equilibrium.register_autograd(lambda ctx, g: _ad._Equilibrium.backward(ctx, g), setup_context=_save_inputs)
+
+
+def _collision_backward(kind):
+    def bwd(ctx, g):
+        f, feq = ctx.saved_tensors
+        g = _V.cont(g)
+        gf, gfeq = torch.empty_like(f), torch.empty_like(f)
+        _V.call("vs_collision_vjp", f.shape[0], _V.dtype_code(f), kind, _V.ptr(_V.cont(f)), _V.ptr(_V.cont(feq)),
+                float(ctx.scalars[0]), _V.ptr(g), _V.ptr(gf), _V.ptr(gfeq), None, int(f[0].numel()), _V.stream())
+        return gf, gfeq, None
+    return bwd
+
+
+collision_bgk.register_autograd(_collision_backward(_V.VS_COLLIDE_BGK), setup_context=_save_inputs)
+collision_kbc.register_autograd(_collision_backward(_V.VS_COLLIDE_KBC), setup_context=_save_inputs)
+collision_reg.register_autograd(_collision_backward(_V.VS_COLLIDE_REG), setup_context=_save_inputs)
+
+
+def _forcing_edm_backward(ctx, go):
+    f, g, u = ctx.saved_tensors
+    go = _V.cont(go)
+    gg, gu = torch.empty_like(g), torch.empty_like(u)
+    _V.call("vs_forcing_vjp", go.shape[0], _V.dtype_code(go), _V.VS_FORCE_EDM, _V.ptr(_V.cont(g)), _V.ptr(_V.cont(u)),
+            0.0, _V.ptr(go), None, _V.ptr(gg), _V.ptr(gu), None, int(go[0].numel()), _V.stream())
+    return go, gg, gu
+
+
+forcing_edm.register_autograd(_forcing_edm_backward, setup_context=_save_inputs)
+
+
+def _interpolate_backward(ctx, gU):
+    grid, W, I = ctx.saved_tensors
+    gU = _V.cont(gU)
+    return _ad._spread0(gU, W, I, grid.shape), _ad._pair_dot(gU, grid, I, W.shape[1]), None
+
+
+interpolate.register_autograd(_interpolate_backward, setup_context=_save_inputs)
+
+
+def _spread_backward(ctx, go):
+    values, grid, W, I = ctx.saved_tensors
+    go = _V.cont(go)
+    return _ib.interpolate(go, W, I), go, _ad._pair_dot(values, go, I, W.shape[1]), None
+
+
+spread.register_autograd(_spread_backward, setup_context=_save_inputs)
+
+
+def _mdf_backward(ctx, gg, gh):
+    grid_u, W, I, ut = ctx.saved_tensors
+    ds, n_iter = ctx.scalars
+    ds_t = torch.tensor(float(ds), dtype=grid_u.dtype, device=grid_u.device)
+    g_grid, gW, gUt, _ = _ad.mdf_vjp(grid_u, W, I, ut, ds_t, int(n_iter), gg, gh)
+    return g_grid, gW, None, gUt, None, None
+
+
+multi_direct_forcing.register_autograd(_mdf_backward, setup_context=_save_inputs)
