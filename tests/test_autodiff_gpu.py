@@ -33,16 +33,16 @@ def rnd(*shape, seed=0, scale=1.0, shift=0.0):
     return (shift + scale * torch.rand(*shape, generator=g, dtype=DT)).cuda()
 
 
-def populations(q, shape, seed=0):
+def populations(q, shape, seed=0, spread=0.02):
     """Positive populations near an equilibrium with u ~ 0.05 (smooth inputs for the
-    collision models)."""
+    collision models); ``spread`` is the relative size of their non-equilibrium part."""
     from vivsim_gb300 import lbm, lbm3d
     L = lbm if q == 9 else lbm3d
     rho = rnd(*shape, seed=seed, scale=0.05, shift=0.98)
     u = rnd(len(shape), *shape, seed=seed + 1, scale=0.04, shift=-0.02)
     u[0] += 0.05
     f = L.get_equilibrium(rho, u)
-    return (f * rnd(q, *shape, seed=seed + 2, scale=0.02, shift=0.99)).contiguous()
+    return (f * rnd(q, *shape, seed=seed + 2, scale=spread, shift=1.0 - 0.5 * spread)).contiguous()
 
 
 def check(fn, *inputs, atol=1e-7, rtol=1e-5):
@@ -66,11 +66,16 @@ def test_lbm_basic_vjps(ad, q):
 @pytest.mark.parametrize("q", [9, 19])
 @pytest.mark.parametrize("name", ["collision_bgk", "collision_kbc", "collision_reg"])
 def test_collision_vjps(ad, q, name):
-    f = populations(q, SHAPES[q])
+    """KBC divides by <h, h>_feq, which is small where the higher-order non-equilibrium
+    part h is small: its inputs keep a 20 % non-equilibrium part so that the central
+    differences (step 1e-6) resolve the curvature, and its bar is 1e-4 relative."""
+    kbc = name == "collision_kbc"
+    f = populations(q, SHAPES[q], spread=0.2 if kbc else 0.02)
     rho, u = ad.get_macroscopic(f)
     feq = ad.get_equilibrium(rho, u).detach()
     omega = torch.tensor(1.7, dtype=DT, device="cuda")
-    check(lambda a, b, w: getattr(ad, name)(a, b, w), f, feq, omega)
+    tol = dict(atol=1e-6, rtol=1e-4) if kbc else {}
+    check(lambda a, b, w: getattr(ad, name)(a, b, w), f, feq, omega, **tol)
 
 
 def test_collision_mrt_vjp(ad):
@@ -165,10 +170,10 @@ def test_newmark_vjp(ad):
 def test_torch_ops_backward(ad):
     """torch.ops.vivsim.* carry the same backward rules (tensor arguments)."""
     import vivsim_gb300.torch_ops  # noqa: F401
-    f = populations(9, SHAPES[9])
+    f = populations(9, SHAPES[9], spread=0.2)
     feq = ad.get_equilibrium(*ad.get_macroscopic(f)).detach()
     check(lambda a: torch.ops.vivsim.streaming(a), f)
-    check(lambda a, b: torch.ops.vivsim.collision_kbc(a, b, 1.7), f, feq)
+    check(lambda a, b: torch.ops.vivsim.collision_kbc(a, b, 1.7), f, feq, atol=1e-6, rtol=1e-4)
     nx, ny = SHAPES[9]
     x, y = _markers(6, nx, ny, 2)
     W, I = ad.get_ib_stencil(x, y, ny)

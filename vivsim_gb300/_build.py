@@ -38,8 +38,11 @@ def nvcc():
     raise RuntimeError("nvcc not found: the CUDA toolkit is required to build vivsim_gb300")
 
 
-def lib_path():
-    return os.path.join(OUT, LIB_NAME)
+CHECKED_LIB_NAME = "libvivsim_gb300_checked.so"
+
+
+def lib_path(checked=False):
+    return os.path.join(OUT, CHECKED_LIB_NAME if checked else LIB_NAME)
 
 
 def _common_flags():
@@ -54,8 +57,12 @@ def _stale(target, deps):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build(verbose=False, force=False):
-    """Compile and link; returns the library path.  Rebuilds only what changed."""
+def build(verbose=False, force=False, checked=False):
+    """Compile and link; returns the library path.  Rebuilds only what changed.
+
+    checked=True builds libvivsim_gb300_checked.so with -DVIVSIM_BOUNDS_CHECK: the grid
+    kernels test every gather and scatter index and report VS_ERR_RANGE instead of
+    touching memory outside their arrays (a slower library for debugging and the tests)."""
     os.makedirs(OUT, exist_ok=True)
     headers = [os.path.join(SRC, f) for f in os.listdir(SRC) if f.endswith(".cuh")]
     headers.append(os.path.join(ROOT, "include", "vivsim_gb300.h"))
@@ -64,10 +71,11 @@ def build(verbose=False, force=False):
     objs = []
     for unit, extra in UNITS.items():
         src = os.path.join(SRC, unit)
-        obj = os.path.join(OUT, unit.replace(".cu", ".o"))
+        obj = os.path.join(OUT, unit.replace(".cu", "_chk.o" if checked else ".o"))
         objs.append(obj)
         if force or _stale(obj, [src] + headers + [__file__]):
-            jobs.append([cc, "-c", src, "-o", obj] + _common_flags() + extra)
+            jobs.append([cc, "-c", src, "-o", obj] + _common_flags() + extra +
+                        (["-DVIVSIM_BOUNDS_CHECK"] if checked else []))
 
     def run(cmd):
         if verbose:
@@ -81,7 +89,7 @@ def build(verbose=False, force=False):
         for msg in ex.map(run, jobs):
             if verbose and msg:
                 print(msg)
-    lib = lib_path()
+    lib = lib_path(checked)
     if force or jobs or _stale(lib, objs):
         tmp = lib + ".tmp"
         run([cc, "-shared", "-o", tmp] + objs + ARCH + ["-Xcompiler", "-fPIC"])

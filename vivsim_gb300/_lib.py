@@ -174,7 +174,8 @@ def load(path=None):
     global _LIB
     if _LIB is not None and path is None:
         return _LIB
-    path = path or _build.lib_path()
+    # VIVSIM_GB300_LIBRARY selects another build of the library, e.g. the bounds-checked one
+    path = path or os.environ.get("VIVSIM_GB300_LIBRARY") or _build.lib_path()
     if not os.path.exists(path):
         raise RuntimeError(f"vivsim_gb300 CUDA library not found at {path}; build it with "
                            f"`python -c 'import __graft_entry__ as g; g.build()'`")

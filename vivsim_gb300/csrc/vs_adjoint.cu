@@ -150,6 +150,7 @@ struct GridArgs {
   int nx, ny;
   T omega, U0, rho_out;
   double* acc;  // [0] d/dU0 (boundaries), [1] d/domega
+  double* acc_bc; // per-block partial sums of the inflow's d/dU0 (one slot per boundary block)
   double* acc_w;  // per-block partial sums of d/domega (one slot per grid-adjoint block)
   int slot0;      // first slot of this launch
   int mode;       // 0: every node; 1: outside the body's window; 2: the window only
@@ -163,10 +164,10 @@ struct GridArgs {
 
 __device__ __forceinline__ int wrap(int a, int n) { return a < 0 ? a + n : (a >= n ? a - n : a); }
 
-// block sum of v into *acc (one atomic per block; the order of the atomics varies, the
-// per-block partial sums do not)
+// block sum of v into part[blockIdx.x] (a fixed tree per block; the host sums the block
+// slots in order, so the result does not depend on scheduling)
 template <int NT>
-__device__ __forceinline__ void block_accumulate(double v, double* acc) {
+__device__ __forceinline__ void block_accumulate(double v, double* part) {
   __shared__ double red[NT / 32];
 #pragma unroll
   for (int o = 16; o >= 1; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -176,7 +177,7 @@ __device__ __forceinline__ void block_accumulate(double v, double* acc) {
   if (threadIdx.x == 0) {
     double s = 0;
     for (int k = 0; k < NT / 32; ++k) s += red[k];
-    if (s != 0.0) atomicAdd(acc, s);
+    part[blockIdx.x] = s;
   }
 }
 
@@ -238,7 +239,7 @@ __global__ void __launch_bounds__(kRows * 18) k_adj_bc(GridArgs<T> A) {
   if (threadIdx.x == 0) {
     double sum = 0.0;
     for (int i = 0; i < kRows * 18; ++i) sum += red[i];
-    if (sum != 0.0) atomicAdd(A.acc + 0, sum);
+    A.acc_bc[blockIdx.x] += sum;  // this block's slot; the steps run in order
   }
 }
 
@@ -746,6 +747,9 @@ struct vs_adjoint_plan {
   void* d_hist = nullptr;          // n_steps x 3
   double* d_acc = nullptr;         // [0] dU0 (boundary), [1] domega, [2] dK, [3] dU0 (initial state), [4..] dX0, dY0
   double* d_acc_w = nullptr;       // per-block partial sums of d/domega (grid adjoint)
+  double* d_acc_bc = nullptr;      // per-block partial sums of the inflow's d/dU0 (boundary adjoint)
+  double* d_acc_init = nullptr;    // per-block partial sums of d/dU0 through the initial state
+  int n_acc_bc = 0;
   int n_accw = 0, n_accw_grid = 0; // all slots; slots of the outside-window launch
   double lo[2] = {0, 0};           // smallest marker x, y (plan precision)
   void* d_op = nullptr;            // MRT operator and its omega derivative (9 x 9 each)
@@ -762,6 +766,8 @@ static void free_plan(vs_adjoint_plan* p) {
   if (p->body) vs_body_plan_destroy(p->body);
   if (p->lat) vs_lattice_plan_destroy(p->lat);
   if (p->d_acc_w) cudaFree(p->d_acc_w);
+  if (p->d_acc_bc) cudaFree(p->d_acc_bc);
+  if (p->d_acc_init) cudaFree(p->d_acc_init);
   if (p->d_op) cudaFree(p->d_op);
   void* bufs[] = {p->d_f0,  p->d_fa,       p->d_fb,     p->d_ck,        p->d_ck_state, p->d_seg[0],
                   p->d_seg[1], p->d_seg_state[0], p->d_seg_state[1], p->d_lam[0], p->d_lam[1], p->d_g,
@@ -839,6 +845,7 @@ static int reverse_steps(vs_adjoint_plan* P, int b, int len, int* cur, cudaStrea
     G.rho_out = (T)c.rho_out;
     G.acc = P->d_acc;
     G.acc_w = P->d_acc_w;
+    G.acc_bc = P->d_acc_bc;
     G.kind = c.collision;
     G.op = (const T*)P->d_op;
     G.dop = (const T*)P->d_op + 81;
@@ -939,6 +946,7 @@ static int backward_t(vs_adjoint_plan* P, cudaStream_t st) {
   }
   cudaError_t e = cudaMemsetAsync(P->d_acc, 0, sizeof(double) * (4 + 2 * P->M), st);
   if (e == cudaSuccess) e = cudaMemsetAsync(P->d_acc_w, 0, sizeof(double) * P->n_accw, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(P->d_acc_bc, 0, sizeof(double) * P->n_acc_bc, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(P->d_lam[0], 0, fb, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(P->d_lstate, 0, sizeof(T) * 12, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(P->d_g, 0, sizeof(T) * 2 * n, st);
@@ -998,7 +1006,7 @@ static int backward_t(vs_adjoint_plan* P, cudaStream_t st) {
     if (e != cudaSuccess) return cuda_status(e, "vs_adjoint_backward event");
     rev_pending[b] = true;
   }
-  k_adj_initial<T><<<256, 256, 0, st>>>((const T*)P->d_lam[cur], n, (T)c.U0, P->d_acc + 3);
+  k_adj_initial<T><<<256, 256, 0, st>>>((const T*)P->d_lam[cur], n, (T)c.U0, P->d_acc_init);
   VS_CHECK_LAUNCH("vs_adjoint_backward initial state");
   return VS_OK;
 }
@@ -1164,6 +1172,9 @@ int vs_adjoint_plan_create(const vs_adjoint_cfg* cfg, vs_adjoint_plan** out) {
   P->n_accw_grid = (int)grid_for(cfg->ny, 256) * cfg->nx;
   P->n_accw = P->n_accw_grid + (int)grid_for((int64_t)P->wcap[0] * P->wcap[1], 256);
   alloc((void**)&P->d_acc_w, sizeof(double) * P->n_accw);
+  P->n_acc_bc = (cfg->ny + kRows - 1) / kRows;
+  alloc((void**)&P->d_acc_bc, sizeof(double) * P->n_acc_bc);
+  alloc((void**)&P->d_acc_init, sizeof(double) * 256);
   if (e != cudaSuccess) return fail(cuda_status(e, "vs_adjoint_plan_create"));
   rc = dispatch_t(cfg->dtype, [&](auto t) -> int {
     using T = typename decltype(t)::type;
@@ -1263,13 +1274,20 @@ int vs_adjoint_backward(vs_adjoint_plan* P, double seed, double* grad_U0, double
   });
   if (rc) return rc;
   const int M = P->M;
-  std::vector<double> acc(4 + 2 * M), accw(P->n_accw);
+  std::vector<double> acc(4 + 2 * M), accw(P->n_accw), accbc(P->n_acc_bc), accinit(256);
   cudaError_t e = cudaMemcpyAsync(acc.data(), P->d_acc, sizeof(double) * acc.size(), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(accw.data(), P->d_acc_w, sizeof(double) * accw.size(), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(accbc.data(), P->d_acc_bc, sizeof(double) * accbc.size(), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(accinit.data(), P->d_acc_init, sizeof(double) * 256, cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return cuda_status(e, "vs_adjoint_backward result");
-  for (double v : accw) acc[1] += v;  // d/domega, block partials in a fixed order
+  // block partials summed in a fixed order: the gradients are the same bits run to run
+  for (double v : accw) acc[1] += v;      // d/domega
+  for (double v : accbc) acc[0] += v;     // d/dU0 through the inflow boundary
+  for (double v : accinit) acc[3] += v;   // d/dU0 through the initial state
   const vs_adjoint_cfg& c = P->cfg;
   const double domega = -3.0 * (c.D / c.Re) * P->omega * P->omega;
   if (grad_U0) *grad_U0 = seed * (acc[0] + acc[3] + acc[1] * domega);

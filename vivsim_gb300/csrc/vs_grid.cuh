@@ -8,6 +8,21 @@
 
 namespace vs {
 
+// Bounds-checked build (nvcc -DVIVSIM_BOUNDS_CHECK, vivsim_gb300._build.build(checked=True)):
+// every gather and scatter index of the grid kernels is tested against its array first; an
+// index outside it sets VS_ERR_RANGE in the plan's status word (vs_lattice_status) and the
+// access is skipped.  The default build compiles the tests out.
+#ifdef VIVSIM_BOUNDS_CHECK
+__device__ __forceinline__ bool in_range(int64_t i, int64_t lim, int* status) {
+  if (i >= 0 && i < lim) return true;
+  if (status) atomicMax(status, VS_ERR_RANGE);
+  return false;
+}
+#define VS_IN_RANGE(i, lim, st) ::vs::in_range((int64_t)(i), (int64_t)(lim), (st))
+#else
+#define VS_IN_RANGE(i, lim, st) true
+#endif
+
 // device window descriptor (int[8]): origin, extent, sticky status
 // META_PX/PY: lower corner of the body's last stencil bounding box (2-D moving bodies
 // predict their next window from it)
@@ -43,6 +58,7 @@ struct StepParams {
   T guo_scale;                   // 1 - omega / 2 (Guo-BGK)
   const T* gw;                   // IB force window (D, wx, wy, wz) or null
   const int* meta;               // window descriptor (device)
+  int* status;                   // the plan's status word (bounds-checked build)
   int box[6];
   int reg[3][6];                 // regions x0, x1, y0, y1, z0, z1 (half-open)
   int rowstart[4];               // first launch row (x plane) of each region
@@ -85,7 +101,7 @@ __device__ __forceinline__ void step_node(const StepParams<L, T>& P, int x, int 
       const int stride = a == 0 ? syz : (a == 1 ? P.nz : 1);
       const int pn = p + sg * stride;
 #pragma unroll
-      for (int i = 0; i < Q; ++i) nb[i] = __ldg(P.fin + (size_t)i * P.n + pn);
+      for (int i = 0; i < Q; ++i) nb[i] = VS_IN_RANGE(pn, P.n, P.status) ? __ldg(P.fin + (size_t)i * P.n + pn) : T(0);
     }
     bc_node<L, T>(A, 0, f, nb, nullptr, out);
 #pragma unroll
@@ -93,7 +109,7 @@ __device__ __forceinline__ void step_node(const StepParams<L, T>& P, int x, int 
   }
   // the previous step's obstacle bounce-back (lbm/boundary/bb.py:98-110), which follows its
   // face boundaries: an obstacle cell's populations swap with their opposites
-  if ((FEAT & kFeatMask) && P.mask_load && P.mask[p]) {
+  if ((FEAT & kFeatMask) && P.mask_load && VS_IN_RANGE(p, P.n, P.status) && P.mask[p]) {
 #pragma unroll
     for (int i = 0; i < Q; ++i) {
       const int o = L::opp(i);
@@ -121,7 +137,10 @@ __device__ __forceinline__ void step_node(const StepParams<L, T>& P, int x, int 
       const int cells = ex * ey * ez;
       const int c = (wx * ey + wy) * ez + wz;
 #pragma unroll
-      for (int d = 0; d < L::D; ++d) g[d] = has_g ? g[d] + P.gw[d * cells + c] : P.gw[d * cells + c];
+      for (int d = 0; d < L::D; ++d) {
+        const T gc = VS_IN_RANGE(c, cells, P.status) ? P.gw[d * cells + c] : T(0);
+        g[d] = has_g ? g[d] + gc : gc;
+      }
       has_g = true;
     }
   }
@@ -171,7 +190,8 @@ __device__ __forceinline__ void step_node(const StepParams<L, T>& P, int x, int 
     const int64_t nf = face_size(loc, nn);
     const int64_t j = (int64_t)cc[b0] * nn[b1] + cc[b1];
 #pragma unroll
-    for (int i = 0; i < Q; ++i) P.pre_buf[k][i * nf + j] = f[i];
+    for (int i = 0; i < Q; ++i)
+      if (VS_IN_RANGE(j, nf, P.status)) P.pre_buf[k][i * nf + j] = f[i];
   }
 
   // push streaming with periodic wrap on every axis (lbm/basic.py:60-85):
@@ -187,7 +207,7 @@ __device__ __forceinline__ void step_node(const StepParams<L, T>& P, int x, int 
     const int cx = L::c(i, 0), cy = L::c(i, 1), cz = L::c(i, 2);
     const int d = (cx > 0 ? dxp : (cx < 0 ? dxm : 0)) + (cy > 0 ? dyp : (cy < 0 ? dym : 0)) +
                   (cz > 0 ? dzp : (cz < 0 ? dzm : 0));
-    P.fout[(size_t)i * P.n + (p + d)] = f[i];
+    if (VS_IN_RANGE(p + d, P.n, P.status)) P.fout[(size_t)i * P.n + (p + d)] = f[i];
   }
 }
 
@@ -247,7 +267,7 @@ __device__ __forceinline__ void step_block(const StepParams<L, T>& P, int bx, in
   const int p = (x * P.ny + y) * P.nz + z;
   T f[Q];
 #pragma unroll
-  for (int i = 0; i < Q; ++i) f[i] = __ldg(P.fin + (size_t)i * P.n + p);
+  for (int i = 0; i < Q; ++i) f[i] = VS_IN_RANGE(p, P.n, P.status) ? __ldg(P.fin + (size_t)i * P.n + p) : T(0);
   step_node<L, T, COLL, FEAT>(P, x, y, z, p, f);
 }
 
@@ -264,8 +284,8 @@ __device__ __forceinline__ void step_block2(const StepParams<L9, T>& P, int bx, 
   T f0[9], f1[9];
 #pragma unroll
   for (int i = 0; i < 9; ++i) {
-    if (a) f0[i] = __ldg(P.fin + (size_t)i * P.n + p0);
-    if (b) f1[i] = __ldg(P.fin + (size_t)i * P.n + p1);
+    if (a) f0[i] = VS_IN_RANGE(p0, P.n, P.status) ? __ldg(P.fin + (size_t)i * P.n + p0) : T(0);
+    if (b) f1[i] = VS_IN_RANGE(p1, P.n, P.status) ? __ldg(P.fin + (size_t)i * P.n + p1) : T(0);
   }
   if (a) step_node<L9, T, COLL, FEAT>(P, x, y0, 0, p0, f0);
   if (b) step_node<L9, T, COLL, FEAT>(P, x, y1, 0, p1, f1);
@@ -294,7 +314,7 @@ __device__ __forceinline__ void step_flat(const StepParams<L, T>& P, int chunk) 
   if ((FEAT & kFeatSkip) && skipped(P, x, y, z)) return;
   T f[L::Q];
 #pragma unroll
-  for (int i = 0; i < L::Q; ++i) f[i] = __ldg(P.fin + (size_t)i * P.n + p);
+  for (int i = 0; i < L::Q; ++i) f[i] = VS_IN_RANGE(p, P.n, P.status) ? __ldg(P.fin + (size_t)i * P.n + p) : T(0);
   step_node<L, T, COLL, FEAT>(P, x, y, z, p, f);
 }
 

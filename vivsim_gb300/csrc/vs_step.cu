@@ -63,11 +63,13 @@ __global__ void __launch_bounds__(FastShape<L, COLL>::TB, FastShape<L, COLL>::MI
 
 // (6 blocks of 256 threads per SM by registers: at the default 48 registers the loads in
 // flight were too few, 5 % slower on the 64-case sweep; 8 blocks spill)
-template <class L, typename T, int COLL>
+// FEAT: kFeatGeneral, or kFeatSkip when no case of the batch has a uniform body force,
+// pre-stream copies or an obstacle mask (the usual sweep).
+template <class L, typename T, int COLL, int FEAT>
 __global__ void __launch_bounds__(256, 6) k_step_batch_flat(const StepParams<L, T>* __restrict__ Ps,
                                                          const int2* __restrict__ blk) {
   const int2 cb = blk[blockIdx.x];
-  step_flat<L, T, COLL, kFeatGeneral>(Ps[cb.x], cb.y);
+  step_flat<L, T, COLL, FEAT>(Ps[cb.x], cb.y);
 }
 
 // Grid kernel over many independent lattices in one launch: block b works on lattice
@@ -1921,6 +1923,7 @@ static StepParams<L, T> make_step_params(const vs_lattice_plan* LP, const vs_bod
   P.guo_scale = (T)(1.0 - 0.5 * c.omega);
   P.gw = B ? (const T*)B->d_gw : nullptr;
   P.meta = B ? B->d_meta : nullptr;
+  P.status = LP->d_status;
   P.mask = c.obstacle_mask;
   P.mask_load = c.obstacle_mask && LP->bb_load ? 1 : 0;
   P.n_pre = 0;
@@ -2543,6 +2546,7 @@ int vs_lattice_status(const vs_lattice_plan* plan, int reset, void* stream) {
   if (e == cudaSuccess && reset && v) e = cudaMemset(plan->d_status, 0, sizeof(int));
   if (e != cudaSuccess) return cuda_status(e, "vs_lattice_status");
   if (v == VS_ERR_NONFINITE) set_error("the watchdog found a NaN or Inf population");
+  else if (v == VS_ERR_RANGE) set_error("a grid kernel met an index outside its array (bounds-checked build)");
   else if (v == VS_ERR_TIMEOUT_INFLIGHT)
     set_error("a grid kernel gave up waiting for its bulk copies and one had still not landed when it left");
   else if (v) set_error("a grid kernel gave up waiting for its bulk copies (device status %d)", v);
@@ -3116,6 +3120,7 @@ struct vs_batch_plan {
   int2* d_blk_main = nullptr;
   int2* d_blk_reg[2] = {};
   int n_blk_main = 0, n_blk_reg[2] = {0, 0};
+  int main_skip_only = 0;       // the main launch needs no per-node feature but the skip tests
   void* d_body[2] = {};         // [parity] BodyParams per chain body
   cudaStream_t side = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
@@ -3160,6 +3165,7 @@ static int batch_build(vs_batch_plan* bp, void* const* fa, void* const* fb) {
   std::vector<StepParams<L, T>> main[2][2], reg[2][2];
   std::vector<int2> bm, br[2];
   std::vector<BodyParams<T>> body[2];
+  bool skip_only = true;
   for (int p = 0; p < 2; ++p)
     for (int first = 0; first < 2; ++first) {
       for (int k = 0; k < bp->n; ++k) {
@@ -3185,6 +3191,7 @@ static int batch_build(vs_batch_plan* bp, void* const* fa, void* const* fb) {
         if (grid_setup<L, T>(bp->L[k], Bk, fin, fout, Bk ? 1 : 0, lazy_in, bp->tb, P, g, tb)) {
           const int idx = (int)main[p][first].size();
           main[p][first].push_back(P);
+          skip_only = skip_only && !P.gw && !P.has_g0 && !P.mask_load && P.n_pre == 0 && P.n_lazy == 0;
           if (p == 0 && first == 1) {  // flat chunks of the case's nodes (k_step_batch_flat)
             const int nch = (int)((bp->L[k]->n + bp->tb - 1) / bp->tb);
             for (int j = 0; j < nch; ++j) bm.push_back(make_int2(idx, j));
@@ -3212,6 +3219,7 @@ static int batch_build(vs_batch_plan* bp, void* const* fa, void* const* fb) {
   }
   if (e == cudaSuccess) e = upload((void**)&bp->d_blk_main, bm);
   bp->n_blk_main = (int)bm.size();
+  bp->main_skip_only = skip_only ? 1 : 0;
   if (e != cudaSuccess) {
     batch_free_params(bp);
     return cuda_status(e, "vs_batch_run parameters");
@@ -3246,9 +3254,14 @@ static int batch_step_t(vs_batch_plan* bp, int s, int n_steps, void* const* fa, 
       if (rc) return rc;
     }
   }
-  if (bp->n_blk_main > 0)
-    k_step_batch_flat<L, T, COLL><<<bp->n_blk_main, bp->tb, 0, st>>>(
-        (const StepParams<L, T>*)bp->d_main[p][first], bp->d_blk_main);
+  if (bp->n_blk_main > 0) {
+    if (bp->main_skip_only)
+      k_step_batch_flat<L, T, COLL, kFeatSkip><<<bp->n_blk_main, bp->tb, 0, st>>>(
+          (const StepParams<L, T>*)bp->d_main[p][first], bp->d_blk_main);
+    else
+      k_step_batch_flat<L, T, COLL, kFeatGeneral><<<bp->n_blk_main, bp->tb, 0, st>>>(
+          (const StepParams<L, T>*)bp->d_main[p][first], bp->d_blk_main);
+  }
   if (fork) {
     e = cudaEventRecord(bp->ev_join, bp->side);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(st, bp->ev_join, 0);
