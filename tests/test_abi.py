@@ -94,7 +94,28 @@ def test_jax_adapter_needs_jax():
     except ImportError:
         pass
     with pytest.raises(ImportError):
-        jax_ffi.collision_kbc(None, None, 1.7)
+        jax_ffi.lbm.collision_kbc(None, None, 1.7)
+    with pytest.raises(ImportError):
+        jax_ffi.ib.interpolate(None, None, None)
+
+
+def test_xla_ffi_handlers_match_their_bindings():
+    """Every custom-call target of jax_ffi has a handler symbol in xla/vs_xla_ffi.cc, every
+    handler is registered, and the handlers compile (g++ -fsyntax-only) against a
+    stand-in FFI header that checks each handler's parameters against its binding."""
+    import shutil
+    import subprocess
+    from vivsim_gb300 import jax_ffi
+    src = os.path.join(ROOT, "vivsim_gb300", "xla", "vs_xla_ffi.cc")
+    symbols = set(re.findall(r"XLA_FFI_DEFINE_HANDLER_SYMBOL\((\w+),", open(src).read()))
+    assert symbols == set(jax_ffi.TARGETS.values())
+    if shutil.which("g++") is None:
+        pytest.skip("no g++")
+    cuda_inc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include")
+    cmd = ["g++", "-std=c++17", "-fsyntax-only", "-I", os.path.join(ROOT, "tests", "c_host", "xla_ffi_standin"),
+           "-I", os.path.join(ROOT, "include"), "-I", cuda_inc, src]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-4000:]
 
 
 def test_plain_c_host(tmp_path):
