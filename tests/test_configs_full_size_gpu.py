@@ -161,3 +161,31 @@ def test_sphere_256x128x128_per_step(cfg, collision):
     assert worst[0] <= PER_STEP and worst[1] <= PER_STEP and worst[2] <= U_PER_STEP_OUTFLOW, worst
     assert worst[3] <= BODY_FORCE, worst
     assert ef <= 1e-5 and er <= 1e-5 and eu <= 1e-5, (ef, er, eu)
+
+
+def drift(cfg, case, n_steps):
+    """The fused float32 run, the float32 oracle and the float64 oracle over n_steps: errors
+    (rho, u) of the kernel and of the float32 oracle against the float64 oracle, and of the
+    kernel against the float32 oracle."""
+    fk, _ = free_run(cfg, case, n_steps)
+    t32 = ThreadedStep(case)
+    t64 = ThreadedStep(case, dtype=np.float64)
+    for _ in range(n_steps):
+        t32()
+        t64()
+    _, kr, ku = field_errors(fk, t64.f)
+    _, orr, ou = field_errors(t32.f, t64.f)
+    _, er, eu = field_errors(fk, t32.f)
+    return dict(kernel64=(kr, ku), oracle64=(orr, ou), kernel32=(er, eu))
+
+
+@pytest.mark.parametrize("name,n_steps", [("viv2d", 2000), ("sphere3d", 20)])
+def test_float32_drift_matches_the_oracles(cfg, name, n_steps):
+    """Over a longer run the float32 kernel drifts from the float64 oracle no more than the
+    float32 oracle does (both carry float32 rounding; the flow amplifies it alike)."""
+    d = drift(cfg, cfg.CASES[name](), n_steps)
+    print(f"\n{name} {n_steps} steps vs oracle64: kernel rho {d['kernel64'][0]:.2e} u {d['kernel64'][1]:.2e}, "
+          f"oracle32 rho {d['oracle64'][0]:.2e} u {d['oracle64'][1]:.2e}; kernel vs oracle32 rho "
+          f"{d['kernel32'][0]:.2e} u {d['kernel32'][1]:.2e}")
+    for i in (0, 1):
+        assert d["kernel64"][i] <= 2.0 * d["oracle64"][i] + 1e-7, d

@@ -435,6 +435,59 @@ def test_obstacle_mask_matches_oracle(S, dt):
         assert rel_err(N(sim.f), f) <= tol, how
 
 
+def _sphere_run(S, moving, graph, steps=6):
+    nx, ny, nz, D, U0 = 40, 32, 32, 10.0, 0.05
+    M = 301
+    X = recipes.fibonacci_sphere(M, D / 2, (14.3, 15.8, 16.1)).astype(np.float32).astype(np.float64)
+    om = L3.get_omega(U0 * D / 50.0)
+    rng = np.random.default_rng(7)
+    u = (1e-4 * rng.standard_normal((3, nx, ny, nz))).astype(np.float32)
+    u[0] += U0
+    f0 = L3.get_equilibrium(np.ones((nx, ny, nz), np.float32), u)
+    ds = 4 * math.pi * (D / 2) ** 2 / M
+    step = S.LatticeStep(19, (nx, ny, nz), "reg", om, forcing="edm",
+                         boundaries=[S.boundary("equilibrium", "left", ux_wall=U0),
+                                     S.boundary("nee", "right", mode="pressure", rho_wall=1.0)])
+    if moving:
+        vol = 4 / 3 * math.pi * (D / 2) ** 3
+        body = S.RigidBody(step, X, ds, moving=True, free_dof=(True, True, False), mass=2 * vol, stiffness=0.05,
+                           added_mass_area=vol, v0=(0, 2e-3, 0))
+    else:
+        body = S.RigidBody(step, X, ds, moving=False)
+    with torch.cuda.stream(torch.cuda.Stream()):
+        sim = S.Simulation(step, T(f0), body)
+        hist = sim.run(steps, force_history=True, graph=graph)
+        torch.cuda.synchronize()
+    step.check()
+    return N(sim.f), N(hist), body.state()
+
+
+@pytest.mark.parametrize("moving", [False, True])
+def test_sphere_fused_body_kernel_equals_phase_kernels(S, moving, monkeypatch):
+    """The 3-D body step as one thread-block cluster (fixed bodies; 2 to 16 CTAs), as one
+    cooperative launch (any number of CTAs) and as seven per-phase launches sums every
+    marker and node in the same order: identical bits, eager and in graph replay, for a
+    fixed and a moving sphere."""
+    monkeypatch.setenv("VIVSIM_GB300_BODY3D_CLUSTER", "0")
+    monkeypatch.setenv("VIVSIM_GB300_BODY3D_CTAS", "0")
+    fa, ha, sa = _sphere_run(S, moving, False)
+    variants = [("0", "7"), ("0", "64"), ("0", None)]
+    if not moving:
+        variants += [("2", None), ("8", None), (None, None)]
+    for cluster, ctas in variants:
+        for name, val in (("VIVSIM_GB300_BODY3D_CLUSTER", cluster), ("VIVSIM_GB300_BODY3D_CTAS", ctas)):
+            if val is None:
+                monkeypatch.delenv(name, raising=False)
+            else:
+                monkeypatch.setenv(name, val)
+        for graph in (False, True):
+            fb, hb, sb = _sphere_run(S, moving, graph)
+            assert np.array_equal(fa, fb), (cluster, ctas, graph)
+            assert np.array_equal(ha, hb), (cluster, ctas, graph)
+            for k in ("a", "v", "d", "h"):
+                assert np.array_equal(sa[k], sb[k]), (cluster, ctas, graph, k)
+
+
 @pytest.mark.parametrize("dt", ["f32", "f64"])
 def test_moving_sphere_3d_matches_oracle(S, dt):
     """A spring-mounted sphere moving through a D3Q19 channel (the 3-D moving-body step of

@@ -1,11 +1,14 @@
 """Error of the float32 fused step against float64 over whole runs of the benchmark cases.
 
-    python -m vivsim_gb300.accuracy [--cases cavity viv2d sphere3d] [--out FILE]
+    python -m vivsim_gb300.accuracy [--cases cavity viv2d sphere3d adjoint sweep] [--out FILE]
 
 Each case runs its full step count in float32 and in float64 (the float64 fused step
 matches the float64 oracle to ~1e-12 per step) from the same float32 initial state, and
 the norm-relative differences max|a - b| / max|b| of rho and u (and of the body
-displacement) are printed as one JSON line per case.
+displacement) are printed as one JSON line per case.  ``adjoint`` is the differentiable
+cylinder (512 x 256, 4000 steps): the objective and its gradients in float32 against
+float64.  ``sweep`` is the 64-case VIV sweep advanced as one batch: the largest rho and u
+error over the cases.
 """
 
 import argparse
@@ -15,7 +18,7 @@ import torch
 
 from . import configs
 
-FULL_STEPS = {"cavity": 1000, "viv2d": 20000, "sphere3d": 5000}
+FULL_STEPS = {"cavity": 1000, "viv2d": 20000, "sphere3d": 5000, "adjoint": 4000, "sweep": 2000}
 
 
 def _velocities(q, dtype, device):
@@ -68,6 +71,42 @@ def compare(name, steps):
     return out
 
 
+def compare_adjoint(steps):
+    from .adjoint import CylinderDrag
+    res = {}
+    for dt in (torch.float32, torch.float64):
+        plan = CylinderDrag(n_steps=steps, dtype=dt)
+        J = plan.forward(keep_checkpoints=True)
+        gU0, gK, goff = plan.backward()
+        plan.close()
+        res[dt] = (J, gU0, gK, goff)
+    (J32, u32, k32, o32), (J64, u64, k64, o64) = res[torch.float32], res[torch.float64]
+    return {"case": "adjoint cylinder D2Q9 BGK 512 x 256, 64 markers", "steps": steps,
+            "J_rel_err": abs(J32 - J64) / abs(J64), "dU0_rel_err": abs(u32 - u64) / abs(u64),
+            "dK_rel_err": abs(k32 - k64) / abs(k64),
+            "doffsets_rel_err": float(abs(o32 - o64).max() / abs(o64).max())}
+
+
+def compare_sweep(steps, n_cases=64):
+    from . import solver
+    out = {}
+    for dt in (torch.float32, torch.float64):
+        stream = torch.cuda.Stream()
+        with torch.cuda.stream(stream):
+            sims = [configs.build_solver(c, dtype=dt)[2] for c in configs.viv_sweep(n_cases)]
+            batch = solver.Batch(sims)
+            batch.run(steps)
+            torch.cuda.synchronize()
+        out[dt] = [s.f.clone() for s in sims]
+        batch.close()
+    er = eu = 0.0
+    for a, b in zip(out[torch.float32], out[torch.float64]):
+        ra, ua = rho_u(a)
+        rb, ub = rho_u(b)
+        er, eu = max(er, rel(ra, rb)), max(eu, rel(ua, ub))
+    return {"case": f"VIV sweep, {n_cases} cases batched", "steps": steps, "rho_rel_err": er, "u_rel_err": eu}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--cases", nargs="*", default=list(FULL_STEPS))
@@ -76,7 +115,13 @@ def main():
     a = ap.parse_args()
     lines = []
     for name in a.cases:
-        res = compare(name, a.steps or FULL_STEPS[name])
+        steps = a.steps or FULL_STEPS[name]
+        if name == "adjoint":
+            res = compare_adjoint(steps)
+        elif name == "sweep":
+            res = compare_sweep(steps)
+        else:
+            res = compare(name, steps)
         print(json.dumps(res), flush=True)
         lines.append(res)
     if a.out:

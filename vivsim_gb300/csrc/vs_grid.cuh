@@ -78,11 +78,25 @@ enum {
   kFeatForce = 4,  // body force: uniform g and the IB force window
   kFeatMask = 8,   // the previous step's obstacle bounce-back applied on load
   kFeatPre = 16,   // pre-stream populations kept for bounce-back faces
+  kFeatStream = 32,  // streaming loads and stores (evict-first in L2), so that a grid larger
+                     // than L2 does not evict the body kernels' small working set
   kFeatGeneral = kFeatSkip | kFeatForce | kFeatMask | kFeatPre
 };
 
 // Per-node work of the grid kernels: (lazy face boundaries,) moments, equilibrium,
 // collision, forcing, push streaming.  f holds the node's loaded populations.
+// population load and store of the grid kernels: plain, or cache-streaming (kFeatStream)
+template <int FEAT, typename T>
+__device__ __forceinline__ T pop_load(const T* p) {
+  if constexpr ((FEAT & kFeatStream) != 0) return __ldcs(p);
+  else return __ldg(p);
+}
+template <int FEAT, typename T>
+__device__ __forceinline__ void pop_store(T* p, T v) {
+  if constexpr ((FEAT & kFeatStream) != 0) __stcs(p, v);
+  else *p = v;
+}
+
 template <class L, typename T, int COLL, int FEAT>
 __device__ __forceinline__ void step_node(const StepParams<L, T>& P, int x, int y, int z, int p, T* f) {
   constexpr int Q = L::Q;
@@ -101,7 +115,7 @@ __device__ __forceinline__ void step_node(const StepParams<L, T>& P, int x, int 
       const int stride = a == 0 ? syz : (a == 1 ? P.nz : 1);
       const int pn = p + sg * stride;
 #pragma unroll
-      for (int i = 0; i < Q; ++i) nb[i] = VS_IN_RANGE(pn, P.n, P.status) ? __ldg(P.fin + (size_t)i * P.n + pn) : T(0);
+      for (int i = 0; i < Q; ++i) nb[i] = VS_IN_RANGE(pn, P.n, P.status) ? pop_load<FEAT>(P.fin + (size_t)i * P.n + pn) : T(0);
     }
     bc_node<L, T>(A, 0, f, nb, nullptr, out);
 #pragma unroll
@@ -207,7 +221,7 @@ __device__ __forceinline__ void step_node(const StepParams<L, T>& P, int x, int 
     const int cx = L::c(i, 0), cy = L::c(i, 1), cz = L::c(i, 2);
     const int d = (cx > 0 ? dxp : (cx < 0 ? dxm : 0)) + (cy > 0 ? dyp : (cy < 0 ? dym : 0)) +
                   (cz > 0 ? dzp : (cz < 0 ? dzm : 0));
-    if (VS_IN_RANGE(p + d, P.n, P.status)) P.fout[(size_t)i * P.n + (p + d)] = f[i];
+    if (VS_IN_RANGE(p + d, P.n, P.status)) pop_store<FEAT>(P.fout + (size_t)i * P.n + (p + d), f[i]);
   }
 }
 
@@ -267,7 +281,7 @@ __device__ __forceinline__ void step_block(const StepParams<L, T>& P, int bx, in
   const int p = (x * P.ny + y) * P.nz + z;
   T f[Q];
 #pragma unroll
-  for (int i = 0; i < Q; ++i) f[i] = VS_IN_RANGE(p, P.n, P.status) ? __ldg(P.fin + (size_t)i * P.n + p) : T(0);
+  for (int i = 0; i < Q; ++i) f[i] = VS_IN_RANGE(p, P.n, P.status) ? pop_load<FEAT>(P.fin + (size_t)i * P.n + p) : T(0);
   step_node<L, T, COLL, FEAT>(P, x, y, z, p, f);
 }
 
@@ -284,8 +298,8 @@ __device__ __forceinline__ void step_block2(const StepParams<L9, T>& P, int bx, 
   T f0[9], f1[9];
 #pragma unroll
   for (int i = 0; i < 9; ++i) {
-    if (a) f0[i] = VS_IN_RANGE(p0, P.n, P.status) ? __ldg(P.fin + (size_t)i * P.n + p0) : T(0);
-    if (b) f1[i] = VS_IN_RANGE(p1, P.n, P.status) ? __ldg(P.fin + (size_t)i * P.n + p1) : T(0);
+    if (a) f0[i] = VS_IN_RANGE(p0, P.n, P.status) ? pop_load<FEAT>(P.fin + (size_t)i * P.n + p0) : T(0);
+    if (b) f1[i] = VS_IN_RANGE(p1, P.n, P.status) ? pop_load<FEAT>(P.fin + (size_t)i * P.n + p1) : T(0);
   }
   if (a) step_node<L9, T, COLL, FEAT>(P, x, y0, 0, p0, f0);
   if (b) step_node<L9, T, COLL, FEAT>(P, x, y1, 0, p1, f1);

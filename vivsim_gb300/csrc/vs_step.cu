@@ -20,6 +20,7 @@
 #include <cstdlib>
 #include <new>
 #include <type_traits>
+#include <algorithm>
 #include <vector>
 
 #include "vs_boundary.cuh"
@@ -1422,40 +1423,54 @@ static int chain_width(const double* x, const double* y, int M, int R, int rot) 
 // The stencil of a fixed body never moves, so its (node, pair) CSR is built once; each
 // step then runs node-parallel and marker-parallel kernels over the compacted node list.
 
-// u at the touched nodes (vivsim/lbm3d/basic.py:90-106)
-template <class L, typename T>
-__global__ void k_static_node_u(const T* __restrict__ fin, int nx, int ny, int nz, const int* __restrict__ meta,
-                                const int32_t* __restrict__ node_cell, int U, T* __restrict__ nu,
-                                const int* __restrict__ Ud) {
-  // U: the node-array stride; Ud (moving bodies): the number of touched nodes this step
-  const int ey = meta[META_WY], ez = meta[META_WZ];
-  const int ox = meta[META_OX], oy = meta[META_OY], oz = meta[META_OZ];
-  const int64_t n = (int64_t)nx * ny * nz;
-  const int nU = Ud ? *Ud : U;
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nU; k += gridDim.x * blockDim.x) {
-    const int cell = node_cell[k];
-    const int wx = cell / (ey * ez), wy = (cell / ez) % ey, wz = cell % ez;
-    const int64_t pn = ((int64_t)(ox + wx) * ny + (oy + wy)) * nz + (oz + wz);
-    T fl[L::Q];
-#pragma unroll
-    for (int i = 0; i < L::Q; ++i) fl[i] = __ldg(fin + i * n + pn);
-    T r, uu[3] = {T(0), T(0), T(0)};
-    macro(L{}, fl, r, uu);
-#pragma unroll
-    for (int d = 0; d < 3; ++d) nu[d * U + k] = uu[d];
+// The stencil weights and marker ids of the pairs in CSR (node) order: wsort[i] = W[sids[i]],
+// msort[i] = sids[i] / S.
+template <typename T>
+__global__ void k_csr_gather(const int32_t* __restrict__ sids, const T* __restrict__ W, int S, int64_t P,
+                             T* __restrict__ wsort, int32_t* __restrict__ msort) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P; i += (int64_t)gridDim.x * blockDim.x) {
+    const int p = sids[i];
+    wsort[i] = W[p];
+    msort[i] = p / S;
   }
 }
 
-// One warp per marker: U (+)= sum_s W nodes[uid] per component, lanes over the stencil,
+// How the body phases load node and marker values: kLoadRO through the read-only path (the
+// per-phase kernels), kLoadL2 bypassing L1 (values written earlier in the same launch by
+// other CTAs: the cooperative kernel), kLoadPlain with a generic load (shared memory:
+// the cluster kernel).
+enum { kLoadRO = 0, kLoadL2 = 1, kLoadPlain = 2 };
+template <int MODE, typename T>
+__device__ __forceinline__ T body_load(const T* p) {
+  if constexpr (MODE == kLoadL2) return __ldcg(p);
+  else if constexpr (MODE == kLoadPlain) return *p;
+  else return __ldg(p);
+}
+
+// u at touched node k (vivsim/lbm3d/basic.py:90-106)
+template <class L, typename T>
+__device__ __forceinline__ void static_node_u(int k, const T* __restrict__ fin, int ny, int nz, int64_t n, int ox,
+                                              int oy, int oz, int ey, int ez, const int32_t* __restrict__ node_cell,
+                                              int U, T* __restrict__ nu) {
+  const int cell = node_cell[k];
+  const int wx = cell / (ey * ez), wy = (cell / ez) % ey, wz = cell % ez;
+  const int64_t pn = ((int64_t)(ox + wx) * ny + (oy + wy)) * nz + (oz + wz);
+  T fl[L::Q];
+#pragma unroll
+  for (int i = 0; i < L::Q; ++i) fl[i] = __ldg(fin + i * n + pn);
+  T r, uu[3] = {T(0), T(0), T(0)};
+  macro(L{}, fl, r, uu);
+#pragma unroll
+  for (int d = 0; d < 3; ++d) nu[d * U + k] = uu[d];
+}
+
+// Marker m, one warp: U (+)= sum_s W nodes[uid] per component, lanes over the stencil,
 // shuffle-reduced in a fixed tree; then F_step = (v_body - U) 2 ds, F_total (ib/mdf.py:38-52).
-template <typename T>
-__global__ void k_static_marker(int first, int use_step, const T* __restrict__ W, const int32_t* __restrict__ pair_uid,
-                                int M, int S, const T* __restrict__ nodes, int U, const T* __restrict__ state,
-                                const T* __restrict__ ds, T ds_scalar, T* __restrict__ Ua, T* __restrict__ Fs,
-                                T* __restrict__ Ft) {
-  const int lane = threadIdx.x & 31;
-  const int m = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (m >= M) return;
+template <int MODE, typename T>
+__device__ __forceinline__ void static_marker(int m, int lane, int first, int use_step, const T* __restrict__ W,
+                                              const int32_t* __restrict__ pair_uid, int S, const T* nodes, int U,
+                                              const T* state, const T* __restrict__ ds, T ds_scalar, T* Ua, T* Fs,
+                                              T* Ft) {
   T acc[3] = {T(0), T(0), T(0)};
   bool firstterm = true;
   for (int s = lane; s < S; s += 32) {
@@ -1464,7 +1479,7 @@ __global__ void k_static_marker(int first, int use_step, const T* __restrict__ W
     const int id = pair_uid[q];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      const T t = mul_rn(w, nodes[c * U + id]);
+      const T t = mul_rn(w, body_load<MODE>(nodes + c * U + id));
       acc[c] = firstterm ? t : add_rn(acc[c], t);
     }
     firstterm = false;
@@ -1487,43 +1502,38 @@ __global__ void k_static_marker(int first, int use_step, const T* __restrict__ W
   }
 }
 
-// Node-parallel spread in pair order: out[c][k] = scale * sum F[m(p)][c] W[p].  With
-// gw != null the sums land in the force window at node_cell[k] instead (scale 1), and
-// block 0 then also forms the total force h = sum_m(-F_total) (dyn.py:126-136).
-template <typename T>
-__global__ void k_static_spread(const int32_t* __restrict__ seg, const int32_t* __restrict__ sids,
-                                const int32_t* __restrict__ node_cell, const T* __restrict__ W,
-                                const T* __restrict__ F, int U, int S, T scale, T* __restrict__ out, T* gw, int cells,
-                                int M, T* state, T* force_hist, const int* __restrict__ Ud) {
-  const int nU = Ud ? *Ud : U;
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nU; k += gridDim.x * blockDim.x) {
-    const int lo = seg[k], hi = seg[k + 1];
-    T a[3] = {T(0), T(0), T(0)};
-    for (int i = lo; i < hi; ++i) {
-      const int p = sids[i];
-      const int m = p / S;
-      const T w = W[p];
+// Node k of the spread in pair order: sum_p F[m(p)][c] W[p] over the pairs of node k,
+// wsort/msort[seg[k] .. seg[k+1]) (weights and marker ids in CSR order, so the loop's loads
+// are independent of one another).
+template <int MODE, typename T>
+__device__ __forceinline__ void static_spread_node(int k, const int32_t* __restrict__ seg,
+                                                   const int32_t* __restrict__ msort, const T* __restrict__ wsort,
+                                                   const T* F, T a[3]) {
+  const int lo = seg[k], hi = seg[k + 1];
+  a[0] = a[1] = a[2] = T(0);
+#pragma unroll 4
+  for (int i = lo; i < hi; ++i) {
+    const int m = msort[i];
+    const T w = wsort[i];
 #pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        const T t = mul_rn(F[m * 3 + c], w);
-        a[c] = i == lo ? t : add_rn(a[c], t);
-      }
-    }
-    if (gw) {
-      const int cell = node_cell[k];
-#pragma unroll
-      for (int c = 0; c < 3; ++c) gw[c * cells + cell] = a[c];
-    } else {
-#pragma unroll
-      for (int c = 0; c < 3; ++c) out[c * U + k] = a[c] * scale;
+    for (int c = 0; c < 3; ++c) {
+      const T t = mul_rn(body_load<MODE>(F + m * 3 + c), w);
+      a[c] = i == lo ? t : add_rn(a[c], t);
     }
   }
-  if (!gw || blockIdx.x != 0) return;
+}
+
+// h = sum_m(-F_total) by one block (256 threads) in a fixed tree (dyn.py:126-136)
+template <int MODE, typename T>
+__device__ __forceinline__ void static_total_force(const T* F, int M, T* state, T* force_hist) {
   __shared__ T red[3][256];
   const int tid = threadIdx.x;
   for (int c = 0; c < 3; ++c) {
     T acc = T(0);
-    for (int m = tid; m < M; m += blockDim.x) acc = m == tid ? -F[m * 3 + c] : acc + (-F[m * 3 + c]);
+    for (int m = tid; m < M; m += blockDim.x) {
+      const T v = -body_load<MODE>(F + m * 3 + c);
+      acc = m == tid ? v : acc + v;
+    }
     red[c][tid] = acc;
   }
   __syncthreads();
@@ -1535,6 +1545,401 @@ __global__ void k_static_spread(const int32_t* __restrict__ seg, const int32_t* 
   if (tid < 3) {
     state[9 + tid] = red[tid][0];
     if (force_hist) force_hist[tid] = red[tid][0];
+  }
+}
+
+// u at the touched nodes
+template <class L, typename T>
+__global__ void k_static_node_u(const T* __restrict__ fin, int nx, int ny, int nz, const int* __restrict__ meta,
+                                const int32_t* __restrict__ node_cell, int U, T* __restrict__ nu,
+                                const int* __restrict__ Ud) {
+  // U: the node-array stride; Ud (moving bodies): the number of touched nodes this step
+  const int ey = meta[META_WY], ez = meta[META_WZ];
+  const int ox = meta[META_OX], oy = meta[META_OY], oz = meta[META_OZ];
+  const int64_t n = (int64_t)nx * ny * nz;
+  const int nU = Ud ? *Ud : U;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nU; k += gridDim.x * blockDim.x)
+    static_node_u<L, T>(k, fin, ny, nz, n, ox, oy, oz, ey, ez, node_cell, U, nu);
+}
+
+// One warp per marker
+template <typename T>
+__global__ void k_static_marker(int first, int use_step, const T* __restrict__ W, const int32_t* __restrict__ pair_uid,
+                                int M, int S, const T* __restrict__ nodes, int U, const T* __restrict__ state,
+                                const T* __restrict__ ds, T ds_scalar, T* __restrict__ Ua, T* __restrict__ Fs,
+                                T* __restrict__ Ft) {
+  const int m = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (m >= M) return;
+  static_marker<kLoadRO, T>(m, threadIdx.x & 31, first, use_step, W, pair_uid, S, nodes, U, state, ds, ds_scalar, Ua,
+                          Fs, Ft);
+}
+
+// Node-parallel spread: out[c][k] = scale * sum F[m(p)][c] W[p].  With gw != null the sums
+// land in the force window at node_cell[k] instead (scale 1), and block 0 then also forms
+// the total force h = sum_m(-F_total).
+template <typename T>
+__global__ void k_static_spread(const int32_t* __restrict__ seg, const int32_t* __restrict__ msort,
+                                const int32_t* __restrict__ node_cell, const T* __restrict__ wsort,
+                                const T* __restrict__ F, int U, T scale, T* __restrict__ out, T* gw, int cells,
+                                int M, T* state, T* force_hist, const int* __restrict__ Ud) {
+  const int nU = Ud ? *Ud : U;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nU; k += gridDim.x * blockDim.x) {
+    T a[3];
+    static_spread_node<kLoadRO, T>(k, seg, msort, wsort, F, a);
+    if (gw) {
+      const int cell = node_cell[k];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) gw[c * cells + cell] = a[c];
+    } else {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) out[c * U + k] = a[c] * scale;
+    }
+  }
+  if (!gw || blockIdx.x != 0) return;
+  static_total_force<kLoadRO, T>(F, M, state, force_hist);
+}
+
+// ---- the whole 3-D body step in one launch
+// The phases of the per-phase kernels above (node u, then per MDF iteration markers and a
+// spread, then the force window and h) in one cooperative launch of G CTAs: CTA b owns the
+// nodes [U b / G, U (b + 1) / G) and the markers [M b / G, M (b + 1) / G), and a grid
+// barrier separates the phases.  The arithmetic and its order are the per-phase kernels',
+// so the results are equal.  On a grid larger than L2 the launch runs beside the grid
+// kernel with the HBM saturated; one launch replaces seven dependent ones, each of which
+// would wait for SM slots and for its first loads behind the grid kernel's traffic.
+constexpr int kBody3Threads = 256;
+constexpr int kGridBarrierLimit = 1 << 22;  // polls of a grid barrier (about 0.3 s) before it gives up
+
+template <typename T>
+struct Body3Params {
+  const T* fin;
+  int nx, ny, nz;
+  const int* meta;
+  const int32_t* node_cell;
+  int U;
+  const int* Ud;
+  const T* W;
+  const int32_t* pair_uid;
+  int M, S;
+  const int32_t* seg;
+  const int32_t* msort;
+  const T* wsort;
+  T* state;
+  const T* ds;
+  T ds_scalar;
+  T* nu;
+  T* nv;
+  T* Ua;
+  T* Fs;
+  T* Ft;
+  T* gw;
+  int cells;
+  T* force_hist;
+  int n_iter;
+  unsigned* bar;  // [0] arrivals, [1] generation, [2] abort flag, [3] CTAs done
+  int* status;
+};
+
+// Grid barrier over the launch's CTAs (a cooperative launch: all of them are resident).
+// Thread 0 arrives with a device-scope release and waits (bounded) for the generation to
+// move on; the last CTA to arrive resets the count and publishes the next generation.
+// After kGridBarrierLimit polls, or when another CTA gave up, the CTA records
+// VS_ERR_TIMEOUT, sets the abort flag and the launch skips its remaining phases.
+__device__ __forceinline__ bool grid_barrier(unsigned* bar, int* status) {
+  __shared__ int ok_s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    unsigned gen;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(gen) : "l"(bar + 1) : "memory");
+    unsigned abort_flag;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(abort_flag) : "l"(bar + 2) : "memory");
+    if (abort_flag) {
+      ok = 0;
+    } else {
+      __threadfence();
+      const unsigned arrived = atomicAdd(bar, 1u);
+      if (arrived == gridDim.x - 1) {
+        atomicExch(bar, 0u);
+        __threadfence();
+        asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(bar + 1), "r"(gen + 1) : "memory");
+      } else {
+        int it = 0;
+        for (;;) {
+          unsigned g, ab;
+          asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(g) : "l"(bar + 1) : "memory");
+          if (g != gen) break;
+          asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(ab) : "l"(bar + 2) : "memory");
+          if (ab || ++it > kGridBarrierLimit) {
+            atomicExch(bar + 2, 1u);
+            atomicMax(status, VS_ERR_TIMEOUT);
+            ok = 0;
+            break;
+          }
+          __nanosleep(64);
+        }
+      }
+    }
+    ok_s = ok;
+  }
+  __syncthreads();
+  return ok_s != 0;
+}
+
+template <class L, typename T>
+__global__ void __launch_bounds__(kBody3Threads) k_body3d_fused(const __grid_constant__ Body3Params<T> B) {
+  const int G = (int)gridDim.x, b = (int)blockIdx.x, tid = (int)threadIdx.x;
+  const int nU = B.Ud ? *B.Ud : B.U;
+  const int k0 = (int)((int64_t)nU * b / G), k1 = (int)((int64_t)nU * (b + 1) / G);
+  const int m0 = (int)((int64_t)B.M * b / G), m1 = (int)((int64_t)B.M * (b + 1) / G);
+  const int lane = tid & 31, warp = tid >> 5, nwarps = kBody3Threads / 32;
+  // the static data of this CTA's markers and nodes into L2 while the node phase runs
+  {
+    const char* wb = (const char*)(B.W + (int64_t)m0 * B.S);
+    const char* ub = (const char*)(B.pair_uid + (int64_t)m0 * B.S);
+    const int64_t mbytes = (int64_t)(m1 - m0) * B.S * (int64_t)sizeof(T);
+    const int64_t ubytes = (int64_t)(m1 - m0) * B.S * 4;
+    for (int64_t o = (int64_t)tid * 128; o < mbytes; o += kBody3Threads * 128)
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(wb + o));
+    for (int64_t o = (int64_t)tid * 128; o < ubytes; o += kBody3Threads * 128)
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(ub + o));
+  }
+  bool ok = true;
+  {
+    const int ey = B.meta[META_WY], ez = B.meta[META_WZ];
+    const int ox = B.meta[META_OX], oy = B.meta[META_OY], oz = B.meta[META_OZ];
+    const int64_t n = (int64_t)B.nx * B.ny * B.nz;
+    for (int k = k0 + tid; k < k1; k += kBody3Threads)
+      static_node_u<L, T>(k, B.fin, B.ny, B.nz, n, ox, oy, oz, ey, ez, B.node_cell, B.U, B.nu);
+  }
+  ok = grid_barrier(B.bar, B.status);
+  for (int m = m0 + warp; ok && m < m1; m += nwarps)
+    static_marker<kLoadL2, T>(m, lane, 1, B.n_iter > 0, B.W, B.pair_uid, B.S, B.nu, B.U, B.state, B.ds, B.ds_scalar, B.Ua,
+                           B.Fs, B.Ft);
+  for (int it = 0; ok && it + 1 < B.n_iter; ++it) {
+    ok = grid_barrier(B.bar, B.status);
+    if (!ok) break;
+    for (int k = k0 + tid; k < k1; k += kBody3Threads) {
+      T a[3];
+      static_spread_node<kLoadL2, T>(k, B.seg, B.msort, B.wsort, B.Fs, a);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) B.nv[c * B.U + k] = a[c] * T(0.5);
+    }
+    ok = grid_barrier(B.bar, B.status);
+    if (!ok) break;
+    for (int m = m0 + warp; m < m1; m += nwarps)
+      static_marker<kLoadL2, T>(m, lane, 0, 1, B.W, B.pair_uid, B.S, B.nv, B.U, B.state, B.ds, B.ds_scalar, B.Ua, B.Fs,
+                             B.Ft);
+  }
+  if (ok) ok = grid_barrier(B.bar, B.status);
+  if (ok) {
+    for (int k = k0 + tid; k < k1; k += kBody3Threads) {
+      T a[3];
+      static_spread_node<kLoadL2, T>(k, B.seg, B.msort, B.wsort, B.Ft, a);
+      const int cell = B.node_cell[k];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) B.gw[c * B.cells + cell] = a[c];
+    }
+    if (b == 0) static_total_force<kLoadL2, T>(B.Ft, B.M, B.state, B.force_hist);
+  }
+  // the last CTA out clears the arrival count and the abort flag for the next launch (the
+  // generation only ever moves on, so it needs no reset)
+  __syncthreads();
+  if (tid == 0) {
+    __threadfence();
+    if (atomicAdd(B.bar + 3, 1u) == gridDim.x - 1) {
+      atomicExch(B.bar, 0u);
+      atomicExch(B.bar + 2, 0u);
+      atomicExch(B.bar + 3, 0u);
+    }
+  }
+}
+
+// ---- the fixed 3-D body step in one thread-block cluster
+// The phases of the per-phase kernels over a cluster of CL CTAs whose exchanges stay in
+// distributed shared memory: CTA r holds the stencil weights and pair node keys of its
+// markers [part[CL+1+r], part[CL+2+r]), and the CSR slice, weights, marker ids and node
+// values of its nodes [part[r], part[r+1]) (split so that every CTA spreads about the same
+// number of pairs).  A marker reads the nodes of its stencil from the CTAs that own them
+// (key = owner << 16 | local index), and writes the force it spreads into every CTA's
+// replica of the marker forces, so a spread reads only its own shared memory.  Hardware
+// cluster barriers separate the phases.  Global memory is read once at the start (the
+// populations at the touched nodes, the plan's static arrays) and written once at the end
+// (the force window and h), so the phases do not queue behind the grid launch's traffic.
+// The arithmetic and its order are the per-phase kernels': the results are equal.
+constexpr int kBody3ClusterThreads = 1024;
+
+template <typename T>
+struct Body3ClusterParams {
+  const T* fin;
+  int nx, ny, nz;
+  const int* meta;
+  const int32_t* node_cell;
+  const T* W;          // (M, S) stencil weights
+  const int32_t* pkey; // (M, S) owner << 16 | index in the owner's node slice
+  int M, S;
+  const int32_t* seg;
+  const int32_t* msort;
+  const T* wsort;
+  T* state;
+  const T* ds;
+  T ds_scalar;
+  T* gw;
+  int cells;
+  T* force_hist;
+  int n_iter;
+  const int* part;     // node bounds [CL + 1], then marker bounds [CL + 1]
+  int MK, NK, PK;      // per-CTA capacities: markers, nodes, node-side pairs
+};
+
+template <typename T>
+__host__ __device__ inline size_t body3_cluster_smem(int M, int S, int MK, int NK, int PK) {
+  const size_t nT = (size_t)MK * S + PK + 3 * (size_t)NK + 3 * (size_t)M + 6 * (size_t)MK + 3 * 256;
+  const size_t nI = (size_t)MK * S + (NK + 1) + PK;
+  return nT * sizeof(T) + nI * sizeof(int32_t);
+}
+
+template <class L, typename T>
+__global__ void __launch_bounds__(kBody3ClusterThreads) k_body3d_cluster(const __grid_constant__ Body3ClusterParams<T> B) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int CL = (int)cluster.num_blocks(), r = (int)cluster.block_rank();
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarps = nt >> 5;
+  const int M = B.M, S = B.S, MK = B.MK, NK = B.NK, PK = B.PK;
+  T* Wm = (T*)smem;           // [MK S]
+  T* wsl = Wm + MK * S;       // [PK]
+  T* nodes = wsl + PK;        // [3 NK] u, then the spread force step, of this CTA's nodes
+  T* Frep = nodes + 3 * NK;   // [3 M] the forces being spread, every marker
+  T* Ua = Frep + 3 * M;       // [3 MK] this CTA's markers
+  T* Ftl = Ua + 3 * MK;       // [3 MK]
+  T* red = Ftl + 3 * MK;      // [3 256]
+  int32_t* keym = (int32_t*)(red + 3 * 256);  // [MK S]
+  int32_t* segl = keym + MK * S;              // [NK + 1]
+  int32_t* msl = segl + NK + 1;               // [PK]
+  const int n0 = B.part[r], n1 = B.part[r + 1];
+  const int m0 = B.part[CL + 1 + r], m1 = B.part[CL + 2 + r];
+  const int nn = n1 - n0, nm = m1 - m0;
+  const int q0 = B.seg[n0], nq = B.seg[n1] - q0;
+  // static slices
+  for (int i = tid; i < nm * S; i += nt) {
+    Wm[i] = B.W[(int64_t)m0 * S + i];
+    keym[i] = B.pkey[(int64_t)m0 * S + i];
+  }
+  for (int i = tid; i <= nn; i += nt) segl[i] = B.seg[n0 + i] - q0;
+  for (int i = tid; i < nq; i += nt) {
+    msl[i] = B.msort[q0 + i];
+    wsl[i] = B.wsort[q0 + i];
+  }
+  // u at this CTA's nodes (vivsim/lbm3d/basic.py:90-106)
+  {
+    const int ey = B.meta[META_WY], ez = B.meta[META_WZ];
+    const int ox = B.meta[META_OX], oy = B.meta[META_OY], oz = B.meta[META_OZ];
+    const int64_t n = (int64_t)B.nx * B.ny * B.nz;
+    for (int k = tid; k < nn; k += nt) {
+      const int cell = B.node_cell[n0 + k];
+      const int wx = cell / (ey * ez), wy = (cell / ez) % ey, wz = cell % ez;
+      const int64_t pn = ((int64_t)(ox + wx) * B.ny + (oy + wy)) * B.nz + (oz + wz);
+      T fl[L::Q];
+#pragma unroll
+      for (int i = 0; i < L::Q; ++i) fl[i] = __ldg(B.fin + i * n + pn);
+      T rr, uu[3] = {T(0), T(0), T(0)};
+      macro(L{}, fl, rr, uu);
+#pragma unroll
+      for (int d = 0; d < 3; ++d) nodes[d * NK + k] = uu[d];
+    }
+  }
+  cluster.sync();
+  T v_body[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) v_body[c] = B.state[3 + c];
+  const int n_marker_phases = B.n_iter > 1 ? B.n_iter : 1;
+  for (int ph = 0; ph < n_marker_phases; ++ph) {
+    const bool first = ph == 0, last = ph + 1 == n_marker_phases;
+    const int use_step = first ? (B.n_iter > 0) : 1;
+    // markers: interpolate the node values (ib/stencil.py:54-78), force step and total
+    // (ib/mdf.py:38-52), in k_static_marker's order
+    for (int ml = warp; ml < nm; ml += nwarps) {
+      const int m = m0 + ml;
+      T acc[3] = {T(0), T(0), T(0)};
+      bool firstterm = true;
+      for (int s = lane; s < S; s += 32) {
+        const T w = Wm[ml * S + s];
+        const int key = keym[ml * S + s];
+        const T* rn = cluster.map_shared_rank(nodes, key >> 16);
+        const int li = key & 0xffff;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const T t = mul_rn(w, rn[c * NK + li]);
+          acc[c] = firstterm ? t : add_rn(acc[c], t);
+        }
+        firstterm = false;
+      }
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int o = 16; o >= 1; o >>= 1) acc[c] = acc[c] + __shfl_down_sync(0xffffffffu, acc[c], o);
+      T out[3];
+      if (lane == 0) {
+        const T d2 = (B.ds ? B.ds[m] : B.ds_scalar) * T(2);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const T u = first ? acc[c] : Ua[ml * 3 + c] + acc[c];
+          Ua[ml * 3 + c] = u;
+          const T fs = mul_rn(v_body[c] - u, d2);
+          const T ft = first ? (use_step ? fs : T(0)) : Ftl[ml * 3 + c] + fs;
+          Ftl[ml * 3 + c] = ft;
+          out[c] = last ? ft : fs;  // the spread that follows: a force step, or the totals
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < 3; ++c) out[c] = __shfl_sync(0xffffffffu, out[c], 0);
+      // into every CTA's replica: lane j writes component j % 3 to CTA j / 3
+      for (int j = lane; j < 3 * CL; j += 32) {
+        T* dst = cluster.map_shared_rank(Frep, j / 3);
+        const int c = j % 3;
+        dst[m * 3 + c] = c == 0 ? out[0] : (c == 1 ? out[1] : out[2]);
+      }
+    }
+    cluster.sync();
+    if (last) break;
+    // spread of the force step to this CTA's nodes (k_static_spread's order), times 0.5
+    for (int k = tid; k < nn; k += nt) {
+      T a[3];
+      static_spread_node<kLoadPlain, T>(k, segl, msl, wsl, Frep, a);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) nodes[c * NK + k] = a[c] * T(0.5);
+    }
+    cluster.sync();
+  }
+  // the totals into the force window, and h = sum_m(-F_total) (dyn.py:126-136)
+  for (int k = tid; k < nn; k += nt) {
+    T a[3];
+    static_spread_node<kLoadPlain, T>(k, segl, msl, wsl, Frep, a);
+    const int cell = B.node_cell[n0 + k];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) B.gw[c * B.cells + cell] = a[c];
+  }
+  if (r == 0) {
+    // static_total_force's order over 256 threads
+    for (int c = 0; c < 3 && tid < 256; ++c) {
+      T acc = T(0);
+      for (int m = tid; m < M; m += 256) {
+        const T v = -Frep[m * 3 + c];
+        acc = m == tid ? v : acc + v;
+      }
+      red[c * 256 + tid] = acc;
+    }
+    __syncthreads();
+    for (int o = 128; o >= 1; o >>= 1) {
+      if (tid < o)
+        for (int c = 0; c < 3; ++c) red[c * 256 + tid] = red[c * 256 + tid] + red[c * 256 + tid + o];
+      __syncthreads();
+    }
+    if (tid < 3) {
+      B.state[9 + tid] = red[tid * 256];
+      if (B.force_hist) B.force_hist[tid] = red[tid * 256];
+    }
   }
 }
 
@@ -1690,6 +2095,8 @@ struct vs_lattice_plan {
   int tma_tb;                // tile width of the TMA grid kernel, 0 when it does not apply
   int bb_load;               // set per step: the input still lacks the obstacle bounce-back
   int tma_grid;              // persistent CTAs of the TMA grid kernel
+  int stream_pop;            // one population buffer is larger than L2: a grid launch beside
+                             // body kernels streams it (evict-first) past their working set
   // graph cache
   cudaGraphExec_t graph;
   const void* g_fa;
@@ -1720,6 +2127,16 @@ struct vs_body_plan {
   int32_t* pair_uid;
   int32_t* d_node_cell;
   int32_t* d_seg;
+  int prio;         // priority of the side-stream launches (the device's highest)
+  unsigned* d_bar;  // grid barrier words of the fused 3-D body kernel
+  int c3;           // CTAs of the 3-D body cluster kernel (0: not used)
+  size_t c3_smem;
+  int c3_cap[3];    // per-CTA markers, nodes, node-side pairs
+  int* d_c3part;    // node bounds [c3 + 1], marker bounds [c3 + 1]
+  int32_t* d_pkey;  // (M, S): owner CTA << 16 | index in its node slice
+  int fused3;       // CTAs of the fused 3-D body kernel (0: the per-phase kernels)
+  void* d_wsort;    // stencil weights of the pairs in CSR order
+  int32_t* d_msort; // marker ids of the pairs in CSR order
   int U;            // touched nodes
   void* d_nu;       // 3 x U node velocity
   void* d_nv;       // 3 x U node force step
@@ -1775,7 +2192,7 @@ static void free_lattice(vs_lattice_plan* p) {
 static void free_body(vs_body_plan* b) {
   if (!b) return;
   void* ptrs[] = {b->d_X0, b->d_ds, b->d_state, b->d_base, b->d_gw, b->d_meta, b->d_W, b->d_I, b->d_ws,
-                  b->d_node_cell, b->d_seg, b->d_nu, b->d_nv, b->d_mk, b->d_U};
+                  b->d_node_cell, b->d_seg, b->d_nu, b->d_nv, b->d_mk, b->d_U, b->d_wsort, b->d_msort, b->d_bar, b->d_c3part, b->d_pkey};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   if (b->ev_fork) cudaEventDestroy(b->ev_fork);
@@ -2063,11 +2480,99 @@ static int enqueue_body(vs_body_plan* B, const vs_lattice_plan* LP, const void* 
       if (rc) return rc;
       k_csr_count<<<1, 1, 0, st>>>(v.uid, P, B->d_U, B->d_seg);
       k_compact_csr<<<grid_for(P, 256), 256, 0, st>>>(v.skeys, v.head, v.uid, P, B->d_node_cell, B->d_seg);
+      k_csr_gather<T><<<grid_for(P, 256), 256, 0, st>>>(v.sids, (const T*)B->d_W, S, P, (T*)B->d_wsort, B->d_msort);
     }
     T* Ua = (T*)B->d_mk;
     T* Fs = Ua + 3 * M;
     T* Ft = Fs + 3 * M;
     const T ds2 = (T)B->cfg.ds_scalar;
+    if (B->c3 > 0 && !B->cfg.moving) {  // one cluster launch for the whole body step
+      Body3ClusterParams<T> cp{};
+      cp.fin = (const T*)fin;
+      cp.nx = LP->cfg.nx;
+      cp.ny = LP->cfg.ny;
+      cp.nz = LP->cfg.nz;
+      cp.meta = B->d_meta;
+      cp.node_cell = B->d_node_cell;
+      cp.W = (const T*)B->d_W;
+      cp.pkey = B->d_pkey;
+      cp.M = M;
+      cp.S = S;
+      cp.seg = B->d_seg;
+      cp.msort = B->d_msort;
+      cp.wsort = (const T*)B->d_wsort;
+      cp.state = (T*)B->d_state;
+      cp.ds = (const T*)B->d_ds;
+      cp.ds_scalar = ds2;
+      cp.gw = (T*)B->d_gw;
+      cp.cells = cells;
+      cp.force_hist = (T*)force_hist;
+      cp.n_iter = B->cfg.n_iter;
+      cp.part = B->d_c3part;
+      cp.MK = B->c3_cap[0];
+      cp.NK = B->c3_cap[1];
+      cp.PK = B->c3_cap[2];
+      cudaLaunchConfig_t lc = {};
+      lc.gridDim = dim3((unsigned)B->c3);
+      lc.blockDim = dim3(kBody3ClusterThreads);
+      lc.dynamicSmemBytes = B->c3_smem;
+      lc.stream = st;
+      cudaLaunchAttribute at[2];
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = (unsigned)B->c3;
+      at[0].val.clusterDim.y = 1;
+      at[0].val.clusterDim.z = 1;
+      at[1].id = cudaLaunchAttributePriority;
+      at[1].val.priority = B->prio;
+      lc.attrs = at;
+      lc.numAttrs = 2;
+      cudaError_t e = cudaLaunchKernelEx(&lc, k_body3d_cluster<L19, T>, cp);
+      if (e != cudaSuccess) return cuda_status(e, "vs_step 3-D body cluster kernel");
+    } else if (B->fused3 > 0) {  // one cooperative launch for the whole body step
+      Body3Params<T> bp{};
+      bp.fin = (const T*)fin;
+      bp.nx = LP->cfg.nx;
+      bp.ny = LP->cfg.ny;
+      bp.nz = LP->cfg.nz;
+      bp.meta = B->d_meta;
+      bp.node_cell = B->d_node_cell;
+      bp.U = U;
+      bp.Ud = B->d_U;
+      bp.W = (const T*)B->d_W;
+      bp.pair_uid = B->pair_uid;
+      bp.M = M;
+      bp.S = S;
+      bp.seg = B->d_seg;
+      bp.msort = B->d_msort;
+      bp.wsort = (const T*)B->d_wsort;
+      bp.state = (T*)B->d_state;
+      bp.ds = (const T*)B->d_ds;
+      bp.ds_scalar = ds2;
+      bp.nu = (T*)B->d_nu;
+      bp.nv = (T*)B->d_nv;
+      bp.Ua = Ua;
+      bp.Fs = Fs;
+      bp.Ft = Ft;
+      bp.gw = (T*)B->d_gw;
+      bp.cells = cells;
+      bp.force_hist = B->cfg.moving ? nullptr : (T*)force_hist;
+      bp.n_iter = B->cfg.n_iter;
+      bp.bar = B->d_bar;
+      bp.status = LP->d_status;
+      cudaLaunchConfig_t lc = {};
+      lc.gridDim = dim3((unsigned)B->fused3);
+      lc.blockDim = dim3(kBody3Threads);
+      lc.stream = st;
+      cudaLaunchAttribute at[2];
+      at[0].id = cudaLaunchAttributeCooperative;
+      at[0].val.cooperative = 1;
+      at[1].id = cudaLaunchAttributePriority;
+      at[1].val.priority = B->prio;
+      lc.attrs = at;
+      lc.numAttrs = 2;
+      cudaError_t e = cudaLaunchKernelEx(&lc, k_body3d_fused<L19, T>, bp);  // 3-D bodies live on D3Q19 lattices
+      if (e != cudaSuccess) return cuda_status(e, "vs_step 3-D body kernel");
+    } else {
     const unsigned gn = grid_for(B->cfg.moving ? (int64_t)M * S : U, 128), gm = grid_for((int64_t)M * 32, 128);
     k_static_node_u<L, T><<<gn, 128, 0, st>>>((const T*)fin, LP->cfg.nx, LP->cfg.ny, LP->cfg.nz, B->d_meta,
                                                B->d_node_cell, U, (T*)B->d_nu, B->d_U);
@@ -2075,14 +2580,15 @@ static int enqueue_body(vs_body_plan* B, const vs_lattice_plan* LP, const void* 
                                            (const T*)B->d_nu, U, (const T*)B->d_state, (const T*)B->d_ds, ds2, Ua, Fs,
                                            Ft);
     for (int it = 0; it + 1 < B->cfg.n_iter; ++it) {
-      k_static_spread<T><<<gn, 128, 0, st>>>(B->d_seg, B->sids, B->d_node_cell, (const T*)B->d_W, Fs, U, S, T(0.5),
-                                             (T*)B->d_nv, nullptr, cells, M, nullptr, nullptr, B->d_U);
+      k_static_spread<T><<<gn, 128, 0, st>>>(B->d_seg, B->d_msort, B->d_node_cell, (const T*)B->d_wsort, Fs, U,
+                                             T(0.5), (T*)B->d_nv, nullptr, cells, M, nullptr, nullptr, B->d_U);
       k_static_marker<T><<<gm, 128, 0, st>>>(0, 1, (const T*)B->d_W, B->pair_uid, M, S, (const T*)B->d_nv, U,
                                              (const T*)B->d_state, (const T*)B->d_ds, ds2, Ua, Fs, Ft);
     }
-    k_static_spread<T><<<gn, 256, 0, st>>>(B->d_seg, B->sids, B->d_node_cell, (const T*)B->d_W, Ft, U, S, T(1),
+    k_static_spread<T><<<gn, 256, 0, st>>>(B->d_seg, B->d_msort, B->d_node_cell, (const T*)B->d_wsort, Ft, U, T(1),
                                            nullptr, (T*)B->d_gw, cells, M, (T*)B->d_state,
                                            B->cfg.moving ? nullptr : (T*)force_hist, B->d_U);
+    }
     if (B->cfg.moving) {  // added mass and Newmark on the free DOFs
       k_body_newmark<T><<<1, 32, 0, st>>>((T*)B->d_state, B->cfg.free_dof[0], B->cfg.free_dof[1], B->cfg.free_dof[2],
                                           (T)B->nm[0], (T)B->nm[1], (T)B->nm[2], (T)B->nm[3], (T)B->nm[4],
@@ -2203,17 +2709,39 @@ static bool grid_setup(const vs_lattice_plan* LP, const vs_body_plan* B, const v
   return true;
 }
 
+// A launch with a priority attribute (kept by graph capture as the node's priority); prio 0
+// launches plainly, with the stream's priority.
+template <typename... KArgs, typename... Args>
+static void launch_prio(void (*k)(KArgs...), dim3 grid, dim3 block, cudaStream_t st, int prio, Args... args) {
+  if (prio == 0) {
+    k<<<grid, block, 0, st>>>(args...);
+    return;
+  }
+  cudaLaunchConfig_t lc = {};
+  lc.gridDim = grid;
+  lc.blockDim = block;
+  lc.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributePriority;
+  at[0].val.priority = prio;
+  lc.attrs = at;
+  lc.numAttrs = 1;
+  cudaLaunchKernelEx(&lc, k, args...);
+}
+
 // Launch geometry of k_step_fast: NPT nodes per thread along the contiguous axis, whole grid.
 // (false: the contiguous extent is shorter than one block's nodes; the general kernel runs)
+// stream: the launch runs beside body kernels on a grid larger than L2 (kFeatStream).
 template <class L, int COLL>
-static bool launch_fast(StepParams<L, float> P, bool skip, cudaStream_t st) {
+static bool launch_fast(StepParams<L, float> P, bool skip, bool stream, cudaStream_t st) {
   using S = FastShape<L, COLL>;
   const int ext = L::D == 2 ? P.ny : P.nz;
   if (ext < S::TB * S::NPT) return false;
   P.chunks = (ext + S::TB * S::NPT - 1) / (S::TB * S::NPT);
   const dim3 grid(L::D == 2 ? P.chunks : P.chunks * P.ny, P.nx);
   P.gx = (int)grid.x;
-  if (skip) k_step_fast<L, float, COLL, kFeatSkip><<<grid, S::TB, 0, st>>>(P);
+  if (skip && stream) k_step_fast<L, float, COLL, kFeatSkip | kFeatStream><<<grid, S::TB, 0, st>>>(P);
+  else if (skip) k_step_fast<L, float, COLL, kFeatSkip><<<grid, S::TB, 0, st>>>(P);
   else k_step_fast<L, float, COLL, 0><<<grid, S::TB, 0, st>>>(P);
   return true;
 }
@@ -2249,12 +2777,13 @@ static int enqueue_grid(const vs_lattice_plan* LP, const vs_body_plan* B, const 
                         !P.mask_load && P.n_pre == 0;
       if (bulk) {
         const bool skip = P.skip_box || P.dyn_meta || P.skip_walls;
+        const bool stream = B && LP->stream_pop && !getenv_flag("VIVSIM_GB300_NO_STREAM");
         bool done;
         switch (c.collision) {
-          case VS_COLLIDE_BGK: done = launch_fast<L, VS_COLLIDE_BGK>(P, skip, st); break;
-          case VS_COLLIDE_KBC: done = launch_fast<L, VS_COLLIDE_KBC>(P, skip, st); break;
-          case VS_COLLIDE_REG: done = launch_fast<L, VS_COLLIDE_REG>(P, skip, st); break;
-          default: done = launch_fast<L, VS_COLLIDE_MRT>(P, skip, st); break;
+          case VS_COLLIDE_BGK: done = launch_fast<L, VS_COLLIDE_BGK>(P, skip, stream, st); break;
+          case VS_COLLIDE_KBC: done = launch_fast<L, VS_COLLIDE_KBC>(P, skip, stream, st); break;
+          case VS_COLLIDE_REG: done = launch_fast<L, VS_COLLIDE_REG>(P, skip, stream, st); break;
+          default: done = launch_fast<L, VS_COLLIDE_MRT>(P, skip, stream, st); break;
         }
         if (done) {
           VS_CHECK_LAUNCH("vs_step grid kernel");
@@ -2262,8 +2791,10 @@ static int enqueue_grid(const vs_lattice_plan* LP, const vs_body_plan* B, const 
         }
       }
     }
+    // the box and face-plane launches beside the grid launch carry the side streams' priority
+    const int prio = B && (mode == 2 || mode == 3) ? B->prio : 0;
 #define VS_LAUNCH_STEP(K)                                                              \
-  (walls ? k_step<L, T, K, true><<<grid, tb, 0, st>>>(P) : k_step<L, T, K, false><<<grid, tb, 0, st>>>(P))
+  (walls ? launch_prio(k_step<L, T, K, true>, grid, tb, st, prio, P) : launch_prio(k_step<L, T, K, false>, grid, tb, st, prio, P))
     switch (c.collision) {
       case VS_COLLIDE_BGK: VS_LAUNCH_STEP(VS_COLLIDE_BGK); break;
       case VS_COLLIDE_KBC: VS_LAUNCH_STEP(VS_COLLIDE_KBC); break;
@@ -2293,13 +2824,15 @@ static cudaError_t launch_cluster_t(vs_body_plan* B, const BodyParams<T>& P, con
   cfg.blockDim = dim3((unsigned)B->cl_threads);
   cfg.dynamicSmemBytes = B->cl_smem;
   cfg.stream = st;
-  cudaLaunchAttribute attr[1];
+  cudaLaunchAttribute attr[2];
   attr[0].id = cudaLaunchAttributeClusterDimension;
   attr[0].val.clusterDim.x = (unsigned)B->cl_size;
   attr[0].val.clusterDim.y = 1;
   attr[0].val.clusterDim.z = 1;
+  attr[1].id = cudaLaunchAttributePriority;
+  attr[1].val.priority = B->prio;
   cfg.attrs = attr;
-  cfg.numAttrs = 1;
+  cfg.numAttrs = 2;
   return cudaLaunchKernelEx(&cfg, k_body2d_cluster<T, R, COLL>, P, SP);
 }
 
@@ -2444,6 +2977,88 @@ static bool lazy_boundaries(const vs_lattice_plan* LP, const vs_body_plan* B) {
   return true;
 }
 
+// The cluster form of a fixed 3-D body step: the largest cluster of up to 16 CTAs (8
+// where the device allows no larger one) whose per-CTA shared memory fits, with the nodes
+// split by pair count.  VIVSIM_GB300_BODY3D_CLUSTER: another largest size, 0 for none.
+template <typename T>
+static int body3_cluster_setup(vs_body_plan* b) {
+  b->c3 = 0;
+  int maxcl = 16;
+  if (const char* v = getenv("VIVSIM_GB300_BODY3D_CLUSTER")) maxcl = atoi(v);
+  int dev = 0, cl_ok = 0, optin = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&cl_ok, cudaDevAttrClusterLaunch, dev);
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (!cl_ok || maxcl < 1) return VS_OK;
+  const int M = b->M, S = b->S, U = b->U;
+  const int64_t P = (int64_t)M * S;
+  std::vector<int32_t> seg(U + 1), uid(P);
+  cudaError_t e = cudaMemcpy(seg.data(), b->d_seg, sizeof(int32_t) * (U + 1), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(uid.data(), b->pair_uid, sizeof(int32_t) * P, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_status(e, "vs_body_plan_create cluster layout");
+  auto kern = k_body3d_cluster<L19, T>;
+  e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  if (e != cudaSuccess) return cuda_status(e, "vs_body_plan_create cluster attributes");
+  for (int CL = 16; CL >= 1; CL /= 2) {
+    if (CL > maxcl || CL > M || CL > U) continue;
+    std::vector<int> part(2 * (CL + 1));
+    part[0] = 0;
+    for (int r = 1; r < CL; ++r) {
+      const int64_t target = P * r / CL;
+      int k = (int)(std::lower_bound(seg.begin(), seg.end(), (int32_t)target) - seg.begin());
+      k = k < part[r - 1] ? part[r - 1] : (k > U ? U : k);
+      part[r] = k;
+    }
+    part[CL] = U;
+    for (int r = 0; r <= CL; ++r) part[CL + 1 + r] = (int)((int64_t)M * r / CL);
+    int MK = 0, NK = 0, PK = 0;
+    for (int r = 0; r < CL; ++r) {
+      MK = std::max(MK, part[CL + 2 + r] - part[CL + 1 + r]);
+      NK = std::max(NK, part[r + 1] - part[r]);
+      PK = std::max(PK, seg[part[r + 1]] - seg[part[r]]);
+    }
+    if (NK > 65535 || NK < 1) continue;
+    const size_t smem = body3_cluster_smem<T>(M, S, MK, NK, PK);
+    if ((int64_t)smem > optin) continue;
+    cudaLaunchConfig_t lc = {};
+    lc.gridDim = dim3((unsigned)CL);
+    lc.blockDim = dim3(kBody3ClusterThreads);
+    lc.dynamicSmemBytes = smem;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = (unsigned)CL;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    lc.attrs = at;
+    lc.numAttrs = 1;
+    int nclusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&nclusters, kern, &lc) != cudaSuccess || nclusters < 1) {
+      cudaGetLastError();
+      continue;
+    }
+    std::vector<int32_t> key(P);
+    for (int64_t p = 0; p < P; ++p) {
+      const int u = uid[p];
+      const int owner = (int)(std::upper_bound(part.begin(), part.begin() + CL + 1, u) - part.begin()) - 1;
+      key[p] = (owner << 16) | (u - part[owner]);
+    }
+    if ((e = cudaMalloc((void**)&b->d_pkey, sizeof(int32_t) * P)) != cudaSuccess ||
+        (e = cudaMalloc((void**)&b->d_c3part, sizeof(int) * part.size())) != cudaSuccess ||
+        (e = cudaMemcpy(b->d_pkey, key.data(), sizeof(int32_t) * P, cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(b->d_c3part, part.data(), sizeof(int) * part.size(), cudaMemcpyHostToDevice)) !=
+            cudaSuccess)
+      return cuda_status(e, "vs_body_plan_create cluster layout");
+    b->c3 = CL;
+    b->c3_smem = smem;
+    b->c3_cap[0] = MK;
+    b->c3_cap[1] = NK;
+    b->c3_cap[2] = PK;
+    return VS_OK;
+  }
+  return VS_OK;
+}
+
 extern "C" {
 
 int vs_lattice_plan_create(const vs_lattice_cfg* cfg, vs_lattice_plan** out) {
@@ -2521,6 +3136,10 @@ int vs_lattice_plan_create(const vs_lattice_cfg* cfg, vs_lattice_plan** out) {
   {
     const int nl = cfg->q == 9 ? cfg->ny : nz;
     p->tma_tb = cfg->variant != VS_GRID_TMA ? 0 : ((cfg->q == 9 && nl % 256 == 0) ? 256 : (nl % 128 == 0 ? 128 : 0));
+    int dev = 0, l2 = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev);
+    p->stream_pop = l2 > 0 && (double)cfg->q * (double)p->n * (cfg->dtype == VS_F64 ? 8.0 : 4.0) > (double)l2;
     cudaError_t e = cudaMalloc(&p->d_status, sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(p->d_status, 0, sizeof(int));
     if (e != cudaSuccess) {
@@ -2668,6 +3287,7 @@ int vs_body_plan_create(const vs_body_cfg* cfg, const vs_lattice_plan* lattice, 
   {
     int prio_lo = 0, prio_hi = 0;
     cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
+    b->prio = prio_hi;
     cudaError_t es = cudaStreamCreateWithPriority(&b->side, cudaStreamNonBlocking, prio_hi);
     if (es == cudaSuccess) es = cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming);
     if (es == cudaSuccess) es = cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming);
@@ -2863,6 +3483,8 @@ int vs_body_plan_create(const vs_body_cfg* cfg, const vs_lattice_plan* lattice, 
     }
     if ((e = cudaMalloc(&b->d_node_cell, sizeof(int32_t) * P)) != cudaSuccess) return fail(e);
     if ((e = cudaMalloc(&b->d_seg, sizeof(int32_t) * (P + 1))) != cudaSuccess) return fail(e);
+    if ((e = cudaMalloc(&b->d_wsort, ts * P)) != cudaSuccess) return fail(e);
+    if ((e = cudaMalloc((void**)&b->d_msort, sizeof(int32_t) * P)) != cudaSuccess) return fail(e);
     if ((e = cudaMalloc((void**)&b->d_U, sizeof(int))) != cudaSuccess) return fail(e);
     if ((e = cudaMalloc(&b->d_nu, ts * 3 * P)) != cudaSuccess) return fail(e);
     if ((e = cudaMalloc(&b->d_nv, ts * 3 * P)) != cudaSuccess) return fail(e);
@@ -2931,6 +3553,14 @@ int vs_body_plan_create(const vs_body_cfg* cfg, const vs_lattice_plan* lattice, 
     if ((e = cudaMalloc(&b->d_node_cell, sizeof(int32_t) * b->U)) != cudaSuccess) return fail(e);
     if ((e = cudaMalloc(&b->d_seg, sizeof(int32_t) * (b->U + 1))) != cudaSuccess) return fail(e);
     k_compact_csr<<<grid_for(P, 256), 256>>>(v.skeys, v.head, v.uid, P, b->d_node_cell, b->d_seg);
+    if ((e = cudaMalloc(&b->d_wsort, ts * P)) != cudaSuccess) return fail(e);
+    if ((e = cudaMalloc((void**)&b->d_msort, sizeof(int32_t) * P)) != cudaSuccess) return fail(e);
+    if (ts == 8)
+      k_csr_gather<double><<<grid_for(P, 256), 256>>>(v.sids, (const double*)b->d_W, b->S, P, (double*)b->d_wsort,
+                                                      b->d_msort);
+    else
+      k_csr_gather<float><<<grid_for(P, 256), 256>>>(v.sids, (const float*)b->d_W, b->S, P, (float*)b->d_wsort,
+                                                     b->d_msort);
     const int32_t endP = (int32_t)P;
     if ((e = cudaMemcpy(b->d_seg + b->U, &endP, sizeof(int32_t), cudaMemcpyHostToDevice)) != cudaSuccess)
       return fail(e);
@@ -2938,6 +3568,32 @@ int vs_body_plan_create(const vs_body_cfg* cfg, const vs_lattice_plan* lattice, 
     if ((e = cudaMalloc(&b->d_nv, ts * 3 * b->U)) != cudaSuccess) return fail(e);
     if ((e = cudaMalloc(&b->d_mk, ts * 9 * M)) != cudaSuccess) return fail(e);
     if ((e = cudaDeviceSynchronize()) != cudaSuccess) return fail(e);
+  }
+  if (b->dim == 3 && !cfg->moving) {
+    int rc3 = ts == 8 ? body3_cluster_setup<double>(b) : body3_cluster_setup<float>(b);
+    if (rc3) {
+      free_body(b);
+      return rc3;
+    }
+  }
+  if (b->dim == 3) {
+    // the fused 3-D body kernel: one CTA per SM by default (VIVSIM_GB300_BODY3D_CTAS: another
+    // count, 0 for the per-phase kernels), at most what can be resident at once
+    int dev = 0, coop = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    e = ts == 8 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_body3d_fused<L19, double>, kBody3Threads, 0)
+                : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_body3d_fused<L19, float>, kBody3Threads, 0);
+    if (e != cudaSuccess) return fail(e);
+    int G = sms;
+    if (const char* v = getenv("VIVSIM_GB300_BODY3D_CTAS")) G = atoi(v);
+    if (G > per_sm * sms) G = per_sm * sms;
+    b->fused3 = coop && G > 0 ? G : 0;
+    if (b->fused3) {
+      if ((e = cudaMalloc((void**)&b->d_bar, 4 * sizeof(unsigned))) != cudaSuccess) return fail(e);
+      if ((e = cudaMemset(b->d_bar, 0, 4 * sizeof(unsigned))) != cudaSuccess) return fail(e);
+    }
   }
   *out = b;
   return VS_OK;
@@ -3080,7 +3736,8 @@ int vs_run_graph(vs_lattice_plan* lattice, vs_body_plan* body, void* f_a, void* 
       return rc;
     }
     if (e != cudaSuccess) return cuda_status(e, "vs_run_graph end capture");
-    e = cudaGraphInstantiate(&lattice->graph, g, 0);
+    // side-stream launches keep their priority in the replayed graph
+    e = cudaGraphInstantiateWithFlags(&lattice->graph, g, cudaGraphInstantiateFlagUseNodePriority);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return cuda_status(e, "vs_run_graph instantiate");
     lattice->g_fa = f_a;
@@ -3457,7 +4114,7 @@ int vs_batch_run(vs_batch_plan* plan, void* const* f_a, void* const* f_b, int n_
         return crc;
       }
       if (e != cudaSuccess) return cuda_status(e, "vs_batch_run end capture");
-      e = cudaGraphInstantiate(&plan->graph, g, 0);
+      e = cudaGraphInstantiateWithFlags(&plan->graph, g, cudaGraphInstantiateFlagUseNodePriority);
       cudaGraphDestroy(g);
       if (e != cudaSuccess) return cuda_status(e, "vs_batch_run instantiate");
       plan->g_steps = G;

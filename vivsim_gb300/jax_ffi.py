@@ -55,7 +55,17 @@ TARGETS = {
     "vivsim_newmark_vjp": "VsNewmarkVjp",
 }
 _REGISTERED = False
-_KERNELS = {"peskin3": V.VS_KERNEL_PESKIN3, "peskin4": V.VS_KERNEL_PESKIN4, "cosine4": V.VS_KERNEL_COSINE4}
+_KERNELS = {"peskin3": V.VS_KERNEL_PESKIN3, "peskin4": V.VS_KERNEL_PESKIN4, "cosine4": V.VS_KERNEL_COSINE4,
+            "kernel_peskin_3pt": V.VS_KERNEL_PESKIN3, "kernel_peskin_4pt": V.VS_KERNEL_PESKIN4,
+            "kernel_cosine_4pt": V.VS_KERNEL_COSINE4}
+
+
+def _kernel_code(kernel):
+    """A delta kernel given as the reference's function (vivsim/ib/kernels.py) or its name."""
+    name = kernel if isinstance(kernel, str) else getattr(kernel, "__name__", "")
+    if name not in _KERNELS:
+        raise ValueError("kernel must be kernel_peskin_3pt, kernel_peskin_4pt or kernel_cosine_4pt")
+    return _KERNELS[name]
 
 
 def _jax():
@@ -390,23 +400,23 @@ class _IB:
     """vivsim.ib / vivsim.ib3d on the device."""
 
     @staticmethod
-    def kernel(r, kernel="peskin4"):
-        return _call("vivsim_ib_kernel", _sds(r.shape, r.dtype), r, kernel=_i32(_KERNELS[kernel]))
+    def kernel(r, kernel="kernel_peskin_4pt"):
+        return _call("vivsim_ib_kernel", _sds(r.shape, r.dtype), r, kernel=_i32(_kernel_code(kernel)))
 
     @staticmethod
-    def get_ib_stencil(marker_x, marker_y, ny, kernel="peskin4", radius=2):
+    def get_ib_stencil(marker_x, marker_y, ny, kernel="kernel_peskin_4pt", stencil_radius=2):
         """ib/stencil.py:7-51: W (M, (2r)^2), I int32"""
-        m, s = marker_x.shape[0], (2 * radius) ** 2
+        m, s = marker_x.shape[0], (2 * stencil_radius) ** 2
         return _call("vivsim_ib_stencil_2d", (_sds((m, s), marker_x.dtype), _sds((m, s), np.int32)), marker_x,
-                     marker_y, kernel=_i32(_KERNELS[kernel]), radius=_i32(radius), ny=_i32(ny))
+                     marker_y, kernel=_i32(_kernel_code(kernel)), radius=_i32(stencil_radius), ny=_i32(ny))
 
     @staticmethod
-    def get_ib_stencil_3d(coords, shape, kernel="peskin4", radius=2):
+    def get_ib_stencil_3d(coords, shape, kernel="kernel_peskin_4pt", stencil_radius=2):
         """ib3d/stencil.py:7-59: W (M, (2r)^3), I int32"""
-        m, s = coords.shape[0], (2 * radius) ** 3
+        m, s = coords.shape[0], (2 * stencil_radius) ** 3
         return _call("vivsim_ib_stencil_3d", (_sds((m, s), coords.dtype), _sds((m, s), np.int32)), coords,
-                     kernel=_i32(_KERNELS[kernel]), radius=_i32(radius), nx=_i32(shape[0]), ny=_i32(shape[1]),
-                     nz=_i32(shape[2]))
+                     kernel=_i32(_kernel_code(kernel)), radius=_i32(stencil_radius), nx=_i32(shape[0]),
+                     ny=_i32(shape[1]), nz=_i32(shape[2]))
 
     @staticmethod
     def interpolate(grid, W, I):
