@@ -332,8 +332,14 @@ def gb300_arm(args, world, rank, local):
         secs = job_seconds(torch, dist, secs, "cuda")
         mlups = aggregate_rate(n * args.chunk * args.steps, world, secs)
         # with a body: body kernel, grid launch outside its box, box launch; the x-face
-        # boundaries of these cases run on the next step's load and once at the end of a chunk
-        launches_per_step = 3 if body is not None else 1 + step_groups(case)
+        # boundaries of these cases run on the next step's load and once at the end of a chunk.
+        # The persistent form: one launch per chunk plus the chunk's closing face launch.
+        persistent = sim.persistent(args.chunk)
+        if persistent:
+            launches_per_chunk = 1 + step_groups(case)
+        else:
+            launches_per_step = 3 if body is not None else 1 + step_groups(case)
+            launches_per_chunk = launches_per_step * args.chunk + (step_groups(case) if body is not None else 0)
         rl = roofline(torch, case, step, body, sim, flush, peak, peak_kind, 2 * args.chunk)
 
         # end to end through the public API with host buffers: H2D f, chunk, D2H f
@@ -362,12 +368,13 @@ def gb300_arm(args, world, rank, local):
                     continue
                 c2 = build_case(name)
                 st2, bd2, sm2 = configs.build_solver(c2)
-                r2 = lambda: sm2.run(10, graph=True)  # noqa: E731
+                r2 = lambda: sm2.run(50, graph=True)  # noqa: E731
                 r2()
                 torch.cuda.synchronize()
                 s2 = time_chunks(torch, r2, 5, 2, flush)
                 extras[name] = {
-                    "workload": c2["name"], "mlups": round(int(math.prod(c2["shape"])) * 10 * 5 / s2 / 1e6, 1),
+                    "workload": c2["name"], "time_steps": 50 * 5,
+                    "mlups": round(int(math.prod(c2["shape"])) * 50 * 5 / s2 / 1e6, 1),
                     "roofline": roofline(torch, c2, st2, bd2, sm2, flush, peak, peak_kind, 10)}
                 del st2, bd2, sm2, c2
                 torch.cuda.empty_cache()
@@ -405,8 +412,8 @@ def gb300_arm(args, world, rank, local):
         "e2e": {"value": round(e2e_mlups, 1), "unit": "MLUPS", "h2d_bytes_per_step": fbytes,
                 "d2h_bytes_per_step": fbytes,
                 "path": "vivsim_gb300.solver.Simulation.run from pinned host populations"},
-        "gpu_launches": (launches_per_step * args.chunk + (step_groups(case) if body is not None else 0))
-        * args.steps,
+        "gpu_launches": launches_per_chunk * args.steps,
+        "step_form": "persistent (one cooperative launch per bench step)" if persistent else "one launch group per step",
         "cpu_baseline": cpu,
         "clocks": clocks,
     }

@@ -304,11 +304,22 @@ int vs_body_set_state_device(vs_body_plan* plan, const void* state, void* stream
 int vs_step(const vs_lattice_plan* lattice, vs_body_plan* body, const void* f_in, void* f_out, void* force_hist,
             void* stream);
 /* n_steps steps ping-ponging between f_a (input) and f_b; the result ends in f_a when
- * n_steps is even, else in f_b.  force_hist (n_steps x 3) may be NULL. */
+ * n_steps is even, else in f_b.  force_hist (n_steps x 3) may be NULL.  The loop of the
+ * reference's examples (examples/2d/vortex_induced_vibration.py:151-157, a lax.scan over
+ * update_step).  With the environment variable VIVSIM_GB300_RUN_FORM=persistent, a
+ * float 2-D plan whose body takes the cluster form (4 x 4 stencil, face boundaries that
+ * can wait for the next step's load) runs all n_steps in one persistent cooperative launch
+ * (the body's thread-block cluster beside groups of grid tiles, a barrier per step; one
+ * launch per watchdog interval); its populations equal the launch-per-step form's bit for
+ * bit. */
 int vs_run(const vs_lattice_plan* lattice, vs_body_plan* body, void* f_a, void* f_b, int n_steps,
            void* force_hist, void* stream);
+/* 1 when vs_run(lattice, body, ..., n_steps, ...) takes the persistent form, else 0 (no
+ * CUDA call).  No counterpart in the reference (its loop is XLA's). */
+int vs_run_persistent(const vs_lattice_plan* lattice, const vs_body_plan* body, int n_steps);
 /* As vs_run, but the n_steps launches are captured once into a CUDA graph owned by the
- * lattice plan (re-captured when the arguments change) and replayed. */
+ * lattice plan (re-captured when the arguments change) and replayed.  A run that takes
+ * the persistent form is already one launch: vs_run_graph then runs vs_run. */
 int vs_run_graph(vs_lattice_plan* lattice, vs_body_plan* body, void* f_a, void* f_b, int n_steps,
                  void* force_hist, void* stream);
 

@@ -760,3 +760,60 @@ def test_bounded_wait_reports_timeout(S):
     assert int(status.item()) == V.VS_ERR_TIMEOUT
     t = torch.ones(64, device="cuda")
     assert S.check_finite(t)
+
+
+def _viv_case_run(S, case_kw, chunks, watchdog=0, graph=False):
+    """The benchmark VIV configuration (vivsim_gb300.configs.viv2d with case_kw), run as
+    consecutive vs_run calls of the given lengths; populations, body state and forces."""
+    from vivsim_gb300 import configs
+    case = configs.viv2d(**case_kw)
+    bcs = [S.boundary(k, loc, mode=m, **kw) for (k, loc, m, kw) in case["boundaries"]]
+    step = S.LatticeStep(9, case["shape"], case["collision"], case["omega"], forcing="edm", boundaries=bcs,
+                         watchdog_every=watchdog)
+    b = case["body"]
+    body = S.RigidBody(step, b["markers"], b["ds"], moving=True, free_dof=b["free_dof"], mass=b["mass"],
+                       stiffness=b["stiffness"], added_mass_area=b["added_mass_area"])
+    sim = S.Simulation(step, T(case["f0"]), body)
+    persistent = sim.persistent(max(chunks))
+    hists = []
+    with torch.cuda.stream(torch.cuda.Stream()):
+        for n in chunks:
+            hists.append(N(sim.run(n, graph=graph, force_history=True)))
+        torch.cuda.synchronize()
+    step.check()
+    return N(sim.f), body.state(), np.concatenate(hists), persistent
+
+
+@pytest.mark.parametrize("collision", ["kbc", "bgk", "mrt", "reg"])
+def test_persistent_run_equals_step_launches(S, monkeypatch, collision):
+    """The persistent run (one cooperative launch: the body's cluster beside groups of grid
+    tiles, a barrier per step) and the launch-per-step form give identical bits on the
+    benchmark VIV case, over runs of odd and even lengths in a row (prediction slots and
+    deferred boundaries carried across calls)."""
+    kw = dict(nx=256, ny=128, D=20.0, center=(64.0, 64.0), n_markers=63, collision=collision)
+    chunks = [7, 12, 1, 30]
+    monkeypatch.setenv("VIVSIM_GB300_RUN_FORM", "persistent")
+    fa, sa, ha, pa = _viv_case_run(S, kw, chunks)
+    monkeypatch.delenv("VIVSIM_GB300_RUN_FORM")
+    fb, sb, hb, pb = _viv_case_run(S, kw, chunks)
+    assert pa and not pb
+    assert np.array_equal(fa, fb)
+    assert np.array_equal(ha, hb)
+    for k in ("a", "v", "d", "h"):
+        assert np.array_equal(sa[k], sb[k]), k
+
+
+def test_persistent_run_full_size_and_watchdog(S, monkeypatch):
+    """At the benchmark size (1024 x 512, 126 markers) with the watchdog splitting the run
+    into launches of 9 steps, and through vs_run_graph: identical bits to the per-step form."""
+    monkeypatch.setenv("VIVSIM_GB300_RUN_FORM", "persistent")
+    fa, sa, ha, pa = _viv_case_run(S, {}, [40, 25], watchdog=9)
+    fg, sg, hg, pg = _viv_case_run(S, {}, [40, 25], graph=True)
+    monkeypatch.delenv("VIVSIM_GB300_RUN_FORM")
+    fb, sb, hb, pb = _viv_case_run(S, {}, [40, 25])
+    assert pa and pg and not pb
+    for f, h, s in ((fa, ha, sa), (fg, hg, sg)):
+        assert np.array_equal(f, fb)
+        assert np.array_equal(h, hb)
+        for k in ("a", "v", "d", "h"):
+            assert np.array_equal(s[k], sb[k]), k

@@ -127,6 +127,7 @@ _SIGS = {
     "vs_step": (_i, [_p, _p, _p, _p, _p, _p]),
     "vs_run": (_i, [_p, _p, _p, _p, _i, _p, _p]),
     "vs_run_graph": (_i, [_p, _p, _p, _p, _i, _p, _p]),
+    "vs_run_persistent": (_i, [_p, _p, _i]),
     "vs_step_grid_only": (_i, [_p, _p, _p, _p, _p]),
     "vs_body_state_device": (_i, [_p, C.POINTER(C.c_void_p)]),
     "vs_body_set_state_device": (_i, [_p, _p, _p]),

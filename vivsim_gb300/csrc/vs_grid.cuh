@@ -245,19 +245,22 @@ __device__ __forceinline__ bool skipped(const StepParams<L, T>& P, int x, int y,
   return P.skip_walls && (x == 0 || x == P.nx - 1);
 }
 
+// (tid, width): the thread's index in a group of `width` threads that works as one block of
+// the launch geometry (the block itself in the grid kernels; a part of a CTA in the
+// persistent run kernel).
 template <class L, typename T, int COLL, int FEAT>
-__device__ __forceinline__ void step_block(const StepParams<L, T>& P, int bx, int by) {
+__device__ __forceinline__ void step_block_t(const StepParams<L, T>& P, int bx, int by, int tid, int width) {
   constexpr int Q = L::Q;
   int x, y, z;
   if (!(FEAT & kFeatSkip) || P.nreg == 0) {
     x = by;
     if constexpr (L::D == 2) {
-      y = bx * blockDim.x + threadIdx.x;
+      y = bx * width + tid;
       if (y >= P.ny) return;
       z = 0;
     } else {
       y = bx / P.chunks;
-      z = (bx - y * P.chunks) * blockDim.x + threadIdx.x;
+      z = (bx - y * P.chunks) * width + tid;
       if (z >= P.nz) return;
     }
   } else {
@@ -266,13 +269,13 @@ __device__ __forceinline__ void step_block(const StepParams<L, T>& P, int bx, in
     const int* R = P.reg[g];
     x = R[0] + (r - P.rowstart[g]);
     if constexpr (L::D == 2) {
-      y = R[2] + bx * blockDim.x + threadIdx.x;
+      y = R[2] + bx * width + tid;
       if (y >= R[3]) return;
       z = 0;
     } else {
       const int cy = bx / P.chunks;
       y = R[2] + cy;
-      z = R[4] + (bx - cy * P.chunks) * blockDim.x + threadIdx.x;
+      z = R[4] + (bx - cy * P.chunks) * width + tid;
       if (y >= R[3] || z >= R[5]) return;
     }
   }
@@ -285,13 +288,18 @@ __device__ __forceinline__ void step_block(const StepParams<L, T>& P, int bx, in
   step_node<L, T, COLL, FEAT>(P, x, y, z, p, f);
 }
 
-// A D2Q9 block of the whole grid with two nodes per thread, blockDim.x apart along y: both
+template <class L, typename T, int COLL, int FEAT>
+__device__ __forceinline__ void step_block(const StepParams<L, T>& P, int bx, int by) {
+  step_block_t<L, T, COLL, FEAT>(P, bx, by, (int)threadIdx.x, (int)blockDim.x);
+}
+
+// A D2Q9 block of the whole grid with two nodes per thread, `width` apart along y: both
 // nodes' populations are loaded before either is updated, which doubles the loads in flight
 // per thread.  No regions.
 template <typename T, int COLL, int FEAT>
-__device__ __forceinline__ void step_block2(const StepParams<L9, T>& P, int bx, int by) {
+__device__ __forceinline__ void step_block2_t(const StepParams<L9, T>& P, int bx, int by, int tid, int width) {
   const int x = by;
-  const int y0 = bx * 2 * (int)blockDim.x + (int)threadIdx.x, y1 = y0 + (int)blockDim.x;
+  const int y0 = bx * 2 * width + tid, y1 = y0 + width;
   const bool a = y0 < P.ny && !((FEAT & kFeatSkip) && skipped(P, x, y0, 0));
   const bool b = y1 < P.ny && !((FEAT & kFeatSkip) && skipped(P, x, y1, 0));
   const int p0 = x * P.ny + y0, p1 = x * P.ny + y1;
@@ -303,6 +311,11 @@ __device__ __forceinline__ void step_block2(const StepParams<L9, T>& P, int bx, 
   }
   if (a) step_node<L9, T, COLL, FEAT>(P, x, y0, 0, p0, f0);
   if (b) step_node<L9, T, COLL, FEAT>(P, x, y1, 0, p1, f1);
+}
+
+template <typename T, int COLL, int FEAT>
+__device__ __forceinline__ void step_block2(const StepParams<L9, T>& P, int bx, int by) {
+  step_block2_t<T, COLL, FEAT>(P, bx, by, (int)threadIdx.x, (int)blockDim.x);
 }
 
 // The main launch of a batch walks each case's nodes in memory order: chunk j of a

@@ -16,6 +16,7 @@
 #include <cudaTypedefs.h>
 
 #include <climits>
+#include <cstring>
 #include <cmath>
 #include <cstdlib>
 #include <new>
@@ -359,7 +360,7 @@ struct Kin2 {
 // `for _ in range(FSI_ITER)` loop does (examples/2d/vortex_induced_vibration.py:114-139).
 template <typename T>
 __device__ __forceinline__ void body2d_finish(const BodyParams<T>& B, const Kin2<T>& K, const T* Ft, int M,
-                                              const T* a, const T* v, const T* d) {
+                                              const T* a, const T* v, const T* d, T* hist) {
   const int tid = threadIdx.x;
   T h[3];
 #pragma unroll
@@ -390,7 +391,7 @@ __device__ __forceinline__ void body2d_finish(const BodyParams<T>& B, const Kin2
     const int c = tid;
     if (c == 2 && !K.rot) {
       B.state[9 + 2] = T(0);
-      if (B.force_hist) B.force_hist[2] = T(0);
+      if (hist) hist[2] = T(0);
       return;
     }
     // selects, not indexing by the thread: the state stays in registers
@@ -425,8 +426,14 @@ __device__ __forceinline__ void body2d_finish(const BodyParams<T>& B, const Kin2
     B.state[3 + c] = vn;
     B.state[6 + c] = dn;
     B.state[9 + c] = hh;
-    if (B.force_hist) B.force_hist[c] = hh;
+    if (hist) hist[c] = hh;
   }
+}
+
+template <typename T>
+__device__ __forceinline__ void body2d_finish(const BodyParams<T>& B, const Kin2<T>& K, const T* Ft, int M,
+                                              const T* a, const T* v, const T* d) {
+  body2d_finish<T>(B, K, Ft, M, a, v, d, B.force_hist);
 }
 
 // Block scan over the window cells: cnt[k] pairs per cell -> CSR.  Writes, per cell,
@@ -1090,9 +1097,10 @@ __global__ void __launch_bounds__(kBodyThreads) k_body2d_chain_batch(const BodyP
 constexpr int kClusterPairs = 256;    // stencil pairs a CTA holds (one per thread)
 constexpr int kClusterThreads = 384;  // launch bound; a plan uses enough threads for its window
 
+// One time step of the body over the CTAs of the calling cluster (the body of
+// k_body2d_cluster, also run by the persistent k_viv_run); hist: where h goes (or null).
 template <typename T, int R, int COLL>
-__global__ void __launch_bounds__(kClusterThreads) k_body2d_cluster(const __grid_constant__ BodyParams<T> B,
-                                                                   const __grid_constant__ StepParams<L9, T> SP) {
+__device__ __forceinline__ void body2d_cluster_step(const BodyParams<T>& B, const StepParams<L9, T>& SP, T* hist) {
   namespace cg = cooperative_groups;
   constexpr int WD = 2 * R, S = WD * WD;
   cg::cluster_group cluster = cg::this_cluster();
@@ -1344,7 +1352,7 @@ __global__ void __launch_bounds__(kClusterThreads) k_body2d_cluster(const __grid
   cluster.sync();
   if (ok && rank == 0 && tid < 32) {
     // h = sum_m(-F_total) (and the torque) in warp 0's fixed tree, added mass, Newmark
-    body2d_finish<T>(B, kin, Ft, M, a, v, d);
+    body2d_finish<T>(B, kin, Ft, M, a, v, d, hist);
     if (tid == 2) {
       B.meta[slot ? META_PX : META_PX2] = flags[1];  // the next step reads the other slot
       B.meta[slot ? META_PY : META_PY2] = flags[2];
@@ -1362,6 +1370,12 @@ __global__ void __launch_bounds__(kClusterThreads) k_body2d_cluster(const __grid
     for (int i = 0; i < 9; ++i) f[i] = __ldg(SP.fin + (size_t)i * SP.n + p);
     step_node<L9, T, COLL, kFeatGeneral>(SP, x, y, 0, p, f);
   }
+}
+
+template <typename T, int R, int COLL>
+__global__ void __launch_bounds__(kClusterThreads) k_body2d_cluster(const __grid_constant__ BodyParams<T> B,
+                                                                   const __grid_constant__ StepParams<L9, T> SP) {
+  body2d_cluster_step<T, R, COLL>(B, SP, B.force_hist);
 }
 
 template <typename T>
@@ -1751,6 +1765,132 @@ __global__ void __launch_bounds__(kBody3Threads) k_body3d_fused(const __grid_con
       atomicExch(B.bar, 0u);
       atomicExch(B.bar + 2, 0u);
       atomicExch(B.bar + 3, 0u);
+    }
+  }
+}
+
+// ---- many 2-D time steps in one persistent launch
+// One cooperative launch of G CTAs in clusters of CL (the body's cluster size) advances
+// n_steps time steps of a plan whose body takes the cluster form.  Cluster 0 runs the
+// body's step (body2d_cluster_step: markers, stencil, MDF, Newmark, and the nodes of the
+// predicted window); every other CTA works as groups of kRunGroup threads, each group
+// updating whole tiles of the bulk grid launch's geometry (a row x and kRunGroup * NPT
+// consecutive nodes along y, k_step_fast's node order) and, while the face boundaries are
+// deferred to the next step's load, tiles of the two x-face planes.  A barrier over all
+// CTAs ends every step.  Every node goes through the device functions of the per-step
+// launches, so the populations equal vs_run's launch-per-step form bit for bit; what the
+// persistent form removes is the launches, the fork and join of streams per step, and the
+// body kernel's start-up behind the grid launch's traffic.
+constexpr int kRunThreads = 384;
+constexpr int kRunGroup = 128;
+
+template <typename T>
+struct VivRunParams {
+  BodyParams<T> B[2];           // [parity of the step]: populations read, prediction slot
+  StepParams<L9, T> SPb[2][2];  // [parity][lazy_in]: the body's window nodes
+  StepParams<L9, T> SPm[2][2];  // [parity][lazy_in]: tiles of the bulk launch
+  StepParams<L9, T> SPw[2];     // [parity]: x-face plane tiles (lazy_in only)
+  T* hist;                      // force history, 3 values per step, or null
+  unsigned* bar;                // barrier words: arrivals, generation, abort, exits
+  int* status;                  // the plan's status word
+  int n_steps;
+  int lazy;                     // face boundaries deferred to the next step's load
+  int lazy_first;               // the run's first step already reads deferred boundaries
+  int chunks_m, rows_m;         // bulk tiles: chunks along y, rows
+  int chunks_w;                 // plane tiles per plane
+};
+
+// Barrier over every CTA of the run, agreed within each cluster.  After a cluster barrier
+// the cluster's rank-0 CTA arrives at the grid-wide count (one arrival per cluster) and
+// waits for the generation to move on (bounded: kGridBarrierLimit polls, or an abort seen);
+// a second cluster barrier releases the cluster, and every CTA of it reads rank 0's
+// verdict, so a cluster never splits over a timeout and its CTAs keep meeting at the same
+// cluster barriers.  false: the run aborts (VS_ERR_TIMEOUT recorded).
+__device__ __forceinline__ bool run_barrier(unsigned* bar, int* status, int* ok_s) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  __syncthreads();
+  if (threadIdx.x == 0) __threadfence();
+  cluster.sync();
+  if (cluster.block_rank() == 0 && threadIdx.x == 0) {
+    int ok = 1;
+    const unsigned n = gridDim.x / cluster.num_blocks();
+    unsigned gen, abort_flag;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(gen) : "l"(bar + 1) : "memory");
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(abort_flag) : "l"(bar + 2) : "memory");
+    if (abort_flag) {
+      ok = 0;
+    } else {
+      __threadfence();
+      const unsigned arrived = atomicAdd(bar, 1u);
+      if (arrived == n - 1) {
+        atomicExch(bar, 0u);
+        __threadfence();
+        asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(bar + 1), "r"(gen + 1) : "memory");
+      } else {
+        int it = 0;
+        for (;;) {
+          unsigned g, ab;
+          asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(g) : "l"(bar + 1) : "memory");
+          if (g != gen) break;
+          asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(ab) : "l"(bar + 2) : "memory");
+          if (ab || ++it > kGridBarrierLimit) {
+            atomicExch(bar + 2, 1u);
+            atomicMax(status, VS_ERR_TIMEOUT);
+            ok = 0;
+            break;
+          }
+          __nanosleep(32);
+        }
+      }
+    }
+    *ok_s = ok;
+  }
+  cluster.sync();
+  return *cluster.map_shared_rank(ok_s, 0) != 0;
+}
+
+template <typename T, int R, int COLL>
+__global__ void __launch_bounds__(kRunThreads, 1) k_viv_run(const __grid_constant__ VivRunParams<T> P) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  __shared__ int ok_s;
+  constexpr int NPT = FastShape<L9, COLL>::NPT;
+  const int CL = (int)cluster.num_blocks();
+  const bool body = (int)blockIdx.x < CL;
+  const int gpc = (int)blockDim.x / kRunGroup, gt = (int)threadIdx.x % kRunGroup;
+  const int ng = ((int)gridDim.x - CL) * gpc, g0 = ((int)blockIdx.x - CL) * gpc + (int)threadIdx.x / kRunGroup;
+  const int nm = P.chunks_m * P.rows_m;
+  bool ok = true;
+  for (int s = 0; s < P.n_steps && ok; ++s) {
+    const int p = s & 1;
+    const int lz = P.lazy && (s > 0 || P.lazy_first) ? 1 : 0;
+    if (body) {
+      body2d_cluster_step<T, R, COLL>(P.B[p], P.SPb[p][lz], P.hist ? P.hist + 3 * (int64_t)s : nullptr);
+    } else {
+      const int nt = nm + (lz ? 2 * P.chunks_w : 0);
+      for (int t = g0; t < nt; t += ng) {
+        if (t < nm) {
+          const int by = t / P.chunks_m, bx = t - by * P.chunks_m;
+          if constexpr (NPT == 2) step_block2_t<T, COLL, kFeatSkip>(P.SPm[p][lz], bx, by, gt, kRunGroup);
+          else step_block_t<L9, T, COLL, kFeatSkip>(P.SPm[p][lz], bx, by, gt, kRunGroup);
+        } else {
+          const int u = t - nm, by = u / P.chunks_w, bx = u - by * P.chunks_w;
+          step_block_t<L9, T, COLL, kFeatGeneral | kFeatWalls>(P.SPw[p], bx, by, gt, kRunGroup);
+        }
+      }
+    }
+    ok = run_barrier(P.bar, P.status, &ok_s);
+  }
+  // the last cluster out resets the arrivals and the abort flag for the next launch (the
+  // generation only moves on); a CTA leaves only after its cluster read its verdicts
+  cluster.sync();
+  if (cluster.block_rank() == 0 && threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(P.bar + 3, 1u) == gridDim.x / (unsigned)CL - 1) {
+      atomicExch(P.bar, 0u);
+      atomicExch(P.bar + 2, 0u);
+      atomicExch(P.bar + 3, 0u);
     }
   }
 }
@@ -2148,6 +2288,8 @@ struct vs_body_plan {
   int cl_threads;        // threads per CTA of the cluster form
   int parity;            // cluster form: prediction slot of the next step
   size_t cl_smem;
+  int run_ctas;          // CTAs of the persistent run (k_viv_run), 0 where it does not apply
+  size_t run_smem;
   CUtensorMap maps[2]; // tensor maps of the last two population buffers seen
   const void* map_ptr[2];
   int map_next;
@@ -2977,6 +3119,159 @@ static bool lazy_boundaries(const vs_lattice_plan* LP, const vs_body_plan* B) {
   return true;
 }
 
+// ---- host side of the persistent run (k_viv_run)
+static_assert(sizeof(VivRunParams<float>) <= 32000, "k_viv_run parameters exceed the launch parameter space");
+
+template <int COLL>
+static cudaError_t viv_run_launch_t(const vs_body_plan* B, const VivRunParams<float>& P, cudaStream_t st) {
+  cudaLaunchConfig_t lc = {};
+  lc.gridDim = dim3((unsigned)B->run_ctas);
+  lc.blockDim = dim3(kRunThreads);
+  lc.dynamicSmemBytes = B->run_smem;
+  lc.stream = st;
+  cudaLaunchAttribute at[2];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = (unsigned)B->cl_size;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  at[1].id = cudaLaunchAttributeCooperative;
+  at[1].val.cooperative = 1;
+  lc.attrs = at;
+  lc.numAttrs = 2;
+  return cudaLaunchKernelEx(&lc, k_viv_run<float, 2, COLL>, P);
+}
+
+// CTAs of the persistent run: as many whole clusters of the body's size as are resident at
+// once (at least two: the body's and one of grid tiles), 0 where the device has no
+// cooperative cluster launch.
+template <int COLL>
+static cudaError_t viv_run_setup_t(vs_body_plan* B, int& ctas) {
+  ctas = 0;
+  auto kern = k_viv_run<float, 2, COLL>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)B->run_smem);
+  if (e != cudaSuccess) return e;
+  cudaLaunchConfig_t lc = {};
+  lc.gridDim = dim3((unsigned)B->cl_size);
+  lc.blockDim = dim3(kRunThreads);
+  lc.dynamicSmemBytes = B->run_smem;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = (unsigned)B->cl_size;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  lc.attrs = at;
+  lc.numAttrs = 1;
+  int ncl = 0;
+  e = cudaOccupancyMaxActiveClusters(&ncl, kern, &lc);
+  if (e != cudaSuccess) return e;
+  if (ncl >= 2) ctas = ncl * B->cl_size;
+  return cudaSuccess;
+}
+
+static cudaError_t viv_run_setup(vs_body_plan* B, int coll, int& ctas) {
+  switch (coll) {
+    case VS_COLLIDE_BGK: return viv_run_setup_t<VS_COLLIDE_BGK>(B, ctas);
+    case VS_COLLIDE_KBC: return viv_run_setup_t<VS_COLLIDE_KBC>(B, ctas);
+    case VS_COLLIDE_REG: return viv_run_setup_t<VS_COLLIDE_REG>(B, ctas);
+    default: return viv_run_setup_t<VS_COLLIDE_MRT>(B, ctas);
+  }
+}
+
+// The persistent run applies to float 2-D plans whose body takes the cluster form with a
+// 4 x 4 stencil, whose face boundaries are deferred to the next step's load (or absent),
+// and whose bulk nodes need no per-node feature (no uniform force, obstacle mask,
+// characteristic wall or pre-stream faces).  It is selected with
+// VIVSIM_GB300_RUN_FORM=persistent; the default is the launch-per-step form, which measured
+// faster on the benchmark VIV case (14.0 against 18.8 us per step).
+static bool viv_run_applies(const vs_lattice_plan* LP, const vs_body_plan* B, bool lazy) {
+  const char* form = getenv("VIVSIM_GB300_RUN_FORM");
+  if (!form || strcmp(form, "persistent") != 0) return false;
+  if (!B || !B->cluster || B->run_ctas <= 0 || B->dim != 2) return false;
+  const vs_lattice_cfg& c = LP->cfg;
+  if (c.dtype != VS_F32 || c.q != 9 || B->cfg.radius != 2 || c.obstacle_mask) return false;
+  if (!lazy && c.n_bc > 0) return false;
+  for (int k = 0; k < c.n_bc; ++k)
+    if (c.bc[k].mode == VS_WALL_CHARACTERISTIC) return false;
+  for (int q = 0; q < 3; ++q)
+    if (c.g_uniform[q] != 0.0) return false;
+  for (int k = 0; k < c.n_bc; ++k)
+    if (c.bc[k].kind == VS_BC_BB || c.bc[k].kind == VS_BC_SPECULAR) return false;
+  return true;
+}
+
+// n time steps from global step s0 of a run (step s reads f_a when s is even), in one launch.
+static int viv_run_chunk(const vs_lattice_plan* LP, vs_body_plan* B, void* f_a, void* f_b, int s0, int n, bool lazy,
+                         void* force_hist, cudaStream_t st) {
+  VivRunParams<float>* P = new (std::nothrow) VivRunParams<float>();
+  if (!P) {
+    set_error("vs_run: out of host memory");
+    return VS_ERR_INVALID_ARG;
+  }
+  const vs_lattice_cfg& c = LP->cfg;
+  const int parity0 = B->parity;  // prediction slot of step s0
+  for (int p = 0; p < 2; ++p) {
+    void* fin = p == 0 ? f_a : f_b;
+    void* fout = p == 0 ? f_b : f_a;
+    const int slot = parity0 ^ ((p ^ s0) & 1);
+    P->B[p] = body_params2d<float>(B, LP, fin, nullptr, false);
+    P->B[p].pred_slot = slot;
+    for (int lz = 0; lz < 2; ++lz) {
+      dim3 grid;
+      int tb = 0;
+      StepParams<L9, float> SP;
+      grid_setup<L9, float>(LP, B, fin, fout, 2, false, 0, SP, grid, tb);
+      SP.nreg = 0;
+      SP.skip_walls = lz;
+      P->SPb[p][lz] = SP;
+      grid_setup<L9, float>(LP, B, fin, fout, 4, lz != 0, 0, SP, grid, tb, slot);
+      P->SPm[p][lz] = SP;
+    }
+    if (lazy) {
+      dim3 grid;
+      int tb = 0;
+      StepParams<L9, float> SP;
+      grid_setup<L9, float>(LP, B, fin, fout, 3, true, 0, SP, grid, tb);
+      SP.chunks = (c.ny + kRunGroup - 1) / kRunGroup;
+      SP.gx = SP.chunks;
+      P->SPw[p] = SP;
+    }
+  }
+  int npt = 1;
+  switch (c.collision) {
+    case VS_COLLIDE_BGK: npt = FastShape<L9, VS_COLLIDE_BGK>::NPT; break;
+    case VS_COLLIDE_KBC: npt = FastShape<L9, VS_COLLIDE_KBC>::NPT; break;
+    case VS_COLLIDE_REG: npt = FastShape<L9, VS_COLLIDE_REG>::NPT; break;
+    default: npt = FastShape<L9, VS_COLLIDE_MRT>::NPT; break;
+  }
+  P->hist = force_hist ? (float*)force_hist + 3 * (int64_t)s0 : nullptr;
+  P->bar = B->d_bar;
+  P->status = LP->d_status;
+  P->n_steps = n;
+  P->lazy = lazy ? 1 : 0;
+  P->lazy_first = s0 > 0 ? 1 : 0;
+  P->chunks_m = (c.ny + kRunGroup * npt - 1) / (kRunGroup * npt);
+  P->rows_m = c.nx;
+  P->chunks_w = (c.ny + kRunGroup - 1) / kRunGroup;
+  // the kernel numbers its steps from 0: swap the buffers when the chunk starts on an odd step
+  if (s0 & 1) {
+    std::swap(P->B[0], P->B[1]);
+    std::swap(P->SPb[0], P->SPb[1]);
+    std::swap(P->SPm[0], P->SPm[1]);
+    std::swap(P->SPw[0], P->SPw[1]);
+  }
+  cudaError_t e;
+  switch (c.collision) {
+    case VS_COLLIDE_BGK: e = viv_run_launch_t<VS_COLLIDE_BGK>(B, *P, st); break;
+    case VS_COLLIDE_KBC: e = viv_run_launch_t<VS_COLLIDE_KBC>(B, *P, st); break;
+    case VS_COLLIDE_REG: e = viv_run_launch_t<VS_COLLIDE_REG>(B, *P, st); break;
+    default: e = viv_run_launch_t<VS_COLLIDE_MRT>(B, *P, st); break;
+  }
+  delete P;
+  if (e != cudaSuccess) return cuda_status(e, "vs_run persistent launch");
+  B->parity = parity0 ^ (n & 1);
+  return VS_OK;
+}
+
 // The cluster form of a fixed 3-D body step: the largest cluster of up to 16 CTAs (8
 // where the device allows no larger one) whose per-CTA shared memory fits, with the nodes
 // split by pair count.  VIVSIM_GB300_BODY3D_CLUSTER: another largest size, 0 for none.
@@ -3441,6 +3736,23 @@ int vs_body_plan_create(const vs_body_cfg* cfg, const vs_lattice_plan* lattice, 
         }
       }
     }
+    // the persistent run (float, 4 x 4 stencils): its size, and its barrier words
+    b->run_ctas = 0;
+    if (b->cluster && ts == 4 && cfg->radius == 2) {
+      int coop = 0;
+      cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+      b->run_smem = body2d_cluster_smem<float>(M, 2, kRunThreads);
+      int ctas = 0;
+      if (coop && (int64_t)b->run_smem <= optin && viv_run_setup(b, lattice->cfg.collision, ctas) != cudaSuccess) {
+        cudaGetLastError();
+        ctas = 0;
+      }
+      if (ctas > 0) {
+        if ((e = cudaMalloc((void**)&b->d_bar, 4 * sizeof(unsigned))) != cudaSuccess) return fail(e);
+        if ((e = cudaMemset(b->d_bar, 0, 4 * sizeof(unsigned))) != cudaSuccess) return fail(e);
+        b->run_ctas = ctas;
+      }
+    }
   } else if (cfg->moving) {
     // moving 3-D body: the window follows the stencil box (one node of slack per axis for
     // the floor of a moving coordinate); CSR rebuilt every step inside the workspace
@@ -3697,6 +4009,26 @@ int vs_run(const vs_lattice_plan* lattice, vs_body_plan* body, void* f_a, void* 
   VS_REQUIRE(lattice && f_a && f_b && f_a != f_b && n_steps >= 0, "vs_run: bad arguments");
   const size_t hs = 3 * dsize(lattice->cfg.dtype);
   const bool lazy = lazy_boundaries(lattice, body);
+  if (n_steps > 1 && viv_run_applies(lattice, body, lazy)) {
+    // persistent form: one launch per watchdog interval (or for the whole run)
+    const int K = lattice->cfg.watchdog_every;
+    for (int s0 = 0; s0 < n_steps;) {
+      const int n = K > 0 ? std::min(K - s0 % K, n_steps - s0) : n_steps - s0;
+      int rc = viv_run_chunk(lattice, body, f_a, f_b, s0, n, lazy, force_hist, as_stream(stream));
+      if (rc) return rc;
+      s0 += n;
+      void* last = ((s0 - 1) % 2 == 0) ? f_b : f_a;  // the output of step s0 - 1
+      if (s0 == n_steps && lazy) {
+        rc = enqueue_bcs(lattice, last, as_stream(stream));
+        if (rc) return rc;
+      }
+      if (K > 0 && (s0 % K == 0 || s0 == n_steps)) {
+        rc = vs_check_finite(lattice->cfg.dtype, last, lattice->n * lattice->cfg.q, lattice->d_status, stream);
+        if (rc) return rc;
+      }
+    }
+    return VS_OK;
+  }
   for (int s = 0; s < n_steps; ++s) {
     void* src = (s % 2 == 0) ? f_a : f_b;
     void* dst = (s % 2 == 0) ? f_b : f_a;
@@ -3714,11 +4046,19 @@ int vs_run(const vs_lattice_plan* lattice, vs_body_plan* body, void* f_a, void* 
   return VS_OK;
 }
 
+int vs_run_persistent(const vs_lattice_plan* lattice, const vs_body_plan* body, int n_steps) {
+  if (!lattice || n_steps < 2) return 0;
+  return viv_run_applies(lattice, body, lazy_boundaries(lattice, body)) ? 1 : 0;
+}
+
 int vs_run_graph(vs_lattice_plan* lattice, vs_body_plan* body, void* f_a, void* f_b, int n_steps, void* force_hist,
                  void* stream) {
   VS_REQUIRE(lattice && f_a && f_b && f_a != f_b && n_steps > 0, "vs_run_graph: bad arguments");
   cudaStream_t st = as_stream(stream);
   VS_REQUIRE(st != nullptr, "vs_run_graph: needs a non-default stream (stream capture)");
+  // the persistent form is already one launch per run: no graph to capture
+  if (n_steps > 1 && viv_run_applies(lattice, body, lazy_boundaries(lattice, body)))
+    return vs_run(lattice, body, f_a, f_b, n_steps, force_hist, stream);
   const bool hit = lattice->graph && lattice->g_fa == f_a && lattice->g_fb == f_b && lattice->g_steps == n_steps &&
                    lattice->g_hist == force_hist && lattice->g_body == body && lattice->g_stream == st;
   if (!hit) {

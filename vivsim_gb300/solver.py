@@ -279,6 +279,11 @@ class Simulation:
             self._cur_is_a = not self._cur_is_a
         return hist
 
+    def persistent(self, n_steps):
+        """True when run(n_steps) advances all steps in one persistent launch (vs_run_persistent)."""
+        body = self.body.handle if self.body is not None else None
+        return bool(V.lib().vs_run_persistent(self.step.handle, body, int(n_steps)))
+
 
 class Batch:
     """Many independent simulations advanced together: per time step one body launch, one
