@@ -241,8 +241,8 @@ def batched_vs_sequential(torch, steps, n_cases=64, seed=3):
             "time_steps": steps, "sequential_plain_mlups": round(m_seq, 1), "batched_mlups": round(m_bat, 1),
             "batched_over_sequential": round(m_bat / m_seq, 2),
             "launch_shape": {"threads_per_block": batch.threads_per_block,
-                             "steps_per_graph": batch.steps_per_graph},
-            "tuning_ms_per_step": {f"{k[0]}x{k[1]}": round(v, 4) for k, v in tuned.items()}}
+                             "steps_per_graph": batch.steps_per_graph, "nodes_per_thread": batch.nodes_per_thread},
+            "tuning_ms_per_step": {f"{k[0]}x{k[1]}x{k[2]}": round(v, 4) for k, v in tuned.items()}}
 
 
 def adjoint_over_forward(torch, steps):

@@ -345,6 +345,10 @@ int vs_batch_plan_destroy(vs_batch_plan* plan);
 /* Launch shape: threads per block of the grid launches (32, 64, 128, 256) and the number
  * of middle time steps captured per CUDA graph (0: no graph; rounded down to even). */
 int vs_batch_set_launch(vs_batch_plan* plan, int threads_per_block, int steps_per_graph);
+/* Nodes per thread of the main grid launch (1 or 2: two nodes' loads in flight per thread).
+ * Results do not depend on it.  No counterpart in the reference (the batch is this
+ * library's). */
+int vs_batch_set_nodes_per_thread(vs_batch_plan* plan, int nodes_per_thread);
 /* n_steps steps of every case; case k ping-pongs between f_a[k] (input) and f_b[k] as in
  * vs_run.  Device parameter tables are built on the first call for a set of buffers (a
  * synchronous upload); graphs need a non-default stream (else steps are launched one by

@@ -134,6 +134,7 @@ _SIGS = {
     "vs_batch_plan_create": (_i, [C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), _i, C.POINTER(C.c_void_p)]),
     "vs_batch_plan_destroy": (_i, [_p]),
     "vs_batch_set_launch": (_i, [_p, _i, _i]),
+    "vs_batch_set_nodes_per_thread": (_i, [_p, _i]),
     "vs_batch_run": (_i, [_p, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), _i, _p]),
     "vs_post": (_i, [_i, _i, _i, _p, _p, _i, _i, _i, _p, _p, _p]),
     "vs_post_pressure": (_i, [_i, _p, _l, _d, _p, _p]),

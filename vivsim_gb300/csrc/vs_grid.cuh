@@ -318,6 +318,30 @@ __device__ __forceinline__ void step_block2(const StepParams<L9, T>& P, int bx, 
   step_block2_t<T, COLL, FEAT>(P, bx, by, (int)threadIdx.x, (int)blockDim.x);
 }
 
+// NPT nodes per thread, `width` apart along y, all NPT nodes' populations loaded before the
+// first is updated (the loads in flight of NPT threads).  No regions.
+template <typename T, int COLL, int FEAT, int NPT>
+__device__ __forceinline__ void step_block_n_t(const StepParams<L9, T>& P, int bx, int by, int tid, int width) {
+  const int x = by;
+  bool on[NPT];
+  int pp[NPT];
+  T f[NPT][9];
+#pragma unroll
+  for (int k = 0; k < NPT; ++k) {
+    const int y = (bx * NPT + k) * width + tid;
+    on[k] = y < P.ny && !((FEAT & kFeatSkip) && skipped(P, x, y, 0));
+    pp[k] = x * P.ny + y;
+  }
+#pragma unroll
+  for (int i = 0; i < 9; ++i)
+#pragma unroll
+    for (int k = 0; k < NPT; ++k)
+      if (on[k]) f[k][i] = VS_IN_RANGE(pp[k], P.n, P.status) ? pop_load<FEAT>(P.fin + (size_t)i * P.n + pp[k]) : T(0);
+#pragma unroll
+  for (int k = 0; k < NPT; ++k)
+    if (on[k]) step_node<L9, T, COLL, FEAT>(P, x, (bx * NPT + k) * width + tid, 0, pp[k], f[k]);
+}
+
 // The main launch of a batch walks each case's nodes in memory order: chunk j of a
 // case is nodes [j * blockDim.x, (j + 1) * blockDim.x) of its flattened grid, so a block is
 // full whatever the case's row length (rows of 64 nodes would leave 3/4 of a 256-thread
@@ -343,6 +367,41 @@ __device__ __forceinline__ void step_flat(const StepParams<L, T>& P, int chunk) 
 #pragma unroll
   for (int i = 0; i < L::Q; ++i) f[i] = VS_IN_RANGE(p, P.n, P.status) ? __ldg(P.fin + (size_t)i * P.n + p) : T(0);
   step_node<L, T, COLL, FEAT>(P, x, y, z, p, f);
+}
+
+// step_flat with two nodes per thread, blockDim.x apart in memory order (chunk j of the
+// case: nodes [2 j blockDim.x, 2 (j + 1) blockDim.x)); both nodes' populations are loaded
+// before either is updated.
+template <class L, typename T, int COLL, int FEAT>
+__device__ __forceinline__ void step_flat2(const StepParams<L, T>& P, int chunk) {
+  int p[2], x[2], y[2], z[2];
+  bool on[2];
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    p[k] = (2 * chunk + k) * (int)blockDim.x + (int)threadIdx.x;
+    on[k] = p[k] < P.n;
+    if constexpr (L::D == 2) {
+      x[k] = p[k] / P.ny;
+      y[k] = p[k] - x[k] * P.ny;
+      z[k] = 0;
+    } else {
+      const int syz = P.ny * P.nz;
+      x[k] = p[k] / syz;
+      const int r = p[k] - x[k] * syz;
+      y[k] = r / P.nz;
+      z[k] = r - y[k] * P.nz;
+    }
+    on[k] = on[k] && !((FEAT & kFeatSkip) && skipped(P, x[k], y[k], z[k]));
+  }
+  T f[2][L::Q];
+#pragma unroll
+  for (int i = 0; i < L::Q; ++i)
+#pragma unroll
+    for (int k = 0; k < 2; ++k)
+      if (on[k]) f[k][i] = VS_IN_RANGE(p[k], P.n, P.status) ? __ldg(P.fin + (size_t)i * P.n + p[k]) : T(0);
+#pragma unroll
+  for (int k = 0; k < 2; ++k)
+    if (on[k]) step_node<L, T, COLL, FEAT>(P, x[k], y[k], z[k], p[k], f[k]);
 }
 
 }  // namespace vs

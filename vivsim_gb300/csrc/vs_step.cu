@@ -74,6 +74,14 @@ __global__ void __launch_bounds__(256, 6) k_step_batch_flat(const StepParams<L, 
   step_flat<L, T, COLL, FEAT>(Ps[cb.x], cb.y);
 }
 
+// Two nodes per thread (the loads of two nodes in flight; 4 blocks of 256 threads per SM).
+template <class L, typename T, int COLL, int FEAT>
+__global__ void __launch_bounds__(256, 4) k_step_batch_flat2(const StepParams<L, T>* __restrict__ Ps,
+                                                          const int2* __restrict__ blk) {
+  const int2 cb = blk[blockIdx.x];
+  step_flat2<L, T, COLL, FEAT>(Ps[cb.x], cb.y);
+}
+
 // Grid kernel over many independent lattices in one launch: block b works on lattice
 // blk[b].x, as block blk[b].y of that lattice's own launch geometry (chunks x rows,
 // row-major), with that lattice's parameters (the batch's region launch).
@@ -1783,6 +1791,7 @@ __global__ void __launch_bounds__(kBody3Threads) k_body3d_fused(const __grid_con
 // body kernel's start-up behind the grid launch's traffic.
 constexpr int kRunThreads = 384;
 constexpr int kRunGroup = 128;
+constexpr int kRunNodes = 4;  // nodes per thread of a grid tile (their loads in flight together)
 
 template <typename T>
 struct VivRunParams {
@@ -1800,51 +1809,35 @@ struct VivRunParams {
   int chunks_w;                 // plane tiles per plane
 };
 
-// Barrier over every CTA of the run, agreed within each cluster.  After a cluster barrier
-// the cluster's rank-0 CTA arrives at the grid-wide count (one arrival per cluster) and
-// waits for the generation to move on (bounded: kGridBarrierLimit polls, or an abort seen);
-// a second cluster barrier releases the cluster, and every CTA of it reads rank 0's
-// verdict, so a cluster never splits over a timeout and its CTAs keep meeting at the same
-// cluster barriers.  false: the run aborts (VS_ERR_TIMEOUT recorded).
-__device__ __forceinline__ bool run_barrier(unsigned* bar, int* status, int* ok_s) {
+// Barrier over every CTA of the run, agreed within each cluster.  After a cluster barrier,
+// thread 0 of the cluster's rank-0 CTA adds one to word 0 (release; bit 31: abort) and polls
+// it until it reaches (k + 1) x clusters for the k-th barrier of the launch, then acquires;
+// it gives up after kGridBarrierLimit polls (abort bit, VS_ERR_TIMEOUT), as does every
+// poller that sees the bit.  A second cluster barrier releases the cluster, whose CTAs all
+// read rank 0's verdict, so a cluster never splits over a timeout and its CTAs keep meeting
+// at the same cluster barriers.  false: the run aborts.
+__device__ __forceinline__ bool run_barrier(unsigned* bar, int* status, int k, int* ok_s) {
   namespace cg = cooperative_groups;
   cg::cluster_group cluster = cg::this_cluster();
-  __syncthreads();
-  if (threadIdx.x == 0) __threadfence();
   cluster.sync();
   if (cluster.block_rank() == 0 && threadIdx.x == 0) {
-    int ok = 1;
-    const unsigned n = gridDim.x / cluster.num_blocks();
-    unsigned gen, abort_flag;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(gen) : "l"(bar + 1) : "memory");
-    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(abort_flag) : "l"(bar + 2) : "memory");
-    if (abort_flag) {
-      ok = 0;
-    } else {
-      __threadfence();
-      const unsigned arrived = atomicAdd(bar, 1u);
-      if (arrived == n - 1) {
-        atomicExch(bar, 0u);
-        __threadfence();
-        asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(bar + 1), "r"(gen + 1) : "memory");
-      } else {
-        int it = 0;
-        for (;;) {
-          unsigned g, ab;
-          asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(g) : "l"(bar + 1) : "memory");
-          if (g != gen) break;
-          asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(ab) : "l"(bar + 2) : "memory");
-          if (ab || ++it > kGridBarrierLimit) {
-            atomicExch(bar + 2, 1u);
-            atomicMax(status, VS_ERR_TIMEOUT);
-            ok = 0;
-            break;
-          }
-          __nanosleep(32);
-        }
+    const unsigned target = (unsigned)(k + 1) * (gridDim.x / cluster.num_blocks());
+    asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(bar) : "memory");
+    unsigned v;
+    int it = 0;
+    for (;;) {
+      asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(bar) : "memory");
+      if ((v & 0x7fffffffu) >= target || (v & 0x80000000u)) break;
+      if (++it > kGridBarrierLimit) {
+        atomicOr(bar, 0x80000000u);
+        atomicMax(status, VS_ERR_TIMEOUT);
+        v |= 0x80000000u;
+        break;
       }
+      __nanosleep(20);
     }
-    *ok_s = ok;
+    asm volatile("fence.acq_rel.gpu;" ::: "memory");
+    *ok_s = (v & 0x80000000u) ? 0 : 1;
   }
   cluster.sync();
   return *cluster.map_shared_rank(ok_s, 0) != 0;
@@ -1855,7 +1848,6 @@ __global__ void __launch_bounds__(kRunThreads, 1) k_viv_run(const __grid_constan
   namespace cg = cooperative_groups;
   cg::cluster_group cluster = cg::this_cluster();
   __shared__ int ok_s;
-  constexpr int NPT = FastShape<L9, COLL>::NPT;
   const int CL = (int)cluster.num_blocks();
   const bool body = (int)blockIdx.x < CL;
   const int gpc = (int)blockDim.x / kRunGroup, gt = (int)threadIdx.x % kRunGroup;
@@ -1872,26 +1864,21 @@ __global__ void __launch_bounds__(kRunThreads, 1) k_viv_run(const __grid_constan
       for (int t = g0; t < nt; t += ng) {
         if (t < nm) {
           const int by = t / P.chunks_m, bx = t - by * P.chunks_m;
-          if constexpr (NPT == 2) step_block2_t<T, COLL, kFeatSkip>(P.SPm[p][lz], bx, by, gt, kRunGroup);
-          else step_block_t<L9, T, COLL, kFeatSkip>(P.SPm[p][lz], bx, by, gt, kRunGroup);
+          step_block_n_t<T, COLL, kFeatSkip, kRunNodes>(P.SPm[p][lz], bx, by, gt, kRunGroup);
         } else {
           const int u = t - nm, by = u / P.chunks_w, bx = u - by * P.chunks_w;
           step_block_t<L9, T, COLL, kFeatGeneral | kFeatWalls>(P.SPw[p], bx, by, gt, kRunGroup);
         }
       }
     }
-    ok = run_barrier(P.bar, P.status, &ok_s);
+    ok = run_barrier(P.bar, P.status, s, &ok_s);
   }
-  // the last cluster out resets the arrivals and the abort flag for the next launch (the
-  // generation only moves on); a CTA leaves only after its cluster read its verdicts
+  // the last cluster out resets the arrival count (and the abort bit) for the next launch;
+  // a CTA leaves only after its cluster has read rank 0's last verdict
   cluster.sync();
-  if (cluster.block_rank() == 0 && threadIdx.x == 0) {
-    __threadfence();
-    if (atomicAdd(P.bar + 3, 1u) == gridDim.x / (unsigned)CL - 1) {
-      atomicExch(P.bar, 0u);
-      atomicExch(P.bar + 2, 0u);
-      atomicExch(P.bar + 3, 0u);
-    }
+  if (cluster.block_rank() == 0 && threadIdx.x == 0 && atomicAdd(P.bar + 1, 1u) == gridDim.x / (unsigned)CL - 1) {
+    atomicExch(P.bar, 0u);
+    atomicExch(P.bar + 1, 0u);
   }
 }
 
@@ -3236,13 +3223,7 @@ static int viv_run_chunk(const vs_lattice_plan* LP, vs_body_plan* B, void* f_a, 
       P->SPw[p] = SP;
     }
   }
-  int npt = 1;
-  switch (c.collision) {
-    case VS_COLLIDE_BGK: npt = FastShape<L9, VS_COLLIDE_BGK>::NPT; break;
-    case VS_COLLIDE_KBC: npt = FastShape<L9, VS_COLLIDE_KBC>::NPT; break;
-    case VS_COLLIDE_REG: npt = FastShape<L9, VS_COLLIDE_REG>::NPT; break;
-    default: npt = FastShape<L9, VS_COLLIDE_MRT>::NPT; break;
-  }
+  const int npt = kRunNodes;
   P->hist = force_hist ? (float*)force_hist + 3 * (int64_t)s0 : nullptr;
   P->bar = B->d_bar;
   P->status = LP->d_status;
@@ -4013,7 +3994,8 @@ int vs_run(const vs_lattice_plan* lattice, vs_body_plan* body, void* f_a, void* 
     // persistent form: one launch per watchdog interval (or for the whole run)
     const int K = lattice->cfg.watchdog_every;
     for (int s0 = 0; s0 < n_steps;) {
-      const int n = K > 0 ? std::min(K - s0 % K, n_steps - s0) : n_steps - s0;
+      // (at most 2^20 steps per launch: the barrier's arrival count stays below 2^31)
+      const int n = std::min(K > 0 ? std::min(K - s0 % K, n_steps - s0) : n_steps - s0, 1 << 20);
       int rc = viv_run_chunk(lattice, body, f_a, f_b, s0, n, lazy, force_hist, as_stream(stream));
       if (rc) return rc;
       s0 += n;
@@ -4108,6 +4090,8 @@ struct vs_batch_plan {
   std::vector<int> chain_bodies, other_bodies;  // case indices
   int q = 0, dtype = 0, collision = 0, radius = 0;
   int tb = 128;                 // threads per block of the grid launches
+  int npt = 1;                  // nodes per thread of the main launch (1 or 2)
+  int built_npt = 0;
   int spg = 64;                 // default steps per graph
   size_t body_smem = 0;
   std::vector<const void*> fa, fb;  // buffers the device parameters were built for
@@ -4190,7 +4174,8 @@ static int batch_build(vs_batch_plan* bp, void* const* fa, void* const* fb) {
           main[p][first].push_back(P);
           skip_only = skip_only && !P.gw && !P.has_g0 && !P.mask_load && P.n_pre == 0 && P.n_lazy == 0;
           if (p == 0 && first == 1) {  // flat chunks of the case's nodes (k_step_batch_flat)
-            const int nch = (int)((bp->L[k]->n + bp->tb - 1) / bp->tb);
+            const int64_t per = (int64_t)bp->tb * bp->npt;
+            const int nch = (int)((bp->L[k]->n + per - 1) / per);
             for (int j = 0; j < nch; ++j) bm.push_back(make_int2(idx, j));
           }
         }
@@ -4224,6 +4209,7 @@ static int batch_build(vs_batch_plan* bp, void* const* fa, void* const* fb) {
   bp->fa.assign(fa, fa + bp->n);
   bp->fb.assign(fb, fb + bp->n);
   bp->built_tb = bp->tb;
+  bp->built_npt = bp->npt;
   return VS_OK;
 }
 
@@ -4252,12 +4238,17 @@ static int batch_step_t(vs_batch_plan* bp, int s, int n_steps, void* const* fa, 
     }
   }
   if (bp->n_blk_main > 0) {
-    if (bp->main_skip_only)
-      k_step_batch_flat<L, T, COLL, kFeatSkip><<<bp->n_blk_main, bp->tb, 0, st>>>(
-          (const StepParams<L, T>*)bp->d_main[p][first], bp->d_blk_main);
-    else
-      k_step_batch_flat<L, T, COLL, kFeatGeneral><<<bp->n_blk_main, bp->tb, 0, st>>>(
-          (const StepParams<L, T>*)bp->d_main[p][first], bp->d_blk_main);
+    const StepParams<L, T>* mp = (const StepParams<L, T>*)bp->d_main[p][first];
+    if (bp->npt == 2) {
+      if (bp->main_skip_only)
+        k_step_batch_flat2<L, T, COLL, kFeatSkip><<<bp->n_blk_main, bp->tb, 0, st>>>(mp, bp->d_blk_main);
+      else
+        k_step_batch_flat2<L, T, COLL, kFeatGeneral><<<bp->n_blk_main, bp->tb, 0, st>>>(mp, bp->d_blk_main);
+    } else if (bp->main_skip_only) {
+      k_step_batch_flat<L, T, COLL, kFeatSkip><<<bp->n_blk_main, bp->tb, 0, st>>>(mp, bp->d_blk_main);
+    } else {
+      k_step_batch_flat<L, T, COLL, kFeatGeneral><<<bp->n_blk_main, bp->tb, 0, st>>>(mp, bp->d_blk_main);
+    }
   }
   if (fork) {
     e = cudaEventRecord(bp->ev_join, bp->side);
@@ -4408,6 +4399,13 @@ int vs_batch_set_launch(vs_batch_plan* plan, int threads_per_block, int steps_pe
   return VS_OK;
 }
 
+int vs_batch_set_nodes_per_thread(vs_batch_plan* plan, int nodes_per_thread) {
+  VS_REQUIRE(plan, "vs_batch_set_nodes_per_thread: null plan");
+  VS_REQUIRE(nodes_per_thread == 1 || nodes_per_thread == 2, "vs_batch_set_nodes_per_thread: 1 or 2");
+  plan->npt = nodes_per_thread;
+  return VS_OK;
+}
+
 int vs_batch_run(vs_batch_plan* plan, void* const* f_a, void* const* f_b, int n_steps, void* stream) {
   VS_REQUIRE(plan && f_a && f_b && n_steps >= 0, "vs_batch_run: bad arguments");
   for (int k = 0; k < plan->n; ++k)
@@ -4425,7 +4423,7 @@ int vs_batch_run(vs_batch_plan* plan, void* const* f_a, void* const* f_b, int n_
       Bk->parity = 0;
     }
   }
-  bool same = plan->built_tb == plan->tb && (int)plan->fa.size() == plan->n;
+  bool same = plan->built_tb == plan->tb && plan->built_npt == plan->npt && (int)plan->fa.size() == plan->n;
   for (int k = 0; same && k < plan->n; ++k) same = plan->fa[k] == f_a[k] && plan->fb[k] == f_b[k];
   if (!same) {
     const int rc = dispatch(plan->q, plan->dtype, [&](auto l, auto t) -> int {

@@ -289,7 +289,7 @@ class Batch:
     """Many independent simulations advanced together: per time step one body launch, one
     grid launch over all cases and one launch over all body boxes (vs_batch_run)."""
 
-    def __init__(self, sims, threads_per_block=128, steps_per_graph=64):
+    def __init__(self, sims, threads_per_block=128, steps_per_graph=64, nodes_per_thread=1):
         self.sims = list(sims)
         n = len(self.sims)
         if n == 0:
@@ -299,29 +299,33 @@ class Batch:
         h = C.c_void_p()
         V.call("vs_batch_plan_create", lat, bod, n, C.byref(h))
         self.handle = h
-        self.set_launch(threads_per_block, steps_per_graph)
+        self.set_launch(threads_per_block, steps_per_graph, nodes_per_thread)
 
-    def set_launch(self, threads_per_block=128, steps_per_graph=64):
+    def set_launch(self, threads_per_block=128, steps_per_graph=64, nodes_per_thread=1):
         V.call("vs_batch_set_launch", self.handle, int(threads_per_block), int(steps_per_graph))
+        V.call("vs_batch_set_nodes_per_thread", self.handle, int(nodes_per_thread))
         self.threads_per_block, self.steps_per_graph = int(threads_per_block), int(steps_per_graph)
+        self.nodes_per_thread = int(nodes_per_thread)
 
     def tune(self, trial_steps=64, candidates=None):
-        """Pick the launch shape (threads per block, steps per graph) with the shortest time
-        for `trial_steps` steps; each candidate runs twice (the first run builds its tables
-        and graph) and the second is timed with CUDA events.  Advances the simulations by
-        2 * trial_steps * len(candidates) steps.  Returns {(tb, spg): ms per step}."""
+        """Pick the launch shape (threads per block, steps per graph, nodes per thread of the
+        main launch) with the shortest time for `trial_steps` steps; each candidate runs
+        twice (the first run builds its tables and graph) and the second is timed with CUDA
+        events.  Advances the simulations by 2 * trial_steps * len(candidates) steps.
+        Returns {(tb, spg, npt): ms per step}."""
         if candidates is None:
-            candidates = [(tb, spg) for tb in (64, 128, 256) for spg in (16, 64)]
+            candidates = [(tb, spg, npt) for npt in (1, 2) for tb in (64, 128, 256) for spg in (16, 64)]
         times = {}
-        for tb, spg in candidates:
-            self.set_launch(tb, spg)
+        for cand in candidates:
+            tb, spg, npt = (tuple(cand) + (1,))[:3]
+            self.set_launch(tb, spg, npt)
             self.run(trial_steps)
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record()
             self.run(trial_steps)
             e1.record()
             torch.cuda.synchronize()
-            times[(tb, spg)] = e0.elapsed_time(e1) / trial_steps
+            times[(tb, spg, npt)] = e0.elapsed_time(e1) / trial_steps
         best = min(times, key=times.get)
         self.set_launch(*best)
         return times
