@@ -84,7 +84,9 @@ def compare_adjoint(steps):
     return {"case": "adjoint cylinder D2Q9 BGK 512 x 256, 64 markers", "steps": steps,
             "J_rel_err": abs(J32 - J64) / abs(J64), "dU0_rel_err": abs(u32 - u64) / abs(u64),
             "dK_rel_err": abs(k32 - k64) / abs(k64),
-            "doffsets_rel_err": float(abs(o32 - o64).max() / abs(o64).max())}
+            "doffsets_rel_err": float(abs(o32 - o64).max() / abs(o64).max()),
+            "values_f32": {"J": float(J32), "dU0": float(u32), "dK": float(k32)},
+            "values_f64": {"J": float(J64), "dU0": float(u64), "dK": float(k64)}}
 
 
 def compare_sweep(steps, n_cases=64):
