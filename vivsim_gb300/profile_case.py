@@ -3,11 +3,12 @@
     python -m vivsim_gb300.profile_case --case periodic2d --n 4096 --steps 3
     python -m vivsim_gb300.profile_case --case sphere3d --steps 3
     python -m vivsim_gb300.profile_case --case viv2d --steps 20 --graph
-    python -m vivsim_gb300.profile_case --batch 64 --steps 8
+    python -m vivsim_gb300.profile_case --batch 64 --steps 8 [--npt 2]
     python -m vivsim_gb300.profile_case --adjoint --steps 400
 
 Each step launches the body kernel (cases with a body), the grid kernel ``k_step`` and
-the face kernel(s); ``--grid-only`` launches only ``k_step``.  ``--batch N`` runs the
+the face kernel(s); ``--grid-only`` launches only the grid kernel (with ``--no-body`` the
+whole grid's bulk launch ``k_step_fast``, as bench.py's roofline times it).  ``--batch N`` runs the
 N-case VIV sweep as one batch (seed 3, as bench.py), ``--adjoint`` the differentiable
 cylinder's forward and reverse sweep over ``--steps`` steps.  Prints the mean step time.
 """
@@ -29,12 +30,15 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--graph", action="store_true")
     ap.add_argument("--grid-only", action="store_true")
+    ap.add_argument("--no-body", action="store_true",
+                    help="with --grid-only: the whole grid without the body (the bulk launch bench.py times)")
+    ap.add_argument("--npt", type=int, default=1, help="--batch: nodes per thread of the main launch")
     ap.add_argument("--variant", choices=["auto", "plain", "tma"], default="auto")
     ap.add_argument("--batch", type=int, default=0, help="run the N-case VIV sweep as one batch")
     ap.add_argument("--adjoint", action="store_true", help="forward + reverse sweep of the adjoint cylinder")
     a = ap.parse_args()
     if a.batch:
-        return batch(a.batch, a.steps)
+        return batch(a.batch, a.steps, a.npt)
     if a.adjoint:
         return adjoint(a.steps)
     kw = {}
@@ -53,7 +57,7 @@ def main():
         e0.record()
         if a.grid_only:
             src, dst = sim.f, torch.empty_like(sim.f)
-            bh = body.handle if body is not None else None
+            bh = body.handle if body is not None and not a.no_body else None
             for _ in range(a.steps):
                 V.call("vs_step_grid_only", step.handle, bh, V.ptr(src), V.ptr(dst), V.stream())
                 src, dst = dst, src
@@ -75,13 +79,14 @@ def _timed(fn):
     return e0.elapsed_time(e1)
 
 
-def batch(n_cases, steps):
+def batch(n_cases, steps, npt=1):
     from . import solver
     cases = configs.viv_sweep(n_cases, 3)
     nodes = sum(math.prod(c["shape"]) for c in cases)
     stream = torch.cuda.Stream()
     with torch.cuda.stream(stream):
-        b = solver.Batch([configs.build_solver(c)[2] for c in cases], threads_per_block=64, steps_per_graph=0)
+        b = solver.Batch([configs.build_solver(c)[2] for c in cases], threads_per_block=64, steps_per_graph=0,
+                         nodes_per_thread=npt)
         b.run(2)
         torch.cuda.synchronize()
         ms = _timed(lambda: b.run(steps)) / steps
