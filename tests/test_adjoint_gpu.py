@@ -83,3 +83,39 @@ def test_adjoint_float32_runs_close_to_float64(A):
     assert abs(g32[0] - g64[0]) <= 1e-2 * abs(g64[0])
     assert abs(g32[1] - g64[1]) <= 1e-2 * abs(g64[1])
     assert np.max(np.abs(g32[2] - g64[2])) <= 1e-2 * np.max(np.abs(g64[2]))
+
+
+def test_adjoint_config4_size_matches_finite_differences(A):
+    """The differentiable-cylinder configuration itself (512 x 256, D = 20, Re 100, 64
+    markers with N(0, 0.1) radial offsets, 4000 steps, checkpoints every 100, objective the
+    mean drag over the second half), in FP64: the adjoint gradients against central finite
+    differences with h = 1e-3 relative (1e-4 absolute for an offset)."""
+    full = dict(nx=512, ny=256, D=20.0, Re=100.0, n_markers=64, n_steps=4000, checkpoint_every=100, obj_start=2000,
+                dtype=torch.float64)
+    off = np.random.default_rng(2).normal(0.0, 0.1, 64)
+
+    def J(U0, K, o):
+        p = A.CylinderDrag(U0=U0, stiffness=K, offsets=o, **full)
+        v = p.forward(keep_checkpoints=False)
+        p.close()
+        return v
+
+    base = A.CylinderDrag(U0=0.05, offsets=off, **full)
+    K = base.stiffness
+    J0 = base.forward()
+    gU0, gK, goff = base.backward()
+    base.close()
+    h = 1e-3
+    fd_U0 = (J(0.05 * (1 + h), K, off) - J(0.05 * (1 - h), K, off)) / (2 * 0.05 * h)
+    fd_K = (J(0.05, K * (1 + h), off) - J(0.05, K * (1 - h), off)) / (2 * K * h)
+    print(f"\nconfig 4: J {J0:.12e}; dJ/dU0 adjoint {gU0:.10e} fd {fd_U0:.10e}; dJ/dK adjoint {gK:.6e} fd {fd_K:.6e}")
+    assert abs(gU0 - fd_U0) <= 1e-3 * abs(fd_U0), (gU0, fd_U0)
+    scale = np.max(np.abs(goff))
+    assert abs(gK - fd_K) <= 1e-3 * max(abs(fd_K), 1e-6 * abs(fd_U0)), (gK, fd_K)
+    for m in (3, 40):
+        op, om = off.copy(), off.copy()
+        op[m] += 1e-4
+        om[m] -= 1e-4
+        fd = (J(0.05, K, op) - J(0.05, K, om)) / 2e-4
+        print(f"dJ/d offset[{m}] adjoint {goff[m]:.8e} fd {fd:.8e}")
+        assert abs(goff[m] - fd) <= 1e-3 * max(abs(fd), 1e-2 * scale), (m, goff[m], fd)
