@@ -97,8 +97,11 @@ __device__ __forceinline__ void pop_store(T* p, T v) {
   else *p = v;
 }
 
+// gext: the node's IB force, given by the caller (the cluster-form body kernel holds its
+// window's force in shared memory), in place of the lookup in the force window P.gw.
 template <class L, typename T, int COLL, int FEAT>
-__device__ __forceinline__ void step_node(const StepParams<L, T>& P, int x, int y, int z, int p, T* f) {
+__device__ __forceinline__ void step_node(const StepParams<L, T>& P, int x, int y, int z, int p, T* f,
+                                          const T* gext = nullptr) {
   constexpr int Q = L::Q;
   const int syz = P.ny * P.nz;
 
@@ -144,7 +147,11 @@ __device__ __forceinline__ void step_node(const StepParams<L, T>& P, int x, int 
 #pragma unroll
     for (int d = 0; d < L::D; ++d) g[d] = P.g0[d];
   }
-  if ((FEAT & kFeatForce) && P.gw) {
+  if ((FEAT & kFeatForce) && gext) {
+#pragma unroll
+    for (int d = 0; d < L::D; ++d) g[d] = has_g ? g[d] + gext[d] : gext[d];
+    has_g = true;
+  } else if ((FEAT & kFeatForce) && P.gw) {
     const int wx = x - P.meta[META_OX], wy = y - P.meta[META_OY], wz = z - P.meta[META_OZ];
     const int ex = P.meta[META_WX], ey = P.meta[META_WY], ez = P.meta[META_WZ];
     if (wx >= 0 && wx < ex && wy >= 0 && wy < ey && wz >= 0 && wz < ez) {

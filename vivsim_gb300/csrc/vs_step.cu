@@ -1125,7 +1125,11 @@ __device__ __forceinline__ void body2d_cluster_step(const BodyParams<T>& B, cons
   T* U = Ft + 2 * M;            // [2M] own markers' velocity
   T* prod = U + 2 * M;          // [2 nt] interpolation products (generic radius)
   T* xs = prod + 2 * nt;        // [2M] marker positions X0 + d, Y0 + d
-  int* fxy = (int*)(xs + 2 * M);     // [2M]
+  // the IB force of this CTA's window nodes: node k belongs to CTA (k mod CL nt) / nt, at
+  // slot (k mod CL nt) mod nt + nt (k / CL nt); x components, then y after GW entries
+  const int GW = nt * ((EX * EY + CL * nt - 1) / (CL * nt));
+  T* gl = xs + 2 * M;           // [2 GW]
+  int* fxy = (int*)(gl + 2 * GW);    // [2M]
   unsigned* cm = (unsigned*)(fxy + 2 * M);  // [nt] contributor mask of the thread's pair
   int* flags = (int*)(cm + nt);      // [0] a pair of this CTA left the predicted region, [1..2] min corner
   // every CTA of the cluster must be running before any distributed shared memory access:
@@ -1193,9 +1197,8 @@ __device__ __forceinline__ void body2d_cluster_step(const BodyParams<T>& B, cons
     B.meta[META_OX] = ox; B.meta[META_OY] = oy; B.meta[META_OZ] = 0;
     B.meta[META_WX] = EX; B.meta[META_WY] = EY; B.meta[META_WZ] = 1;
   }
-  // the force window starts at zero (split over the cluster)
-  if (region_ok)
-    for (int k = kw; k < 2 * NB; k += CL * nt) B.gw[k] = T(0);
+  // the window force starts at zero (remote writes come after several cluster barriers)
+  for (int i = tid; i < 2 * GW; i += nt) gl[i] = T(0);
   __syncthreads();
   // every marker's stencil corner (and their minimum, the next prediction); weights of the
   // own markers and their +-K neighbours
@@ -1344,13 +1347,16 @@ __device__ __forceinline__ void body2d_cluster_step(const BodyParams<T>& B, cons
       publish(Ft, t0, t1, true);
       cluster.sync();
     }
-    // g = spread(F_total): each pair writes its node's sum
+    // g = spread(F_total): each pair writes its node's sum into the node's owner CTA
     if (has_pair) {
       T g0, g1;
       chain_node_sum<T, WD>(msk, a0, nA, b0, nxp, nyp, fxy, W, Ft, g0, g1);
       const int k = (nxp - ox) * EY + (nyp - oy);
-      B.gw[k] = g0;
-      B.gw[NB + k] = g1;
+      const int kr = k % (CL * nt);
+      T* dst = cluster.map_shared_rank(gl, kr / nt);
+      const int li = kr % nt + nt * (k / (CL * nt));
+      dst[li] = g0;
+      dst[GW + li] = g1;
     }
   } else if (rank == 0 && tid == 0) {
     B.meta[META_STATUS] = VS_ERR_RANGE;
@@ -1368,15 +1374,21 @@ __device__ __forceinline__ void body2d_cluster_step(const BodyParams<T>& B, cons
   }
   // the nodes of the predicted window, which the concurrent grid launch skips (the same
   // slot gives it the same window); lazy face planes are another launch's
-  if (wp >= 0) step_node<L9, T, COLL, kFeatGeneral>(SP, wx, wy, 0, wp, fw);
-  for (int k = kw + CL * nt; k < NB; k += CL * nt) {
+  // (their force from shared memory; with the window out of its region no force, as the
+  // emptied window descriptor gives the per-node lookup)
+  if (wp >= 0) {
+    const T gn[2] = {gl[tid], gl[GW + tid]};
+    step_node<L9, T, COLL, kFeatGeneral>(SP, wx, wy, 0, wp, fw, ok ? gn : nullptr);
+  }
+  for (int k = kw + CL * nt, j = 1; k < NB; k += CL * nt, ++j) {
     const int x = ox + k / EY, y = oy + k % EY;
     if (x < 0 || x >= SP.nx || y < 0 || y >= SP.ny || (SP.skip_walls && (x == 0 || x == SP.nx - 1))) continue;
     const int p = x * SP.ny + y;
     T f[9];
 #pragma unroll
     for (int i = 0; i < 9; ++i) f[i] = __ldg(SP.fin + (size_t)i * SP.n + p);
-    step_node<L9, T, COLL, kFeatGeneral>(SP, x, y, 0, p, f);
+    const T gn[2] = {gl[tid + nt * j], gl[GW + tid + nt * j]};
+    step_node<L9, T, COLL, kFeatGeneral>(SP, x, y, 0, p, f, ok ? gn : nullptr);
   }
 }
 
@@ -1387,10 +1399,11 @@ __global__ void __launch_bounds__(kClusterThreads) k_body2d_cluster(const __grid
 }
 
 template <typename T>
-static size_t body2d_cluster_smem(int M, int R, int nt) {
+static size_t body2d_cluster_smem(int M, int R, int nt, int CL, int NB) {
   const size_t S = 4 * R * R;
-  return sizeof(T) * (M * S + 10 * (size_t)M + 2 * (size_t)nt) + sizeof(int) * (2 * (size_t)M + (size_t)nt + 4) +
-         16;
+  const size_t GW = (size_t)nt * ((NB + CL * nt - 1) / (CL * nt));
+  return sizeof(T) * (M * S + 10 * (size_t)M + 2 * (size_t)nt + 2 * GW) +
+         sizeof(int) * (2 * (size_t)M + (size_t)nt + 4) + 16;
 }
 
 template <typename T>
@@ -3708,8 +3721,8 @@ int vs_body_plan_create(const vs_body_cfg* cfg, const vs_lattice_plan* lattice, 
       if (cl_ok && c <= 8 && c <= M) {
         b->cl_size = c;
         b->cl_threads = th;
-        b->cl_smem = ts == 8 ? body2d_cluster_smem<double>(M, cfg->radius, th)
-                             : body2d_cluster_smem<float>(M, cfg->radius, th);
+        b->cl_smem = ts == 8 ? body2d_cluster_smem<double>(M, cfg->radius, th, c, NB)
+                             : body2d_cluster_smem<float>(M, cfg->radius, th, c, NB);
         if ((int64_t)b->cl_smem <= optin) {
           e = cluster_attr(cfg->dtype, cfg->radius, lattice->cfg.collision, optin);
           if (e != cudaSuccess) return fail(e);
@@ -3722,7 +3735,7 @@ int vs_body_plan_create(const vs_body_cfg* cfg, const vs_lattice_plan* lattice, 
     if (b->cluster && ts == 4 && cfg->radius == 2) {
       int coop = 0;
       cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
-      b->run_smem = body2d_cluster_smem<float>(M, 2, kRunThreads);
+      b->run_smem = body2d_cluster_smem<float>(M, 2, kRunThreads, b->cl_size, (b->cap[0] + 2) * (b->cap[1] + 2));
       int ctas = 0;
       if (coop && (int64_t)b->run_smem <= optin && viv_run_setup(b, lattice->cfg.collision, ctas) != cudaSuccess) {
         cudaGetLastError();
