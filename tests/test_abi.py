@@ -75,6 +75,18 @@ def test_refinement_and_watchdog_validation_without_gpu(lib):
     assert lib.vs_selftest_bounded_wait(1 << 21, p, None) == 1
 
 
+def test_run_form_and_batch_shape_queries_without_gpu(lib):
+    """vs_run_persistent answers without a CUDA call (0 for no plan or fewer than two steps),
+    and the batch's nodes-per-thread setter validates its arguments first."""
+    import ctypes as C
+    assert lib.vs_run_persistent(None, None, 100) == 0
+    assert lib.vs_run_persistent(C.c_void_p(64), None, 1) == 0
+    assert lib.vs_batch_set_nodes_per_thread(None, 2) == 1
+    assert b"null plan" in lib.vs_last_error()
+    assert lib.vs_batch_set_nodes_per_thread(C.c_void_p(64), 3) == 1
+    assert b"1 or 2" in lib.vs_last_error()
+
+
 def test_plan_validation_without_gpu(lib):
     """A lattice plan is validated before it allocates: bad wall combinations raise."""
     from vivsim_gb300 import _lib as V
