@@ -48,16 +48,21 @@ __global__ void __launch_bounds__(256) k_step(const __grid_constant__ StepParams
 // nodes x 128 threads, 8 blocks 0.90; D2Q9 BGK and MRT 256 threads, 8 blocks 0.99 and 0.93;
 // D3Q19 BGK and REG 128 threads, 10 blocks 0.96 and 0.95; D3Q19 KBC 64 threads, 16 blocks
 // 0.80 (the general kernel: 0.69-0.83).
+// MINB_SKIP: the D2Q9 launch beside a 2-D body (the skip tests compiled in) holds 6 blocks
+// per SM: the VIV step (1024 x 512, KBC) replays at 13.3 us against 14.0 us with 8, its
+// bulk launch alone taking the same 8.7 us either way.
 template <class L, int COLL>
 struct FastShape {
   static constexpr bool heavy3 = L::Q == 19 && (COLL == VS_COLLIDE_KBC || COLL == VS_COLLIDE_MRT);
   static constexpr int NPT = (L::Q == 9 && COLL == VS_COLLIDE_KBC) ? 2 : 1;
   static constexpr int TB = L::Q == 9 ? (NPT == 2 ? 128 : 256) : (heavy3 ? 64 : 128);
   static constexpr int MINB = L::Q == 9 ? 8 : (heavy3 ? 16 : 10);
+  static constexpr int MINB_SKIP = L::Q == 9 ? 6 : MINB;
 };
 
 template <class L, typename T, int COLL, int FEAT>
-__global__ void __launch_bounds__(FastShape<L, COLL>::TB, FastShape<L, COLL>::MINB)
+__global__ void __launch_bounds__(FastShape<L, COLL>::TB,
+                                  (FEAT & kFeatSkip) ? FastShape<L, COLL>::MINB_SKIP : FastShape<L, COLL>::MINB)
     k_step_fast(const __grid_constant__ StepParams<L, T> P) {
   if constexpr (FastShape<L, COLL>::NPT == 2) step_block2<T, COLL, FEAT>(P, blockIdx.x, blockIdx.y);
   else step_block<L, T, COLL, FEAT>(P, blockIdx.x, blockIdx.y);
