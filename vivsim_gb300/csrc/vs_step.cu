@@ -1832,7 +1832,7 @@ struct VivRunParams {
 // it until it reaches (k + 1) x clusters for the k-th barrier of the launch, then acquires;
 // it gives up after kGridBarrierLimit polls (abort bit, VS_ERR_TIMEOUT), as does every
 // poller that sees the bit.  A second cluster barrier releases the cluster, whose CTAs all
-// read rank 0's verdict, so a cluster never splits over a timeout and its CTAs keep meeting
+// read rank 0's decision, so a cluster never splits over a timeout and its CTAs keep meeting
 // at the same cluster barriers.  false: the run aborts.
 __device__ __forceinline__ bool run_barrier(unsigned* bar, int* status, int k, int* ok_s) {
   namespace cg = cooperative_groups;
@@ -1892,7 +1892,7 @@ __global__ void __launch_bounds__(kRunThreads, 1) k_viv_run(const __grid_constan
     ok = run_barrier(P.bar, P.status, s, &ok_s);
   }
   // the last cluster out resets the arrival count (and the abort bit) for the next launch;
-  // a CTA leaves only after its cluster has read rank 0's last verdict
+  // a CTA leaves only after its cluster has read rank 0's last decision
   cluster.sync();
   if (cluster.block_rank() == 0 && threadIdx.x == 0 && atomicAdd(P.bar + 1, 1u) == gridDim.x / (unsigned)CL - 1) {
     atomicExch(P.bar, 0u);
