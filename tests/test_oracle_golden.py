@@ -495,3 +495,27 @@ def test_oracle_streaming_is_a_permutation():
         back = L.streaming(g[list(opp)])[list(opp)]
         assert np.array_equal(back, f)
         assert np.allclose(g.sum(axis=tuple(range(1, g.ndim))), f.sum(axis=tuple(range(1, f.ndim))))
+
+
+def test_oracle_drift_measurement():
+    """oracle.drift: the perturbed start differs from the original by exactly one float32 ulp
+    in population 0 at every 97th node; after a few cavity steps the float32 run sits within
+    float32 rounding of the float64 run, and the one-ulp float64 pair stays far closer."""
+    import subprocess
+    import sys
+    from conftest import ROOT
+    from oracle.drift import perturbed
+    f0 = np.random.default_rng(0).uniform(0.01, 0.2, (9, 20, 30)).astype(np.float32)
+    fp = perturbed(f0)
+    flat0, flatp = f0.reshape(9, -1), fp.reshape(9, -1)
+    changed = np.nonzero(flat0 != flatp)
+    assert set(changed[0]) == {0} and np.array_equal(changed[1], np.arange(0, 600, 97))
+    assert np.all(flatp[0, ::97] == np.nextafter(flat0[0, ::97], np.float32(2.0)))
+    out = subprocess.run([sys.executable, "-m", "oracle.drift", "--case", "cavity", "--steps", "3", "--perturb"],
+                         cwd=ROOT, capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stderr[-2000:]
+    import json
+    d = json.loads(out.stdout.strip().splitlines()[-1])
+    assert d["steps"] == 3
+    assert 0.0 < d["oracle32_vs_64_u"] < 1e-5 and 0.0 < d["oracle32_vs_64_rho"] < 1e-5
+    assert d["perturbed64_vs_64_u"] < 1e-6
