@@ -240,6 +240,13 @@ int vs_lattice_plan_destroy(vs_lattice_plan* plan);
  * after a second bounded wait, or VS_ERR_NONFINITE when the watchdog found a NaN/Inf
  * population.  Synchronises the stream; reset != 0 clears it. */
 int vs_lattice_status(const vs_lattice_plan* plan, int reset, void* stream);
+/* Run form of vs_run for this plan: VS_RUN_STEPS (default: launches per time step) or
+ * VS_RUN_PERSISTENT (one cooperative launch per run where vs_run_persistent says it
+ * applies; elsewhere the per-step launches).  Both give the same bits.  No CUDA call.  No
+ * counterpart in the reference (its loop is XLA's). */
+#define VS_RUN_STEPS 0
+#define VS_RUN_PERSISTENT 1
+int vs_lattice_set_run_form(vs_lattice_plan* plan, int form);
 /* NaN/Inf scan of n values: sets *status_dev (a device int) to VS_ERR_NONFINITE when one is
  * not finite and leaves it unchanged otherwise.  Asynchronous.  The reference has no
  * counterpart (a JAX run would carry the NaN on); this is the fused run's watchdog. */
@@ -306,7 +313,8 @@ int vs_step(const vs_lattice_plan* lattice, vs_body_plan* body, const void* f_in
 /* n_steps steps ping-ponging between f_a (input) and f_b; the result ends in f_a when
  * n_steps is even, else in f_b.  force_hist (n_steps x 3) may be NULL.  The loop of the
  * reference's examples (examples/2d/vortex_induced_vibration.py:151-157, a lax.scan over
- * update_step).  With the environment variable VIVSIM_GB300_RUN_FORM=persistent, a
+ * update_step).  With the run form VS_RUN_PERSISTENT (vs_lattice_set_run_form, or the
+ * environment variable VIVSIM_GB300_RUN_FORM=persistent for every plan), a
  * float 2-D plan whose body takes the cluster form (4 x 4 stencil, face boundaries that
  * can wait for the next step's load) runs all n_steps in one persistent cooperative launch
  * (the body's thread-block cluster beside groups of grid tiles, a barrier per step; one

@@ -85,6 +85,9 @@ def test_run_form_and_batch_shape_queries_without_gpu(lib):
     assert b"null plan" in lib.vs_last_error()
     assert lib.vs_batch_set_nodes_per_thread(C.c_void_p(64), 3) == 1
     assert b"1 or 2" in lib.vs_last_error()
+    assert lib.vs_lattice_set_run_form(None, 1) == 1
+    assert lib.vs_lattice_set_run_form(C.c_void_p(64), 2) == 1
+    assert b"VS_RUN_STEPS or VS_RUN_PERSISTENT" in lib.vs_last_error()
 
 
 def test_plan_validation_without_gpu(lib):

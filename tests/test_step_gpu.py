@@ -817,3 +817,24 @@ def test_persistent_run_full_size_and_watchdog(S, monkeypatch):
         assert np.array_equal(h, hb)
         for k in ("a", "v", "d", "h"):
             assert np.array_equal(s[k], sb[k]), k
+
+
+def test_run_form_tuner(S):
+    """Simulation.tune times the run forms that apply (launches per step; the persistent
+    run) and keeps the faster; runs then give the same bits whichever it chose."""
+    from vivsim_gb300 import configs
+    kw = dict(nx=256, ny=128, D=20.0, center=(64.0, 64.0), n_markers=63)
+    _, _, a = configs.build_solver(configs.viv2d(**kw))
+    times = a.tune(trial_steps=20)
+    assert set(times) == {"steps", "persistent"}, times
+    assert a.step.run_form == min(times, key=times.get)
+    _, _, b = configs.build_solver(configs.viv2d(**kw))
+    b.step.set_run_form("persistent" if a.step.run_form == "steps" else "steps")
+    with torch.cuda.stream(torch.cuda.Stream()):
+        b.run(80, graph=True)  # the tuner advanced a by 4 x 20 steps
+        a.run(30, graph=True)
+        b.run(30, graph=True)
+        torch.cuda.synchronize()
+    assert np.array_equal(N(a.f), N(b.f))
+    with pytest.raises(ValueError):
+        a.step.set_run_form("fast")

@@ -25,6 +25,7 @@ VS_WALL_GIVEN, VS_WALL_VELOCITY, VS_WALL_PRESSURE, VS_WALL_FORCE_CORRECTED, VS_W
 VS_KERNEL_PESKIN3, VS_KERNEL_PESKIN4, VS_KERNEL_COSINE4 = range(3)
 VS_MAX_BC = 8
 VS_GRID_AUTO, VS_GRID_PLAIN, VS_GRID_TMA = 0, 1, 2
+VS_RUN_STEPS, VS_RUN_PERSISTENT = 0, 1
 
 REFINE_DIRS = {"left": 0, "right": 1, "up": 2, "down": 3}
 LOCS = {"left": VS_LEFT, "right": VS_RIGHT, "bottom": VS_BOTTOM, "top": VS_TOP, "back": VS_BACK,
@@ -128,6 +129,7 @@ _SIGS = {
     "vs_run": (_i, [_p, _p, _p, _p, _i, _p, _p]),
     "vs_run_graph": (_i, [_p, _p, _p, _p, _i, _p, _p]),
     "vs_run_persistent": (_i, [_p, _p, _i]),
+    "vs_lattice_set_run_form": (_i, [_p, _i]),
     "vs_step_grid_only": (_i, [_p, _p, _p, _p, _p]),
     "vs_body_state_device": (_i, [_p, C.POINTER(C.c_void_p)]),
     "vs_body_set_state_device": (_i, [_p, _p, _p]),

@@ -2240,6 +2240,7 @@ struct vs_lattice_plan {
   int tma_tb;                // tile width of the TMA grid kernel, 0 when it does not apply
   int bb_load;               // set per step: the input still lacks the obstacle bounce-back
   int tma_grid;              // persistent CTAs of the TMA grid kernel
+  int run_form;              // VS_RUN_STEPS or VS_RUN_PERSISTENT (vs_lattice_set_run_form)
   int stream_pop;            // one population buffer is larger than L2: a grid launch beside
                              // body kernels streams it (evict-first) past their working set
   // graph cache
@@ -3185,12 +3186,13 @@ static cudaError_t viv_run_setup(vs_body_plan* B, int coll, int& ctas) {
 // The persistent run applies to float 2-D plans whose body takes the cluster form with a
 // 4 x 4 stencil, whose face boundaries are deferred to the next step's load (or absent),
 // and whose bulk nodes need no per-node feature (no uniform force, obstacle mask,
-// characteristic wall or pre-stream faces).  It is selected with
-// VIVSIM_GB300_RUN_FORM=persistent; the default is the launch-per-step form, which measured
-// faster on the benchmark VIV case (14.0 against 18.8 us per step).
+// characteristic wall or pre-stream faces).  It is selected per plan with
+// vs_lattice_set_run_form (or for every plan with VIVSIM_GB300_RUN_FORM=persistent); the
+// default is the launch-per-step form, which measured faster on the benchmark VIV case
+// (14.0 against 17.1 us per step).
 static bool viv_run_applies(const vs_lattice_plan* LP, const vs_body_plan* B, bool lazy) {
   const char* form = getenv("VIVSIM_GB300_RUN_FORM");
-  if (!form || strcmp(form, "persistent") != 0) return false;
+  if (LP->run_form != VS_RUN_PERSISTENT && (!form || strcmp(form, "persistent") != 0)) return false;
   if (!B || !B->cluster || B->run_ctas <= 0 || B->dim != 2) return false;
   const vs_lattice_cfg& c = LP->cfg;
   if (c.dtype != VS_F32 || c.q != 9 || B->cfg.radius != 2 || c.obstacle_mask) return false;
@@ -3447,6 +3449,14 @@ int vs_lattice_plan_create(const vs_lattice_cfg* cfg, vs_lattice_plan** out) {
         cfg->bc[k].mode == VS_WALL_CHARACTERISTIC)
       p->lazy_ok = 0;
   *out = p;
+  return VS_OK;
+}
+
+int vs_lattice_set_run_form(vs_lattice_plan* plan, int form) {
+  VS_REQUIRE(plan, "vs_lattice_set_run_form: null plan");
+  VS_REQUIRE(form == VS_RUN_STEPS || form == VS_RUN_PERSISTENT,
+             "vs_lattice_set_run_form: form must be VS_RUN_STEPS or VS_RUN_PERSISTENT");
+  plan->run_form = form;
   return VS_OK;
 }
 

@@ -127,6 +127,15 @@ class LatticeStep:
     def n_nodes(self):
         return int(np.prod(self.shape))
 
+    def set_run_form(self, form):
+        """'steps' (launches per time step, the default) or 'persistent' (one cooperative
+        launch per run where it applies): vs_lattice_set_run_form.  Same bits either way."""
+        codes = {"steps": V.VS_RUN_STEPS, "persistent": V.VS_RUN_PERSISTENT}
+        if form not in codes:
+            raise ValueError("form must be 'steps' or 'persistent'")
+        V.call("vs_lattice_set_run_form", self.handle, codes[form])
+        self.run_form = form
+
     def check(self, reset=True):
         """Raise if a grid kernel of this plan reported a device-side error, or the watchdog
         found a NaN/Inf population (synchronises)."""
@@ -283,6 +292,38 @@ class Simulation:
         """True when run(n_steps) advances all steps in one persistent launch (vs_run_persistent)."""
         body = self.body.handle if self.body is not None else None
         return bool(V.lib().vs_run_persistent(self.step.handle, body, int(n_steps)))
+
+    def tune(self, trial_steps=200):
+        """Choose the faster run form of this plan (LatticeStep.set_run_form): each form that
+        applies runs trial_steps twice from a CUDA graph on a side stream, the second time
+        timed with CUDA events; the faster stays set.  Advances the simulation by
+        4 * trial_steps steps or fewer.  Returns {form: ms per step}."""
+        old = getattr(self.step, "run_form", "steps")
+        forms = ["steps"]
+        self.step.set_run_form("persistent")
+        if self.persistent(trial_steps):
+            forms.append("persistent")
+        cur = torch.cuda.current_stream()
+        side = torch.cuda.Stream()
+        side.wait_stream(cur)
+        times = {}
+        try:
+            with torch.cuda.stream(side):
+                for form in forms:
+                    self.step.set_run_form(form)
+                    self.run(trial_steps, graph=True)
+                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    e0.record()
+                    self.run(trial_steps, graph=True)
+                    e1.record()
+                    e1.synchronize()
+                    times[form] = e0.elapsed_time(e1) / trial_steps
+        except Exception:
+            self.step.set_run_form(old)
+            raise
+        cur.wait_stream(side)
+        self.step.set_run_form(min(times, key=times.get))
+        return times
 
 
 class Batch:
