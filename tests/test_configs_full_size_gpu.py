@@ -230,11 +230,13 @@ def test_float32_drift_matches_the_oracles(cfg, name, n_steps):
     In the fluid (nodes farther than one diameter from the body) the kernel's distance from
     float64 is at most twice the float32 oracle's.  At the body the KBC step is sensitive to
     float32 rounding (not the flow: a float64 run started one float32 ulp away stays within
-    ~1e-8): nodes just inside the immersed cylinder's surface, which the forcing holds near
-    rest, move by 7e-5 of max|u| in the float32 oracle and by 3e-4 in the fused float32
-    step when the initial state changes by one ulp at 1 % of the nodes, after 1000 steps
-    (the MRT step's whole-field drift is 1.6e-5).  So the whole field is held to 5e-4 of
-    max|u|, with the oracle's own numbers printed beside the kernel's."""
+    ~1e-8).  Just inside the immersed cylinder's front surface the entropic stabiliser is
+    active (gamma/2 ~ 1.1) on a higher-order part of only 2e-5 that float32 resolves to
+    ~1e-3, so every float32 KBC run carries extra noise there.  One ulp at 1 % of the initial
+    nodes moves u there by 7e-5 of max|u| in the float32 oracle and by 3e-4 in the fused
+    float32 step after 1000 steps (the MRT step's whole-field drift is 1.6e-5).  So the whole
+    field is held to 5e-4 of max|u|, with the oracle's own numbers printed beside the
+    kernel's."""
     d = drift(cfg, cfg.CASES[name](), n_steps)
     print(f"\n{name} {n_steps} steps vs oracle64: kernel rho {d['kernel64'][0]:.2e} u {d['kernel64'][1]:.2e}, "
           f"oracle32 rho {d['oracle64'][0]:.2e} u {d['oracle64'][1]:.2e}; fluid: kernel rho "
